@@ -1,0 +1,196 @@
+// BinningKKSort on the device (binning_kksort.cpp:71-140).
+//
+// Bin of a particle: per-dimension int((x_d - min_d) * nbin_d/(max_d - min_d)),
+// flattened with x slowest (the decode of binning_kksort.cpp:61-63).  The
+// permutation is a stable counting sort: each bin lists its particles in
+// ascending index, which is what a serial BinSort produces.  Four kernels:
+// bin + histogram, scan, scatter through per-bin cursors, and a per-bin
+// rank pass that restores ascending order inside each bin.  With sort=true
+// a gather reorders x, v, f, type, id, q of the binned range.
+#include <algorithm>
+
+#include "emd_device.cuh"
+#include "emd_internal.h"
+
+namespace emd {
+namespace {
+
+__global__ void __launch_bounds__(256) k_bin_index(const double4_32a* __restrict__ x4, int first, int n, int nbx,
+                                                   int nby, int nbz, double minx, double miny, double minz,
+                                                   double mulx, double muly, double mulz, int* __restrict__ binof,
+                                                   int* __restrict__ bincount, unsigned* status) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const double4_32a p = x4[first + r];
+  int ix = int((p.x - minx) * mulx);
+  int iy = int((p.y - miny) * muly);
+  int iz = int((p.z - minz) * mulz);
+  if (ix < 0 || ix >= nbx || iy < 0 || iy >= nby || iz < 0 || iz >= nbz) {
+    // outside the binned box: the reference would index out of bounds; keep
+    // the particle in the nearest bin and report it
+    latch_status(status, ST_BOUNDS);
+    ix = min(max(ix, 0), nbx - 1);
+    iy = min(max(iy, 0), nby - 1);
+    iz = min(max(iz, 0), nbz - 1);
+  }
+  const int b = (ix * nby + iy) * nbz + iz;
+  binof[r] = b;
+  atomicAdd(&bincount[b], 1);
+}
+
+__global__ void __launch_bounds__(256) k_bin_scatter(const int* __restrict__ binof, int n,
+                                                     const int* __restrict__ binoffsets, int* __restrict__ cursor,
+                                                     int* __restrict__ perm_tmp) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int b = binof[r];
+  const int slot = atomicAdd(&cursor[b], 1);
+  perm_tmp[binoffsets[b] + slot] = r;
+}
+
+// One warp per bin: each member's rank = number of members with a smaller
+// index, which puts the bin in ascending order (members are distinct).
+__global__ void __launch_bounds__(256) k_bin_rank(const int* __restrict__ bincount,
+                                                  const int* __restrict__ binoffsets, int nbins,
+                                                  const int* __restrict__ perm_tmp, int* __restrict__ permute) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nbins) return;
+  const int n = bincount[warp];
+  const int off = binoffsets[warp];
+  for (int e = lane; e < n; e += 32) {
+    const int val = perm_tmp[off + e];
+    int rank = 0;
+    for (int k = 0; k < n; ++k) rank += perm_tmp[off + k] < val ? 1 : 0;
+    permute[off + rank] = val;
+  }
+}
+
+template <class T>
+__global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst, const int* __restrict__ perm, int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) dst[r] = src[perm[r]];
+}
+__global__ void k_gather3(const double* __restrict__ src, double* __restrict__ dst, const int* __restrict__ perm,
+                          int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int s = perm[r];
+  dst[3 * r] = src[3 * s];
+  dst[3 * r + 1] = src[3 * s + 1];
+  dst[3 * r + 2] = src[3 * s + 2];
+}
+
+}  // namespace
+}  // namespace emd
+
+using namespace emd;
+
+extern "C" {
+
+emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double dz_in, int halo_depth, int do_local,
+                              int do_ghost, int sort, int nbin_out[3]) {
+  EMD_API_BEGIN
+  require(dx_in > 0 && dy_in > 0 && dz_in > 0 && halo_depth >= 0, EMD_ERR_ARG, "emd_binning_create: bad bin size");
+  if (!(do_local || do_ghost)) return EMD_OK;
+  const int first = do_local ? 0 : c.N_local;
+  const int last = do_ghost ? c.N_local + c.N_ghost : c.N_local;
+  const int n = last - first;
+  // host-side geometry, same expressions and order as binning_kksort.cpp:76-99
+  const double sub[3] = {c.sub_hi[0] - c.sub_lo[0], c.sub_hi[1] - c.sub_lo[1], c.sub_hi[2] - c.sub_lo[2]};
+  int nb[3] = {int(sub[0] / dx_in), int(sub[1] / dy_in), int(sub[2] / dz_in)};
+  for (int d = 0; d < 3; ++d)
+    if (nb[d] == 0) nb[d] = 1;
+  const double dxyz[3] = {sub[0] / nb[0], sub[1] / nb[1], sub[2] / nb[2]};
+  for (int d = 0; d < 3; ++d) nb[d] += 2 * halo_depth;
+  const double eps = dxyz[0] / 1000;
+  for (int d = 0; d < 3; ++d) {
+    c.bmin[d] = -dxyz[d] * halo_depth - eps + c.sub_lo[d];
+    c.bmax[d] = dxyz[d] * halo_depth + eps + c.sub_hi[d];
+    c.bmul[d] = double(nb[d]) / (c.bmax[d] - c.bmin[d]);
+    c.nbin[d] = nb[d];
+  }
+  c.nhalo = halo_depth;
+  c.bin_first = first;
+  c.bin_count_n = n;
+  const long long nbins_ll = (long long)nb[0] * nb[1] * nb[2];
+  require(nbins_ll < 0x7fffffffLL, EMD_ERR_ARG, "emd_binning_create: too many bins");
+  const int nbins = int(nbins_ll);
+  c.bincount.reserve(size_t(nbins) + 1, c.stream);
+  c.binoffsets.reserve(size_t(nbins) + 1, c.stream);
+  c.bin_cursor.reserve(size_t(nbins) + 1, c.stream);
+  c.binof.reserve(size_t(n) + 1, c.stream);
+  c.permute.reserve(size_t(n) + 1, c.stream);
+  c.perm_tmp.reserve(size_t(n) + 1, c.stream);
+  EMD_CUDA(cudaMemsetAsync(c.bincount.p, 0, sizeof(int) * nbins, c.stream));
+  EMD_CUDA(cudaMemsetAsync(c.bin_cursor.p, 0, sizeof(int) * nbins, c.stream));
+  if (n > 0) {
+    TimedLaunch t(c, "bin_index");
+    k_bin_index<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p, first, n, nb[0], nb[1], nb[2], c.bmin[0],
+                                                          c.bmin[1], c.bmin[2], c.bmul[0], c.bmul[1], c.bmul[2],
+                                                          c.binof.p, c.bincount.p, c.d_status);
+    EMD_CHECK_LAUNCH();
+  }
+  exclusive_scan_int(c, c.bincount.p, c.binoffsets.p, nbins, nullptr);
+  if (n > 0) {
+    {
+      TimedLaunch t(c, "bin_scatter");
+      k_bin_scatter<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.binof.p, n, c.binoffsets.p, c.bin_cursor.p,
+                                                              c.perm_tmp.p);
+      EMD_CHECK_LAUNCH();
+    }
+    {
+      TimedLaunch t(c, "bin_rank");
+      k_bin_rank<<<blocks_for((long long)nbins * 32, 256), 256, 0, c.stream>>>(c.bincount.p, c.binoffsets.p, nbins,
+                                                                               c.perm_tmp.p, c.permute.p);
+      EMD_CHECK_LAUNCH();
+    }
+  }
+  if (sort && n > 0) {
+    // BinSort::sort of x, v, f, type, id, q over the binned range
+    TimedLaunch t(c, "bin_sort_gather");
+    const int* perm = c.permute.p;
+    c.stage_x4.reserve(size_t(n), c.stream);
+    k_gather<double4_32a><<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p + first, c.stage_x4.p, perm, n);
+    EMD_CUDA(cudaMemcpyAsync(c.x4.p + first, c.stage_x4.p, sizeof(double4_32a) * n, cudaMemcpyDeviceToDevice, c.stream));
+    c.stage_d.reserve(3 * size_t(n), c.stream);
+    for (DevBuf<double>* b : {&c.v, &c.f}) {
+      k_gather3<<<blocks_for(n, 256), 256, 0, c.stream>>>(b->p + 3 * size_t(first), c.stage_d.p, perm, n);
+      EMD_CUDA(cudaMemcpyAsync(b->p + 3 * size_t(first), c.stage_d.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice,
+                               c.stream));
+    }
+    k_gather<double><<<blocks_for(n, 256), 256, 0, c.stream>>>(c.q.p + first, c.stage_d.p, perm, n);
+    EMD_CUDA(cudaMemcpyAsync(c.q.p + first, c.stage_d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+    c.stage_i.reserve(size_t(n), c.stream);
+    for (DevBuf<int>* b : {&c.type, &c.id}) {
+      k_gather<int><<<blocks_for(n, 256), 256, 0, c.stream>>>(b->p + first, c.stage_i.p, perm, n);
+      EMD_CUDA(cudaMemcpyAsync(b->p + first, c.stage_i.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    EMD_CHECK_LAUNCH();
+    c.neigh_ready = false;
+  }
+  c.binning_ready = true;
+  if (nbin_out)
+    for (int d = 0; d < 3; ++d) nbin_out[d] = nb[d];
+  EMD_API_END
+}
+
+emd_status emd_binning_get(emd_ctx* ctx, int* bincount, int* binoffsets, int* permute, double bounds[6]) {
+  EMD_API_BEGIN
+  require(c.binning_ready, EMD_ERR_STATE, "emd_binning_get: no binning");
+  const size_t nbins = size_t(c.nbin[0]) * c.nbin[1] * c.nbin[2];
+  if (bincount) EMD_CUDA(cudaMemcpyAsync(bincount, c.bincount.p, sizeof(int) * nbins, cudaMemcpyDeviceToHost, c.stream));
+  if (binoffsets)
+    EMD_CUDA(cudaMemcpyAsync(binoffsets, c.binoffsets.p, sizeof(int) * nbins, cudaMemcpyDeviceToHost, c.stream));
+  if (permute && c.bin_count_n > 0)
+    EMD_CUDA(cudaMemcpyAsync(permute, c.permute.p, sizeof(int) * c.bin_count_n, cudaMemcpyDeviceToHost, c.stream));
+  if (bounds)
+    for (int d = 0; d < 3; ++d) {
+      bounds[2 * d] = c.bmin[d];
+      bounds[2 * d + 1] = c.bmax[d];
+    }
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  EMD_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,498 @@
+// Context lifecycle, System storage, status word, kernel timing, and the
+// device-wide scan / sum primitives used by the module kernels.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+#include "emd_device.cuh"
+#include "emd_internal.h"
+
+namespace emd {
+
+// ---------------------------------------------------------------- timing
+TimedLaunch::TimedLaunch(Ctx& ctx, const char* name) : c(ctx) {
+  if (!c.timer.on) return;
+  slot = &c.timer.slots[name];
+  for (cudaEvent_t* e : {&a, &b}) {
+    if (!c.timer.pool.empty()) {
+      *e = c.timer.pool.back();
+      c.timer.pool.pop_back();
+    } else {
+      EMD_CUDA(cudaEventCreate(e));
+    }
+  }
+  EMD_CUDA(cudaEventRecord(a, c.stream));
+}
+
+TimedLaunch::~TimedLaunch() {
+  if (!slot) return;
+  if (cudaEventRecord(b, c.stream) == cudaSuccess) slot->pending.push_back({a, b});
+}
+
+void timing_collect(Ctx& c) {
+  for (auto& kv : c.timer.slots) {
+    for (auto& p : kv.second.pending) {
+      float ms = 0.f;
+      EMD_CUDA(cudaEventSynchronize(p.b));
+      EMD_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+      kv.second.ms += ms;
+      kv.second.n += 1;
+      c.timer.pool.push_back(p.a);
+      c.timer.pool.push_back(p.b);
+    }
+    kv.second.pending.clear();
+  }
+}
+
+// ---------------------------------------------------------------- scan
+namespace {
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER_THREAD = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(FULL_MASK, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// Exclusive scan of one tile per block; block totals to sums[blockIdx.x].
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(const int* __restrict__ in, int* __restrict__ out,
+                                                              int n, int* __restrict__ sums) {
+  __shared__ int warp_tot[SCAN_THREADS / 32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_PER_THREAD;
+  int vals[SCAN_PER_THREAD];
+  int local = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+    long long idx = base + k;
+    vals[k] = idx < n ? in[idx] : 0;
+    local += vals[k];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = warp_incl_scan(local);
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int t = warp_tot[lane];
+    int ti = warp_incl_scan(t);
+    warp_tot[lane] = ti - t;  // exclusive prefix of warp totals
+  }
+  __syncthreads();
+  int run = warp_tot[w] + incl - local;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+    long long idx = base + k;
+    if (idx < n) out[idx] = run;
+    run += vals[k];
+  }
+  if (threadIdx.x == SCAN_THREADS - 1 && sums) sums[blockIdx.x] = run;
+}
+
+__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ offs) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += offs[i / SCAN_TILE];
+}
+
+__global__ void k_scan_total(const int* __restrict__ in, const int* __restrict__ scanned, int n, int* total) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *total = n > 0 ? scanned[n - 1] + in[n - 1] : 0;
+}
+
+// Deterministic FP64 sum: fixed grid, fixed per-thread partition.
+constexpr int SUM_BLOCKS = 304;
+constexpr int SUM_THREADS = 256;
+__global__ void __launch_bounds__(SUM_THREADS) k_sum_partial(const double* __restrict__ v, int n, double* part) {
+  __shared__ double sh[SUM_THREADS / 32];
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * SUM_THREADS + threadIdx.x; i < n; i += (long long)SUM_BLOCKS * SUM_THREADS)
+    acc += v[i];
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+__global__ void __launch_bounds__(SUM_THREADS) k_sum_final(const double* __restrict__ part, int n, double* out) {
+  __shared__ double sh[SUM_THREADS / 32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += SUM_THREADS) acc += part[i];
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) *out = t;
+}
+}  // namespace
+
+static void scan_rec(Ctx& c, const int* in, int* out, int n, int level) {
+  const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  require(level < (int)c.scan_levels.size(), EMD_ERR_ARG, "scan: too many levels");
+  DevBuf<int>& sums = c.scan_levels[level];
+  sums.reserve(size_t(tiles) + 1, c.stream);
+  {
+    TimedLaunch t(c, "scan_tiles");
+    k_scan_tiles<<<tiles, SCAN_THREADS, 0, c.stream>>>(in, out, n, sums.p);
+    EMD_CHECK_LAUNCH();
+  }
+  if (tiles > 1) {
+    scan_rec(c, sums.p, sums.p, tiles, level + 1);
+    TimedLaunch t(c, "scan_add");
+    k_scan_add<<<blocks_for(n, 256), 256, 0, c.stream>>>(out, n, sums.p);
+    EMD_CHECK_LAUNCH();
+  }
+}
+
+void exclusive_scan_int(Ctx& c, const int* d_in, int* d_out, int n, int* d_total) {
+  if (n <= 0) {
+    if (d_total) EMD_CUDA(cudaMemsetAsync(d_total, 0, sizeof(int), c.stream));
+    return;
+  }
+  // levels are sized once so references into the vector stay valid
+  if (c.scan_levels.size() < 6) c.scan_levels.resize(6);
+  // The total needs the last input, which an in-place scan overwrites.
+  c.scan_aux.reserve(2, c.stream);
+  if (d_total)
+    EMD_CUDA(cudaMemcpyAsync(c.scan_aux.p, d_in + n - 1, sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
+  scan_rec(c, d_in, d_out, n, 0);
+  if (d_total) {
+    k_scan_total<<<1, 32, 0, c.stream>>>(c.scan_aux.p, d_out + n - 1, 1, d_total);
+    EMD_CHECK_LAUNCH();
+  }
+}
+
+double device_sum(Ctx& c, const double* d_vals, int n) {
+  c.red.reserve(SUM_BLOCKS + 2, c.stream);
+  {
+    TimedLaunch t(c, "sum_partial");
+    k_sum_partial<<<SUM_BLOCKS, SUM_THREADS, 0, c.stream>>>(d_vals, n, c.red.p);
+    EMD_CHECK_LAUNCH();
+  }
+  k_sum_final<<<1, SUM_THREADS, 0, c.stream>>>(c.red.p, SUM_BLOCKS, c.red.p + SUM_BLOCKS);
+  EMD_CHECK_LAUNCH();
+  EMD_CUDA(cudaMemcpyAsync(c.h_scalar, c.red.p + SUM_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  return *c.h_scalar;
+}
+
+unsigned read_status(Ctx& c, bool clear) {
+  EMD_CUDA(cudaMemcpyAsync(c.h_status, c.d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, c.stream));
+  if (clear) EMD_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(unsigned), c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  return *c.h_status;
+}
+
+// ---------------------------------------------------------------- System kernels
+namespace {
+__global__ void k_pack_x4(const double* __restrict__ x3, const int* __restrict__ type, double4_32a* __restrict__ x4,
+                          int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x4[i] = make_double4_32a(x3[3 * i], x3[3 * i + 1], x3[3 * i + 2], double(type[i]));
+}
+__global__ void k_pack_x4_keep_type(const double* __restrict__ x3, double4_32a* __restrict__ x4, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4_32a o = x4[i];
+  x4[i] = make_double4_32a(x3[3 * i], x3[3 * i + 1], x3[3 * i + 2], o.w);
+}
+__global__ void k_unpack_x4(const double4_32a* __restrict__ x4, double* __restrict__ x3, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4_32a p = x4[i];
+  x3[3 * i] = p.x;
+  x3[3 * i + 1] = p.y;
+  x3[3 * i + 2] = p.z;
+}
+// Temperature/KinE functor: (v.v) * mass(type) per owned atom
+// (property_temperature.h:54-57), block partial sums in fixed order.
+__global__ void __launch_bounds__(256) k_mv2(const double* __restrict__ v, const int* __restrict__ type,
+                                             const double* __restrict__ mass, int n, double* part) {
+  __shared__ double sh[8];
+  double acc = 0.0;
+  for (int i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
+    const double vx = v[3 * i], vy = v[3 * i + 1], vz = v[3 * i + 2];
+    acc += (vx * vx + vy * vy + vz * vz) * mass[type[i]];
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+}  // namespace
+
+static void system_reserve(Ctx& c, int n_max, bool keep) {
+  const size_t n = size_t(n_max) + 1;
+  c.x4.reserve(n, c.stream, keep);
+  c.v.reserve(3 * n, c.stream, keep);
+  c.f.reserve(3 * n, c.stream, keep);
+  c.q.reserve(n, c.stream, keep);
+  c.type.reserve(n, c.stream, keep);
+  c.id.reserve(n, c.stream, keep);
+  if (n_max > c.N_max) c.N_max = n_max;
+}
+
+}  // namespace emd
+
+using namespace emd;
+
+extern "C" {
+
+int emd_abi_version(void) { return 1; }
+
+const char* emd_status_string(emd_status s) {
+  switch (s) {
+    case EMD_OK: return "ok";
+    case EMD_ERR_OVERFLOW_GHOST: return "ghost capacity overflow";
+    case EMD_ERR_OVERFLOW_NEIGH: return "neighbour capacity overflow";
+    case EMD_ERR_TIMEOUT: return "bounded device wait timed out";
+    case EMD_ERR_BOUNDS: return "device index check failed";
+    case EMD_ERR_CUDA: return "CUDA error";
+    case EMD_ERR_ARG: return "invalid argument";
+    case EMD_ERR_STATE: return "call out of order";
+    case EMD_ERR_NOMEM: return "device allocation failed";
+  }
+  return "unknown";
+}
+
+emd_status emd_create(emd_ctx** out, int device) {
+  if (!out) return EMD_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) {
+    (void)cudaGetLastError();
+    return EMD_ERR_CUDA;
+  }
+  emd_ctx* ctx = new emd_ctx();
+  Ctx& c = ctx->c;
+  try {
+    c.device = device;
+    EMD_CUDA(cudaSetDevice(device));
+    EMD_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    EMD_CUDA(cudaMalloc(&c.d_status, sizeof(unsigned)));
+    EMD_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(unsigned), c.stream));
+    EMD_CUDA(cudaMallocHost(&c.h_status, sizeof(unsigned)));
+    EMD_CUDA(cudaMallocHost(&c.h_scalar, 8 * sizeof(double)));
+    EMD_CUDA(cudaMallocHost(&c.h_ll, 8 * sizeof(long long)));
+    EMD_CUDA(cudaMallocHost(&c.h_int, 16 * sizeof(int)));
+    c.mass.assign(1, 1.0);
+    EMD_CUDA(cudaStreamSynchronize(c.stream));
+  } catch (const Error& e) {
+    fprintf(stderr, "emd_create: %s\n", e.what());
+    delete ctx;
+    return e.code;
+  }
+  *out = ctx;
+  return EMD_OK;
+}
+
+void emd_destroy(emd_ctx* ctx) {
+  if (!ctx) return;
+  Ctx& c = ctx->c;
+  cudaSetDevice(c.device);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  free_snap(c);
+  for (auto* b : {&c.v, &c.f, &c.q, &c.mass_d, &c.stage_d, &c.lj_params, &c.red, &c.red2}) b->release();
+  for (auto* b : {&c.type, &c.id, &c.stage_i, &c.pack, &c.ghost_owner, &c.ghost_img, &c.flags, &c.flags_scan,
+                  &c.bincount, &c.binoffsets, &c.permute, &c.binof, &c.bin_cursor, &c.perm_tmp, &c.num_neighs,
+                  &c.neigh_offsets, &c.neighs, &c.resize_flag, &c.abin})
+    b->release();
+  c.x4.release();
+  c.stage_x4.release();
+  c.xl.release();
+  c.lj_params_f.release();
+  for (auto& b : c.scan_levels) b.release();
+  c.scan_aux.release();
+  for (auto& kv : c.timer.slots)
+    for (auto& p : kv.second.pending) {
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+  for (auto e : c.timer.pool) cudaEventDestroy(e);
+  if (c.d_status) cudaFree(c.d_status);
+  if (c.h_status) cudaFreeHost(c.h_status);
+  if (c.h_scalar) cudaFreeHost(c.h_scalar);
+  if (c.h_ll) cudaFreeHost(c.h_ll);
+  if (c.h_int) cudaFreeHost(c.h_int);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  delete ctx;
+}
+
+const char* emd_last_error(const emd_ctx* ctx) { return ctx ? ctx->c.last_error.c_str() : "null context"; }
+
+void* emd_stream(emd_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
+
+emd_status emd_synchronize(emd_ctx* ctx) {
+  EMD_API_BEGIN
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  EMD_API_END
+}
+
+emd_status emd_get_status(emd_ctx* ctx, unsigned* flags) {
+  EMD_API_BEGIN
+  unsigned s = read_status(c, false);
+  if (flags) *flags = s;
+  EMD_API_END
+}
+
+emd_status emd_system_init(emd_ctx* ctx, int ntypes, const double* mass, double boltz, double mvv2e, double dt,
+                           const double domain[3], const double sub_lo[3], const double sub_hi[3]) {
+  EMD_API_BEGIN
+  require(ntypes >= 1 && mass && domain && sub_lo && sub_hi, EMD_ERR_ARG, "emd_system_init: bad arguments");
+  c.ntypes = ntypes;
+  c.mass.assign(mass, mass + ntypes);
+  c.boltz = boltz;
+  c.mvv2e = mvv2e;
+  c.dt = dt;
+  for (int d = 0; d < 3; ++d) {
+    c.domain[d] = domain[d];
+    c.sub_lo[d] = sub_lo[d];
+    c.sub_hi[d] = sub_hi[d];
+  }
+  c.mass_d.reserve(size_t(ntypes), c.stream);
+  EMD_CUDA(cudaMemcpyAsync(c.mass_d.p, c.mass.data(), sizeof(double) * ntypes, cudaMemcpyHostToDevice, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  EMD_API_END
+}
+
+emd_status emd_system_grow(emd_ctx* ctx, int n_max) {
+  EMD_API_BEGIN
+  require(n_max >= 0, EMD_ERR_ARG, "emd_system_grow: negative size");
+  system_reserve(c, n_max, true);
+  EMD_API_END
+}
+
+emd_status emd_system_set_local(emd_ctx* ctx, int n, const double* x, const double* v, const double* f,
+                                const int* type, const int* id, const double* q) {
+  EMD_API_BEGIN
+  require(n >= 0 && (n == 0 || (x && type && id)), EMD_ERR_ARG, "emd_system_set_local: x, type, id required");
+  for (int i = 0; i < n; ++i)
+    require(type[i] >= 0 && type[i] < c.ntypes, EMD_ERR_ARG, "emd_system_set_local: type out of range");
+  system_reserve(c, std::max(n, c.N_max), false);
+  c.N_local = n;
+  c.N_ghost = 0;
+  c.binning_ready = false;
+  c.neigh_ready = false;
+  if (n > 0) {
+    c.stage_d.reserve(3 * size_t(n), c.stream);
+    EMD_CUDA(cudaMemcpyAsync(c.stage_d.p, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.type.p, type, sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.id.p, id, sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
+    k_pack_x4<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.stage_d.p, c.type.p, c.x4.p, n);
+    EMD_CHECK_LAUNCH();
+    if (v) EMD_CUDA(cudaMemcpyAsync(c.v.p, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c.stream));
+    else EMD_CUDA(cudaMemsetAsync(c.v.p, 0, sizeof(double) * 3 * n, c.stream));
+    if (q) EMD_CUDA(cudaMemcpyAsync(c.q.p, q, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+    else EMD_CUDA(cudaMemsetAsync(c.q.p, 0, sizeof(double) * n, c.stream));
+  }
+  // forces over all N_max rows
+  EMD_CUDA(cudaMemsetAsync(c.f.p, 0, sizeof(double) * 3 * size_t(c.N_max), c.stream));
+  if (n > 0 && f) EMD_CUDA(cudaMemcpyAsync(c.f.p, f, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  EMD_API_END
+}
+
+emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x, const double* v, const double* f) {
+  EMD_API_BEGIN
+  require(first >= 0 && count >= 0 && first + count <= c.N_local, EMD_ERR_ARG, "emd_system_update: range");
+  if (count == 0) return EMD_OK;
+  if (x) {
+    c.stage_d.reserve(3 * size_t(count), c.stream);
+    EMD_CUDA(cudaMemcpyAsync(c.stage_d.p, x, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
+    k_pack_x4_keep_type<<<blocks_for(count, 256), 256, 0, c.stream>>>(c.stage_d.p, c.x4.p + first, count);
+    EMD_CHECK_LAUNCH();
+  }
+  if (v) EMD_CUDA(cudaMemcpyAsync(c.v.p + 3 * size_t(first), v, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
+  if (f) EMD_CUDA(cudaMemcpyAsync(c.f.p + 3 * size_t(first), f, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
+  EMD_API_END
+}
+
+emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double* v, double* f, int* type, int* id,
+                          double* q) {
+  EMD_API_BEGIN
+  const int total = c.N_local + c.N_ghost;
+  require(first >= 0 && count >= 0 && first + count <= total, EMD_ERR_ARG, "emd_system_get: range");
+  if (count == 0) return EMD_OK;
+  if (x) {
+    c.stage_d.reserve(3 * size_t(count), c.stream);
+    k_unpack_x4<<<blocks_for(count, 256), 256, 0, c.stream>>>(c.x4.p + first, c.stage_d.p, count);
+    EMD_CHECK_LAUNCH();
+    EMD_CUDA(cudaMemcpyAsync(x, c.stage_d.p, sizeof(double) * 3 * count, cudaMemcpyDeviceToHost, c.stream));
+  }
+  if (v) EMD_CUDA(cudaMemcpyAsync(v, c.v.p + 3 * size_t(first), sizeof(double) * 3 * count, cudaMemcpyDeviceToHost, c.stream));
+  if (f) EMD_CUDA(cudaMemcpyAsync(f, c.f.p + 3 * size_t(first), sizeof(double) * 3 * count, cudaMemcpyDeviceToHost, c.stream));
+  if (type) EMD_CUDA(cudaMemcpyAsync(type, c.type.p + first, sizeof(int) * count, cudaMemcpyDeviceToHost, c.stream));
+  if (id) EMD_CUDA(cudaMemcpyAsync(id, c.id.p + first, sizeof(int) * count, cudaMemcpyDeviceToHost, c.stream));
+  if (q) EMD_CUDA(cudaMemcpyAsync(q, c.q.p + first, sizeof(double) * count, cudaMemcpyDeviceToHost, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  EMD_API_END
+}
+
+emd_status emd_system_info(emd_ctx* ctx, int* n_local, int* n_ghost, int* n_max) {
+  EMD_API_BEGIN
+  if (n_local) *n_local = c.N_local;
+  if (n_ghost) *n_ghost = c.N_ghost;
+  if (n_max) *n_max = c.N_max;
+  EMD_API_END
+}
+
+emd_status emd_zero_forces(emd_ctx* ctx) {
+  EMD_API_BEGIN
+  if (c.N_max > 0) {
+    TimedLaunch t(c, "zero_forces");
+    EMD_CUDA(cudaMemsetAsync(c.f.p, 0, sizeof(double) * 3 * size_t(c.N_max), c.stream));
+  }
+  EMD_API_END
+}
+
+emd_status emd_thermo_mv2(emd_ctx* ctx, double* sum_mv2) {
+  EMD_API_BEGIN
+  require(sum_mv2 != nullptr, EMD_ERR_ARG, "emd_thermo_mv2: null output");
+  c.red2.reserve(304, c.stream);
+  {
+    TimedLaunch t(c, "thermo_mv2");
+    k_mv2<<<304, 256, 0, c.stream>>>(c.v.p, c.type.p, c.mass_d.p, c.N_local, c.red2.p);
+    EMD_CHECK_LAUNCH();
+  }
+  // second stage through the shared deterministic sum
+  *sum_mv2 = device_sum(c, c.red2.p, 304);
+  EMD_API_END
+}
+
+emd_status emd_timing_enable(emd_ctx* ctx, int on) {
+  EMD_API_BEGIN
+  c.timer.on = on != 0;
+  EMD_API_END
+}
+
+emd_status emd_timing_reset(emd_ctx* ctx) {
+  EMD_API_BEGIN
+  timing_collect(c);
+  for (auto& kv : c.timer.slots) {
+    kv.second.ms = 0;
+    kv.second.n = 0;
+  }
+  EMD_API_END
+}
+
+emd_status emd_timing_report(emd_ctx* ctx, char* buf, int len) {
+  EMD_API_BEGIN
+  timing_collect(c);
+  std::string s;
+  char line[256];
+  for (auto& kv : c.timer.slots) {
+    snprintf(line, sizeof(line), "%s %.6f %lld\n", kv.first.c_str(), kv.second.ms, kv.second.n);
+    s += line;
+  }
+  if (buf && len > 0) {
+    strncpy(buf, s.c_str(), size_t(len - 1));
+    buf[len - 1] = 0;
+  }
+  EMD_API_END
+}
+
+emd_status emd_timing_get(emd_ctx* ctx, const char* kernel, double* ms_total, long long* launches) {
+  EMD_API_BEGIN
+  timing_collect(c);
+  auto it = c.timer.slots.find(kernel ? kernel : "");
+  if (ms_total) *ms_total = it == c.timer.slots.end() ? 0.0 : it->second.ms;
+  if (launches) *launches = it == c.timer.slots.end() ? 0 : it->second.n;
+  EMD_API_END
+}
+
+}  // extern "C"

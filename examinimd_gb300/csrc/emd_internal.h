@@ -1,0 +1,209 @@
+// Internal state of an emd_ctx and launch helpers shared by the kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/emd_gpu.h"
+
+namespace emd {
+
+// A CUDA failure or argument error inside an entry point; converted to
+// emd_status at the ABI boundary.
+struct Error : std::runtime_error {
+  emd_status code;
+  Error(emd_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define EMD_CUDA(expr)                                                                      \
+  do {                                                                                      \
+    cudaError_t e__ = (expr);                                                               \
+    if (e__ != cudaSuccess)                                                                 \
+      throw ::emd::Error(EMD_ERR_CUDA, std::string(#expr " -> ") + cudaGetErrorString(e__)); \
+  } while (0)
+
+#define EMD_CHECK_LAUNCH() EMD_CUDA(cudaGetLastError())
+
+inline void require(bool ok, emd_status code, const char* msg) {
+  if (!ok) throw Error(code, msg);
+}
+
+// Growable device buffer (contents preserved on grow when keep = true).
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  void reserve(size_t n, cudaStream_t s, bool keep = false) {
+    if (n <= cap) return;
+    size_t ncap = n + n / 5 + 64;
+    T* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, ncap * sizeof(T));
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      throw Error(EMD_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    if (keep && p && cap) EMD_CUDA(cudaMemcpyAsync(q, p, cap * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    if (p) {
+      EMD_CUDA(cudaStreamSynchronize(s));
+      EMD_CUDA(cudaFree(p));
+    }
+    p = q;
+    cap = ncap;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Status bits latched by kernels (bit k = emd_status k).
+enum : unsigned {
+  ST_GHOST = 1u << EMD_ERR_OVERFLOW_GHOST,
+  ST_NEIGH = 1u << EMD_ERR_OVERFLOW_NEIGH,
+  ST_TIMEOUT = 1u << EMD_ERR_TIMEOUT,
+  ST_BOUNDS = 1u << EMD_ERR_BOUNDS,
+};
+
+struct LaunchTimer {
+  struct Pending {
+    cudaEvent_t a, b;
+  };
+  struct Slot {
+    double ms = 0;
+    long long n = 0;
+    std::vector<Pending> pending;
+  };
+  std::map<std::string, Slot> slots;
+  std::vector<cudaEvent_t> pool;
+  bool on = false;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  unsigned* d_status = nullptr;  // device status word
+  unsigned* h_status = nullptr;  // pinned mirror
+
+  // ---- System (SoA on device; x4.w holds the type as a double)
+  int ntypes = 1;
+  std::vector<double> mass;
+  double boltz = 0, mvv2e = 0, dt = 0;
+  double domain[3] = {0, 0, 0}, sub_lo[3] = {0, 0, 0}, sub_hi[3] = {0, 0, 0};
+  int N_local = 0, N_ghost = 0, N_max = 0;
+  DevBuf<double4_32a> x4;
+  DevBuf<double> v, f, q;
+  DevBuf<int> type, id;
+  DevBuf<double> mass_d;  // per type
+  // staging for uploads / sorting gathers
+  DevBuf<double> stage_d;
+  DevBuf<int> stage_i;
+  DevBuf<double4_32a> stage_x4;
+
+  // ---- Comm
+  double comm_depth = 0;
+  int num_ghost[6] = {0, 0, 0, 0, 0, 0};
+  int ghost_offsets[6] = {0, 0, 0, 0, 0, 0};
+  DevBuf<int> pack;         // concatenated per-phase source indices
+  DevBuf<int> ghost_owner;  // owned atom each ghost images (for the one-launch halo update)
+  DevBuf<int> ghost_img;    // 6 bits: shift sign per dimension
+  DevBuf<int> flags, flags_scan;
+
+  // ---- Binning
+  int nbin[3] = {0, 0, 0}, nhalo = 0;
+  double bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0}, bmul[3] = {0, 0, 0};
+  int bin_first = 0, bin_count_n = 0;
+  DevBuf<int> bincount, binoffsets, permute, binof, bin_cursor, perm_tmp;
+  bool binning_ready = false;
+
+  // ---- Neighbor
+  int neigh_kind = EMD_NEIGH_CSR;
+  double neigh_cut = 0;
+  int comm_newton = 0;
+  int half_neigh = 0;
+  bool neigh_ready = false;
+  int neigh_rows = 0;       // N_local at build time
+  long long neigh_total = 0;
+  int maxneighs = 16;       // 2D stride
+  int neigh_stride = 0;     // 2D: rows (column-major leading dimension)
+  DevBuf<int> num_neighs, neigh_offsets, neighs;
+  DevBuf<int> resize_flag;  // [0] = resize, [1] = new max
+  int neigh_packed = 0;     // entries are (j << 5) | stencil code
+  DevBuf<int> abin;         // bin of every particle at the last list build (packed rows)
+  DevBuf<float4> xl;        // FP32 bin-relative positions (mixed force)
+
+  // ---- LJ
+  int lj_ntypes = 0, lj_half = 0, lj_prec = EMD_PREC_FP64;
+  bool lj_ready = false;
+  DevBuf<double> lj_params;  // lj1 | lj2 | cutsq, ntypes^2 each
+  DevBuf<float> lj_params_f; // FP32 copy for the mixed form
+  DevBuf<double> red, red2;  // reduction partials
+
+  // ---- SNAP (defined in snap.cu)
+  void* snap = nullptr;
+
+  // ---- scan scratch
+  std::vector<DevBuf<int>> scan_levels;
+  DevBuf<int> scan_aux;
+
+  LaunchTimer timer;
+  double* h_scalar = nullptr;  // pinned scratch for read-backs
+  long long* h_ll = nullptr;
+  int* h_int = nullptr;
+};
+
+// Kernel timing: brackets a launch with events when enabled.
+struct TimedLaunch {
+  Ctx& c;
+  LaunchTimer::Slot* slot = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TimedLaunch(Ctx& ctx, const char* name);
+  ~TimedLaunch();
+};
+
+void timing_collect(Ctx& c);
+void free_snap(Ctx& c);
+
+inline int blocks_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  return int(b < 1 ? 1 : b);
+}
+
+// exclusive scan of n ints in d_in into d_out (may alias); returns total via
+// *d_total (device int) when non-null.  Uses ctx scratch.
+void exclusive_scan_int(Ctx& c, const int* d_in, int* d_out, int n, int* d_total);
+// deterministic FP64 sum of n doubles (device) -> host value
+double device_sum(Ctx& c, const double* d_vals, int n);
+
+void set_status_check(Ctx& c);
+unsigned read_status(Ctx& c, bool clear);
+
+}  // namespace emd
+
+struct emd_ctx {
+  emd::Ctx c;
+};
+
+// Entry-point wrappers: map exceptions to emd_status, record the message.
+#define EMD_API_BEGIN           \
+  if (!ctx) return EMD_ERR_ARG; \
+  ::emd::Ctx& c = ctx->c;       \
+  try {
+#define EMD_API_END                  \
+  }                                  \
+  catch (const ::emd::Error& e) {    \
+    c.last_error = e.what();         \
+    return e.code;                   \
+  }                                  \
+  catch (const std::exception& e) {  \
+    c.last_error = e.what();         \
+    return EMD_ERR_CUDA;             \
+  }                                  \
+  return EMD_OK;

@@ -1,0 +1,248 @@
+// ForceLJNeigh on the device, FP64 drop-in (force_lj_neigh_impl.h:57-343).
+//
+// Full list: one thread per owned atom accumulates its row in list order and
+// adds the sum to f(i) once -- the same operations in the same order as the
+// serial reference, so with -fmad=false the forces are bit-identical.
+// Half list: the partner's force is scattered with FP64 atomics (as the
+// reference's Atomic-trait view does on a GPU); the order of those adds is
+// not fixed, so half-list forces agree to rounding only.
+// Energy: per-atom shifted-LJ sums, deterministic block + device reduction.
+#include "emd_device.cuh"
+#include "emd_internal.h"
+#include "neigh_rows.cuh"
+
+namespace emd {
+namespace {
+
+struct LJParams {
+  const double* lj1;
+  const double* lj2;
+  const double* cutsq;
+  int ntypes;
+};
+
+__device__ __forceinline__ int entry_j(int e, bool packed) { return packed ? (e >> 5) : e; }
+
+// TagFullNeigh (force_lj_neigh_impl.h:164-206)
+template <bool TWO_D>
+__global__ void __launch_bounds__(128) k_lj_full_fp64(const double4_32a* __restrict__ x4, double* __restrict__ f,
+                                                      ListView L, LJParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a xi = x4[i];
+  const int ti = int(xi.w);
+  const Row<TWO_D> row(L, i);
+  double fxi = 0.0, fyi = 0.0, fzi = 0.0;
+  for (int jj = 0; jj < row.n; ++jj) {
+    const int j = row[jj];
+    const double4_32a xj = x4[j];
+    const double dx = xi.x - xj.x;
+    const double dy = xi.y - xj.y;
+    const double dz = xi.z - xj.z;
+    const int tj = int(xj.w);
+    const double rsq = dx * dx + dy * dy + dz * dz;
+    const int tp = ti * P.ntypes + tj;
+    const double cutsq_ij = __ldg(P.cutsq + tp);
+    if (rsq < cutsq_ij) {
+      const double lj1_ij = __ldg(P.lj1 + tp);
+      const double lj2_ij = __ldg(P.lj2 + tp);
+      const double r2inv = 1.0 / rsq;
+      const double r6inv = r2inv * r2inv * r2inv;
+      const double fpair = (r6inv * (lj1_ij * r6inv - lj2_ij)) * r2inv;
+      fxi += dx * fpair;
+      fyi += dy * fpair;
+      fzi += dz * fpair;
+    }
+  }
+  f[3 * i] += fxi;
+  f[3 * i + 1] += fyi;
+  f[3 * i + 2] += fzi;
+}
+
+// TagHalfNeigh (force_lj_neigh_impl.h:211-254)
+template <bool TWO_D>
+__global__ void __launch_bounds__(128) k_lj_half_fp64(const double4_32a* __restrict__ x4, double* __restrict__ f,
+                                                      ListView L, LJParams P, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a xi = x4[i];
+  const int ti = int(xi.w);
+  const Row<TWO_D> row(L, i);
+  double fxi = 0.0, fyi = 0.0, fzi = 0.0;
+  for (int jj = 0; jj < row.n; ++jj) {
+    const int j = row[jj];
+    const double4_32a xj = x4[j];
+    const double dx = xi.x - xj.x;
+    const double dy = xi.y - xj.y;
+    const double dz = xi.z - xj.z;
+    const int tj = int(xj.w);
+    const double rsq = dx * dx + dy * dy + dz * dz;
+    const int tp = ti * P.ntypes + tj;
+    if (rsq < __ldg(P.cutsq + tp)) {
+      const double r2inv = 1.0 / rsq;
+      const double r6inv = r2inv * r2inv * r2inv;
+      const double fpair = (r6inv * (__ldg(P.lj1 + tp) * r6inv - __ldg(P.lj2 + tp))) * r2inv;
+      fxi += dx * fpair;
+      fyi += dy * fpair;
+      fzi += dz * fpair;
+      atomicAdd(f + 3 * j, -(dx * fpair));
+      atomicAdd(f + 3 * j + 1, -(dy * fpair));
+      atomicAdd(f + 3 * j + 2, -(dz * fpair));
+    }
+  }
+  atomicAdd(f + 3 * i, fxi);
+  atomicAdd(f + 3 * i + 1, fyi);
+  atomicAdd(f + 3 * i + 2, fzi);
+}
+
+// TagFullNeighPE / TagHalfNeighPE (force_lj_neigh_impl.h:259-343), one
+// partial per block.
+template <bool TWO_D>
+__global__ void __launch_bounds__(256) k_lj_energy(const double4_32a* __restrict__ x4, ListView L, LJParams P, int n,
+                                                   int half, int packed, double* __restrict__ part) {
+  __shared__ double sh[8];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double pe = 0.0;
+  if (i < n) {
+    const double4_32a xi = x4[i];
+    const int ti = int(xi.w);
+    const Row<TWO_D> row(L, i);
+    for (int jj = 0; jj < row.n; ++jj) {
+      const int j = entry_j(row[jj], packed);
+      const double4_32a xj = x4[j];
+      const double dx = xi.x - xj.x;
+      const double dy = xi.y - xj.y;
+      const double dz = xi.z - xj.z;
+      const int tj = int(xj.w);
+      const double rsq = dx * dx + dy * dy + dz * dz;
+      const int tp = ti * P.ntypes + tj;
+      const double cutsq_ij = __ldg(P.cutsq + tp);
+      if (rsq < cutsq_ij) {
+        const double lj1_ij = __ldg(P.lj1 + tp);
+        const double lj2_ij = __ldg(P.lj2 + tp);
+        const double r2inv = 1.0 / rsq;
+        const double r6inv = r2inv * r2inv * r2inv;
+        const double r2invc = 1.0 / cutsq_ij;
+        const double r6invc = r2invc * r2invc * r2invc;
+        if (!half) {
+          pe += 0.5 * r6inv * (0.5 * lj1_ij * r6inv - lj2_ij) / 6.0;
+          pe -= 0.5 * r6invc * (0.5 * lj1_ij * r6invc - lj2_ij) / 6.0;
+        } else {
+          const double fac = j < n ? 1.0 : 0.5;
+          pe += fac * r6inv * (0.5 * lj1_ij * r6inv - lj2_ij) / 6.0;
+          pe -= fac * r6invc * (0.5 * lj1_ij * r6invc - lj2_ij) / 6.0;
+        }
+      }
+    }
+  }
+  const double t = block_sum(pe, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+}  // namespace
+
+// shared with lj_mixed.cu
+void lj_mixed_compute(Ctx& c);
+void lj_mixed_prepare(Ctx& c);
+
+ListView list_view(Ctx& c) {
+  ListView L;
+  L.entries = c.neighs.p;
+  L.offsets = c.neigh_offsets.p;
+  L.num_neighs = c.num_neighs.p;
+  L.stride = c.neigh_kind == EMD_NEIGH_2D ? c.neigh_stride : 0;
+  return L;
+}
+
+static LJParams lj_params(Ctx& c) {
+  const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
+  return LJParams{c.lj_params.p, c.lj_params.p + nt2, c.lj_params.p + 2 * nt2, c.lj_ntypes};
+}
+
+}  // namespace emd
+
+using namespace emd;
+
+extern "C" {
+
+emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double* lj2, const double* cutsq,
+                       int half_neigh, int precision) {
+  EMD_API_BEGIN
+  require(ntypes >= 1 && lj1 && lj2 && cutsq, EMD_ERR_ARG, "emd_lj_init: bad parameter tables");
+  require(precision == EMD_PREC_FP64 || precision == EMD_PREC_MIXED, EMD_ERR_ARG, "emd_lj_init: precision");
+  require(!(precision == EMD_PREC_MIXED && half_neigh), EMD_ERR_ARG,
+          "emd_lj_init: the mixed-precision form uses the full list");
+  const size_t nt2 = size_t(ntypes) * ntypes;
+  std::vector<double> h(3 * nt2);
+  for (size_t k = 0; k < nt2; ++k) {
+    h[k] = lj1[k];
+    h[nt2 + k] = lj2[k];
+    h[2 * nt2 + k] = cutsq[k];
+  }
+  c.lj_params.reserve(3 * nt2, c.stream);
+  EMD_CUDA(cudaMemcpyAsync(c.lj_params.p, h.data(), sizeof(double) * 3 * nt2, cudaMemcpyHostToDevice, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  c.lj_ntypes = ntypes;
+  c.lj_half = half_neigh ? 1 : 0;
+  c.lj_prec = precision;
+  c.lj_ready = true;
+  c.neigh_ready = false;  // rows must be rebuilt in the format this form reads
+  if (precision == EMD_PREC_MIXED) lj_mixed_prepare(c);
+  EMD_API_END
+}
+
+emd_status emd_lj_compute(emd_ctx* ctx) {
+  EMD_API_BEGIN
+  require(c.lj_ready, EMD_ERR_STATE, "emd_lj_compute: emd_lj_init not called");
+  require(c.neigh_ready && c.neigh_rows == c.N_local, EMD_ERR_STATE, "emd_lj_compute: no current neighbour list");
+  require(c.half_neigh == c.lj_half, EMD_ERR_STATE, "emd_lj_compute: list fullness does not match the force");
+  const int n = c.N_local;
+  if (n == 0) return EMD_OK;
+  if (c.lj_prec == EMD_PREC_MIXED) {
+    require(c.neigh_packed, EMD_ERR_STATE, "emd_lj_compute: mixed form needs a list built after emd_lj_init");
+    lj_mixed_compute(c);
+    return EMD_OK;
+  }
+  require(!c.neigh_packed, EMD_ERR_STATE, "emd_lj_compute: list was built for the mixed form");
+  const ListView L = list_view(c);
+  const LJParams P = lj_params(c);
+  const bool two_d = c.neigh_kind == EMD_NEIGH_2D;
+  const int grid = blocks_for(n, 128);
+  TimedLaunch t(c, c.lj_half ? "lj_half_fp64" : "lj_full_fp64");
+  if (!c.lj_half) {
+    if (two_d) k_lj_full_fp64<true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    else k_lj_full_fp64<false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+  } else {
+    if (two_d) k_lj_half_fp64<true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    else k_lj_half_fp64<false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+  }
+  EMD_CHECK_LAUNCH();
+  EMD_API_END
+}
+
+emd_status emd_lj_energy(emd_ctx* ctx, double* pe) {
+  EMD_API_BEGIN
+  require(pe != nullptr, EMD_ERR_ARG, "emd_lj_energy: null output");
+  require(c.lj_ready && c.neigh_ready && c.neigh_rows == c.N_local, EMD_ERR_STATE, "emd_lj_energy: not ready");
+  const int n = c.N_local;
+  if (n == 0) {
+    *pe = 0.0;
+    return EMD_OK;
+  }
+  const int grid = blocks_for(n, 256);
+  c.red2.reserve(size_t(grid), c.stream);
+  const ListView L = list_view(c);
+  const LJParams P = lj_params(c);
+  {
+    TimedLaunch t(c, "lj_energy");
+    if (c.neigh_kind == EMD_NEIGH_2D)
+      k_lj_energy<true><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, c.red2.p);
+    else
+      k_lj_energy<false><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, c.red2.p);
+    EMD_CHECK_LAUNCH();
+  }
+  *pe = device_sum(c, c.red2.p, grid);
+  EMD_API_END
+}
+
+}  // extern "C"

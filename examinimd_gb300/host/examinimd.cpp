@@ -1,0 +1,321 @@
+// The ExaMiniMD driver re-hosted on the GB300 modules (examinimd.cpp:47-488):
+// the same init sequence, timestep loop, thermo lines, PERFORMANCE line,
+// --dumpbinary files and --correctness report.  Phase timers are CUDA events
+// on the context stream, so the four buckets measure device time without
+// adding host synchronisations to the loop.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+
+#include "emd_host.h"
+
+namespace emdhost {
+
+namespace {
+struct PhaseClock {
+  cudaStream_t s;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> marks[4];
+  std::vector<cudaEvent_t> pool;
+  explicit PhaseClock(void* stream) : s((cudaStream_t)stream) {}
+  ~PhaseClock() {
+    for (auto& v : marks)
+      for (auto& p : v) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+      }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+  cudaEvent_t ev() {
+    cudaEvent_t e;
+    if (!pool.empty()) {
+      e = pool.back();
+      pool.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  }
+  cudaEvent_t begin() {
+    cudaEvent_t e = ev();
+    cudaEventRecord(e, s);
+    return e;
+  }
+  void end(int bucket, cudaEvent_t a) {
+    cudaEvent_t b = ev();
+    cudaEventRecord(b, s);
+    marks[bucket].push_back({a, b});
+  }
+  double collect(int bucket) {
+    double t = 0;
+    for (auto& p : marks[bucket]) {
+      float ms = 0;
+      cudaEventSynchronize(p.second);
+      cudaEventElapsedTime(&ms, p.first, p.second);
+      t += ms * 1e-3;
+      pool.push_back(p.first);
+      pool.push_back(p.second);
+    }
+    marks[bucket].clear();
+    return t;
+  }
+};
+enum { B_FORCE = 0, B_NEIGH = 1, B_COMM = 2, B_OTHER = 3 };
+
+double wall() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+ExaMiniMD::ExaMiniMD() {
+  system = new System();
+  input = new Input(system);
+}
+
+ExaMiniMD::~ExaMiniMD() { shutdown(); }
+
+void ExaMiniMD::shutdown() {
+  delete integrator;
+  delete binning;
+  delete neighbor;
+  delete force;
+  delete comm;
+  integrator = nullptr;
+  binning = nullptr;
+  neighbor = nullptr;
+  force = nullptr;
+  comm = nullptr;
+  if (system && system->ctx) {
+    emd_destroy(system->ctx);
+    system->ctx = nullptr;
+  }
+  delete input;
+  delete system;
+  input = nullptr;
+  system = nullptr;
+}
+
+void ExaMiniMD::init(int argc, const char* const* argv) {
+  input->read_command_line_args(argc, argv);
+  check(emd_create(&system->ctx, input->device), nullptr, "emd_create (no usable CUDA device)");
+  input->read_file();
+  system->sync_params();
+
+  integrator = new IntegratorNVE_GB300(system);
+  binning = new BinningGB300(system);
+
+  const bool half_neigh = input->force_iteration_type == FORCE_ITER_NEIGH_HALF;
+  if (input->force_type == FORCE_LJ) force = new ForceLJNeigh_GB300(system, half_neigh, input->precision);
+  else force = new ForceSNAP_GB300(system, half_neigh, input->precision);
+  if (input->force_line < 0) throw HostError("Invalid ForceType: no pair_style line");
+  for (int line : input->force_coeff_lines) {
+    std::vector<char*> args;
+    for (auto& w : input->lines[size_t(line)]) args.push_back(const_cast<char*>(w.c_str()));
+    force->init_coeff(int(args.size()), args.data());
+  }
+
+  neighbor = new NeighborGB300(system, input->neighbor_type);
+  neighbor->init(input->force_cutoff + input->neighbor_skin);
+  comm = new CommSerial_GB300(system, input->force_cutoff + input->neighbor_skin);
+
+  force->comm_newton = input->comm_newton;
+  neighbor->comm_newton = input->comm_newton;
+
+  if (system->do_print && !input->quiet)
+    printf("Using: %s %s %s %s\n", force->name(), neighbor->name(), comm->name(), binning->name());
+
+  if (system->N == 0) input->create_lattice(comm);
+
+  comm->exchange();
+  const double neigh_cutoff = input->force_cutoff + input->neighbor_skin;
+  binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, false, true);
+  comm->exchange_halo();
+  binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, true, false);
+  neighbor->create_neigh_list(system, binning, force->half_neigh, false);
+
+  check(emd_zero_forces(system->ctx), system->ctx, "emd_zero_forces");
+  force->compute(system, binning, neighbor);
+  if (input->comm_newton) comm->update_force();
+
+  step_done = 0;
+  if (input->thermo_rate > 0) thermo(0, system->do_print, 0.0, 0.0);
+  if (input->dumpbinaryflag) dump_binary(0);
+  if (input->correctnessflag) check_correctness(0);
+}
+
+// Temperature / PotE / KinE (property_*.cpp) and the thermo line
+void ExaMiniMD::thermo(int step, bool print, double elapsed, double rate) {
+  double mv2 = 0.0;
+  check(emd_thermo_mv2(system->ctx, &mv2), system->ctx, "emd_thermo_mv2");
+  const int dof = 3 * system->N - 3;
+  last_T = mv2 * (system->mvv2e / (1.0 * dof * system->boltz));
+  last_PE = force->compute_energy(system, binning, neighbor) / system->N;
+  last_KE = mv2 * (0.5 * system->mvv2e) / system->N;
+  if (!print) return;
+  if (step == 0) {
+    printf("\n#Timestep Temperature PotE ETot Time Atomsteps/s\n");
+    printf("%i %lf %lf %lf %lf %e\n", step, last_T, last_PE, last_PE + last_KE, 0.0, 0.0);
+  } else {
+    printf("%i %lf %lf %lf %lf %e\n", step, last_T, last_PE, last_PE + last_KE, elapsed, rate);
+  }
+}
+
+void ExaMiniMD::run(int nsteps) {
+  const double neigh_cutoff = input->force_cutoff + input->neighbor_skin;
+  PhaseClock clk(emd_stream(system->ctx));
+  const double t0 = wall();
+  double last_time = 0.0;
+  for (int step = step_done + 1; step <= step_done + nsteps; step++) {
+    cudaEvent_t e = clk.begin();
+    integrator->initial_integrate();
+    clk.end(B_OTHER, e);
+
+    if (step % input->comm_exchange_rate == 0 && step > 0) {
+      e = clk.begin();
+      comm->exchange();
+      clk.end(B_COMM, e);
+      e = clk.begin();
+      binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, false, true);
+      clk.end(B_OTHER, e);
+      e = clk.begin();
+      comm->exchange_halo();
+      clk.end(B_COMM, e);
+      e = clk.begin();
+      binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, true, false);
+      neighbor->create_neigh_list(system, binning, force->half_neigh, false);
+      clk.end(B_NEIGH, e);
+    } else {
+      e = clk.begin();
+      comm->update_halo();
+      clk.end(B_COMM, e);
+    }
+
+    e = clk.begin();
+    check(emd_zero_forces(system->ctx), system->ctx, "emd_zero_forces");
+    force->compute(system, binning, neighbor);
+    clk.end(B_FORCE, e);
+
+    if (input->comm_newton) {
+      e = clk.begin();
+      comm->update_force();
+      clk.end(B_COMM, e);
+    }
+
+    e = clk.begin();
+    integrator->final_integrate();
+    clk.end(B_OTHER, e);
+
+    if (input->thermo_rate > 0 && step % input->thermo_rate == 0) {
+      check(emd_synchronize(system->ctx), system->ctx, "emd_synchronize");
+      const double now = wall() - t0;
+      thermo(step, system->do_print, now, 1.0 * system->N * input->thermo_rate / (now - last_time));
+      last_time = now;
+    }
+    if (input->dumpbinaryflag) dump_binary(step);
+    if (input->correctnessflag) check_correctness(step);
+  }
+  check(emd_synchronize(system->ctx), system->ctx, "emd_synchronize");
+  const double time = wall() - t0;
+  step_done += nsteps;
+  time_total += time;
+  const double tf = clk.collect(B_FORCE), tn = clk.collect(B_NEIGH), tc = clk.collect(B_COMM),
+               to = clk.collect(B_OTHER);
+  time_force += tf;
+  time_neigh += tn;
+  time_comm += tc;
+  time_other += to;
+  thermo(step_done, false, 0, 0);
+  if (system->do_print && !input->quiet && nsteps > 0) {
+    printf("\n#Procs Particles | Time T_Force T_Neigh T_Comm T_Other | Steps/s Atomsteps/s Atomsteps/(proc*s)\n");
+    printf("%i %i | %lf %lf %lf %lf %lf | %lf %e %e PERFORMANCE\n", comm->num_processes(), system->N, time, tf, tn, tc,
+           to, 1.0 * nsteps / time, 1.0 * system->N * nsteps / time,
+           1.0 * system->N * nsteps / time / comm->num_processes());
+  }
+}
+
+// --dumpbinary (examinimd.cpp:296-346): n, id[n], type[n], q[n], x[3n], v[3n], f[3n]
+void ExaMiniMD::dump_binary(int step) {
+  if (step % input->dumpbinary_rate) return;
+  char filename[4096];
+  snprintf(filename, sizeof(filename), "%s/output.%010d.%03d", input->dumpbinary_path.c_str(), step,
+           comm->process_rank());
+  FILE* fp = fopen(filename, "wb");
+  if (!fp) comm->error((std::string("Cannot open dump file ") + filename).c_str());
+  const int n = system->N_local;
+  std::vector<int> id(static_cast<size_t>(n)), type(static_cast<size_t>(n));
+  std::vector<double> q(static_cast<size_t>(n)), x(3 * size_t(n)), v(3 * size_t(n)), f(3 * size_t(n));
+  check(emd_system_get(system->ctx, 0, n, x.data(), v.data(), f.data(), type.data(), id.data(), q.data()), system->ctx,
+        "emd_system_get");
+  fwrite(&n, sizeof(int), 1, fp);
+  fwrite(id.data(), sizeof(int), size_t(n), fp);
+  fwrite(type.data(), sizeof(int), size_t(n), fp);
+  fwrite(q.data(), sizeof(double), size_t(n), fp);
+  fwrite(x.data(), sizeof(double), 3 * size_t(n), fp);
+  fwrite(v.data(), sizeof(double), 3 * size_t(n), fp);
+  fwrite(f.data(), sizeof(double), 3 * size_t(n), fp);
+  fclose(fp);
+}
+
+// --correctness (examinimd.cpp:355-482): same report, atoms matched by id
+// through a hash map instead of the reference's O(N^2) fallback search.
+void ExaMiniMD::check_correctness(int step) {
+  if (step % input->correctness_rate) return;
+  char filename[4096];
+  snprintf(filename, sizeof(filename), "%s/output.%010d.%03d", input->reference_path.c_str(), step,
+           comm->process_rank());
+  FILE* fp = fopen(filename, "rb");
+  if (!fp) comm->error((std::string("Cannot open input file ") + filename).c_str());
+  const int n = system->N_local;
+  int ntmp = 0;
+  if (fread(&ntmp, sizeof(int), 1, fp) != 1 || ntmp != n) {
+    fclose(fp);
+    comm->error("Mismatch in current and reference atom counts");
+  }
+  std::vector<int> idref(static_cast<size_t>(n)), typeref(static_cast<size_t>(n));
+  std::vector<double> qref(static_cast<size_t>(n)), xref(3 * size_t(n)), vref(3 * size_t(n)), fref(3 * size_t(n));
+  size_t ok = fread(idref.data(), sizeof(int), size_t(n), fp);
+  ok += fread(typeref.data(), sizeof(int), size_t(n), fp);
+  ok += fread(qref.data(), sizeof(double), size_t(n), fp);
+  ok += fread(xref.data(), sizeof(double), 3 * size_t(n), fp);
+  ok += fread(vref.data(), sizeof(double), 3 * size_t(n), fp);
+  ok += fread(fref.data(), sizeof(double), 3 * size_t(n), fp);
+  fclose(fp);
+  if (ok != 12 * size_t(n)) comm->error("Truncated reference dump");
+  std::vector<int> id(static_cast<size_t>(n));
+  std::vector<double> x(3 * size_t(n)), v(3 * size_t(n)), f(3 * size_t(n));
+  check(emd_system_get(system->ctx, 0, n, x.data(), v.data(), f.data(), nullptr, id.data(), nullptr), system->ctx,
+        "emd_system_get");
+  std::unordered_map<int, int> where;
+  where.reserve(size_t(n) * 2);
+  for (int i = 0; i < n; i++) where[id[size_t(i)]] = i;
+  double sr = 0, sv = 0, sf = 0, mr = 0, mv = 0, mf = 0;
+  for (int i = 0; i < n; i++) {
+    auto it = where.find(idref[size_t(i)]);
+    if (it == where.end()) {
+      printf("Unable to find current id matchinf reference id %d \n", idref[size_t(i)]);
+      continue;
+    }
+    const size_t a = 3 * size_t(it->second), b = 3 * size_t(i);
+    for (int d = 0; d < 3; d++) {
+      const double dr = x[a + d] - xref[b + d], dv = v[a + d] - vref[b + d], df = f[a + d] - fref[b + d];
+      sr += dr * dr;
+      sv += dv * dv;
+      sf += df * df;
+      mr = std::max(std::fabs(dr), mr);
+      mv = std::max(std::fabs(dv), mv);
+      mf = std::max(std::fabs(df), mf);
+    }
+  }
+  if (system->do_print) {
+    FILE* out = fopen(input->correctness_file.c_str(), step == 0 ? "w" : "a");
+    if (!out) comm->error("Cannot open correctness file");
+    if (step == 0) fprintf(out, "# timestep deltarnorm maxdelr deltavnorm maxdelv deltafnorm maxdelf\n");
+    fprintf(out, "%d %g %g %g %g %g %g\n", step, std::sqrt(sr), mr, std::sqrt(sv), mv, std::sqrt(sf), mf);
+    fclose(out);
+  }
+}
+
+}  // namespace emdhost

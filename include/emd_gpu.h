@@ -1,0 +1,179 @@
+/*
+ * emd_gpu.h -- C ABI of the GB300 (sm_103a) ExaMiniMD hot path.
+ *
+ * Every entry point replaces one virtual method of ExaMiniMD's module API
+ * (cited below as file:line inside the ExaMiniMD source tree).  The GB300
+ * module classes (BinningGB300, NeighborCSR_GB300, Neighbor2D_GB300,
+ * ForceLJNeigh_GB300, ForceSNAP_GB300, IntegratorNVE_GB300,
+ * CommSerial_GB300) are thin C++ shells over these calls.
+ *
+ * Conventions
+ *  - All device state (particle arrays, bins, neighbour lists, ghosts) is
+ *    owned by one emd_ctx; callers pass scalars, small parameter tables and
+ *    host arrays only.  Host particle arrays use ExaMiniMD's dump layout:
+ *    n rows of 3 doubles (x,y,z) row-major, int ids/types, double charges.
+ *  - Every call returns emd_status; nothing is thrown across the ABI.  Device
+ *    kernels never trap: overflow and out-of-range conditions latch a status
+ *    word that the host reads at the same synchronisation points ExaMiniMD
+ *    has (ghost count, neighbour total, 2D resize flag, thermo).
+ *  - All work of a context is ordered on one CUDA stream (emd_stream);
+ *    calls from one host thread per context.
+ *  - There is no CPU fallback: without a usable CUDA device emd_create
+ *    fails with EMD_ERR_CUDA.
+ */
+#ifndef EMD_GPU_H
+#define EMD_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct emd_ctx emd_ctx;
+
+typedef enum {
+  EMD_OK = 0,
+  EMD_ERR_OVERFLOW_GHOST = 1, /* ghost capacity exceeded (grown and retried internally) */
+  EMD_ERR_OVERFLOW_NEIGH = 2, /* neighbour capacity exceeded (grown and retried internally) */
+  EMD_ERR_TIMEOUT = 3,        /* a bounded device wait gave up */
+  EMD_ERR_BOUNDS = 4,         /* a device index check failed; the access was skipped */
+  EMD_ERR_CUDA = 5,           /* CUDA runtime error (see emd_last_error) */
+  EMD_ERR_ARG = 6,            /* invalid argument */
+  EMD_ERR_STATE = 7,          /* call out of order (e.g. force before neighbour list) */
+  EMD_ERR_NOMEM = 8           /* device allocation failed */
+} emd_status;
+
+enum { EMD_PREC_FP64 = 0, EMD_PREC_MIXED = 1 };
+enum { EMD_NEIGH_CSR = 0, EMD_NEIGH_2D = 1 };
+
+/* ------------------------------------------------------------ lifecycle */
+int emd_abi_version(void);
+/* Creates a context on CUDA device `device` with its own stream. */
+emd_status emd_create(emd_ctx** out, int device);
+void emd_destroy(emd_ctx* ctx);
+const char* emd_status_string(emd_status s);
+/* Text of the last error recorded on this context ("" if none). */
+const char* emd_last_error(const emd_ctx* ctx);
+/* The cudaStream_t (as void*) every kernel of this context is launched on. */
+void* emd_stream(emd_ctx* ctx);
+emd_status emd_synchronize(emd_ctx* ctx);
+/* Device status word: bitmask of (1u << emd_status) latched by kernels. */
+emd_status emd_get_status(emd_ctx* ctx, unsigned* flags);
+
+/* --------------------------------------------------------------- System
+ * System::init / grow / units / domain (system.h:57-143, system.cpp:71-109,
+ * Comm::create_domain_decomposition comm.cpp:58-65). */
+emd_status emd_system_init(emd_ctx* ctx, int ntypes, const double* mass, double boltz, double mvv2e,
+                           double dt, const double domain[3], const double sub_lo[3],
+                           const double sub_hi[3]);
+/* System::grow (system.cpp:95-109): capacity for n_max owned+ghost rows. */
+emd_status emd_system_grow(emd_ctx* ctx, int n_max);
+/* Replaces the owned particles (N_local = n_local, N_ghost = 0).  Any of v,
+ * f, q may be NULL (zero); x, type, id are required. */
+emd_status emd_system_set_local(emd_ctx* ctx, int n_local, const double* x, const double* v,
+                                const double* f, const int* type, const int* id, const double* q);
+/* Overwrites rows [first, first+count) of the owned particles in place
+ * (positions, velocities, forces; NULL = leave unchanged). */
+emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x, const double* v,
+                             const double* f);
+/* Copies rows [first, first+count) (owned and ghost) to the host; any NULL
+ * output is skipped. */
+emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double* v, double* f,
+                          int* type, int* id, double* q);
+emd_status emd_system_info(emd_ctx* ctx, int* n_local, int* n_ghost, int* n_max);
+/* Kokkos::deep_copy(system->f, 0.0) over all N_max rows (examinimd.cpp:232). */
+emd_status emd_zero_forces(emd_ctx* ctx);
+
+/* ---------------------------------------------------- Integrator NVE
+ * IntegratorNVE::initial_integrate / final_integrate
+ * (integrator_nve.cpp:41-44, 64-83, 105-121): dtv = dt, dtf = 0.5*dt/mvv2e. */
+emd_status emd_nve_initial(emd_ctx* ctx);
+emd_status emd_nve_final(emd_ctx* ctx);
+
+/* ------------------------------------------------------- CommSerial
+ * CommSerial (comm_serial.h:95-213, comm_serial.cpp:41-127). */
+emd_status emd_comm_init(emd_ctx* ctx, double comm_depth);
+/* exchange(): periodic wrap of owned atoms (comm_serial.cpp:47-53). */
+emd_status emd_comm_exchange(emd_ctx* ctx);
+/* exchange_halo(): six-phase ghost creation (comm_serial.cpp:55-97);
+ * ghosts are appended in the serial order of the reference.  Writes the
+ * resulting N_ghost (host) if n_ghost_out is non-NULL. */
+emd_status emd_comm_exchange_halo(emd_ctx* ctx, int* n_ghost_out);
+/* update_halo(): ghost positions from their owners (comm_serial.cpp:99-110). */
+emd_status emd_comm_update_halo(emd_ctx* ctx);
+/* update_force(): ghost forces added to owners, phases 5..0 (comm_serial.cpp:112-127). */
+emd_status emd_comm_update_force(emd_ctx* ctx);
+/* Per-phase ghost counts and pack lists (pack may be NULL): pack_indices is
+ * 6 consecutive runs of num_ghost[p] source indices. */
+emd_status emd_comm_get_ghosts(emd_ctx* ctx, int num_ghost[6], int* pack_indices);
+
+/* --------------------------------------------------------- Binning
+ * BinningKKSort::create_binning (binning_kksort.cpp:71-140).  nbin_out
+ * receives nbinx,nbiny,nbinz including the halo layers. */
+emd_status emd_binning_create(emd_ctx* ctx, double dx, double dy, double dz, int halo_depth,
+                              int do_local, int do_ghost, int sort, int nbin_out[3]);
+/* Copies bincount / binoffsets (nbinx*nbiny*nbinz, x slowest), the
+ * permutation (length of the binned range) and min/max bounds (6 doubles). */
+emd_status emd_binning_get(emd_ctx* ctx, int* bincount, int* binoffsets, int* permute,
+                           double bounds[6]);
+
+/* -------------------------------------------------------- Neighbor
+ * NeighborCSR / Neighbor2D (neighbor_csr.h:176-435, neighbor_2d.h:175-331).
+ * kind: EMD_NEIGH_CSR or EMD_NEIGH_2D. */
+emd_status emd_neigh_init(emd_ctx* ctx, int kind, double neigh_cut, int comm_newton);
+/* create_neigh_list(system, binning, half_neigh, ghost_neighs=false).
+ * total_out (host, may be NULL): number of entries (CSR) or sum of row
+ * lengths (2D). */
+emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out);
+/* Row lengths (N_local) and entries row by row (total) in list order. */
+emd_status emd_neigh_get(emd_ctx* ctx, int* num_neighs, int* entries);
+/* 2D list stride (maxneighs); 0 for CSR. */
+emd_status emd_neigh_maxneighs(emd_ctx* ctx, int* maxneighs);
+
+/* ------------------------------------------------------- Force LJ
+ * ForceLJNeigh (force_lj_neigh_impl.h:57-343).  Per-type tables are
+ * ntypes*ntypes row-major: lj1 = 48 eps sigma^12, lj2 = 24 eps sigma^6,
+ * cutsq = cut^2.  precision: EMD_PREC_FP64 (bit-compatible drop-in) or
+ * EMD_PREC_MIXED (FP32 pair math, FP64 displacements and accumulation). */
+emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double* lj2,
+                       const double* cutsq, int half_neigh, int precision);
+/* compute(): f += pair forces over the current neighbour list. */
+emd_status emd_lj_compute(emd_ctx* ctx);
+/* compute_energy(): shifted LJ potential energy (force_lj_neigh_impl.h:129-156, 259-343). */
+emd_status emd_lj_energy(emd_ctx* ctx, double* pe);
+
+/* ----------------------------------------------------- Force SNAP
+ * ForceSNAP::init_coeff / compute (force_snap_neigh_impl.h:160-336,
+ * 591-724) and SNA (sna_impl.hpp).  beta: nelem x ncoeffall row-major
+ * (ncoeffall = ncoeff+1, beta[.,0] the constant term); map[type] = element
+ * index (ntypes entries, 0-based types).  switchflag as in the .snapparam. */
+emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, int switchflag,
+                         double rcutfac, int nelem, const double* radelem, const double* wjelem,
+                         const double* beta, int ncoeffall, int ntypes, const int* map,
+                         int precision);
+/* compute(): f += SNAP forces (owner and ghost rows; update_force follows). */
+emd_status emd_snap_compute(emd_ctx* ctx);
+/* SNAP energy sum_i (beta_0 + sum_k beta_k B_k^i) plus the 1.25e5/r^12 term
+ * per ordered pair that integrates the reference's extra repulsion.
+ * ExaMiniMD has no SNAP energy (force.h:54); this is an extension. */
+emd_status emd_snap_energy(emd_ctx* ctx, double* pe);
+/* Number of bispectrum components (55 at twojmax 8). */
+emd_status emd_snap_ncoeff(emd_ctx* ctx, int* ncoeff);
+
+/* ------------------------------------------------------ Properties
+ * Temperature / KinE (property_temperature.cpp:43-62, property_kine.cpp:43-61):
+ * sum over owned atoms of m v^2. */
+emd_status emd_thermo_mv2(emd_ctx* ctx, double* sum_mv2);
+
+/* --------------------------------------------------- Kernel timing
+ * When enabled, every kernel launch of the context is bracketed by CUDA
+ * events on the context stream; totals are per kernel name. */
+emd_status emd_timing_enable(emd_ctx* ctx, int on);
+emd_status emd_timing_reset(emd_ctx* ctx);
+/* Writes "name ms launches\n" lines into buf (truncated to len). */
+emd_status emd_timing_report(emd_ctx* ctx, char* buf, int len);
+emd_status emd_timing_get(emd_ctx* ctx, const char* kernel, double* ms_total, long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EMD_GPU_H */

@@ -1,0 +1,114 @@
+"""Decks of the golden cases (LAMMPS subset read by ExaMiniMD and emd_gb300).
+
+Shared by make_golden.py (which runs ExaMiniMD on them) and the parity tests
+(which run the GB300 driver on the same decks).  SNAP cases need a
+.snapcoeff / .snapparam pair: make_golden.py parses the W files that ship with
+ExaMiniMD into numbers (element, radius, weight, coefficients, parameters) and
+stores them in the fixture; write_snap_files() writes a plain pair back from
+those numbers for either program.
+"""
+from __future__ import annotations
+
+import os
+
+LJ = """units lj
+atom_style atomic
+newton {newton}
+lattice fcc 0.8442
+region box block 0 {n} 0 {n} 0 {n}
+create_box 1 box
+create_atoms 1 box
+mass 1 {mass}
+velocity all create {temp} 87287 loop geom
+pair_style lj/cut 2.5
+pair_coeff 1 1 1.0 1.0 2.5
+neighbor 0.3 bin
+neigh_modify delay 0 every {every} check no
+fix 1 all nve
+thermo {thermo}
+run {steps}
+"""
+
+SNAP = """units metal
+newton on
+lattice sc {a}
+region box block 0 {nx} 0 {ny} 0 {nz}
+create_box 1 box
+create_atoms 1 box
+mass 1 {mass}
+pair_style snap
+pair_coeff * * {coeff} {elem} {param} {elem}
+thermo {thermo}
+neighbor 1.0 bin
+neigh_modify once no every {every} delay 0 check yes
+velocity all create 300.0 4928459 loop geom
+fix 1 all nve
+run {steps}
+"""
+
+CASES = {
+    # LJ, full CSR list, newton off (the configuration BASELINE names)
+    "lj_fcc6_full_csr": dict(kind="lj", n=6, mass=1.0, temp=1.44, newton="off", every=20, thermo=10, steps=100,
+                             args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL", "--comm-type", "SERIAL"],
+                             dump_every=1, keep_steps=[0, 20, 21, 100]),
+    # LJ, full 2D list (ExaMiniMD's default neighbour module), mass 2 as in.lj
+    "lj_fcc4_full_2d": dict(kind="lj", n=4, mass=2.0, temp=1.4, newton="off", every=20, thermo=10, steps=40,
+                            args=["--neigh-type", "2D", "--comm-type", "SERIAL"],
+                            dump_every=20, keep_steps=[0, 20, 40]),
+    # LJ, half CSR list with newton off (ghost pairs kept in both directions)
+    "lj_fcc4_half_csr": dict(kind="lj", n=4, mass=1.0, temp=1.44, newton="off", every=10, thermo=10, steps=30,
+                             args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_HALF", "--comm-type", "SERIAL"],
+                             dump_every=10, keep_steps=[0, 10, 30]),
+    # LJ, half 2D list with newton on (exercises CommSerial::update_force)
+    "lj_fcc4_half_2d_newton": dict(kind="lj", n=4, mass=1.0, temp=1.44, newton="on", every=10, thermo=10, steps=30,
+                                   args=["--neigh-type", "2D", "--force-iteration", "NEIGH_HALF",
+                                         "--comm-type", "SERIAL"],
+                                   dump_every=10, keep_steps=[0, 10, 30]),
+    # SNAP W, the shipped in.snap.W geometry (sc 4x8x8 = 256 atoms)
+    "snap_W_sc": dict(kind="snap", a=3.1803, nx=4, ny=8, nz=8, mass=183.84, elem="W", every=1, thermo=5, steps=5,
+                      coeff="W.snapcoeff", param="W.snapparam",
+                      args=["--neigh-type", "CSR", "--comm-type", "SERIAL"], dump_every=5, keep_steps=[0, 5]),
+}
+
+
+def deck_text(case: dict) -> str:
+    if case["kind"] == "lj":
+        return LJ.format(**case)
+    return SNAP.format(**case)
+
+
+def write_snap_files(work: str, case: dict, snap: dict) -> None:
+    """snap: elem, radius, weight, beta (ncoeffall floats), params {key: value}."""
+    with open(os.path.join(work, case["coeff"]), "w") as fp:
+        fp.write(f"1 {len(snap['beta'])}\n{snap['elem']} {snap['radius']!r} {snap['weight']!r}\n")
+        for b in snap["beta"]:
+            fp.write(f"{float(b)!r}\n")
+    with open(os.path.join(work, case["param"]), "w") as fp:
+        for k, v in snap["params"].items():
+            fp.write(f"{k} {v}\n")
+
+
+def read_snap_files(coeff_path: str, param_path: str) -> dict:
+    """Parses a one-element .snapcoeff and a .snapparam into numbers."""
+    lines = [ln.split("#")[0].split() for ln in open(coeff_path)]
+    lines = [ln for ln in lines if ln]
+    ncoeff = int(lines[0][1])
+    elem, radius, weight = lines[1][0], float(lines[1][1]), float(lines[1][2])
+    beta = [float(ln[0]) for ln in lines[2:2 + ncoeff]]
+    params = {}
+    for ln in open(param_path):
+        if "#" in ln or not ln.strip():
+            continue
+        k, v = ln.split()[:2]
+        params[k] = v
+    return dict(elem=elem, radius=radius, weight=weight, beta=beta, params=params)
+
+
+def write_case(case: dict, work: str, snap: dict | None = None) -> tuple[str, list[str]]:
+    """Writes the deck (and SNAP files from `snap`) into work/; returns (deck path, args)."""
+    deck = os.path.join(work, "in.deck")
+    with open(deck, "w") as fp:
+        fp.write(deck_text(case))
+    if case["kind"] == "snap":
+        write_snap_files(work, case, snap)
+    return deck, list(case["args"])

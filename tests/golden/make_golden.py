@@ -1,0 +1,132 @@
+"""Regenerates the golden fixtures in tests/golden/ from ExaMiniMD itself.
+
+Requires the ExaMiniMD source tree (default /root/reference) and builds it
+against the serial Kokkos shim (oracle/Makefile.ref).  For every case it runs
+
+  * ref_examinimd -il DECK ... --dumpbinary EVERY DIR  (the reference's own
+    binary dumps: id, type, q, x, v, f of the owned atoms), and
+  * ref_probe OUT DECK ...  (the reference's binning, ghosts, neighbour rows
+    and initial forces right after ExaMiniMD::init),
+
+and stores the selected steps plus the thermo lines in CASE.npz.
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import re
+import shutil
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from tests.golden.decks import CASES, read_snap_files, write_case  # noqa: E402
+
+
+def read_probe(path: str) -> dict:
+    out = {}
+    with open(path, "rb") as fp:
+        while True:
+            head = fp.read(32)
+            if len(head) < 32:
+                break
+            name = head.split(b"\0")[0].decode()
+            t = fp.read(1).decode()
+            (n,) = struct.unpack("q", fp.read(8))
+            dt = np.int32 if t == "i" else np.float64
+            out[name] = np.frombuffer(fp.read(n * np.dtype(dt).itemsize), dtype=dt).copy()
+    return out
+
+
+def read_dump(path: str) -> dict:
+    with open(path, "rb") as fp:
+        (n,) = struct.unpack("i", fp.read(4))
+        idv = np.frombuffer(fp.read(4 * n), np.int32).copy()
+        typ = np.frombuffer(fp.read(4 * n), np.int32).copy()
+        q = np.frombuffer(fp.read(8 * n), np.float64).copy()
+        x = np.frombuffer(fp.read(24 * n), np.float64).reshape(n, 3).copy()
+        v = np.frombuffer(fp.read(24 * n), np.float64).reshape(n, 3).copy()
+        f = np.frombuffer(fp.read(24 * n), np.float64).reshape(n, 3).copy()
+    return dict(id=idv, type=typ, q=q, x=x, v=v, f=f)
+
+
+def parse_thermo(stdout: str) -> np.ndarray:
+    rows = []
+    on = False
+    for line in stdout.splitlines():
+        if line.startswith("#Timestep"):
+            on = True
+            continue
+        if on:
+            m = re.match(r"^(\d+) (\S+) (\S+) (\S+) ", line)
+            if m:
+                rows.append([float(m.group(i)) for i in range(1, 5)])
+            elif line.strip() == "":
+                if rows:
+                    break
+    return np.array(rows)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    sys.path.insert(0, ROOT)
+    from oracle.build import build_reference  # noqa: E402
+
+    exe = build_reference(a.ref)
+    if exe is None:
+        sys.exit(f"ExaMiniMD sources not found under {a.ref}")
+    probe = os.path.join(os.path.dirname(exe), "ref_probe")
+    for name, case in CASES.items():
+        if a.only and name != a.only:
+            continue
+        work = tempfile.mkdtemp(prefix="golden_")
+        try:
+            snap = None
+            if case["kind"] == "snap":
+                sd = os.path.join(a.ref, "input", "snap")
+                snap = read_snap_files(os.path.join(sd, case["coeff"]), os.path.join(sd, case["param"]))
+            deck, args = write_case(case, work, snap)
+            dump_dir = os.path.join(work, "dump")
+            os.makedirs(dump_dir)
+            r = subprocess.run([exe, "-il", deck] + args + ["--dumpbinary", str(case["dump_every"]), dump_dir],
+                               cwd=work, capture_output=True, text=True, check=True)
+            thermo = parse_thermo(r.stdout)
+            pr = os.path.join(work, "probe.bin")
+            subprocess.run([probe, pr, "-il", deck] + args, cwd=work, capture_output=True, text=True, check=True)
+            P = read_probe(pr)
+            data = {f"probe_{k}": v for k, v in P.items()}
+            data["thermo"] = thermo
+            for step in case["keep_steps"]:
+                d = read_dump(os.path.join(dump_dir, f"output.{step:010d}.000"))
+                for k, v in d.items():
+                    data[f"s{step}_{k}"] = v
+            data["keep_steps"] = np.array(case["keep_steps"], np.int32)
+            if snap is not None:
+                data["snap_elem"] = np.array(snap["elem"])
+                data["snap_radius"] = np.array(snap["radius"])
+                data["snap_weight"] = np.array(snap["weight"])
+                data["snap_beta"] = np.array(snap["beta"])
+                data["snap_param_keys"] = np.array(list(snap["params"].keys()))
+                data["snap_param_vals"] = np.array(list(snap["params"].values()))
+            out = os.path.join(HERE, f"{name}.npz")
+            np.savez_compressed(out, **data)
+            print(f"{name}: {os.path.getsize(out) / 1024:.1f} KiB, N={len(data['s0_id'])}, "
+                  f"ghosts={P['counts'][1]}, thermo rows={len(thermo)}")
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    main()

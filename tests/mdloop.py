@@ -1,0 +1,169 @@
+"""ExaMiniMD's init + timestep sequence (examinimd.cpp:60-276) over a backend.
+
+A backend is anything with the Context method set: the GB300 library
+(examinimd_gb300.Context) or the CPU oracle (oracle.orc.Oracle).  Tests run
+the same sequence on both and compare the state between calls.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+class Setup:
+    """Deck parameters common to LJ and SNAP runs."""
+    lattice_style = 1  # 0 sc, 1 fcc, 2 bcc
+    boltz, mvv2e = 1.0, 1.0
+
+    def __init__(self, n, mass, temp, seed, cut, skin, every, newton, half, kind, a, dt, ny=None, nz=None):
+        self.nx, self.ny, self.nz = n, (ny or n), (nz or n)
+        self.mass, self.temp, self.seed = mass, temp, seed
+        self.cut, self.skin, self.every = cut, skin, every
+        self.newton, self.half, self.kind = newton, half, kind
+        self.a, self.dt = a, dt
+        self.neigh_cut = cut + skin
+
+    @property
+    def domain(self):
+        return [self.a * self.nx, self.a * self.ny, self.a * self.nz]
+
+    def force_init(self, b, precision=0):
+        raise NotImplementedError
+
+    def force_compute(self, b):
+        raise NotImplementedError
+
+    def energy(self, b):
+        raise NotImplementedError
+
+
+class LJSetup(Setup):
+    """fcc LJ deck (in.lj style; lattice constant (4/rho)^(1/3), input.cpp:311-323)."""
+
+    def __init__(self, n, mass=1.0, temp=1.44, seed=87287, cut=2.5, skin=0.3, every=20, newton=False, half=False,
+                 kind=0, rho=0.8442, dt=0.005):
+        super().__init__(n, mass, temp, seed, cut, skin, every, newton, half, kind, math.pow(4.0 / rho, 1.0 / 3.0), dt)
+        self.lj1 = np.array([48.0 * 1.0 * math.pow(1.0, 12.0)])
+        self.lj2 = np.array([24.0 * 1.0 * math.pow(1.0, 6.0)])
+        self.cutsq = np.array([cut * cut])
+
+    def force_init(self, b, precision=0):
+        b.lj_init(self.lj1, self.lj2, self.cutsq, half=self.half, precision=precision)
+
+    def force_compute(self, b):
+        b.lj_compute()
+
+    def energy(self, b):
+        return b.lj_energy()
+
+
+class SnapSetup(Setup):
+    """SNAP deck in metal units (in.snap.W style); sc by default, bcc optional."""
+    boltz, mvv2e = 8.617343e-5, 1.0364269e-4
+
+    def __init__(self, nx, ny, nz, snap: dict, a=3.1803, mass=183.84, temp=300.0, seed=4928459, skin=1.0, every=1,
+                 lattice_style=0, dt=0.001):
+        super().__init__(nx, mass, temp, seed, 4.73442, skin, every, True, False, 0, a, dt, ny, nz)
+        self.lattice_style = lattice_style
+        self.snap = snap
+        p = snap["params"]
+        self.twojmax = int(p["twojmax"])
+        self.rcutfac = float(p["rcutfac"])
+        self.rfac0 = float(p.get("rfac0", 0.99363))
+        self.rmin0 = float(p.get("rmin0", 0.0))
+        self.switchflag = int(p.get("switchflag", 1))
+
+    def force_init(self, b, precision=0):
+        b.snap_init(self.twojmax, self.rfac0, self.rmin0, self.switchflag, self.rcutfac, [self.snap["radius"]],
+                    [self.snap["weight"]], np.asarray(self.snap["beta"], float)[None, :], [0], precision=precision)
+
+    def force_compute(self, b):
+        b.snap_compute()
+
+    def energy(self, b):
+        return b.snap_energy()
+
+
+def make_lattice(setup: Setup, threads=1):
+    """Initial owned particles from the oracle's Input::create_lattice restatement."""
+    from oracle.orc import Oracle
+    o = Oracle(threads)
+    o.system_init([setup.mass], setup.boltz, setup.mvv2e, setup.dt, setup.domain)
+    o.create_lattice(setup.lattice_style, setup.a, setup.nx, setup.ny, setup.nz, setup.temp, setup.seed)
+    return o.get()
+
+
+def init(b, setup: Setup, state: dict, precision=0):
+    """ExaMiniMD::init from the lattice on (examinimd.cpp:120-144)."""
+    b.system_init([setup.mass], setup.boltz, setup.mvv2e, setup.dt, setup.domain)
+    b.set_local(state["x"], state["type"], state["id"], v=state["v"], q=state.get("q"))
+    setup.force_init(b, precision)
+    b.comm_init(setup.neigh_cut)
+    b.neigh_init(setup.kind, setup.neigh_cut, setup.newton)
+    c = setup.neigh_cut
+    b.comm_exchange()
+    b.binning_create(c, c, c, 1, True, False, True)
+    b.comm_exchange_halo()
+    b.binning_create(c, c, c, 1, True, True, False)
+    total = b.neigh_create(setup.half)
+    b.zero_forces()
+    setup.force_compute(b)
+    if setup.newton:
+        b.comm_update_force()
+    return total
+
+
+def step(b, setup: Setup, step_no: int):
+    """One pass of the ExaMiniMD::run loop body (examinimd.cpp:192-276)."""
+    c = setup.neigh_cut
+    b.nve_initial()
+    if step_no % setup.every == 0:
+        b.comm_exchange()
+        b.binning_create(c, c, c, 1, True, False, True)
+        b.comm_exchange_halo()
+        b.binning_create(c, c, c, 1, True, True, False)
+        b.neigh_create(setup.half)
+    else:
+        b.comm_update_halo()
+    b.zero_forces()
+    setup.force_compute(b)
+    if setup.newton:
+        b.comm_update_force()
+    b.nve_final()
+
+
+def thermo(b, setup: Setup, natoms: int):
+    """T, PE/N, ETot/N as printed by ExaMiniMD (examinimd.cpp:252-267)."""
+    mv2 = b.thermo_mv2()
+    T = mv2 * (setup.mvv2e / (1.0 * (3 * natoms - 3) * setup.boltz))
+    pe = setup.energy(b) / natoms
+    ke = mv2 * (0.5 * setup.mvv2e) / natoms
+    return T, pe, pe + ke
+
+
+def by_id(state: dict) -> dict:
+    """Rows sorted by atom id (the correctness check's matching, examinimd.cpp:397-408)."""
+    order = np.argsort(state["id"], kind="stable")
+    return {k: v[order] for k, v in state.items()}
+
+
+def rows(num, ent):
+    off = np.concatenate([[0], np.cumsum(num)])
+    return [ent[off[i]:off[i + 1]] for i in range(len(num))]
+
+
+def golden_snap(g) -> dict:
+    """SNAP file numbers stored in a golden fixture."""
+    return dict(elem=str(g["snap_elem"]), radius=float(g["snap_radius"]), weight=float(g["snap_weight"]),
+                beta=list(g["snap_beta"]), params=dict(zip([str(k) for k in g["snap_param_keys"]],
+                                                           [str(v) for v in g["snap_param_vals"]])))
+
+
+def setup_for_case(name: str, case: dict, g=None) -> Setup:
+    if case["kind"] == "lj":
+        return LJSetup(case["n"], mass=case["mass"], temp=case["temp"], every=case["every"],
+                       newton=case["newton"] == "on", half="NEIGH_HALF" in case["args"],
+                       kind=1 if "2D" in case["args"] else 0)
+    return SnapSetup(case["nx"], case["ny"], case["nz"], golden_snap(g), a=case["a"], mass=case["mass"],
+                     every=case["every"])
