@@ -17,8 +17,9 @@ namespace {
 
 __global__ void __launch_bounds__(256) k_bin_index(const double4_32a* __restrict__ x4, int first, int n, int nbx,
                                                    int nby, int nbz, double minx, double miny, double minz,
-                                                   double mulx, double muly, double mulz, int* __restrict__ binof,
-                                                   int* __restrict__ bincount, unsigned* status) {
+                                                   double mulx, double muly, double mulz, double wx, double wy,
+                                                   double wz, int* __restrict__ binof, int* __restrict__ bincount,
+                                                   float4* __restrict__ xl, unsigned* status) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const double4_32a p = x4[first + r];
@@ -36,6 +37,9 @@ __global__ void __launch_bounds__(256) k_bin_index(const double4_32a* __restrict
   const int b = (ix * nby + iy) * nbz + iz;
   binof[r] = b;
   atomicAdd(&bincount[b], 1);
+  // FP32 position relative to the bin centre, for the neighbour candidate tests
+  xl[first + r] = make_float4(float(p.x - (minx + (ix + 0.5) * wx)), float(p.y - (miny + (iy + 0.5) * wy)),
+                              float(p.z - (minz + (iz + 0.5) * wz)), p.w);
 }
 
 __global__ void __launch_bounds__(256) k_bin_scatter(const int* __restrict__ binof, int n,
@@ -66,19 +70,25 @@ __global__ void __launch_bounds__(256) k_bin_rank(const int* __restrict__ bincou
   }
 }
 
-template <class T>
-__global__ void k_gather(const T* __restrict__ src, T* __restrict__ dst, const int* __restrict__ perm, int n) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < n) dst[r] = src[perm[r]];
-}
-__global__ void k_gather3(const double* __restrict__ src, double* __restrict__ dst, const int* __restrict__ perm,
-                          int n) {
+// BinSort::sort of every particle field at once: dst(r) = src(perm(r))
+__global__ void __launch_bounds__(256) k_sort_gather(const int* __restrict__ perm, int n,
+                                                     const double4_32a* __restrict__ x4, const double* __restrict__ v,
+                                                     const double* __restrict__ f, const double* __restrict__ q,
+                                                     const int* __restrict__ type, const int* __restrict__ id,
+                                                     double4_32a* __restrict__ ox4, double* __restrict__ ov,
+                                                     double* __restrict__ of, double* __restrict__ oq,
+                                                     int* __restrict__ otype, int* __restrict__ oid) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const int s = perm[r];
-  dst[3 * r] = src[3 * s];
-  dst[3 * r + 1] = src[3 * s + 1];
-  dst[3 * r + 2] = src[3 * s + 2];
+  ox4[r] = x4[s];
+  for (int d = 0; d < 3; ++d) {
+    ov[3 * r + d] = v[3 * s + d];
+    of[3 * r + d] = f[3 * s + d];
+  }
+  oq[r] = q[s];
+  otype[r] = type[s];
+  oid[r] = id[s];
 }
 
 }  // namespace
@@ -124,11 +134,13 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
   c.perm_tmp.reserve(size_t(n) + 1, c.stream);
   EMD_CUDA(cudaMemsetAsync(c.bincount.p, 0, sizeof(int) * nbins, c.stream));
   EMD_CUDA(cudaMemsetAsync(c.bin_cursor.p, 0, sizeof(int) * nbins, c.stream));
+  c.xl_bin.reserve(size_t(first + n) + 1, c.stream, true);
   if (n > 0) {
     TimedLaunch t(c, "bin_index");
-    k_bin_index<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p, first, n, nb[0], nb[1], nb[2], c.bmin[0],
-                                                          c.bmin[1], c.bmin[2], c.bmul[0], c.bmul[1], c.bmul[2],
-                                                          c.binof.p, c.bincount.p, c.d_status);
+    k_bin_index<<<blocks_for(n, 256), 256, 0, c.stream>>>(
+        c.x4.p, first, n, nb[0], nb[1], nb[2], c.bmin[0], c.bmin[1], c.bmin[2], c.bmul[0], c.bmul[1], c.bmul[2],
+        (c.bmax[0] - c.bmin[0]) / nb[0], (c.bmax[1] - c.bmin[1]) / nb[1], (c.bmax[2] - c.bmin[2]) / nb[2], c.binof.p,
+        c.bincount.p, c.xl_bin.p, c.d_status);
     EMD_CHECK_LAUNCH();
   }
   exclusive_scan_int(c, c.bincount.p, c.binoffsets.p, nbins, nullptr);
@@ -147,26 +159,29 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
     }
   }
   if (sort && n > 0) {
-    // BinSort::sort of x, v, f, type, id, q over the binned range
-    TimedLaunch t(c, "bin_sort_gather");
+    // BinSort::sort of x, v, f, type, id, q over the binned range: one
+    // fused gather kernel into staging buffers, then copies back
     const int* perm = c.permute.p;
     c.stage_x4.reserve(size_t(n), c.stream);
-    k_gather<double4_32a><<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p + first, c.stage_x4.p, perm, n);
+    c.stage_d.reserve(7 * size_t(n), c.stream);
+    c.stage_i.reserve(2 * size_t(n), c.stream);
+    {
+      TimedLaunch t(c, "bin_sort_gather");
+      k_sort_gather<<<blocks_for(n, 256), 256, 0, c.stream>>>(
+          perm, n, c.x4.p + first, c.v.p + 3 * size_t(first), c.f.p + 3 * size_t(first), c.q.p + first,
+          c.type.p + first, c.id.p + first, c.stage_x4.p, c.stage_d.p, c.stage_d.p + 3 * size_t(n),
+          c.stage_d.p + 6 * size_t(n), c.stage_i.p, c.stage_i.p + n);
+      EMD_CHECK_LAUNCH();
+    }
     EMD_CUDA(cudaMemcpyAsync(c.x4.p + first, c.stage_x4.p, sizeof(double4_32a) * n, cudaMemcpyDeviceToDevice, c.stream));
-    c.stage_d.reserve(3 * size_t(n), c.stream);
-    for (DevBuf<double>* b : {&c.v, &c.f}) {
-      k_gather3<<<blocks_for(n, 256), 256, 0, c.stream>>>(b->p + 3 * size_t(first), c.stage_d.p, perm, n);
-      EMD_CUDA(cudaMemcpyAsync(b->p + 3 * size_t(first), c.stage_d.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice,
-                               c.stream));
-    }
-    k_gather<double><<<blocks_for(n, 256), 256, 0, c.stream>>>(c.q.p + first, c.stage_d.p, perm, n);
-    EMD_CUDA(cudaMemcpyAsync(c.q.p + first, c.stage_d.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
-    c.stage_i.reserve(size_t(n), c.stream);
-    for (DevBuf<int>* b : {&c.type, &c.id}) {
-      k_gather<int><<<blocks_for(n, 256), 256, 0, c.stream>>>(b->p + first, c.stage_i.p, perm, n);
-      EMD_CUDA(cudaMemcpyAsync(b->p + first, c.stage_i.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, c.stream));
-    }
-    EMD_CHECK_LAUNCH();
+    EMD_CUDA(cudaMemcpyAsync(c.v.p + 3 * size_t(first), c.stage_d.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice,
+                             c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.f.p + 3 * size_t(first), c.stage_d.p + 3 * size_t(n), sizeof(double) * 3 * n,
+                             cudaMemcpyDeviceToDevice, c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.q.p + first, c.stage_d.p + 6 * size_t(n), sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                             c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.type.p + first, c.stage_i.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.id.p + first, c.stage_i.p + n, sizeof(int) * n, cudaMemcpyDeviceToDevice, c.stream));
     c.neigh_ready = false;
   }
   c.binning_ready = true;

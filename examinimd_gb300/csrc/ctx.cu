@@ -153,6 +153,7 @@ void exclusive_scan_int(Ctx& c, const int* d_in, int* d_out, int n, int* d_total
     EMD_CUDA(cudaMemcpyAsync(c.scan_aux.p, d_in + n - 1, sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
   scan_rec(c, d_in, d_out, n, 0);
   if (d_total) {
+    TimedLaunch t(c, "scan_total");
     k_scan_total<<<1, 32, 0, c.stream>>>(c.scan_aux.p, d_out + n - 1, 1, d_total);
     EMD_CHECK_LAUNCH();
   }
@@ -165,8 +166,11 @@ double device_sum(Ctx& c, const double* d_vals, int n) {
     k_sum_partial<<<SUM_BLOCKS, SUM_THREADS, 0, c.stream>>>(d_vals, n, c.red.p);
     EMD_CHECK_LAUNCH();
   }
-  k_sum_final<<<1, SUM_THREADS, 0, c.stream>>>(c.red.p, SUM_BLOCKS, c.red.p + SUM_BLOCKS);
-  EMD_CHECK_LAUNCH();
+  {
+    TimedLaunch t(c, "sum_final");
+    k_sum_final<<<1, SUM_THREADS, 0, c.stream>>>(c.red.p, SUM_BLOCKS, c.red.p + SUM_BLOCKS);
+    EMD_CHECK_LAUNCH();
+  }
   EMD_CUDA(cudaMemcpyAsync(c.h_scalar, c.red.p + SUM_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   return *c.h_scalar;
@@ -295,6 +299,9 @@ void emd_destroy(emd_ctx* ctx) {
   c.x4.release();
   c.stage_x4.release();
   c.xl.release();
+  c.xl_bin.release();
+  c.bin_ctr.release();
+  c.neigh_rows2d.release();
   c.lj_params_f.release();
   for (auto& b : c.scan_levels) b.release();
   c.scan_aux.release();
@@ -373,8 +380,11 @@ emd_status emd_system_set_local(emd_ctx* ctx, int n, const double* x, const doub
     EMD_CUDA(cudaMemcpyAsync(c.stage_d.p, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c.stream));
     EMD_CUDA(cudaMemcpyAsync(c.type.p, type, sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
     EMD_CUDA(cudaMemcpyAsync(c.id.p, id, sizeof(int) * n, cudaMemcpyHostToDevice, c.stream));
-    k_pack_x4<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.stage_d.p, c.type.p, c.x4.p, n);
-    EMD_CHECK_LAUNCH();
+    {
+      TimedLaunch t(c, "system_pack_x");
+      k_pack_x4<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.stage_d.p, c.type.p, c.x4.p, n);
+      EMD_CHECK_LAUNCH();
+    }
     if (v) EMD_CUDA(cudaMemcpyAsync(c.v.p, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c.stream));
     else EMD_CUDA(cudaMemsetAsync(c.v.p, 0, sizeof(double) * 3 * n, c.stream));
     if (q) EMD_CUDA(cudaMemcpyAsync(c.q.p, q, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
@@ -394,6 +404,7 @@ emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x
   if (x) {
     c.stage_d.reserve(3 * size_t(count), c.stream);
     EMD_CUDA(cudaMemcpyAsync(c.stage_d.p, x, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
+    TimedLaunch t(c, "system_pack_x");
     k_pack_x4_keep_type<<<blocks_for(count, 256), 256, 0, c.stream>>>(c.stage_d.p, c.x4.p + first, count);
     EMD_CHECK_LAUNCH();
   }
@@ -410,6 +421,7 @@ emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double*
   if (count == 0) return EMD_OK;
   if (x) {
     c.stage_d.reserve(3 * size_t(count), c.stream);
+    TimedLaunch t(c, "system_unpack_x");
     k_unpack_x4<<<blocks_for(count, 256), 256, 0, c.stream>>>(c.x4.p + first, c.stage_d.p, count);
     EMD_CHECK_LAUNCH();
     EMD_CUDA(cudaMemcpyAsync(x, c.stage_d.p, sizeof(double) * 3 * count, cudaMemcpyDeviceToHost, c.stream));

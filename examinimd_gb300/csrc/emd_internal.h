@@ -136,6 +136,11 @@ struct Ctx {
   DevBuf<int> num_neighs, neigh_offsets, neighs;
   DevBuf<int> resize_flag;  // [0] = resize, [1] = new max
   int neigh_packed = 0;     // entries are (j << 5) | stencil code
+  int neigh_maxrow = 0;     // longest row of the current list
+  int neigh_scratch_k = 16; // capacity of the column-major rows behind a CSR list
+  bool neigh_layout_2d = false;  // force kernels read column-major rows
+  DevBuf<int> neigh_rows2d;      // column-major rows behind a CSR list
+  DevBuf<float4> xl_bin;         // FP32 position relative to the bin centre (last binning)
   DevBuf<int> abin;         // bin of every particle at the last list build (packed rows)
   DevBuf<float4> xl;        // FP32 bin-relative positions (mixed force)
 
@@ -144,6 +149,11 @@ struct Ctx {
   bool lj_ready = false;
   DevBuf<double> lj_params;  // lj1 | lj2 | cutsq, ntypes^2 each
   DevBuf<float> lj_params_f; // FP32 copy for the mixed form
+  bool lj_uniform = false;   // every type pair has the same parameters
+  float lj_single[3] = {0, 0, 0};
+  double lj_single_cutsq_d = 0;
+  DevBuf<double4_32a> bin_ctr;  // FP64 bin centre per particle (mixed form)
+  long long neigh_builds = 0, ctr_build = -1;
   DevBuf<double> red, red2;  // reduction partials
 
   // ---- SNAP (defined in snap.cu)

@@ -21,7 +21,7 @@ struct LJParams {
   int ntypes;
 };
 
-__device__ __forceinline__ int entry_j(int e, bool packed) { return packed ? (e >> 5) : e; }
+__device__ __forceinline__ int entry_j(int e, bool packed) { return packed ? (e >> 6) : e; }
 
 // TagFullNeigh (force_lj_neigh_impl.h:164-206)
 template <bool TWO_D>
@@ -147,10 +147,12 @@ void lj_mixed_prepare(Ctx& c);
 
 ListView list_view(Ctx& c) {
   ListView L;
-  L.entries = c.neighs.p;
+  // CSR rows live in neighs; column-major rows in neighs (Neighbor2D) or in
+  // the scratch rows behind a packed CSR list
+  L.entries = (c.neigh_layout_2d && c.neigh_kind != EMD_NEIGH_2D) ? c.neigh_rows2d.p : c.neighs.p;
   L.offsets = c.neigh_offsets.p;
   L.num_neighs = c.num_neighs.p;
-  L.stride = c.neigh_kind == EMD_NEIGH_2D ? c.neigh_stride : 0;
+  L.stride = c.neigh_layout_2d ? c.neigh_stride : 0;
   return L;
 }
 
@@ -206,7 +208,7 @@ emd_status emd_lj_compute(emd_ctx* ctx) {
   require(!c.neigh_packed, EMD_ERR_STATE, "emd_lj_compute: list was built for the mixed form");
   const ListView L = list_view(c);
   const LJParams P = lj_params(c);
-  const bool two_d = c.neigh_kind == EMD_NEIGH_2D;
+  const bool two_d = c.neigh_layout_2d;
   const int grid = blocks_for(n, 128);
   TimedLaunch t(c, c.lj_half ? "lj_half_fp64" : "lj_full_fp64");
   if (!c.lj_half) {
@@ -235,7 +237,7 @@ emd_status emd_lj_energy(emd_ctx* ctx, double* pe) {
   const LJParams P = lj_params(c);
   {
     TimedLaunch t(c, "lj_energy");
-    if (c.neigh_kind == EMD_NEIGH_2D)
+    if (c.neigh_layout_2d)
       k_lj_energy<true><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, c.red2.p);
     else
       k_lj_energy<false><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, c.red2.p);

@@ -1,15 +1,16 @@
-// ForceLJNeigh, mixed-precision form (FP32 pair arithmetic, FP64 per-atom
-// accumulation of the compensated FP32 sums, FP64 positions).
+// ForceLJNeigh, mixed-precision form: FP32 pair arithmetic, FP64 positions,
+// FP64 per-atom force sums of Kahan-compensated FP32 partials.
 //
-// Positions stay FP64 in x4.  Before each force pass every particle gets an
-// FP32 copy of its position relative to the centre of the bin it occupied
-// when the list was built (|xl| is about half a bin plus the skin drift), and
-// each packed list entry carries the stencil offset between the two bins, so
-// x_i - x_j = (xl_i - xl_j) + (o_i - o_j) is formed in FP32 from small
-// numbers.  Pairs whose FP32 r^2 lies within 1e-6 relative of the cutoff
-// are re-tested in FP64, so the set of interacting pairs is exactly the FP64
-// drop-in's.  Per-atom force sums use Kahan-compensated FP32 and are added
-// to the FP64 force array once.
+// Each force pass first refreshes an FP32 copy of every position relative to
+// the centre of the bin the particle occupied when the list was built
+// (|xl| is half a bin plus the skin drift, so FP32 keeps ~1e-7 absolute).
+// List rows are column-major (entry k of row i at k*stride + i: one warp's
+// 32 rows load as one 128-byte line) and each packed entry carries the
+// per-dimension bin offset k = (bin_j - bin_i) + 1, so
+//   x_i - x_j = (xl_i - xl_j) + (1 - k) * w
+// is formed in FP32 from small numbers.  Pairs whose FP32 r^2 lies within
+// 1e-6 relative of the cutoff are re-tested with the FP64 positions, so the
+// set of interacting pairs equals the FP64 drop-in's.
 #include "emd_device.cuh"
 #include "emd_internal.h"
 #include "neigh_rows.cuh"
@@ -26,19 +27,26 @@ struct BinFrame {
   double wx, wy, wz;  // bin widths
 };
 
-__global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restrict__ x4, const int* __restrict__ abin,
-                                                    int n, BinFrame F, float4* __restrict__ xl) {
+// FP64 centre of every particle's bin at the last list build
+__global__ void __launch_bounds__(256) k_bin_centres(const int* __restrict__ abin, int n, BinFrame F,
+                                                     double4_32a* __restrict__ ctr) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
   const int b = abin[a];
   const int bx = b / (F.nby * F.nbz);
   const int by = (b / F.nbz) % F.nby;
   const int bz = b % F.nbz;
+  ctr[a] = make_double4_32a(F.minx + (bx + 0.5) * F.wx, F.miny + (by + 0.5) * F.wy, F.minz + (bz + 0.5) * F.wz, 0.0);
+}
+
+__global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restrict__ x4,
+                                                    const double4_32a* __restrict__ ctr, int n,
+                                                    float4* __restrict__ xl) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
   const double4_32a p = x4[a];
-  const double ox = F.minx + (bx + 0.5) * F.wx;
-  const double oy = F.miny + (by + 0.5) * F.wy;
-  const double oz = F.minz + (bz + 0.5) * F.wz;
-  xl[a] = make_float4(float(p.x - ox), float(p.y - oy), float(p.z - oz), __int_as_float(int(p.w)));
+  const double4_32a o = ctr[a];
+  xl[a] = make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(int(p.w)));
 }
 
 struct LJParamsF {
@@ -47,6 +55,8 @@ struct LJParamsF {
   const float* cutsq;
   const double* cutsq_d;
   int ntypes;
+  float lj1_0, lj2_0, cutsq_0;  // single-type values
+  double cutsq_d0;
 };
 
 __device__ __forceinline__ void kahan_add(float& s, float& comp, float v) {
@@ -56,40 +66,56 @@ __device__ __forceinline__ void kahan_add(float& s, float& comp, float v) {
   s = t;
 }
 
-template <bool TWO_D>
+// (1 - k) * w for k in {0, 1, 2}
+__device__ __forceinline__ float bin_shift(int k, float w) { return k == 0 ? w : (k == 2 ? -w : 0.0f); }
+
+template <bool SINGLE>
 __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict__ xl,
                                                        const double4_32a* __restrict__ x4, double* __restrict__ f,
-                                                       ListView L, LJParamsF P, float wx, float wy, float wz, int n) {
+                                                       const int* __restrict__ rows, int stride,
+                                                       const int* __restrict__ num, LJParamsF P, float wx, float wy,
+                                                       float wz, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = xl[i];
   const int ti = __float_as_int(xi.w);
-  const Row<TWO_D> row(L, i);
+  const int cnt = num[i];
+  const int* row = rows + i;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  for (int jj = 0; jj < row.n; ++jj) {
-    const int e = row[jj];
-    const int j = e >> 5;
-    const int code = e & 31;
-    const int kx = code / 9, ky = (code / 3) % 3, kz = code % 3;
+#pragma unroll 2
+  for (int jj = 0; jj < cnt; ++jj) {
+    const int e = __ldg(row + (size_t)jj * stride);
+    const int j = e >> 6;
     const float4 xj = xl[j];
-    // o_i - o_j = -(b_j - b_i) * w
-    const float dx = (xi.x - xj.x) + float(1 - kx) * wx;
-    const float dy = (xi.y - xj.y) + float(1 - ky) * wy;
-    const float dz = (xi.z - xj.z) + float(1 - kz) * wz;
+    const float dx = (xi.x - xj.x) + bin_shift((e >> 4) & 3, wx);
+    const float dy = (xi.y - xj.y) + bin_shift((e >> 2) & 3, wy);
+    const float dz = (xi.z - xj.z) + bin_shift(e & 3, wz);
     const float rsq = dx * dx + dy * dy + dz * dz;
-    const int tp = ti * P.ntypes + __float_as_int(xj.w);
-    const float cutsq = __ldg(P.cutsq + tp);
+    float lj1, lj2, cutsq;
+    double cutsq_d;
+    if (SINGLE) {
+      lj1 = P.lj1_0;
+      lj2 = P.lj2_0;
+      cutsq = P.cutsq_0;
+      cutsq_d = P.cutsq_d0;
+    } else {
+      const int tp = ti * P.ntypes + __float_as_int(xj.w);
+      lj1 = __ldg(P.lj1 + tp);
+      lj2 = __ldg(P.lj2 + tp);
+      cutsq = __ldg(P.cutsq + tp);
+      cutsq_d = __ldg(P.cutsq_d + tp);
+    }
     bool in = rsq < cutsq;
     if (fabsf(rsq - cutsq) <= 1e-6f * cutsq) {
       // borderline: decide exactly as the FP64 form does
       const double4_32a pi = x4[i], pj = x4[j];
       const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
-      in = (ddx * ddx + ddy * ddy + ddz * ddz) < __ldg(P.cutsq_d + tp);
+      in = (ddx * ddx + ddy * ddy + ddz * ddz) < cutsq_d;
     }
     if (in) {
-      const float r2inv = 1.0f / rsq;
+      const float r2inv = __fdividef(1.0f, rsq);
       const float r6inv = r2inv * r2inv * r2inv;
-      const float fpair = (r6inv * (__ldg(P.lj1 + tp) * r6inv - __ldg(P.lj2 + tp))) * r2inv;
+      const float fpair = (r6inv * (lj1 * r6inv - lj2)) * r2inv;
       kahan_add(sx, cx, dx * fpair);
       kahan_add(sy, cy, dy * fpair);
       kahan_add(sz, cz, dz * fpair);
@@ -114,23 +140,32 @@ void lj_mixed_compute(Ctx& c) {
   F.wx = (c.bmax[0] - c.bmin[0]) / c.nbin[0];
   F.wy = (c.bmax[1] - c.bmin[1]) / c.nbin[1];
   F.wz = (c.bmax[2] - c.bmin[2]) / c.nbin[2];
+  if (c.ctr_build != c.neigh_builds) {
+    c.bin_ctr.reserve(size_t(n_all) + 1, c.stream);
+    TimedLaunch t(c, "lj_bin_centres");
+    k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, F, c.bin_ctr.p);
+    EMD_CHECK_LAUNCH();
+    c.ctr_build = c.neigh_builds;
+  }
   {
     TimedLaunch t(c, "lj_refresh_xl");
-    k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, c.abin.p, n_all, F, c.xl.p);
+    k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, c.bin_ctr.p, n_all, c.xl.p);
     EMD_CHECK_LAUNCH();
   }
   const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
   LJParamsF P{c.lj_params_f.p, c.lj_params_f.p + nt2, c.lj_params_f.p + 2 * nt2, c.lj_params.p + 2 * nt2,
-              c.lj_ntypes};
+              c.lj_ntypes, c.lj_single[0], c.lj_single[1], c.lj_single[2], c.lj_single_cutsq_d};
   const ListView L = list_view(c);
   const int n = c.N_local;
   TimedLaunch t(c, "lj_full_mixed");
-  if (c.neigh_kind == EMD_NEIGH_2D)
-    k_lj_full_mixed<true><<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, L, P, float(F.wx),
-                                                                    float(F.wy), float(F.wz), n);
+  if (c.lj_uniform)
+    k_lj_full_mixed<true><<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, L.entries, L.stride,
+                                                                    L.num_neighs, P, float(F.wx), float(F.wy),
+                                                                    float(F.wz), n);
   else
-    k_lj_full_mixed<false><<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, L, P, float(F.wx),
-                                                                     float(F.wy), float(F.wz), n);
+    k_lj_full_mixed<false><<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, L.entries, L.stride,
+                                                                     L.num_neighs, P, float(F.wx), float(F.wy),
+                                                                     float(F.wz), n);
   EMD_CHECK_LAUNCH();
 }
 
@@ -141,6 +176,16 @@ void lj_mixed_prepare(Ctx& c) {
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   std::vector<float> hf(3 * nt2);
   for (size_t k = 0; k < 3 * nt2; ++k) hf[k] = float(h[k]);
+  // every type pair identical (ExaMiniMD's stack parameters for <= 12 types
+  // always are): keep the values in registers
+  bool uniform = true;
+  for (size_t k = 1; k < nt2; ++k)
+    uniform = uniform && h[k] == h[0] && h[nt2 + k] == h[nt2] && h[2 * nt2 + k] == h[2 * nt2];
+  c.lj_uniform = uniform;
+  c.lj_single[0] = hf[0];
+  c.lj_single[1] = hf[nt2];
+  c.lj_single[2] = hf[2 * nt2];
+  c.lj_single_cutsq_d = h[2 * nt2];
   c.lj_params_f.reserve(3 * nt2, c.stream);
   EMD_CUDA(cudaMemcpyAsync(c.lj_params_f.p, hf.data(), sizeof(float) * 3 * nt2, cudaMemcpyHostToDevice, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));

@@ -1,17 +1,26 @@
 // NeighborCSR / Neighbor2D on the device (neighbor_csr.h:176-435,
 // neighbor_2d.h:175-331).
 //
-// One warp per owned atom i.  The warp walks the 27-bin stencil in the
-// reference order (bx_j slowest, bz_j fastest) and each stencil bin in
-// permutation order, 32 candidates at a time; accepted candidates are
+// One CTA per interior bin.  The CTA stages the particles of its 27-bin
+// stencil in the reference order (bx_j slowest, bz_j fastest; inside a bin
+// in permutation order) into shared memory as FP32 positions relative to the
+// centre of ITS bin (exact bin-relative FP32 coordinates come from the
+// binning pass), so a candidate test is three FP32 subtractions and an FP32
+// r^2.  Only when r^2 lies within 4e-5 relative of the cutoff is the pair
+// re-tested with the FP64 positions, so every accept / reject equals the FP64
+// test `rsq <= neigh_cut^2` of the reference.  Each warp owns centre atoms
+// and walks the staged candidates 32 at a time; accepted candidates are
 // compacted with ballot + popc, so row i lists its neighbours in exactly the
-// order the serial reference appends them.  CSR = count pass, scan, fill
-// pass; 2D = fill with overflow detection and a host regrow loop.
+// order the serial reference appends them.
 //
-// Rows built for the mixed-precision force carry a packed entry
-// (j << 5) | stencil code (code = 9*(dbx+1) + 3*(dby+1) + (dbz+1)), which
-// lets the force kernel difference FP32 bin-relative coordinates.  The
-// default FP64 drop-in stores plain j.
+// One pass writes rows column-major (entry k of row i at k*stride + i, the
+// layout of the reference's Neighbor2D view on a GPU) with capacity K; the
+// host grows K like Neighbor2D's regrow loop (x1.2) when a row overflows.
+// NeighborCSR rows are then compacted behind an exclusive scan of the
+// counts.  Rows built for the mixed-precision force carry packed entries
+// (j << 6) | (kx << 4) | (ky << 2) | kz with k = (bin_j - bin_i) + 1 per
+// dimension, which the force kernel uses to difference FP32 bin-relative
+// coordinates; the FP64 drop-in stores plain j.
 #include <algorithm>
 
 #include "emd_device.cuh"
@@ -20,105 +29,164 @@
 namespace emd {
 namespace {
 
-enum { MODE_COUNT = 0, MODE_FILL_CSR = 1, MODE_FILL_2D = 2 };
+constexpr int NB_THREADS = 128;
+constexpr int NB_WARPS = NB_THREADS / 32;
+constexpr int NB_CAP = 1024;  // staged candidates per chunk
 
 struct NeighArgs {
   const double4_32a* x4;
-  const int* binof;
+  const float4* xl;  // FP32 position relative to the particle's bin centre
   const int* bincount;
   const int* binoffsets;
   const int* permute;
   int nbx, nby, nbz, nhalo;
+  float wx, wy, wz;  // bin widths
   int n_local;
   double cutsq;
+  float cut_lo, cut_hi;  // FP32 decision band
   int half, newton, packed;
   int* num_neighs;
-  const int* offsets;  // CSR row starts
-  int* entries;        // CSR entries or 2D base
-  int stride;          // 2D leading dimension (rows)
-  int maxneighs;
-  int* resize;  // [0] flag, [1] max row length seen
+  int* rows;  // column-major, leading dimension `stride`, capacity K
+  int stride, K;
+  int* flags;  // [0] overflow, [1] longest row
 };
 
-template <int MODE>
-__global__ void __launch_bounds__(256) k_neigh(NeighArgs a) {
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (i >= a.n_local) return;
-  const int b = a.binof[i];
-  const int bx = b / (a.nby * a.nbz);
-  const int by = (b / a.nbz) % a.nby;
-  const int bz = b % a.nbz;
-  const bool interior = bx >= a.nhalo && bx < a.nbx - a.nhalo && by >= a.nhalo && by < a.nby - a.nhalo &&
-                        bz >= a.nhalo && bz < a.nbz - a.nhalo;
-  int cnt = 0;
-  if (interior) {
-    const double4_32a xi = a.x4[i];
-    int row = 0;
-    if (MODE == MODE_FILL_CSR) row = a.offsets[i];
-    const unsigned lt = (1u << lane) - 1u;
-    for (int dbx = -1; dbx <= 1; ++dbx)
-      for (int dby = -1; dby <= 1; ++dby)
-        for (int dbz = -1; dbz <= 1; ++dbz) {
-          const int bj = ((bx + dbx) * a.nby + (by + dby)) * a.nbz + (bz + dbz);
-          const int n = a.bincount[bj];
-          const int off = a.binoffsets[bj];
-          const int code = 9 * (dbx + 1) + 3 * (dby + 1) + (dbz + 1);
-          for (int base = 0; base < n; base += 32) {
-            const int k = base + lane;
-            bool take = false;
-            int j = 0;
-            if (k < n) {
-              j = a.permute[off + k];
-              const double4_32a xj = a.x4[j];
-              if (a.half) {
-                // neighbor_csr.h:287-291: skip unless j is "above" i
-                // lexicographically, or j is a ghost with newton off
-                const bool above = (xj.x > xi.x) || ((xj.x == xi.x) && ((xj.y > xi.y) || ((xj.y == xi.y) && (xj.z > xi.z))));
-                const bool skip = ((j == i) || (j < a.n_local || a.newton)) && !above;
-                if (!skip) {
-                  const double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-                  const double rsq = dx * dx + dy * dy + dz * dz;
-                  take = rsq <= a.cutsq;
-                }
-              } else {
-                const double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-                const double rsq = dx * dx + dy * dy + dz * dz;
-                take = (rsq <= a.cutsq) && (i != j);
+// monotone integer key of a double (exact ordering, integer pipe)
+__device__ __forceinline__ long long okey(double v) {
+  const long long b = __double_as_longlong(v);
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+__global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
+  __shared__ float4 cand[NB_CAP];
+  __shared__ int pre[28];
+  __shared__ int boff[27];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // interior bin of this CTA
+  const int ix = a.nbx - 2 * a.nhalo, iy = a.nby - 2 * a.nhalo, iz = a.nbz - 2 * a.nhalo;
+  const int bx = blockIdx.x / (iy * iz) + a.nhalo;
+  const int by = (blockIdx.x / iz) % iy + a.nhalo;
+  const int bz = blockIdx.x % iz + a.nhalo;
+  const int bc = (bx * a.nby + by) * a.nbz + bz;
+  if (tid < 27) {
+    const int dbx = tid / 9 - 1, dby = (tid / 3) % 3 - 1, dbz = tid % 3 - 1;
+    const int b = ((bx + dbx) * a.nby + (by + dby)) * a.nbz + (bz + dbz);
+    pre[tid + 1] = a.bincount[b];
+    boff[tid] = a.binoffsets[b];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    pre[0] = 0;
+    for (int s = 0; s < 27; ++s) pre[s + 1] += pre[s];
+  }
+  __syncthreads();
+  const int M = pre[27];
+  const int nc = a.bincount[bc], oc = a.binoffsets[bc];
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = 0; base < M; base += NB_CAP) {
+    const int m = min(NB_CAP, M - base);
+    for (int t = tid; t < m; t += NB_THREADS) {
+      const int g = base + t;
+      int s = 0;
+      while (pre[s + 1] <= g) ++s;
+      const int j = a.permute[boff[s] + (g - pre[s])];
+      const float4 p = a.xl[j];
+      const float sx = float(s / 9 - 1) * a.wx, sy = float((s / 3) % 3 - 1) * a.wy, sz = float(s % 3 - 1) * a.wz;
+      const int code = ((s / 9) << 4) | (((s / 3) % 3) << 2) | (s % 3);
+      const int w = a.packed ? ((j << 6) | code) : j;
+      cand[t] = make_float4(p.x + sx, p.y + sy, p.z + sz, __int_as_float(w));
+    }
+    __syncthreads();
+    for (int bi = warp; bi < nc; bi += NB_WARPS) {
+      const int i = a.permute[oc + bi];
+      if (i >= a.n_local) continue;  // ghosts own no row
+      const float4 xi = a.xl[i];
+      double4_32a xd = make_double4_32a(0, 0, 0, 0);
+      long long kx = 0, ky = 0, kz = 0;
+      if (a.half) {
+        xd = a.x4[i];
+        kx = okey(xd.x);
+        ky = okey(xd.y);
+        kz = okey(xd.z);
+      }
+      int cnt = base == 0 ? 0 : a.num_neighs[i];
+      for (int k0 = 0; k0 < m; k0 += 32) {
+        const int k = k0 + lane;
+        bool take = false;
+        int w = 0;
+        if (k < m) {
+          const float4 c = cand[k];
+          w = __float_as_int(c.w);
+          const int j = a.packed ? (w >> 6) : w;
+          const float dx = xi.x - c.x, dy = xi.y - c.y, dz = xi.z - c.z;
+          const float rsq = dx * dx + dy * dy + dz * dz;
+          bool in = rsq < a.cut_lo;
+          bool decided = in || rsq > a.cut_hi;
+          if (a.half) {
+            // neighbor_csr.h:287-291: skip unless j is "above" i
+            // lexicographically, or j is a ghost with newton off
+            const double4_32a xj = a.x4[j];
+            const long long jx = okey(xj.x), jy = okey(xj.y), jz = okey(xj.z);
+            const bool above = (jx > kx) || ((jx == kx) && ((jy > ky) || ((jy == ky) && (jz > kz))));
+            const bool skip = ((j == i) || (j < a.n_local || a.newton)) && !above;
+            if (!skip) {
+              if (!decided) {
+                const double ddx = xd.x - xj.x, ddy = xd.y - xj.y, ddz = xd.z - xj.z;
+                in = (ddx * ddx + ddy * ddy + ddz * ddz) <= a.cutsq;
               }
+              take = in;
             }
-            const unsigned m = __ballot_sync(FULL_MASK, take);
-            if (MODE != MODE_COUNT && take) {
-              const int pos = cnt + __popc(m & lt);
-              const int e = a.packed ? ((j << 5) | code) : j;
-              if (MODE == MODE_FILL_CSR) a.entries[row + pos] = e;
-              else if (pos < a.maxneighs) a.entries[(size_t)pos * a.stride + i] = e;
+          } else {
+            if (!decided) {
+              const double4_32a pi = a.x4[i], pj = a.x4[j];
+              const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+              in = (ddx * ddx + ddy * ddy + ddz * ddz) <= a.cutsq;
             }
-            cnt += __popc(m);
+            take = in && (i != j);
           }
         }
-  }
-  if (lane == 0) {
-    if (MODE == MODE_COUNT || MODE == MODE_FILL_2D) a.num_neighs[i] = cnt;
-    if (MODE == MODE_FILL_2D && cnt > a.maxneighs) {
-      a.resize[0] = 1;
-      atomicMax(&a.resize[1], cnt);
+        const unsigned bal = __ballot_sync(FULL_MASK, take);
+        if (take) {
+          const int pos = cnt + __popc(bal & lt);
+          if (pos < a.K) a.rows[(size_t)pos * a.stride + i] = w;
+        }
+        cnt += __popc(bal);
+      }
+      if (lane == 0) a.num_neighs[i] = cnt;
     }
+    __syncthreads();
+  }
+  // rows, overflow flag, longest row
+  for (int bi = tid; bi < nc; bi += NB_THREADS) {
+    const int i = a.permute[oc + bi];
+    if (i >= a.n_local) continue;
+    const int cnt = a.num_neighs[i];
+    if (cnt > a.K) a.flags[0] = 1;
+    atomicMax(&a.flags[1], cnt);
   }
 }
 
-// 2D rows -> contiguous row-by-row entries (for emd_neigh_get)
-__global__ void k_compact_2d(const int* __restrict__ neighs, int stride, const int* __restrict__ num,
-                             const int* __restrict__ offs, int n, int* __restrict__ out) {
+// owned atoms outside every interior bin get an empty row (the reference
+// never visits them)
+__global__ void k_zero_rows(int* num, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) num[i] = 0;
+}
+
+// column-major rows -> CSR rows at offs[i]
+__global__ void __launch_bounds__(256) k_rows_to_csr(const int* __restrict__ rows, int stride,
+                                                     const int* __restrict__ num, const int* __restrict__ offs, int n,
+                                                     int* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int m = num[i];
-  for (int k = 0; k < m; ++k) out[offs[i] + k] = neighs[(size_t)k * stride + i];
+  const int m = num[i], o = offs[i];
+  for (int k = 0; k < m; ++k) out[o + k] = rows[(size_t)k * stride + i];
 }
 
+// packed entries -> plain j (for emd_neigh_get)
 __global__ void k_unpack(int* __restrict__ e, long long n) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) e[t] = e[t] >> 5;
+  if (t < n) e[t] = e[t] >> 6;
 }
 
 }  // namespace
@@ -136,25 +204,27 @@ emd_status emd_neigh_init(emd_ctx* ctx, int kind, double neigh_cut, int comm_new
   c.neigh_cut = neigh_cut;
   c.comm_newton = comm_newton ? 1 : 0;
   c.maxneighs = 16;  // NeighList2D() initial capacity (neighbor_2d.h:101-104)
+  c.neigh_scratch_k = 16;
   c.neigh_ready = false;
   EMD_API_END
 }
 
 emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) {
   EMD_API_BEGIN
-  require(c.neigh_cut > 0, EMD_ERR_STATE, "emd_neigh_create: emd_neigh_init not called");
+  require(c.neigh_cut > 0, EMD_ERR_STATE, "emd_neigh_init not called");
   require(c.binning_ready && c.bin_first == 0 && c.bin_count_n == c.N_local + c.N_ghost, EMD_ERR_STATE,
           "emd_neigh_create: needs a binning of owned and ghost particles");
   const int n = c.N_local;
   c.half_neigh = half_neigh ? 1 : 0;
   const int packed = (c.lj_ready && c.lj_prec == EMD_PREC_MIXED) ? 1 : 0;
-  require(!packed || (long long)(c.N_local + c.N_ghost) < (1LL << 26), EMD_ERR_ARG,
-          "emd_neigh_create: packed rows need fewer than 2^26 particles");
+  require(!packed || (long long)(c.N_local + c.N_ghost) < (1LL << 25), EMD_ERR_ARG,
+          "emd_neigh_create: packed rows need fewer than 2^25 particles");
   c.num_neighs.reserve(size_t(n) + 1, c.stream);
   c.neigh_offsets.reserve(size_t(n) + 2, c.stream);
+  c.resize_flag.reserve(2, c.stream);
   NeighArgs a;
   a.x4 = c.x4.p;
-  a.binof = c.binof.p;
+  a.xl = c.xl_bin.p;
   a.bincount = c.bincount.p;
   a.binoffsets = c.binoffsets.p;
   a.permute = c.permute.p;
@@ -162,60 +232,60 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   a.nby = c.nbin[1];
   a.nbz = c.nbin[2];
   a.nhalo = c.nhalo;
+  a.wx = float((c.bmax[0] - c.bmin[0]) / c.nbin[0]);
+  a.wy = float((c.bmax[1] - c.bmin[1]) / c.nbin[1]);
+  a.wz = float((c.bmax[2] - c.bmin[2]) / c.nbin[2]);
   a.n_local = n;
   a.cutsq = c.neigh_cut * c.neigh_cut;
+  a.cut_lo = float(a.cutsq * (1.0 - 4e-5));
+  a.cut_hi = float(a.cutsq * (1.0 + 4e-5));
   a.half = c.half_neigh;
   a.newton = c.comm_newton;
   a.packed = packed;
   a.num_neighs = c.num_neighs.p;
-  a.offsets = c.neigh_offsets.p;
-  a.entries = nullptr;
   a.stride = n + 1;
-  a.maxneighs = 0;
-  a.resize = nullptr;
-  const int grid = blocks_for((long long)n * 32, 256);
-  long long total = 0;
-  if (c.neigh_kind == EMD_NEIGH_CSR) {
+  a.flags = c.resize_flag.p;
+  const int ibins = (c.nbin[0] - 2 * c.nhalo) * (c.nbin[1] - 2 * c.nhalo) * (c.nbin[2] - 2 * c.nhalo);
+  const bool two_d = c.neigh_kind == EMD_NEIGH_2D;
+  int& K = two_d ? c.maxneighs : c.neigh_scratch_k;
+  DevBuf<int>& rows = two_d ? c.neighs : c.neigh_rows2d;
+  while (true) {
+    rows.reserve(size_t(n + 1) * size_t(K) + 1, c.stream);
+    a.rows = rows.p;
+    a.K = K;
+    EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, 2 * sizeof(int), c.stream));
     if (n > 0) {
-      TimedLaunch t(c, "neigh_count");
-      k_neigh<MODE_COUNT><<<grid, 256, 0, c.stream>>>(a);
-      EMD_CHECK_LAUNCH();
-    }
-    exclusive_scan_int(c, c.num_neighs.p, c.neigh_offsets.p, n, c.neigh_offsets.p + n);
-    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.neigh_offsets.p + n, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    EMD_CUDA(cudaStreamSynchronize(c.stream));
-    total = n > 0 ? c.h_int[0] : 0;
-    c.neighs.reserve(size_t(total) + 1, c.stream);
-    a.entries = c.neighs.p;
-    if (n > 0) {
-      TimedLaunch t(c, "neigh_fill_csr");
-      k_neigh<MODE_FILL_CSR><<<grid, 256, 0, c.stream>>>(a);
-      EMD_CHECK_LAUNCH();
-    }
-  } else {
-    c.resize_flag.reserve(2, c.stream);
-    while (true) {
-      const size_t need = size_t(n + 1) * size_t(c.maxneighs);
-      c.neighs.reserve(need + 1, c.stream);
-      EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, 2 * sizeof(int), c.stream));
-      a.entries = c.neighs.p;
-      a.maxneighs = c.maxneighs;
-      a.resize = c.resize_flag.p;
-      if (n > 0) {
-        TimedLaunch t(c, "neigh_fill_2d");
-        k_neigh<MODE_FILL_2D><<<grid, 256, 0, c.stream>>>(a);
+      {
+        TimedLaunch t(c, "neigh_zero_rows");
+        k_zero_rows<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.num_neighs.p, n);
         EMD_CHECK_LAUNCH();
       }
-      EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-      EMD_CUDA(cudaStreamSynchronize(c.stream));
-      if (!c.h_int[0]) break;
-      // neighbor_2d.h:325-327: grow to 1.2x the reported row length and redo
-      c.maxneighs = int(c.h_int[1] * 1.2);
+      if (ibins > 0) {
+        TimedLaunch t(c, "neigh_build");
+        k_neigh_bin<<<ibins, NB_THREADS, 0, c.stream>>>(a);
+        EMD_CHECK_LAUNCH();
+      }
     }
-    exclusive_scan_int(c, c.num_neighs.p, c.neigh_offsets.p, n, c.neigh_offsets.p + n);
-    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.neigh_offsets.p + n, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     EMD_CUDA(cudaStreamSynchronize(c.stream));
-    total = n > 0 ? c.h_int[0] : 0;
+    c.neigh_maxrow = n > 0 ? c.h_int[1] : 0;
+    if (!c.h_int[0]) break;
+    // neighbor_2d.h:325-327: grow to 1.2x the longest row and redo
+    K = int(c.h_int[1] * 1.2);
+  }
+  exclusive_scan_int(c, c.num_neighs.p, c.neigh_offsets.p, n, c.neigh_offsets.p + n);
+  EMD_CUDA(cudaMemcpyAsync(c.h_int, c.neigh_offsets.p + n, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  const long long total = n > 0 ? c.h_int[0] : 0;
+  if (!two_d && !packed) {
+    // NeighListCSR (neighbor_csr.h:81-124): rows contiguous at row_map(i)
+    c.neighs.reserve(size_t(total) + 1, c.stream);
+    if (n > 0) {
+      TimedLaunch t(c, "neigh_rows_to_csr");
+      k_rows_to_csr<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.neigh_rows2d.p, n + 1, c.num_neighs.p,
+                                                                c.neigh_offsets.p, n, c.neighs.p);
+      EMD_CHECK_LAUNCH();
+    }
   }
   if (packed) {
     const int n_all = c.N_local + c.N_ghost;
@@ -227,6 +297,9 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   c.neigh_total = total;
   c.neigh_ready = true;
   c.neigh_packed = packed;
+  c.neigh_builds++;
+  // the force kernels read CSR (plain rows) or column-major rows
+  c.neigh_layout_2d = two_d || packed;
   if (total_out) *total_out = total;
   EMD_API_END
 }
@@ -240,11 +313,12 @@ emd_status emd_neigh_get(emd_ctx* ctx, int* num_neighs, int* entries) {
   if (entries && c.neigh_total > 0) {
     DevBuf<int> tmp;
     tmp.reserve(size_t(c.neigh_total), c.stream);
-    if (c.neigh_kind == EMD_NEIGH_CSR) {
+    if (!c.neigh_layout_2d) {
       EMD_CUDA(cudaMemcpyAsync(tmp.p, c.neighs.p, sizeof(int) * c.neigh_total, cudaMemcpyDeviceToDevice, c.stream));
     } else {
-      k_compact_2d<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.neighs.p, c.neigh_stride, c.num_neighs.p,
-                                                             c.neigh_offsets.p, n, tmp.p);
+      const int* src = c.neigh_kind == EMD_NEIGH_2D ? c.neighs.p : c.neigh_rows2d.p;
+      k_rows_to_csr<<<blocks_for(n, 256), 256, 0, c.stream>>>(src, c.neigh_stride, c.num_neighs.p,
+                                                              c.neigh_offsets.p, n, tmp.p);
       EMD_CHECK_LAUNCH();
     }
     if (c.neigh_packed) {
