@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) k_bin_index(const double4_32a* __restrict
   atomicAdd(&bincount[b], 1);
   // FP32 position relative to the bin centre, for the neighbour candidate tests
   xl[first + r] = make_float4(float(p.x - (minx + (ix + 0.5) * wx)), float(p.y - (miny + (iy + 0.5) * wy)),
-                              float(p.z - (minz + (iz + 0.5) * wz)), p.w);
+                              float(p.z - (minz + (iz + 0.5) * wz)), __int_as_float(int(p.w)));
 }
 
 __global__ void __launch_bounds__(256) k_bin_scatter(const int* __restrict__ binof, int n,
@@ -161,6 +161,8 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
   if (sort && n > 0) {
     // BinSort::sort of x, v, f, type, id, q over the binned range: one
     // fused gather kernel into staging buffers, then copies back
+    materialize_zero(c, true, false);
+    c.xl_ok = 0;
     const int* perm = c.permute.p;
     c.stage_x4.reserve(size_t(n), c.stream);
     c.stage_d.reserve(7 * size_t(n), c.stream);

@@ -71,7 +71,7 @@ __global__ void k_halo_scatter(double4_32a* __restrict__ x4, double* __restrict_
 // for bit.
 __global__ void k_halo_update(double4_32a* __restrict__ x4, const int* __restrict__ owner,
                               const int* __restrict__ img, int n_local, int n_ghost, double lx, double ly,
-                              double lz) {
+                              double lz, const double4_32a* __restrict__ ctr, float4* __restrict__ xl) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_ghost) return;
   const int m = img[g];
@@ -85,6 +85,10 @@ __global__ void k_halo_update(double4_32a* __restrict__ x4, const int* __restric
   double4_32a o = x4[n_local + g];
   p.w = o.w;
   x4[n_local + g] = p;
+  if (xl) {  // mixed form: FP32 position relative to the ghost's bin centre
+    const double4_32a q = ctr[n_local + g];
+    xl[n_local + g] = make_float4(float(p.x - q.x), float(p.y - q.y), float(p.z - q.z), __int_as_float(int(p.w)));
+  }
 }
 
 // TagHaloForceSelf for one phase (comm_serial.h:200-213).  Within a phase
@@ -131,6 +135,7 @@ emd_status emd_comm_exchange(emd_ctx* ctx) {
   EMD_API_BEGIN
   if (c.N_local == 0) return EMD_OK;
   TimedLaunch t(c, "comm_exchange");
+  c.xl_ok &= ~1;
   k_exchange<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.N_local, c.domain[0], c.domain[1],
                                                                c.domain[2]);
   EMD_CHECK_LAUNCH();
@@ -147,6 +152,7 @@ emd_status emd_comm_exchange_halo(emd_ctx* ctx, int* n_ghost_out) {
   int N_ghost = 0;
   int pack_total = 0;
   c.neigh_ready = false;
+  c.xl_ok &= ~2;
   for (int phase = 0; phase < 6; ++phase) {
     const int dim = phase / 2;
     const int upper = phase % 2 == 0;
@@ -195,8 +201,11 @@ emd_status emd_comm_update_halo(emd_ctx* ctx) {
   EMD_API_BEGIN
   if (c.N_ghost == 0) return EMD_OK;
   TimedLaunch t(c, "comm_update_halo");
-  k_halo_update<<<blocks_for(c.N_ghost, 256), 256, 0, c.stream>>>(c.x4.p, c.ghost_owner.p, c.ghost_img.p, c.N_local,
-                                                                   c.N_ghost, c.domain[0], c.domain[1], c.domain[2]);
+  const bool live = mixed_xl_active(c);
+  k_halo_update<<<blocks_for(c.N_ghost, 256), 256, 0, c.stream>>>(
+      c.x4.p, c.ghost_owner.p, c.ghost_img.p, c.N_local, c.N_ghost, c.domain[0], c.domain[1], c.domain[2],
+      live ? c.bin_ctr.p : nullptr, live ? c.xl.p : nullptr);
+  if (!live) c.xl_ok &= ~2;
   EMD_CHECK_LAUNCH();
   EMD_API_END
 }
@@ -209,6 +218,7 @@ emd_status emd_comm_update_force(emd_ctx* ctx) {
     pack_off[p] = acc;
     acc += c.num_ghost[p];
   }
+  materialize_zero(c, true, true);
   for (int phase = 5; phase >= 0; --phase) {
     const int count = c.num_ghost[phase];
     if (count == 0) continue;

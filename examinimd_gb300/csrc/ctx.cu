@@ -176,6 +176,22 @@ double device_sum(Ctx& c, const double* d_vals, int n) {
   return *c.h_scalar;
 }
 
+void materialize_zero(Ctx& c, bool locals, bool ghosts) {
+  const int want = (locals ? 1 : 0) | (ghosts ? 2 : 0);
+  const int todo = c.f_zero_pending & want;
+  if (!todo) return;
+  TimedLaunch t(c, "zero_forces");
+  if (todo == 3) {
+    EMD_CUDA(cudaMemsetAsync(c.f.p, 0, sizeof(double) * 3 * size_t(c.N_max), c.stream));
+  } else if (todo == 1) {
+    EMD_CUDA(cudaMemsetAsync(c.f.p, 0, sizeof(double) * 3 * size_t(c.N_local), c.stream));
+  } else {
+    EMD_CUDA(cudaMemsetAsync(c.f.p + 3 * size_t(c.N_local), 0, sizeof(double) * 3 * size_t(c.N_max - c.N_local),
+                             c.stream));
+  }
+  c.f_zero_pending &= ~todo;
+}
+
 unsigned read_status(Ctx& c, bool clear) {
   EMD_CUDA(cudaMemcpyAsync(c.h_status, c.d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, c.stream));
   if (clear) EMD_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(unsigned), c.stream));
@@ -273,7 +289,7 @@ emd_status emd_create(emd_ctx** out, int device) {
     EMD_CUDA(cudaMallocHost(&c.h_status, sizeof(unsigned)));
     EMD_CUDA(cudaMallocHost(&c.h_scalar, 8 * sizeof(double)));
     EMD_CUDA(cudaMallocHost(&c.h_ll, 8 * sizeof(long long)));
-    EMD_CUDA(cudaMallocHost(&c.h_int, 16 * sizeof(int)));
+    EMD_CUDA(cudaMallocHost(&c.h_int, kHostInts * sizeof(int)));
     c.mass.assign(1, 1.0);
     EMD_CUDA(cudaStreamSynchronize(c.stream));
   } catch (const Error& e) {
@@ -353,6 +369,13 @@ emd_status emd_system_init(emd_ctx* ctx, int ntypes, const double* mass, double 
   }
   c.mass_d.reserve(size_t(ntypes), c.stream);
   EMD_CUDA(cudaMemcpyAsync(c.mass_d.p, c.mass.data(), sizeof(double) * ntypes, cudaMemcpyHostToDevice, c.stream));
+  // dtfm = dtf / mass(type) (integrator_nve.cpp:43, 66): the same IEEE
+  // operations as the per-atom division, done once per type
+  std::vector<double> dtfm(static_cast<size_t>(ntypes));
+  const double dtf = 0.5 * dt / mvv2e;
+  for (int t = 0; t < ntypes; ++t) dtfm[size_t(t)] = dtf / mass[t];
+  c.dtfm_d.reserve(size_t(ntypes), c.stream);
+  EMD_CUDA(cudaMemcpyAsync(c.dtfm_d.p, dtfm.data(), sizeof(double) * ntypes, cudaMemcpyHostToDevice, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   EMD_API_END
 }
@@ -393,6 +416,8 @@ emd_status emd_system_set_local(emd_ctx* ctx, int n, const double* x, const doub
   // forces over all N_max rows
   EMD_CUDA(cudaMemsetAsync(c.f.p, 0, sizeof(double) * 3 * size_t(c.N_max), c.stream));
   if (n > 0 && f) EMD_CUDA(cudaMemcpyAsync(c.f.p, f, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c.stream));
+  c.f_zero_pending = 0;
+  c.xl_ok = 0;
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   EMD_API_END
 }
@@ -401,7 +426,9 @@ emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x
   EMD_API_BEGIN
   require(first >= 0 && count >= 0 && first + count <= c.N_local, EMD_ERR_ARG, "emd_system_update: range");
   if (count == 0) return EMD_OK;
+  if (f) materialize_zero(c, true, false);
   if (x) {
+    c.xl_ok &= ~1;
     c.stage_d.reserve(3 * size_t(count), c.stream);
     EMD_CUDA(cudaMemcpyAsync(c.stage_d.p, x, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
     TimedLaunch t(c, "system_pack_x");
@@ -419,6 +446,7 @@ emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double*
   const int total = c.N_local + c.N_ghost;
   require(first >= 0 && count >= 0 && first + count <= total, EMD_ERR_ARG, "emd_system_get: range");
   if (count == 0) return EMD_OK;
+  if (f) materialize_zero(c, first < c.N_local, first + count > c.N_local);
   if (x) {
     c.stage_d.reserve(3 * size_t(count), c.stream);
     TimedLaunch t(c, "system_unpack_x");
@@ -443,12 +471,12 @@ emd_status emd_system_info(emd_ctx* ctx, int* n_local, int* n_ghost, int* n_max)
   EMD_API_END
 }
 
+// Kokkos::deep_copy(system->f, 0.0): recorded, applied lazily -- a full-list
+// LJ pass overwrites every owned row anyway and folds the zero into its
+// stores; any other reader of f applies it first (materialize_zero).
 emd_status emd_zero_forces(emd_ctx* ctx) {
   EMD_API_BEGIN
-  if (c.N_max > 0) {
-    TimedLaunch t(c, "zero_forces");
-    EMD_CUDA(cudaMemsetAsync(c.f.p, 0, sizeof(double) * 3 * size_t(c.N_max), c.stream));
-  }
+  c.f_zero_pending = 3;
   EMD_API_END
 }
 

@@ -71,6 +71,8 @@ enum : unsigned {
   ST_BOUNDS = 1u << EMD_ERR_BOUNDS,
 };
 
+constexpr int kHostInts = 256;  // pinned integer read-back scratch per context
+
 struct LaunchTimer {
   struct Pending {
     cudaEvent_t a, b;
@@ -153,7 +155,12 @@ struct Ctx {
   float lj_single[3] = {0, 0, 0};
   double lj_single_cutsq_d = 0;
   DevBuf<double4_32a> bin_ctr;  // FP64 bin centre per particle (mixed form)
-  long long neigh_builds = 0, ctr_build = -1;
+  long long neigh_builds = 0;
+  int xl_ok = 0;  // xl == FP32(x - bin centre) holds for owned (1) / ghost (2) rows
+  // deep_copy(f, 0) not yet applied to owned (1) / ghost (2) rows; the full-list
+  // LJ kernels fold it into their stores, every other reader applies it first
+  int f_zero_pending = 0;
+  DevBuf<double> dtfm_d;  // dtf / mass per type (integrator_nve.cpp:66)
   DevBuf<double> red, red2;  // reduction partials
 
   // ---- SNAP (defined in snap.cu)
@@ -166,7 +173,7 @@ struct Ctx {
   LaunchTimer timer;
   double* h_scalar = nullptr;  // pinned scratch for read-backs
   long long* h_ll = nullptr;
-  int* h_int = nullptr;
+  int* h_int = nullptr;  // pinned, kHostInts entries
 };
 
 // Kernel timing: brackets a launch with events when enabled.
@@ -192,8 +199,14 @@ void exclusive_scan_int(Ctx& c, const int* d_in, int* d_out, int n, int* d_total
 // deterministic FP64 sum of n doubles (device) -> host value
 double device_sum(Ctx& c, const double* d_vals, int n);
 
-void set_status_check(Ctx& c);
 unsigned read_status(Ctx& c, bool clear);
+// applies a pending deep_copy(f, 0) to owned and/or ghost rows
+void materialize_zero(Ctx& c, bool locals, bool ghosts);
+// mixed-form hooks (lj_mixed.cu)
+bool mixed_xl_active(const Ctx& c);
+void lj_mixed_after_build(Ctx& c);
+void nve_initial_mixed(Ctx& c);
+void nve_final_mixed(Ctx& c);
 
 }  // namespace emd
 

@@ -1,6 +1,9 @@
 // IntegratorNVE (integrator_nve.cpp:41-121): velocity-Verlet half kick +
 // drift, and the final half kick.  Compiled with -fmad=false so every
-// multiply and add rounds exactly like the serial reference.
+// multiply and add rounds exactly like the serial reference; dtf / mass is
+// taken from a per-type table computed with the same IEEE division.  The
+// mixed-precision form dispatches to the fused-multiply-add kernels that also
+// maintain its FP32 bin-relative positions (lj_mixed.cu).
 #include "emd_device.cuh"
 #include "emd_internal.h"
 
@@ -10,10 +13,10 @@ namespace {
 // InitialIntegrateFunctor (integrator_nve.cpp:64-73)
 __global__ void __launch_bounds__(256) k_nve_initial(double4_32a* __restrict__ x4, double* __restrict__ v,
                                                      const double* __restrict__ f, const int* __restrict__ type,
-                                                     const double* __restrict__ mass, double dtf, double dtv, int n) {
+                                                     const double* __restrict__ dtfm_t, double dtv, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double dtfm = dtf / mass[type[i]];
+  const double dtfm = dtfm_t[type[i]];
   double vx = v[3 * i], vy = v[3 * i + 1], vz = v[3 * i + 2];
   vx += dtfm * f[3 * i];
   vy += dtfm * f[3 * i + 1];
@@ -30,11 +33,11 @@ __global__ void __launch_bounds__(256) k_nve_initial(double4_32a* __restrict__ x
 
 // FinalIntegrateFunctor (integrator_nve.cpp:105-111)
 __global__ void __launch_bounds__(256) k_nve_final(double* __restrict__ v, const double* __restrict__ f,
-                                                   const int* __restrict__ type, const double* __restrict__ mass,
-                                                   double dtf, int n) {
+                                                   const int* __restrict__ type, const double* __restrict__ dtfm_t,
+                                                   int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double dtfm = dtf / mass[type[i]];
+  const double dtfm = dtfm_t[type[i]];
   v[3 * i] += dtfm * f[3 * i];
   v[3 * i + 1] += dtfm * f[3 * i + 1];
   v[3 * i + 2] += dtfm * f[3 * i + 2];
@@ -50,21 +53,29 @@ extern "C" {
 emd_status emd_nve_initial(emd_ctx* ctx) {
   EMD_API_BEGIN
   if (c.N_local == 0) return EMD_OK;
-  const double dtv = c.dt;
-  const double dtf = 0.5 * c.dt / c.mvv2e;
+  materialize_zero(c, true, false);
+  if (c.lj_ready && c.lj_prec == EMD_PREC_MIXED) {
+    nve_initial_mixed(c);
+    return EMD_OK;
+  }
   TimedLaunch t(c, "nve_initial");
-  k_nve_initial<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p, c.mass_d.p, dtf,
-                                                                   dtv, c.N_local);
+  k_nve_initial<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.dt,
+                                                                   c.N_local);
   EMD_CHECK_LAUNCH();
+  c.xl_ok &= ~1;
   EMD_API_END
 }
 
 emd_status emd_nve_final(emd_ctx* ctx) {
   EMD_API_BEGIN
   if (c.N_local == 0) return EMD_OK;
-  const double dtf = 0.5 * c.dt / c.mvv2e;
+  materialize_zero(c, true, false);
+  if (c.lj_ready && c.lj_prec == EMD_PREC_MIXED) {
+    nve_final_mixed(c);
+    return EMD_OK;
+  }
   TimedLaunch t(c, "nve_final");
-  k_nve_final<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.v.p, c.f.p, c.type.p, c.mass_d.p, dtf, c.N_local);
+  k_nve_final<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.N_local);
   EMD_CHECK_LAUNCH();
   EMD_API_END
 }

@@ -23,8 +23,9 @@ struct LJParams {
 
 __device__ __forceinline__ int entry_j(int e, bool packed) { return packed ? (e >> 6) : e; }
 
-// TagFullNeigh (force_lj_neigh_impl.h:164-206)
-template <bool TWO_D>
+// TagFullNeigh (force_lj_neigh_impl.h:164-206).  ZERO folds the pending
+// deep_copy(f, 0) into the store as 0.0 + sum, the reference's exact result.
+template <bool TWO_D, bool ZERO>
 __global__ void __launch_bounds__(128) k_lj_full_fp64(const double4_32a* __restrict__ x4, double* __restrict__ f,
                                                       ListView L, LJParams P, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -54,9 +55,15 @@ __global__ void __launch_bounds__(128) k_lj_full_fp64(const double4_32a* __restr
       fzi += dz * fpair;
     }
   }
-  f[3 * i] += fxi;
-  f[3 * i + 1] += fyi;
-  f[3 * i + 2] += fzi;
+  if (ZERO) {
+    f[3 * i] = 0.0 + fxi;
+    f[3 * i + 1] = 0.0 + fyi;
+    f[3 * i + 2] = 0.0 + fzi;
+  } else {
+    f[3 * i] += fxi;
+    f[3 * i + 1] += fyi;
+    f[3 * i + 2] += fzi;
+  }
 }
 
 // TagHalfNeigh (force_lj_neigh_impl.h:211-254)
@@ -210,10 +217,18 @@ emd_status emd_lj_compute(emd_ctx* ctx) {
   const LJParams P = lj_params(c);
   const bool two_d = c.neigh_layout_2d;
   const int grid = blocks_for(n, 128);
+  if (c.lj_half) materialize_zero(c, true, true);
+  const bool zero = c.f_zero_pending & 1;
   TimedLaunch t(c, c.lj_half ? "lj_half_fp64" : "lj_full_fp64");
   if (!c.lj_half) {
-    if (two_d) k_lj_full_fp64<true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
-    else k_lj_full_fp64<false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    if (two_d) {
+      if (zero) k_lj_full_fp64<true, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      else k_lj_full_fp64<true, false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    } else {
+      if (zero) k_lj_full_fp64<false, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      else k_lj_full_fp64<false, false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    }
+    c.f_zero_pending &= ~1;
   } else {
     if (two_d) k_lj_half_fp64<true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
     else k_lj_half_fp64<false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);

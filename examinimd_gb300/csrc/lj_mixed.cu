@@ -1,16 +1,18 @@
 // ForceLJNeigh, mixed-precision form: FP32 pair arithmetic, FP64 positions,
-// FP64 per-atom force sums of Kahan-compensated FP32 partials.
+// FP64 per-atom force sums of Kahan-compensated FP32 partials, and the FP64
+// velocity-Verlet update (with fused multiply-adds) for this form.
 //
-// Each force pass first refreshes an FP32 copy of every position relative to
-// the centre of the bin the particle occupied when the list was built
-// (|xl| is half a bin plus the skin drift, so FP32 keeps ~1e-7 absolute).
-// List rows are column-major (entry k of row i at k*stride + i: one warp's
-// 32 rows load as one 128-byte line) and each packed entry carries the
-// per-dimension bin offset k = (bin_j - bin_i) + 1, so
-//   x_i - x_j = (xl_i - xl_j) + (1 - k) * w
-// is formed in FP32 from small numbers.  Pairs whose FP32 r^2 lies within
-// 1e-6 relative of the cutoff are re-tested with the FP64 positions, so the
-// set of interacting pairs equals the FP64 drop-in's.
+// Every particle keeps an FP32 copy of its position relative to the centre
+// of the bin it occupied when the list was built (xl; |xl| is half a bin plus
+// the skin drift, so FP32 keeps ~1e-7 absolute).  The copy is produced by the
+// binning pass at each list build, then updated by the integrator (owned
+// atoms) and the halo refresh (ghosts) in the same passes that move the FP64
+// positions.  List rows are column-major int4 granules (neigh_rows.cuh) and
+// each packed entry carries the per-dimension bin offset k = (bin_j - bin_i)
+// + 1, so x_i - x_j = (xl_i - xl_j) + (1 - k) w is formed in FP32 from small
+// numbers.  Pairs whose FP32 r^2 lies within 1e-6 relative of the cutoff are
+// re-tested with the FP64 positions, so the set of interacting pairs equals
+// the FP64 drop-in's.
 #include "emd_device.cuh"
 #include "emd_internal.h"
 #include "neigh_rows.cuh"
@@ -39,14 +41,51 @@ __global__ void __launch_bounds__(256) k_bin_centres(const int* __restrict__ abi
   ctr[a] = make_double4_32a(F.minx + (bx + 0.5) * F.wx, F.miny + (by + 0.5) * F.wy, F.minz + (bz + 0.5) * F.wz, 0.0);
 }
 
+__device__ __forceinline__ float4 rel(const double4_32a& p, const double4_32a& o) {
+  return make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(int(p.w)));
+}
+
 __global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restrict__ x4,
                                                     const double4_32a* __restrict__ ctr, int n,
                                                     float4* __restrict__ xl) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
-  const double4_32a p = x4[a];
-  const double4_32a o = ctr[a];
-  xl[a] = make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(int(p.w)));
+  xl[a] = rel(x4[a], ctr[a]);
+}
+
+// IntegratorNVE::initial_integrate (integrator_nve.cpp:64-73) with FMA, plus
+// the FP32 bin-relative copy of the new position
+__global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restrict__ x4, double* __restrict__ v,
+                                                           const double* __restrict__ f, const int* __restrict__ type,
+                                                           const double* __restrict__ dtfm_t, double dtv,
+                                                           const double4_32a* __restrict__ ctr,
+                                                           float4* __restrict__ xl, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dtfm = dtfm_t[type[i]];
+  const double vx = fma(dtfm, f[3 * i], v[3 * i]);
+  const double vy = fma(dtfm, f[3 * i + 1], v[3 * i + 1]);
+  const double vz = fma(dtfm, f[3 * i + 2], v[3 * i + 2]);
+  v[3 * i] = vx;
+  v[3 * i + 1] = vy;
+  v[3 * i + 2] = vz;
+  double4_32a p = x4[i];
+  p.x = fma(dtv, vx, p.x);
+  p.y = fma(dtv, vy, p.y);
+  p.z = fma(dtv, vz, p.z);
+  x4[i] = p;
+  if (xl) xl[i] = rel(p, ctr[i]);
+}
+
+__global__ void __launch_bounds__(256) k_nve_final_mixed(double* __restrict__ v, const double* __restrict__ f,
+                                                         const int* __restrict__ type,
+                                                         const double* __restrict__ dtfm_t, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dtfm = dtfm_t[type[i]];
+  v[3 * i] = fma(dtfm, f[3 * i], v[3 * i]);
+  v[3 * i + 1] = fma(dtfm, f[3 * i + 1], v[3 * i + 1]);
+  v[3 * i + 2] = fma(dtfm, f[3 * i + 2], v[3 * i + 2]);
 }
 
 struct LJParamsF {
@@ -69,10 +108,55 @@ __device__ __forceinline__ void kahan_add(float& s, float& comp, float v) {
 // (1 - k) * w for k in {0, 1, 2}
 __device__ __forceinline__ float bin_shift(int k, float w) { return k == 0 ? w : (k == 2 ? -w : 0.0f); }
 
+struct Acc {
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+};
+
 template <bool SINGLE>
+__device__ __forceinline__ void lj_pair(const float4& xi, int ti, int i, int e, const float4& xj,
+                                        const double4_32a* __restrict__ x4, const LJParamsF& P, float wx, float wy,
+                                        float wz, Acc& a) {
+  const float dx = (xi.x - xj.x) + bin_shift((e >> 4) & 3, wx);
+  const float dy = (xi.y - xj.y) + bin_shift((e >> 2) & 3, wy);
+  const float dz = (xi.z - xj.z) + bin_shift(e & 3, wz);
+  const float rsq = dx * dx + dy * dy + dz * dz;
+  float lj1, lj2, cutsq;
+  double cutsq_d;
+  if (SINGLE) {
+    lj1 = P.lj1_0;
+    lj2 = P.lj2_0;
+    cutsq = P.cutsq_0;
+    cutsq_d = P.cutsq_d0;
+  } else {
+    const int tp = ti * P.ntypes + __float_as_int(xj.w);
+    lj1 = __ldg(P.lj1 + tp);
+    lj2 = __ldg(P.lj2 + tp);
+    cutsq = __ldg(P.cutsq + tp);
+    cutsq_d = __ldg(P.cutsq_d + tp);
+  }
+  bool in = rsq < cutsq;
+  if (fabsf(rsq - cutsq) <= 1e-6f * cutsq) {
+    // borderline: decide exactly as the FP64 form does
+    const double4_32a pi = x4[i], pj = x4[e >> 6];
+    const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+    in = (ddx * ddx + ddy * ddy + ddz * ddz) < cutsq_d;
+  }
+  if (in) {
+    const float r2inv = __fdividef(1.0f, rsq);
+    const float r6inv = r2inv * r2inv * r2inv;
+    const float fpair = (r6inv * (lj1 * r6inv - lj2)) * r2inv;
+    kahan_add(a.sx, a.cx, dx * fpair);
+    kahan_add(a.sy, a.cy, dy * fpair);
+    kahan_add(a.sz, a.cz, dz * fpair);
+  }
+}
+
+// One thread per owned atom; four list entries per coalesced int4 load, the
+// next granule prefetched while the current four pairs are evaluated.
+template <bool SINGLE, bool ZERO>
 __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict__ xl,
                                                        const double4_32a* __restrict__ x4, double* __restrict__ f,
-                                                       const int* __restrict__ rows, int stride,
+                                                       const int4* __restrict__ rows4, int stride,
                                                        const int* __restrict__ num, LJParamsF P, float wx, float wy,
                                                        float wz, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,57 +164,44 @@ __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict_
   const float4 xi = xl[i];
   const int ti = __float_as_int(xi.w);
   const int cnt = num[i];
-  const int* row = rows + i;
-  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-#pragma unroll 2
-  for (int jj = 0; jj < cnt; ++jj) {
-    const int e = __ldg(row + (size_t)jj * stride);
-    const int j = e >> 6;
-    const float4 xj = xl[j];
-    const float dx = (xi.x - xj.x) + bin_shift((e >> 4) & 3, wx);
-    const float dy = (xi.y - xj.y) + bin_shift((e >> 2) & 3, wy);
-    const float dz = (xi.z - xj.z) + bin_shift(e & 3, wz);
-    const float rsq = dx * dx + dy * dy + dz * dz;
-    float lj1, lj2, cutsq;
-    double cutsq_d;
-    if (SINGLE) {
-      lj1 = P.lj1_0;
-      lj2 = P.lj2_0;
-      cutsq = P.cutsq_0;
-      cutsq_d = P.cutsq_d0;
-    } else {
-      const int tp = ti * P.ntypes + __float_as_int(xj.w);
-      lj1 = __ldg(P.lj1 + tp);
-      lj2 = __ldg(P.lj2 + tp);
-      cutsq = __ldg(P.cutsq + tp);
-      cutsq_d = __ldg(P.cutsq_d + tp);
-    }
-    bool in = rsq < cutsq;
-    if (fabsf(rsq - cutsq) <= 1e-6f * cutsq) {
-      // borderline: decide exactly as the FP64 form does
-      const double4_32a pi = x4[i], pj = x4[j];
-      const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
-      in = (ddx * ddx + ddy * ddy + ddz * ddz) < cutsq_d;
-    }
-    if (in) {
-      const float r2inv = __fdividef(1.0f, rsq);
-      const float r6inv = r2inv * r2inv * r2inv;
-      const float fpair = (r6inv * (lj1 * r6inv - lj2)) * r2inv;
-      kahan_add(sx, cx, dx * fpair);
-      kahan_add(sy, cy, dy * fpair);
-      kahan_add(sz, cz, dz * fpair);
-    }
+  const int4* q = rows4 + i;
+  const int nfull = cnt >> 2;
+  Acc acc;
+  int4 e = nfull > 0 ? __ldg(q) : make_int4(0, 0, 0, 0);
+  for (int kq = 0; kq < nfull; ++kq) {
+    const int4 en = (kq + 1 < nfull) ? __ldg(q + (size_t)(kq + 1) * stride) : e;
+    const float4 x0 = xl[e.x >> 6];
+    const float4 x1 = xl[e.y >> 6];
+    const float4 x2 = xl[e.z >> 6];
+    const float4 x3 = xl[e.w >> 6];
+    lj_pair<SINGLE>(xi, ti, i, e.x, x0, x4, P, wx, wy, wz, acc);
+    lj_pair<SINGLE>(xi, ti, i, e.y, x1, x4, P, wx, wy, wz, acc);
+    lj_pair<SINGLE>(xi, ti, i, e.z, x2, x4, P, wx, wy, wz, acc);
+    lj_pair<SINGLE>(xi, ti, i, e.w, x3, x4, P, wx, wy, wz, acc);
+    e = en;
   }
-  f[3 * i] += double(sx) - double(cx);
-  f[3 * i + 1] += double(sy) - double(cy);
-  f[3 * i + 2] += double(sz) - double(cz);
+  const int rem = cnt & 3;
+  if (rem) {
+    const int4 t = __ldg(q + (size_t)nfull * stride);
+    lj_pair<SINGLE>(xi, ti, i, t.x, xl[t.x >> 6], x4, P, wx, wy, wz, acc);
+    if (rem > 1) lj_pair<SINGLE>(xi, ti, i, t.y, xl[t.y >> 6], x4, P, wx, wy, wz, acc);
+    if (rem > 2) lj_pair<SINGLE>(xi, ti, i, t.z, xl[t.z >> 6], x4, P, wx, wy, wz, acc);
+  }
+  const double fx = double(acc.sx) - double(acc.cx);
+  const double fy = double(acc.sy) - double(acc.cy);
+  const double fz = double(acc.sz) - double(acc.cz);
+  if (ZERO) {  // the pending deep_copy(f, 0) folded into the store
+    f[3 * i] = 0.0 + fx;
+    f[3 * i + 1] = 0.0 + fy;
+    f[3 * i + 2] = 0.0 + fz;
+  } else {
+    f[3 * i] += fx;
+    f[3 * i + 1] += fy;
+    f[3 * i + 2] += fz;
+  }
 }
 
-}  // namespace
-
-void lj_mixed_compute(Ctx& c) {
-  const int n_all = c.N_local + c.N_ghost;
-  c.xl.reserve(size_t(n_all) + 1, c.stream);
+BinFrame frame(const Ctx& c) {
   BinFrame F;
   F.nby = c.nbin[1];
   F.nbz = c.nbin[2];
@@ -140,33 +211,75 @@ void lj_mixed_compute(Ctx& c) {
   F.wx = (c.bmax[0] - c.bmin[0]) / c.nbin[0];
   F.wy = (c.bmax[1] - c.bmin[1]) / c.nbin[1];
   F.wz = (c.bmax[2] - c.bmin[2]) / c.nbin[2];
-  if (c.ctr_build != c.neigh_builds) {
-    c.bin_ctr.reserve(size_t(n_all) + 1, c.stream);
-    TimedLaunch t(c, "lj_bin_centres");
-    k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, F, c.bin_ctr.p);
-    EMD_CHECK_LAUNCH();
-    c.ctr_build = c.neigh_builds;
-  }
-  {
+  return F;
+}
+
+}  // namespace
+
+void materialize_zero(Ctx& c, bool locals, bool ghosts);
+
+// After a packed list build: the binning's FP32 bin-relative positions are
+// exactly the copy the force reads; keep them and record the bin centres.
+void lj_mixed_after_build(Ctx& c) {
+  const int n_all = c.N_local + c.N_ghost;
+  std::swap(c.xl, c.xl_bin);
+  c.bin_ctr.reserve(size_t(n_all) + 1, c.stream);
+  TimedLaunch t(c, "lj_bin_centres");
+  k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, frame(c), c.bin_ctr.p);
+  EMD_CHECK_LAUNCH();
+  c.xl_ok = 3;
+}
+
+bool mixed_xl_active(const Ctx& c) {
+  return c.lj_ready && c.lj_prec == EMD_PREC_MIXED && c.neigh_ready && c.neigh_packed;
+}
+
+void nve_initial_mixed(Ctx& c) {
+  const bool live = mixed_xl_active(c);
+  TimedLaunch t(c, "nve_initial");
+  k_nve_initial_mixed<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(
+      c.x4.p, c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.dt, live ? c.bin_ctr.p : nullptr, live ? c.xl.p : nullptr,
+      c.N_local);
+  EMD_CHECK_LAUNCH();
+  if (!live) c.xl_ok &= ~1;
+}
+
+void nve_final_mixed(Ctx& c) {
+  TimedLaunch t(c, "nve_final");
+  k_nve_final_mixed<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.N_local);
+  EMD_CHECK_LAUNCH();
+}
+
+void lj_mixed_compute(Ctx& c) {
+  const int n_all = c.N_local + c.N_ghost;
+  const BinFrame F = frame(c);
+  if (c.xl_ok != 3) {
     TimedLaunch t(c, "lj_refresh_xl");
     k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, c.bin_ctr.p, n_all, c.xl.p);
     EMD_CHECK_LAUNCH();
+    c.xl_ok = 3;
   }
   const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
   LJParamsF P{c.lj_params_f.p, c.lj_params_f.p + nt2, c.lj_params_f.p + 2 * nt2, c.lj_params.p + 2 * nt2,
               c.lj_ntypes, c.lj_single[0], c.lj_single[1], c.lj_single[2], c.lj_single_cutsq_d};
   const ListView L = list_view(c);
+  const int4* rows4 = reinterpret_cast<const int4*>(L.entries);
   const int n = c.N_local;
-  TimedLaunch t(c, "lj_full_mixed");
-  if (c.lj_uniform)
-    k_lj_full_mixed<true><<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, L.entries, L.stride,
-                                                                    L.num_neighs, P, float(F.wx), float(F.wy),
-                                                                    float(F.wz), n);
-  else
-    k_lj_full_mixed<false><<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, L.entries, L.stride,
-                                                                     L.num_neighs, P, float(F.wx), float(F.wy),
-                                                                     float(F.wz), n);
-  EMD_CHECK_LAUNCH();
+  const bool zero = c.f_zero_pending & 1;
+  const dim3 g(blocks_for(n, 128)), b(128);
+  const float wx = float(F.wx), wy = float(F.wy), wz = float(F.wz);
+  {
+    TimedLaunch t(c, "lj_full_mixed");
+    if (c.lj_uniform) {
+      if (zero) k_lj_full_mixed<true, true><<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n);
+      else k_lj_full_mixed<true, false><<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n);
+    } else {
+      if (zero) k_lj_full_mixed<false, true><<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n);
+      else k_lj_full_mixed<false, false><<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n);
+    }
+    EMD_CHECK_LAUNCH();
+  }
+  c.f_zero_pending &= ~1;
 }
 
 void lj_mixed_prepare(Ctx& c) {

@@ -13,9 +13,10 @@
 // compacted with ballot + popc, so row i lists its neighbours in exactly the
 // order the serial reference appends them.
 //
-// One pass writes rows column-major (entry k of row i at k*stride + i, the
-// layout of the reference's Neighbor2D view on a GPU) with capacity K; the
-// host grows K like Neighbor2D's regrow loop (x1.2) when a row overflows.
+// One pass writes rows column-major in 16-byte granules (neigh_rows.cuh:
+// the LayoutLeft of the reference's Neighbor2D view on a GPU, four entries
+// per granule) with capacity K; the host grows K like Neighbor2D's regrow
+// loop (x1.2) when a row overflows.
 // NeighborCSR rows are then compacted behind an exclusive scan of the
 // counts.  Rows built for the mixed-precision force carry packed entries
 // (j << 6) | (kx << 4) | (ky << 2) | kz with k = (bin_j - bin_i) + 1 per
@@ -25,6 +26,7 @@
 
 #include "emd_device.cuh"
 #include "emd_internal.h"
+#include "neigh_rows.cuh"
 
 namespace emd {
 namespace {
@@ -32,6 +34,8 @@ namespace {
 constexpr int NB_THREADS = 128;
 constexpr int NB_WARPS = NB_THREADS / 32;
 constexpr int NB_CAP = 1024;  // staged candidates per chunk
+constexpr int NB_SLOTS = 64;  // spread slots for the longest-row reduction
+static_assert(1 + NB_SLOTS <= kHostInts, "read-back of the row-length slots exceeds the pinned scratch");
 
 struct NeighArgs {
   const double4_32a* x4;
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
         const unsigned bal = __ballot_sync(FULL_MASK, take);
         if (take) {
           const int pos = cnt + __popc(bal & lt);
-          if (pos < a.K) a.rows[(size_t)pos * a.stride + i] = w;
+          if (pos < a.K) a.rows[quad_index(i, pos, a.stride)] = w;
         }
         cnt += __popc(bal);
       }
@@ -156,13 +160,21 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
     }
     __syncthreads();
   }
-  // rows, overflow flag, longest row
+  // overflow flag and longest row: one atomic per CTA into one of 64 slots
+  // (a single shared address would serialise millions of atomics in L2)
+  int mx = 0;
   for (int bi = tid; bi < nc; bi += NB_THREADS) {
     const int i = a.permute[oc + bi];
-    if (i >= a.n_local) continue;
-    const int cnt = a.num_neighs[i];
-    if (cnt > a.K) a.flags[0] = 1;
-    atomicMax(&a.flags[1], cnt);
+    if (i < a.n_local) mx = max(mx, a.num_neighs[i]);
+  }
+  mx = __reduce_max_sync(FULL_MASK, mx);
+  __shared__ int wmax[NB_WARPS];
+  if (lane == 0) wmax[warp] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < NB_WARPS; ++w) mx = max(mx, wmax[w]);
+    if (mx > 0) atomicMax(&a.flags[1 + (blockIdx.x & (NB_SLOTS - 1))], mx);
+    if (mx > a.K) a.flags[0] = 1;
   }
 }
 
@@ -180,7 +192,7 @@ __global__ void __launch_bounds__(256) k_rows_to_csr(const int* __restrict__ row
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int m = num[i], o = offs[i];
-  for (int k = 0; k < m; ++k) out[o + k] = rows[(size_t)k * stride + i];
+  for (int k = 0; k < m; ++k) out[o + k] = rows[quad_index(i, k, stride)];
 }
 
 // packed entries -> plain j (for emd_neigh_get)
@@ -221,7 +233,7 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
           "emd_neigh_create: packed rows need fewer than 2^25 particles");
   c.num_neighs.reserve(size_t(n) + 1, c.stream);
   c.neigh_offsets.reserve(size_t(n) + 2, c.stream);
-  c.resize_flag.reserve(2, c.stream);
+  c.resize_flag.reserve(1 + NB_SLOTS, c.stream);
   NeighArgs a;
   a.x4 = c.x4.p;
   a.xl = c.xl_bin.p;
@@ -250,10 +262,10 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   int& K = two_d ? c.maxneighs : c.neigh_scratch_k;
   DevBuf<int>& rows = two_d ? c.neighs : c.neigh_rows2d;
   while (true) {
-    rows.reserve(size_t(n + 1) * size_t(K) + 1, c.stream);
+    rows.reserve(size_t(n + 1) * size_t((K + 3) & ~3) + 4, c.stream);
     a.rows = rows.p;
     a.K = K;
-    EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, 2 * sizeof(int), c.stream));
+    EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, (1 + NB_SLOTS) * sizeof(int), c.stream));
     if (n > 0) {
       {
         TimedLaunch t(c, "neigh_zero_rows");
@@ -266,9 +278,13 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
         EMD_CHECK_LAUNCH();
       }
     }
-    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, (1 + NB_SLOTS) * sizeof(int), cudaMemcpyDeviceToHost,
+                             c.stream));
     EMD_CUDA(cudaStreamSynchronize(c.stream));
-    c.neigh_maxrow = n > 0 ? c.h_int[1] : 0;
+    int longest = 0;
+    for (int k = 1; k <= NB_SLOTS; ++k) longest = std::max(longest, c.h_int[k]);
+    c.h_int[1] = longest;
+    c.neigh_maxrow = n > 0 ? longest : 0;
     if (!c.h_int[0]) break;
     // neighbor_2d.h:325-327: grow to 1.2x the longest row and redo
     K = int(c.h_int[1] * 1.2);
@@ -298,6 +314,7 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   c.neigh_ready = true;
   c.neigh_packed = packed;
   c.neigh_builds++;
+  if (packed) lj_mixed_after_build(c);
   // the force kernels read CSR (plain rows) or column-major rows
   c.neigh_layout_2d = two_d || packed;
   if (total_out) *total_out = total;

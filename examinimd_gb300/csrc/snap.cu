@@ -39,6 +39,13 @@ namespace {
 constexpr double MY_PI = 3.14159265358979323846;
 constexpr int SNAP_THREADS = 256;
 constexpr int SNAP_WARPS = SNAP_THREADS / 32;
+// per-neighbour scalar fields (structure of arrays, `cap` entries each)
+enum {
+  ND_AR_U, ND_AI_U, ND_BR_U, ND_BI_U,  // Cayley-Klein a, b of compute_uarray
+  ND_AR, ND_AI, ND_BR, ND_BI,          // a, b of compute_duarray
+  ND_DAR, ND_DAI = ND_DAR + 3, ND_DBR = ND_DAI + 3, ND_DBI = ND_DBR + 3, ND_UK = ND_DBI + 3,
+  ND_SFAC = ND_UK + 3, ND_DSFAC, ND_FP, ND_EP = ND_FP + 3, ND_FIELDS
+};
 
 struct SnapDev {
   int twojmax, L;         // L = twojmax + 1
@@ -238,7 +245,8 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   Cplx<R>* ytot = reinterpret_cast<Cplx<R>*>(rootpq_r + ((L1 * L1 + 1) & ~1));  // nyh
   int* in_j = reinterpret_cast<int*>(ytot + S.nyh);                           // cap
   double* red = reinterpret_cast<double*>(in_j + ((A.cap + 3) & ~3));          // 4*SNAP_WARPS
-  unsigned char* work = reinterpret_cast<unsigned char*>(red + 4 * SNAP_WARPS);
+  double* nd = red + 4 * SNAP_WARPS;                                           // ND_FIELDS*cap
+  unsigned char* work = reinterpret_cast<unsigned char*>(nd + ND_FIELDS * A.cap);
   __shared__ int s_ninside;
 
   for (int k = tid; k < L1 * L1; k += SNAP_THREADS) {
@@ -297,16 +305,66 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   __syncthreads();
   const int ninside = s_ninside;
 
-  // ---- B: U_tot (FP64)
-  for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
+  // ---- per-neighbour scalars, one thread per neighbour (every lane of a
+  // warp would otherwise repeat the FP64 transcendentals)
+  for (int nb = tid; nb < ninside; nb += SNAP_THREADS) {
     const double x = in_r[3 * nb], y = in_r[3 * nb + 1], z = in_r[3 * nb + 2];
+    const double rcut = in_rc[nb], wj = in_w[nb];
     const double rsq = x * x + y * y + z * z;
     const double r = sqrt(rsq);
-    const double theta0 = (r - S.rmin0) * S.rfac0 * MY_PI / (in_rc[nb] - S.rmin0);
-    const double z0 = r / tan(theta0);
+    double* q = nd + nb;
+    // compute_ui (sna_impl.hpp:174-187): a, b of compute_uarray
+    {
+      const double theta0 = (r - S.rmin0) * S.rfac0 * MY_PI / (rcut - S.rmin0);
+      const double z0 = r / tan(theta0);
+      const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
+      q[ND_AR_U * A.cap] = r0inv * z0;
+      q[ND_AI_U * A.cap] = -r0inv * z;
+      q[ND_BR_U * A.cap] = r0inv * y;
+      q[ND_BI_U * A.cap] = -r0inv * x;
+    }
+    // compute_duidrj + the prologue of compute_duarray (sna_impl.hpp:291-321, 729-778)
+    const double rscale0 = S.rfac0 * MY_PI / (rcut - S.rmin0);
+    const double theta0 = (r - S.rmin0) * rscale0;
+    const double cs = cos(theta0), sn = sin(theta0);
+    const double z0 = r * cs / sn;
+    const double dz0dr = z0 / r - (r * rscale0) * (rsq + z0 * z0) / rsq;
+    const double rinv = 1.0 / r;
+    const double uk[3] = {x * rinv, y * rinv, z * rinv};
     const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
-    const double ar = r0inv * z0, ai = -r0inv * z, br = r0inv * y, bi = -r0inv * x;
-    const double sfac = sfac_of(S, r, in_rc[nb]) * in_w[nb];
+    q[ND_AR * A.cap] = z0 * r0inv;
+    q[ND_AI * A.cap] = -z * r0inv;
+    q[ND_BR * A.cap] = y * r0inv;
+    q[ND_BI * A.cap] = -x * r0inv;
+    const double dr0invdr = -(r0inv * r0inv * r0inv) * (r + z0 * dz0dr);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double dr0inv = dr0invdr * uk[k];
+      const double dz0 = dz0dr * uk[k];
+      q[(ND_DAR + k) * A.cap] = dz0 * r0inv + z0 * dr0inv + 0.0;
+      q[(ND_DAI + k) * A.cap] = -z * dr0inv + (k == 2 ? -r0inv : 0.0);
+      q[(ND_DBR + k) * A.cap] = y * dr0inv + (k == 1 ? r0inv : 0.0);
+      q[(ND_DBI + k) * A.cap] = -x * dr0inv + (k == 0 ? -r0inv : 0.0);
+      q[(ND_UK + k) * A.cap] = uk[k];
+    }
+    q[ND_SFAC * A.cap] = sfac_of(S, r, rcut) * wj;
+    q[ND_DSFAC * A.cap] = dsfac_of(S, r, rcut) * wj;
+    // extra repulsion of the reference (force_snap_neigh_impl.h:705-711) and
+    // its energy 1.25e5 / r^12 per ordered pair
+    const double r2 = rsq * rsq, r4 = r2 * r2;
+    const double fdivr = -1.5e6 / (r4 * r2 * rsq);
+    q[ND_FP * A.cap] = x * fdivr;
+    q[(ND_FP + 1) * A.cap] = y * fdivr;
+    q[(ND_FP + 2) * A.cap] = z * fdivr;
+    q[ND_EP * A.cap] = 1.25e5 / (r4 * r2);
+  }
+  __syncthreads();
+
+  // ---- B: U_tot (FP64)
+  for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
+    const double ar = nd[ND_AR_U * A.cap + nb], ai = nd[ND_AI_U * A.cap + nb];
+    const double br = nd[ND_BR_U * A.cap + nb], bi = nd[ND_BI_U * A.cap + nb];
+    const double sfac = nd[ND_SFAC * A.cap + nb];
     if (lane == 0) {
       Pb[0] = Cplx<double>{1.0, 0.0};
       part[0].r += sfac * 1.0;
@@ -407,11 +465,7 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
       const Cplx<double> u = utot[uoff(j) + ma * (j + 1) + mb];
       acc += hw(j, ma, mb) * (u.r * double(ytot[e].r) + u.i * double(ytot[e].i));
     }
-    for (int nb = tid; nb < ninside; nb += SNAP_THREADS) {
-      const double rsq = in_r[3 * nb] * in_r[3 * nb] + in_r[3 * nb + 1] * in_r[3 * nb + 1] +
-                         in_r[3 * nb + 2] * in_r[3 * nb + 2];
-      acc += 1.25e5 / pow(rsq, 6.0) * 1.5;  // scaled by 2/3 below
-    }
+    for (int nb = tid; nb < ninside; nb += SNAP_THREADS) acc += nd[ND_EP * A.cap + nb] * 1.5;  // x 2/3 below
     const double t = block_sum(acc, red);
     if (tid == 0) A.eatom[i] = S.beta0[ei] + (2.0 / 3.0) * t;
     return;
@@ -421,46 +475,18 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
   double fix = 0, fiy = 0, fiz = 0;
   for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
-    const double x = in_r[3 * nb], y = in_r[3 * nb + 1], z = in_r[3 * nb + 2];
-    const double rcut = in_rc[nb], wj = in_w[nb];
-    // compute_duidrj (sna_impl.hpp:291-321) and the prologue of compute_duarray
-    const double rsq = x * x + y * y + z * z;
-    const double r = sqrt(rsq);
-    const double rscale0 = S.rfac0 * MY_PI / (rcut - S.rmin0);
-    const double theta0 = (r - S.rmin0) * rscale0;
-    const double cs = cos(theta0), sn = sin(theta0);
-    const double z0 = r * cs / sn;
-    const double dz0dr = z0 / r - (r * rscale0) * (rsq + z0 * z0) / rsq;
-    const double rinv = 1.0 / r;
-    const double uk[3] = {x * rinv, y * rinv, z * rinv};
-    const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
-    const double ar = z0 * r0inv, ai = -z * r0inv, br = y * r0inv, bi = -x * r0inv;
-    const double dr0invdr = -(r0inv * r0inv * r0inv) * (r + z0 * dz0dr);
-    double dar[3], dai[3], dbr[3], dbi[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const double dr0inv = dr0invdr * uk[k];
-      const double dz0 = dz0dr * uk[k];
-      dar[k] = dz0 * r0inv + z0 * dr0inv;
-      dai[k] = -z * dr0inv;
-      dbr[k] = y * dr0inv;
-      dbi[k] = -x * dr0inv;
-    }
-    dai[2] += -r0inv;
-    dbi[0] += -r0inv;
-    dbr[1] += r0inv;
-    const double sfac = sfac_of(S, r, rcut) * wj;
-    const double dsfac = dsfac_of(S, r, rcut) * wj;
-    const R Rar = R(ar), Rai = R(ai), Rbr = R(br), Rbi = R(bi);
+    const double* q = nd + nb;
+    const R Rar = R(q[ND_AR * A.cap]), Rai = R(q[ND_AI * A.cap]), Rbr = R(q[ND_BR * A.cap]), Rbi = R(q[ND_BI * A.cap]);
     R Rdar[3], Rdai[3], Rdbr[3], Rdbi[3], Ruk[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      Rdar[k] = R(dar[k]);
-      Rdai[k] = R(dai[k]);
-      Rdbr[k] = R(dbr[k]);
-      Rdbi[k] = R(dbi[k]);
-      Ruk[k] = R(uk[k]);
+      Rdar[k] = R(q[(ND_DAR + k) * A.cap]);
+      Rdai[k] = R(q[(ND_DAI + k) * A.cap]);
+      Rdbr[k] = R(q[(ND_DBR + k) * A.cap]);
+      Rdbi[k] = R(q[(ND_DBI + k) * A.cap]);
+      Ruk[k] = R(q[(ND_UK + k) * A.cap]);
     }
+    const double sfac = q[ND_SFAC * A.cap], dsfac = q[ND_DSFAC * A.cap];
     const R Rsfac = R(sfac), Rdsfac = R(dsfac);
     Cplx<R>* P = wd;
     Cplx<R>* C = wd + L2;
@@ -509,11 +535,9 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
     }
     double Fx = warp_sum(double(fx)), Fy = warp_sum(double(fy)), Fz = warp_sum(double(fz));
     if (lane == 0) {
-      // extra repulsion of the reference (force_snap_neigh_impl.h:705-711)
-      const double fdivr = -1.5e6 / pow(rsq, 7.0);
-      Fx += x * fdivr;
-      Fy += y * fdivr;
-      Fz += z * fdivr;
+      Fx += q[ND_FP * A.cap];
+      Fy += q[(ND_FP + 1) * A.cap];
+      Fz += q[(ND_FP + 2) * A.cap];
       const int j = in_j[nb];
       atomicAdd(A.f + 3 * j, -Fx);
       atomicAdd(A.f + 3 * j + 1, -Fy);
@@ -577,6 +601,7 @@ size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes) {
   b += 2 * size_t(real_bytes) * size_t(S.nyh);           // ytot
   b += sizeof(int) * size_t((cap + 3) & ~3);             // inside j
   b += sizeof(double) * 4 * SNAP_WARPS;                  // reductions
+  b += sizeof(double) * ND_FIELDS * size_t(cap);         // per-neighbour scalars
   const size_t wB = 2 * sizeof(double) * size_t(SNAP_WARPS) * (2 * L2 + S.nyh);
   const size_t wC = 2 * size_t(real_bytes) * size_t(S.njobs);
   const size_t wD = 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 8 * L2;
@@ -615,6 +640,7 @@ static void snap_launch(Ctx& c, bool energy) {
   require(!c.neigh_packed, EMD_ERR_STATE, "SNAP reads plain neighbour rows");
   const int n = c.N_local;
   if (n == 0) return;
+  if (!energy) materialize_zero(c, true, true);
   SnapArgs A;
   A.S = h->d;
   A.x4 = c.x4.p;

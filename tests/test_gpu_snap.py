@@ -21,8 +21,10 @@ def _ctx():
     return Context(0)
 
 
-def _max_rel(a, b):
-    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+def _max_rel(a, b, floor=1.0):
+    """max |a-b| over max(|b|, floor): forces on a perfect lattice cancel to
+    ~1e-15, so errors are measured against a 1 eV/A force scale floor."""
+    return np.abs(a - b).max() / max(np.abs(b).max(), floor)
 
 
 def _snap_setup(golden, nx=None, ny=None, nz=None, lattice_style=0, a=3.1803):
@@ -56,8 +58,9 @@ def test_snap_modules_vs_oracle(golden):
     assert abs(eg - eo) <= 1e-11 * abs(eo)
 
 
-def test_snap_driver_vs_reference_dumps(golden, tmp_path):
+def test_snap_driver_vs_reference_dumps(golden, tmp_path, monkeypatch):
     from examinimd_gb300 import MD
+    monkeypatch.chdir(tmp_path)  # the deck names its SNAP files relative to the working directory
     g = golden("snap_W_sc")
     case = CASES["snap_W_sc"]
     deck, args = write_case(case, str(tmp_path), mdloop.golden_snap(g))
