@@ -55,6 +55,16 @@ struct NeighArgs {
   int* flags;  // [0] overflow, [1] longest row
 };
 
+// Exact FP64 re-test of a pair whose FP32 r^2 fell inside the guard band.
+// Kept out of line: inlined, the compiler predicates it into the candidate
+// loop and every batch of 32 candidates then issues its FP64 instructions
+// (64 cycles each on this part) whether or not a lane needs them.
+__device__ __noinline__ bool retest_fp64(const double4_32a* __restrict__ x4, int i, int j, double cutsq) {
+  const double4_32a pi = x4[i], pj = x4[j];
+  const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+  return (ddx * ddx + ddy * ddy + ddz * ddz) <= cutsq;
+}
+
 // monotone integer key of a double (exact ordering, integer pipe)
 __device__ __forceinline__ long long okey(double v) {
   const long long b = __double_as_longlong(v);
@@ -134,18 +144,11 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
             const bool above = (jx > kx) || ((jx == kx) && ((jy > ky) || ((jy == ky) && (jz > kz))));
             const bool skip = ((j == i) || (j < a.n_local || a.newton)) && !above;
             if (!skip) {
-              if (!decided) {
-                const double ddx = xd.x - xj.x, ddy = xd.y - xj.y, ddz = xd.z - xj.z;
-                in = (ddx * ddx + ddy * ddy + ddz * ddz) <= a.cutsq;
-              }
+              if (!decided) in = retest_fp64(a.x4, i, j, a.cutsq);
               take = in;
             }
           } else {
-            if (!decided) {
-              const double4_32a pi = a.x4[i], pj = a.x4[j];
-              const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
-              in = (ddx * ddx + ddy * ddy + ddz * ddz) <= a.cutsq;
-            }
+            if (!decided) in = retest_fp64(a.x4, i, j, a.cutsq);
             take = in && (i != j);
           }
         }

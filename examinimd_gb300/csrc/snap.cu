@@ -101,6 +101,19 @@ __device__ __forceinline__ double hw(int j, int ma, int mb) {
   return 0.0;
 }
 
+template <typename R>
+__device__ __forceinline__ R warp_sum_r(R v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL_MASK, v, o);
+  return v;
+}
+
+// twice that weight, in the contraction type
+template <typename R>
+__device__ __forceinline__ R hw2(int j, int ma, int mb) {
+  return (2 * mb < j || 2 * ma < j) ? R(2) : (2 * ma == j ? R(1) : R(0));
+}
+
 __device__ __forceinline__ double sfac_of(const SnapDev& S, double r, double rcut) {
   if (S.switchflag == 0) return 1.0;
   if (r <= S.rmin0) return 1.0;
@@ -243,10 +256,18 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   Cplx<double>* utot = reinterpret_cast<Cplx<double>*>(in_rc + A.cap);  // nuf
   R* rootpq_r = reinterpret_cast<R*>(utot + S.nuf);                     // L1*L1
   Cplx<R>* ytot = reinterpret_cast<Cplx<R>*>(rootpq_r + ((L1 * L1 + 1) & ~1));  // nyh
-  int* in_j = reinterpret_cast<int*>(ytot + S.nyh);                           // cap
+  // U_tot in the contraction type: the FP64 array itself, or an FP32 copy
+  // made once per atom (converting inside the Z loops would put an FP64-pipe
+  // conversion on every Clebsch-Gordan term)
+  constexpr bool kF64 = sizeof(R) == sizeof(double);
+  Cplx<R>* utot_r = kF64 ? reinterpret_cast<Cplx<R>*>(utot) : ytot + S.nyh;      // nuf
+  int* in_j = reinterpret_cast<int*>(kF64 ? ytot + S.nyh : utot_r + S.nuf);     // cap
   double* red = reinterpret_cast<double*>(in_j + ((A.cap + 3) & ~3));          // 4*SNAP_WARPS
   double* nd = red + 4 * SNAP_WARPS;                                           // ND_FIELDS*cap
-  unsigned char* work = reinterpret_cast<unsigned char*>(nd + ND_FIELDS * A.cap);
+  // the per-neighbour scalars in the contraction type (FP32 copy made once)
+  R* ndr = kF64 ? reinterpret_cast<R*>(nd) : reinterpret_cast<R*>(nd + ND_FIELDS * A.cap);
+  unsigned char* work = reinterpret_cast<unsigned char*>(kF64 ? nd + ND_FIELDS * A.cap
+                                                              : nd + ND_FIELDS * A.cap + (ND_FIELDS * A.cap + 1) / 2);
   __shared__ int s_ninside;
 
   for (int k = tid; k < L1 * L1; k += SNAP_THREADS) {
@@ -359,6 +380,9 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
     q[ND_EP * A.cap] = 1.25e5 / (r4 * r2);
   }
   __syncthreads();
+  if (!kF64) {
+    for (int k = tid; k < ND_FIELDS * A.cap; k += SNAP_THREADS) ndr[k] = R(nd[k]);
+  }
 
   // ---- B: U_tot (FP64)
   for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
@@ -402,9 +426,12 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
     }
     const int uo = uoff(j);
     utot[uo + ma * (j + 1) + mb] = Cplx<double>{sr, si};
+    if (!kF64) utot_r[uo + ma * (j + 1) + mb] = Cplx<R>{R(sr), R(si)};
     if (2 * mb < j || 2 * ma < j) {
       const bool even = ((ma + mb) & 1) == 0;
-      utot[uo + (j - ma) * (j + 1) + (j - mb)] = even ? Cplx<double>{sr, -si} : Cplx<double>{-sr, si};
+      const int t = uo + (j - ma) * (j + 1) + (j - mb);
+      utot[t] = even ? Cplx<double>{sr, -si} : Cplx<double>{-sr, si};
+      if (!kF64) utot_r[t] = even ? Cplx<R>{R(sr), R(-si)} : Cplx<R>{R(-sr), R(si)};
     }
   }
   __syncthreads();
@@ -417,8 +444,8 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
     const int t = code >> 8, ma = (code >> 4) & 15, mb = code & 15;
     const int j1 = S.trip[3 * t], j2 = S.trip[3 * t + 1], j = S.trip[3 * t + 2];
     const R* cgt = cg + S.cg_off[t];
-    const Cplx<double>* U1 = utot + uoff(j1);
-    const Cplx<double>* U2 = utot + uoff(j2);
+    const Cplx<R>* U1 = utot_r + uoff(j1);
+    const Cplx<R>* U2 = utot_r + uoff(j2);
     R zr = 0, zi = 0;
     const int ma1lo = max(0, (2 * ma - j - j2 + j1) / 2), ma1hi = min(j1, (2 * ma - j + j2 + j1) / 2);
     const int mb1lo = max(0, (2 * mb - j - j2 + j1) / 2), mb1hi = min(j1, (2 * mb - j + j2 + j1) / 2);
@@ -428,11 +455,10 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
       for (int mb1 = mb1lo; mb1 <= mb1hi; ++mb1) {
         const int mb2 = (2 * mb - j - (2 * mb1 - j1) + j2) / 2;
         const R cga = cgt[mb1 * (j2 + 1) + mb2];
-        const Cplx<double> a = U1[ma1 * (j1 + 1) + mb1];
-        const Cplx<double> b = U2[ma2 * (j2 + 1) + mb2];
-        const R a_r = R(a.r), a_i = R(a.i), b_r = R(b.r), b_i = R(b.i);
-        sr += cga * (a_r * b_r - a_i * b_i);
-        si += cga * (a_r * b_i + a_i * b_r);
+        const Cplx<R> a = U1[ma1 * (j1 + 1) + mb1];
+        const Cplx<R> b = U2[ma2 * (j2 + 1) + mb2];
+        sr += cga * (a.r * b.r - a.i * b.i);
+        si += cga * (a.r * b.i + a.i * b.r);
       }
       const R cga = cgt[ma1 * (j2 + 1) + ma2];
       zr += sr * cga;
@@ -476,18 +502,18 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   double fix = 0, fiy = 0, fiz = 0;
   for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
     const double* q = nd + nb;
-    const R Rar = R(q[ND_AR * A.cap]), Rai = R(q[ND_AI * A.cap]), Rbr = R(q[ND_BR * A.cap]), Rbi = R(q[ND_BI * A.cap]);
+    const R* qr = ndr + nb;
+    const R Rar = qr[ND_AR * A.cap], Rai = qr[ND_AI * A.cap], Rbr = qr[ND_BR * A.cap], Rbi = qr[ND_BI * A.cap];
     R Rdar[3], Rdai[3], Rdbr[3], Rdbi[3], Ruk[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      Rdar[k] = R(q[(ND_DAR + k) * A.cap]);
-      Rdai[k] = R(q[(ND_DAI + k) * A.cap]);
-      Rdbr[k] = R(q[(ND_DBR + k) * A.cap]);
-      Rdbi[k] = R(q[(ND_DBI + k) * A.cap]);
-      Ruk[k] = R(q[(ND_UK + k) * A.cap]);
+      Rdar[k] = qr[(ND_DAR + k) * A.cap];
+      Rdai[k] = qr[(ND_DAI + k) * A.cap];
+      Rdbr[k] = qr[(ND_DBR + k) * A.cap];
+      Rdbi[k] = qr[(ND_DBI + k) * A.cap];
+      Ruk[k] = qr[(ND_UK + k) * A.cap];
     }
-    const double sfac = q[ND_SFAC * A.cap], dsfac = q[ND_DSFAC * A.cap];
-    const R Rsfac = R(sfac), Rdsfac = R(dsfac);
+    const R Rsfac = qr[ND_SFAC * A.cap], Rdsfac = qr[ND_DSFAC * A.cap];
     Cplx<R>* P = wd;
     Cplx<R>* C = wd + L2;
     Cplx<R>* dP = wd + 2 * L2;
@@ -508,7 +534,7 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
       const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j);
       for (int e = lane; e < nh; e += 32) {
         const int mb = e / (j + 1), ma = e % (j + 1);
-        const R w = R(2.0 * hw(j, ma, mb));
+        const R w = hw2<R>(j, ma, mb);
         if (w == R(0)) continue;
         const int o = ma * (j + 1) + mb;
         const Cplx<R> u = C[o];
@@ -533,7 +559,9 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
       dP = dC;
       dC = t;
     }
-    double Fx = warp_sum(double(fx)), Fy = warp_sum(double(fy)), Fz = warp_sum(double(fz));
+    // the pair force summed over the lanes in the contraction type (an FP64
+    // shuffle tree would cost more FP64-pipe time than the FP32 layers)
+    double Fx = double(warp_sum_r(fx)), Fy = double(warp_sum_r(fy)), Fz = double(warp_sum_r(fz));
     if (lane == 0) {
       Fx += q[ND_FP * A.cap];
       Fy += q[(ND_FP + 1) * A.cap];
@@ -599,9 +627,11 @@ size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes) {
   b += 2 * sizeof(double) * size_t(S.nuf);               // utot
   b += size_t(real_bytes) * size_t((L1 * L1 + 1) & ~1);  // rootpq (R)
   b += 2 * size_t(real_bytes) * size_t(S.nyh);           // ytot
+  if (real_bytes != int(sizeof(double))) b += 2 * size_t(real_bytes) * size_t(S.nuf);  // FP32 U_tot
   b += sizeof(int) * size_t((cap + 3) & ~3);             // inside j
   b += sizeof(double) * 4 * SNAP_WARPS;                  // reductions
   b += sizeof(double) * ND_FIELDS * size_t(cap);         // per-neighbour scalars
+  if (real_bytes != int(sizeof(double))) b += sizeof(double) * ((ND_FIELDS * size_t(cap) + 1) / 2);  // FP32 copy
   const size_t wB = 2 * sizeof(double) * size_t(SNAP_WARPS) * (2 * L2 + S.nyh);
   const size_t wC = 2 * size_t(real_bytes) * size_t(S.njobs);
   const size_t wD = 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 8 * L2;
