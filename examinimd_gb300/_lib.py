@@ -9,6 +9,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 EMD_PREC_FP64, EMD_PREC_MIXED = 0, 1
 EMD_NEIGH_CSR, EMD_NEIGH_2D = 0, 1
+EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL = 4194304  # include/emd_gpu.h
 
 _lib = None
 
@@ -61,6 +62,7 @@ _SIGS = {
     "emd_lj_init": ([_P, _I, _DP, _DP, _DP, _I, _I], _I),
     "emd_lj_compute": ([_P], _I),
     "emd_lj_energy": ([_P, _DP], _I),
+    "emd_lj_energy_noalloc": ([_P, _DP], _I),
     "emd_snap_init": ([_P, _I, _D, _D, _I, _D, _I, _DP, _DP, _DP, _I, _I, _IP, _I], _I),
     "emd_snap_compute": ([_P], _I),
     "emd_snap_energy": ([_P, _DP], _I),
@@ -277,6 +279,12 @@ class Context:
     def lj_energy(self) -> float:
         e = _D()
         self._ok(self.lib.emd_lj_energy(self.h, C.byref(e)), "emd_lj_energy")
+        return e.value
+
+    def lj_energy_noalloc(self) -> float:
+        """emd_lj_energy_noalloc: the same energy, no device allocation."""
+        e = _D()
+        self._ok(self.lib.emd_lj_energy_noalloc(self.h, C.byref(e)), "emd_lj_energy_noalloc")
         return e.value
 
     def snap_init(self, twojmax, rfac0, rmin0, switchflag, rcutfac, radelem, wjelem, beta, type_map,

@@ -176,6 +176,15 @@ double device_sum(Ctx& c, const double* d_vals, int n) {
   return *c.h_scalar;
 }
 
+static_assert(kSumScratchDoubles == SUM_BLOCKS + 1, "scratch of device_sum_launch");
+
+void device_sum_launch(Ctx& c, const double* d_vals, int n, double* scratch) {
+  k_sum_partial<<<SUM_BLOCKS, SUM_THREADS, 0, c.stream>>>(d_vals, n, scratch);
+  EMD_CHECK_LAUNCH();
+  k_sum_final<<<1, SUM_THREADS, 0, c.stream>>>(scratch, SUM_BLOCKS, scratch + SUM_BLOCKS);
+  EMD_CHECK_LAUNCH();
+}
+
 void materialize_zero(Ctx& c, bool locals, bool ghosts) {
   const int want = (locals ? 1 : 0) | (ghosts ? 2 : 0);
   const int todo = c.f_zero_pending & want;

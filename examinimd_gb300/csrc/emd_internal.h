@@ -198,6 +198,11 @@ inline int blocks_for(long long n, int threads) {
 void exclusive_scan_int(Ctx& c, const int* d_in, int* d_out, int n, int* d_total);
 // deterministic FP64 sum of n doubles (device) -> host value
 double device_sum(Ctx& c, const double* d_vals, int n);
+// the same two reduction kernels on caller-provided device scratch of
+// kSumScratchDoubles doubles; the sum lands in its last element.  Launches
+// only: no allocation, no read-back, no timing events.
+constexpr int kSumScratchDoubles = 305;
+void device_sum_launch(Ctx& c, const double* d_vals, int n, double* scratch);
 
 unsigned read_status(Ctx& c, bool clear);
 // applies a pending deep_copy(f, 0) to owned and/or ghost rows

@@ -7,6 +7,8 @@
 // reference's Atomic-trait view does on a GPU); the order of those adds is
 // not fixed, so half-list forces agree to rounding only.
 // Energy: per-atom shifted-LJ sums, deterministic block + device reduction.
+#include <mutex>
+
 #include "emd_device.cuh"
 #include "emd_internal.h"
 #include "neigh_rows.cuh"
@@ -168,6 +170,40 @@ static LJParams lj_params(Ctx& c) {
   return LJParams{c.lj_params.p, c.lj_params.p + nt2, c.lj_params.p + 2 * nt2, c.lj_ntypes};
 }
 
+// ---- scratch of emd_lj_energy_noalloc
+// Some callers cannot let a library call allocate device memory: a host whose
+// own pool allocator already holds the device's free memory (a cudaMalloc
+// would fail or fragment it), or a latency-bound loop that must not meet the
+// device-wide synchronisation a cudaFree implies.  For them the energy
+// reduction runs on a fixed array compiled into this library: one partial per
+// 256-atom block of k_lj_energy, then the deterministic two-stage sum.
+// Nothing in it has to start at zero: every element a call reads was written
+// earlier in that same call.  The array is one per device and per process, so
+// calls that can overlap on one device (two contexts, two host threads, two
+// streams) race on it and must be serialised by the caller.
+constexpr int kNoAllocBlocks = EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL / 256;  // 16,384 partials
+static_assert(kNoAllocBlocks * 256 == EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL, "whole blocks");
+constexpr int kNoAllocDoubles = kNoAllocBlocks + kSumScratchDoubles;  // 133,512 bytes
+static __device__ __align__(256) double g_lj_energy_scratch[kNoAllocDoubles];
+
+// device address of the array per device, looked up on the first call made
+// with that device current
+constexpr int kNoAllocMaxDevices = 64;
+static double* g_lj_energy_scratch_ptr[kNoAllocMaxDevices];
+static std::mutex g_lj_energy_scratch_mu;
+
+static double* lj_energy_scratch(int device) {
+  require(device >= 0 && device < kNoAllocMaxDevices, EMD_ERR_ARG,
+          "emd_lj_energy_noalloc: device ordinal beyond the 64 this library tracks");
+  std::lock_guard<std::mutex> lock(g_lj_energy_scratch_mu);
+  if (!g_lj_energy_scratch_ptr[device]) {
+    void* p = nullptr;
+    EMD_CUDA(cudaGetSymbolAddress(&p, g_lj_energy_scratch));
+    g_lj_energy_scratch_ptr[device] = static_cast<double*>(p);
+  }
+  return g_lj_energy_scratch_ptr[device];
+}
+
 }  // namespace emd
 
 using namespace emd;
@@ -259,6 +295,41 @@ emd_status emd_lj_energy(emd_ctx* ctx, double* pe) {
     EMD_CHECK_LAUNCH();
   }
   *pe = device_sum(c, c.red2.p, grid);
+  EMD_API_END
+}
+
+emd_status emd_lj_energy_noalloc(emd_ctx* ctx, double* pe) {
+  EMD_API_BEGIN
+  require(pe != nullptr, EMD_ERR_ARG, "emd_lj_energy_noalloc: null output");
+  require(c.N_local <= EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL, EMD_ERR_ARG,
+          "emd_lj_energy_noalloc: more than 4,194,304 owned atoms, the limit of its fixed scratch "
+          "(16,384 block partials); use emd_lj_energy");
+  require(c.lj_ready && c.neigh_ready && c.neigh_rows == c.N_local, EMD_ERR_STATE,
+          "emd_lj_energy_noalloc: not ready");
+  int cur = -1;
+  EMD_CUDA(cudaGetDevice(&cur));
+  require(cur == c.device, EMD_ERR_STATE, "emd_lj_energy_noalloc: the context's device must be current");
+  double* scratch = lj_energy_scratch(cur);
+  const int n = c.N_local;
+  if (n == 0) {
+    *pe = 0.0;
+    return EMD_OK;
+  }
+  // the kernels and partition of emd_lj_energy, so both return the same bits
+  const int grid = blocks_for(n, 256);
+  const ListView L = list_view(c);
+  const LJParams P = lj_params(c);
+  if (c.neigh_layout_2d)
+    k_lj_energy<true><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, scratch);
+  else
+    k_lj_energy<false><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, scratch);
+  EMD_CHECK_LAUNCH();
+  double* sum = scratch + kNoAllocBlocks;
+  device_sum_launch(c, scratch, grid, sum);
+  EMD_CUDA(cudaMemcpyAsync(c.h_scalar, sum + kSumScratchDoubles - 1, sizeof(double), cudaMemcpyDeviceToHost,
+                           c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  *pe = *c.h_scalar;
   EMD_API_END
 }
 

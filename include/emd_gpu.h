@@ -141,6 +141,22 @@ emd_status emd_lj_compute(emd_ctx* ctx);
 /* compute_energy(): shifted LJ potential energy (force_lj_neigh_impl.h:129-156, 259-343). */
 emd_status emd_lj_energy(emd_ctx* ctx, double* pe);
 
+/* emd_lj_energy without any device allocation; no counterpart in the
+ * reference.  For callers that must not let a library call allocate device
+ * memory (their own pool allocator holds the free memory, or the loop cannot
+ * take the device-wide synchronisation of a cudaFree).  Same kernels and
+ * summation order as emd_lj_energy, so the same result, with the reduction
+ * scratch in a fixed 133,512-byte array inside the library.
+ * - The context's device must be current.  The first call on a device looks
+ *   up the array's address (cudaGetSymbolAddress) and keeps it; make that
+ *   first call before a stream capture if the call is to be captured.
+ * - More than EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL owned atoms: EMD_ERR_ARG.
+ * - Nothing has to be zeroed beforehand.
+ * - One array per device and process: calls that can overlap on a device
+ *   (two contexts, threads or streams) race and must be serialised. */
+#define EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL 4194304
+emd_status emd_lj_energy_noalloc(emd_ctx* ctx, double* pe);
+
 /* ----------------------------------------------------- Force SNAP
  * ForceSNAP::init_coeff / compute (force_snap_neigh_impl.h:160-336,
  * 591-724) and SNA (sna_impl.hpp).  beta: nelem x ncoeffall row-major
