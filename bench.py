@@ -1,7 +1,7 @@
 """Benchmark of the GB300 ExaMiniMD hot path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload lj4m|lj32k] [--precision mixed|fp64]
+                    [--workload lj4m|lj32k|snapw] [--precision mixed|fp64]
 
 Metric: atom-steps/s (ExaMiniMD's own definition, N * nsteps / time,
 examinimd.cpp:286-289).  A step is one MD timestep of the full hot path --
@@ -30,6 +30,13 @@ reference has no Gaussian option).  Synthetic input generated in-process.
 * cpu_baseline: the CPU oracle (a restatement of ExaMiniMD's serial
   algorithm, OpenMP over atoms) on this host's cores, a bounded sample of
   the same workload.
+* accuracy (mixed form, after the timed region): forces of the final state
+  against the FP64 drop-in on the same positions (RMS and max |dF| over the
+  RMS force), and the NVE total-energy drift of both forms over
+  --drift-steps further steps, per 1000 steps.
+* snap_w: the SNAP-W workload (bcc tungsten, 128,000 atoms, 2J = 8) through
+  the same driver in both forms, device-timed, with the mixed-form force
+  error at step 0.
 """
 from __future__ import annotations
 
@@ -51,8 +58,48 @@ WORKLOADS = {
                                  "rebuild every 20, CSR full list, NVE dt 0.005"),
     "lj32k": dict(cells=20, desc="LJ-32k: fcc rho*=0.8442 20^3 cells = 32,000 atoms, rc 2.5, skin 0.3, "
                                  "rebuild every 20, CSR full list, NVE dt 0.005"),
+    "snapw": dict(cells=40, desc="SNAP-W: bcc W a=3.1803 A, 40^3 cells = 128,000 atoms, twojmax 8, synthetic "
+                                 "coefficients (seed 20261203), 300 K, dt 0.5 fs, rebuild every step, full list"),
 }
 METRIC = "atom-steps/s"
+
+SNAP_DESC = ("SNAP-W: bcc W a=3.1803 A, 40^3 cells = 128,000 atoms, metal units, mass 183.84, twojmax 8, rcutfac "
+             "4.73442, rfac0 0.99363, rmin0 0, 56 coefficients (beta0 = -8, beta1..55 ~ N(0, 0.1), seed 20261203), "
+             "300 K loop-geom velocities, dt 0.5 fs, newton on, skin 1.0, neighbour rebuild every step, full list")
+
+
+def snap_files(work: str) -> tuple[str, str]:
+    """Synthetic tungsten coefficient file and the shipped W.snapparam values."""
+    import numpy as np
+    beta = np.concatenate([[-8.0], np.random.default_rng(20261203).normal(0.0, 0.1, 55)])
+    coeff, param = os.path.join(work, "W.synth.snapcoeff"), os.path.join(work, "W.snapparam")
+    with open(coeff, "w") as fp:
+        fp.write("1 56\nW 0.5 1\n" + "".join(f"{float(b)!r}\n" for b in beta))
+    with open(param, "w") as fp:
+        fp.write("rcutfac 4.73442\ntwojmax 8\nrfac0 0.99363\nrmin0 0\ndiagonalstyle 3\nbzeroflag 0\n"
+                 "quadraticflag 0\n")
+    return coeff, param
+
+
+def snap_deck_text(cells: int, steps: int, coeff: str, param: str) -> str:
+    return f"""units metal
+timestep 0.0005
+atom_style atomic
+newton on
+lattice bcc 3.1803
+region box block 0 {cells} 0 {cells} 0 {cells}
+create_box 1 box
+create_atoms 1 box
+mass 1 183.84
+pair_style snap
+pair_coeff * * {coeff} W {param} W
+neighbor 1.0 bin
+neigh_modify once no every 1 delay 0 check yes
+velocity all create 300.0 4928459 loop geom
+fix 1 all nve
+thermo 0
+run {steps}
+"""
 
 
 def deck_text(cells: int, steps: int, mass=1.0, temp=1.44) -> str:
@@ -205,11 +252,14 @@ def run_reference_arm(a, ws, rank):
 
 # ------------------------------------------------------------------ GPU arm
 def algorithmic_bytes_per_atom(precision: str, mean_row: float) -> float:
-    """Bytes one atom's force evaluation must move: its CSR row entries (4 B
-    each), row metadata (length + start, 8 B), its own position (FP32 float4
-    16 B for mixed, double4 32 B for FP64), the force read + write (48 B)."""
-    pos = 16.0 if precision == "mixed" else 32.0
-    return 4.0 * mean_row + 8.0 + pos + 48.0
+    """Bytes one atom's force evaluation must move from DRAM: its list entries
+    (4 B each), its row metadata (count 4 B; FP64 CSR also the row start),
+    its own position and one fetch of its copy as somebody's neighbour
+    (cell-sorted gathers: FP32 float4 16 B each for mixed, double4 32 B each
+    for FP64), and the force write (24 B; the zeroing is folded in)."""
+    if precision == "mixed":
+        return 4.0 * mean_row + 4.0 + 16.0 + 16.0 + 24.0
+    return 4.0 * mean_row + 8.0 + 32.0 + 32.0 + 24.0
 
 
 def run_gpu_arm(a, ws, rank, local):
@@ -221,10 +271,14 @@ def run_gpu_arm(a, ws, rank, local):
     dist = init_pg(ws, True)
     torch.cuda.set_device(local)
     wl = WORKLOADS[a.workload]
+    snap = a.workload == "snapw"
     tmp = tempfile.mkdtemp(prefix="emdbench_")
-    deck = os.path.join(tmp, "in.lj")
+    deck = os.path.join(tmp, "in.deck")
     with open(deck, "w") as fp:
-        fp.write(deck_text(wl["cells"], a.steps))
+        if snap:
+            fp.write(snap_deck_text(wl["cells"], a.steps, *snap_files(tmp)))
+        else:
+            fp.write(deck_text(wl["cells"], a.steps))
     md = MD(["-il", deck, "--quiet", "--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL",
              "--comm-type", "SERIAL", "--precision", a.precision, "--device", str(local)])
     ctx = md.ctx
@@ -256,24 +310,31 @@ def run_gpu_arm(a, ws, rank, local):
     value = ws * N * a.steps / (ms_max * 1e-3)
 
     # dominant kernel roofline
-    kname = "lj_full_mixed" if a.precision == "mixed" else "lj_full_fp64"
+    kname = (f"snap_{a.precision}" if snap else
+             ("lj_full_mixed" if a.precision == "mixed" else "lj_full_fp64"))
     kms, kn = rep.get(kname, (0.0, 0))
     nl = md.info()["N_local"]
     mean_row = float(md_row_mean(ctx, nl))
-    bytes_launch = algorithmic_bytes_per_atom(a.precision, mean_row) * nl
     peaks = load_peaks()
-    achieved = bytes_launch / (kms / kn * 1e-3) / 1e9 if kn else None
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        tj = json.load(open(tpath))
-        ent = tj.get(f"{kname}@{a.workload}")
-        if ent:
-            traffic = ent.get("bytes_per_launch")
-    roof = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
-            "peak_source": peaks["src"], "bytes_per_launch": bytes_launch, "mean_row": mean_row,
-            "launch_ms": (kms / kn) if kn else None}
+    if snap:
+        # bound by the FP64 pipe (the Wigner-U recursion stays FP64 in both
+        # forms); no measured FP64 peak exists to divide by
+        roof = {"kernel": kname, "bound": "fp64", "achieved": None, "peak": None, "unit": "GFLOP/s",
+                "frac": None, "traffic": None, "mean_row": mean_row, "launch_ms": (kms / kn) if kn else None,
+                "note": "FP64-pipe bound (ncu sm__inst_executed_pipe_fp64); DRAM traffic negligible"}
+    else:
+        bytes_launch = algorithmic_bytes_per_atom(a.precision, mean_row) * nl
+        achieved = bytes_launch / (kms / kn * 1e-3) / 1e9 if kn else None
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            ent = json.load(open(tpath)).get(f"{kname}@{a.workload}")
+            if ent:
+                traffic = ent.get("bytes_per_launch")
+        roof = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
+                "peak_source": peaks["src"], "bytes_per_launch": bytes_launch, "mean_row": mean_row,
+                "launch_ms": (kms / kn) if kn else None}
     kernels = {k: {"ms": v[0], "launches": v[1], "share": v[0] / max(1e-12, sum(x[0] for x in rep.values()))}
                for k, v in sorted(rep.items(), key=lambda kv: -kv[1][0])}
 
@@ -303,7 +364,11 @@ def run_gpu_arm(a, ws, rank, local):
     T, pe, ke = md.thermo(recompute=True)
 
     extra = {}
-    if rank == 0 and not a.no_cpu:
+    if not a.no_accuracy and a.workload.startswith("lj") and a.precision == "mixed":
+        extra["accuracy"] = lj_accuracy(md, wl["cells"], a.drift_steps, local)
+    if not a.no_snap and a.workload == "lj4m":
+        extra["snap_w"] = snap_measure(local, a.snap_steps, max(2, a.snap_steps // 5), 3)
+    if rank == 0 and not a.no_cpu and not snap:
         try:
             r = cpu_sample(WORKLOADS["lj4m"]["cells"] if a.workload == "lj4m" else wl["cells"], a.cpu_steps, 1)
             extra["cpu_baseline"] = {
@@ -318,10 +383,12 @@ def run_gpu_arm(a, ws, rank, local):
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32+f64" if a.precision == "mixed" else "f64",
-                "data": "synthetic (fcc lattice, ExaMiniMD loop-geom velocities)",
+                "data": ("synthetic (bcc W lattice, synthetic SNAP coefficients, loop-geom velocities)" if snap
+                         else "synthetic (fcc lattice, ExaMiniMD loop-geom velocities)"),
                 "config": {"workload": a.workload, "desc": wl["desc"], "atoms_per_gpu": N, "precision": a.precision,
                            "neigh": "CSR full", "parallelism": f"replicas{ws}",
-                           "l2": "working set (positions, forces, 1.2 GB neighbour list) > 129 MB L2; no flush"},
+                           "l2": ("compute-bound (SNAP); inputs re-read every step, no flush" if snap else
+                                  "working set (positions, forces, 1.2 GB neighbour list) > 129 MB L2; no flush")},
                 "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "thermo_end": {"T": T, "PE_per_atom": pe, "KE_per_atom": ke}, "kernels": kernels}
         line.update(extra)
@@ -329,6 +396,126 @@ def run_gpu_arm(a, ws, rank, local):
     md.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def by_id(st: dict, key: str):
+    import numpy as np
+    order = np.argsort(st["id"])
+    return st[key][order]
+
+
+def force_error(f, f_ref) -> dict:
+    """RMS and max of |dF| over the RMS of |F_ref| (per-atom relative errors
+    are unbounded where the net force nearly cancels)."""
+    import numpy as np
+    err = np.linalg.norm(f - f_ref, axis=1)
+    scale = float(np.sqrt(np.mean(np.linalg.norm(f_ref, axis=1) ** 2)))
+    return {"rms_rel": float(np.sqrt(np.mean(err ** 2)) / scale), "max_rel": float(err.max() / scale),
+            "force_scale_rms": scale}
+
+
+def lj_accuracy(md, cells: int, drift_steps: int, device: int) -> dict:
+    """Mixed-form accuracy at full size, from the state the timed run ended in:
+    forces against the FP64 drop-in on the same positions, and the NVE total
+    energy drift of both forms over `drift_steps` further steps."""
+    from examinimd_gb300 import Context, EMD_PREC_FP64
+    from tests import mdloop
+    ctx = md.ctx
+    nl = md.info()["N_local"]
+    st = ctx.get(0, nl)
+    setup = mdloop.LJSetup(cells)
+    ref = Context(device)
+    mdloop.init(ref, setup, st, precision=EMD_PREC_FP64)
+    nr = ref.info()[0]
+    out = force_error(by_id(st, "f"), by_id(ref.get(0, nr), "f"))
+    N = float(nr)
+
+    def e_ref():
+        return (ref.lj_energy() + 0.5 * ref.thermo_mv2()) / N
+    T, pe, ke = md.thermo(recompute=True)
+    e0m, e0r = pe + ke, e_ref()
+    t0 = time.perf_counter()
+    md.run(drift_steps)
+    t_m = time.perf_counter() - t0
+    T, pe, ke = md.thermo(recompute=True)
+    e1m = pe + ke
+    t0 = time.perf_counter()
+    for s_ in range(1, drift_steps + 1):
+        mdloop.step(ref, setup, s_)
+    ref.synchronize()
+    t_r = time.perf_counter() - t0
+    e1r = e_ref()
+    ref.close()
+    out.update({"energy_drift_steps": drift_steps,
+                "energy_drift_rel_mixed": (e1m - e0m) / abs(e0m) * 1000.0 / drift_steps,
+                "energy_drift_rel_fp64": (e1r - e0r) / abs(e0r) * 1000.0 / drift_steps,
+                "drift_units": "relative change of total energy per 1000 steps",
+                "E0_per_atom": e0r, "drift_wall_s": {"mixed": t_m, "fp64": t_r}})
+    return out
+
+
+def snap_accuracy(md, device: int, cells: int, coeff: str, param: str, steps_done: int) -> dict:
+    """Mixed-form SNAP forces of the state the run ended in against the FP64
+    drop-in on the same positions."""
+    from examinimd_gb300 import Context, EMD_PREC_FP64
+    from tests import mdloop
+    from tests.golden.decks import read_snap_files
+    nl = md.info()["N_local"]
+    st = md.ctx.get(0, nl)
+    setup = mdloop.SnapSetup(cells, cells, cells, read_snap_files(coeff, param), a=3.1803, mass=183.84,
+                             lattice_style=2, dt=0.0005)
+    ref = Context(device)
+    mdloop.init(ref, setup, st, precision=EMD_PREC_FP64)
+    out = force_error(by_id(st, "f"), by_id(ref.get(0, ref.info()[0]), "f"))
+    ref.close()
+    out["state"] = f"after {steps_done} mixed-form steps from the 300 K lattice"
+    return out
+
+
+def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells: int = 40) -> dict:
+    """SNAP-W through the driver in both forms: device-timed atom-steps/s, the
+    SNAP kernel's share, and the mixed-form force error at step 0."""
+    import torch
+
+    from examinimd_gb300 import MD
+    tmp = tempfile.mkdtemp(prefix="emdsnap_")
+    coeff, param = snap_files(tmp)
+    res, acc = {}, None
+    for prec, steps in (("mixed", steps_mixed), ("fp64", steps_fp64)):
+        deck = os.path.join(tmp, f"in.snap.{prec}")
+        with open(deck, "w") as fp:
+            fp.write(snap_deck_text(cells, steps, coeff, param))
+        md = MD(["-il", deck, "--quiet", "--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL",
+                 "--comm-type", "SERIAL", "--precision", prec, "--device", str(local)])
+        ctx = md.ctx
+        stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+        md.run(warm)
+        ctx.synchronize()
+        ctx.timing(True)
+        ctx.timing_reset()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        md.run(steps)
+        e1.record(stream)
+        ctx.synchronize()
+        ms = e0.elapsed_time(e1)
+        rep = ctx.timing_report()
+        ctx.timing(False)
+        kname = f"snap_{prec}"
+        kms, kn = rep.get(kname, (0.0, 0))
+        N = md.info()["N"]
+        res[prec] = {"value": N * steps / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms / steps, "steps": steps,
+                     "warmup": warm, "kernel": kname, "kernel_ms_per_launch": (kms / kn) if kn else None,
+                     "kernel_share": kms / max(1e-12, sum(v[0] for v in rep.values())),
+                     "gpu_launches": sum(c for _, c in rep.values())}
+        if prec == "mixed":
+            acc = snap_accuracy(md, local, cells, coeff, param, warm + steps)
+        md.close()
+    res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+    res["accuracy"] = acc
+    res["config"] = SNAP_DESC
+    return res
 
 
 def md_row_mean(ctx, nl) -> float:
@@ -354,11 +541,16 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the full-size force-error / drift check")
+    ap.add_argument("--drift-steps", type=int, default=1000)
+    ap.add_argument("--no-snap", action="store_true", help="skip the SNAP-W measurement")
+    ap.add_argument("--snap-steps", type=int, default=20)
     a = ap.parse_args()
     if a.warmup < 3:
         sys.exit("--warmup must be >= 3")
     if a.cells:
-        WORKLOADS[a.workload] = dict(cells=a.cells, desc=f"LJ fcc rho*=0.8442 {a.cells}^3 cells (profiling case)")
+        kind = "SNAP bcc W" if a.workload == "snapw" else "LJ fcc rho*=0.8442"
+        WORKLOADS[a.workload] = dict(cells=a.cells, desc=f"{kind} {a.cells}^3 cells (profiling case)")
     ws, rank, local = dist_env()
     if a.impl == "reference":
         run_reference_arm(a, ws, rank)

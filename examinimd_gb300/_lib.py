@@ -63,6 +63,8 @@ _SIGS = {
     "emd_lj_compute": ([_P], _I),
     "emd_lj_energy": ([_P, _DP], _I),
     "emd_lj_energy_noalloc": ([_P, _DP], _I),
+    "emd_lj_adjoint": ([_P, _DP, _D, _DP], _I),
+    "emd_snap_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_snap_init": ([_P, _I, _D, _D, _I, _D, _I, _DP, _DP, _DP, _I, _I, _IP, _I], _I),
     "emd_snap_compute": ([_P], _I),
     "emd_snap_energy": ([_P, _DP], _I),
@@ -280,6 +282,20 @@ class Context:
         e = _D()
         self._ok(self.lib.emd_lj_energy(self.h, C.byref(e)), "emd_lj_energy")
         return e.value
+
+    def lj_adjoint(self, dL_dF, dL_dE: float):
+        """(dL/deps, dL/dsigma) for dL/dF (N_local x 3, current order) and dL/dE."""
+        g = _f64(dL_dF, (-1, 3))
+        out = np.zeros(2)
+        self._ok(self.lib.emd_lj_adjoint(self.h, _dp(g), float(dL_dE), _dp(out)), "emd_lj_adjoint")
+        return out
+
+    def snap_adjoint(self, dL_dF, dL_dE: float, nelem: int, ncoeffall: int):
+        """dL/dbeta (nelem x ncoeffall) for dL/dF (N_local x 3, current order) and dL/dE."""
+        g = _f64(dL_dF, (-1, 3))
+        out = np.zeros((nelem, ncoeffall))
+        self._ok(self.lib.emd_snap_adjoint(self.h, _dp(g), float(dL_dE), _dp(out)), "emd_snap_adjoint")
+        return out
 
     def lj_energy_noalloc(self) -> float:
         """emd_lj_energy_noalloc: the same energy, no device allocation."""

@@ -7,7 +7,9 @@
 // reference's Atomic-trait view does on a GPU); the order of those adds is
 // not fixed, so half-list forces agree to rounding only.
 // Energy: per-atom shifted-LJ sums, deterministic block + device reduction.
+#include <cmath>
 #include <mutex>
+#include <vector>
 
 #include "emd_device.cuh"
 #include "emd_internal.h"
@@ -154,6 +156,48 @@ __global__ void __launch_bounds__(256) k_lj_energy(const double4_32a* __restrict
 void lj_mixed_compute(Ctx& c);
 void lj_mixed_prepare(Ctx& c);
 
+// Fitting adjoint of the single-parameter-set LJ model (no counterpart in
+// ExaMiniMD): per owned atom over its full row, the eps- and sigma-
+// derivatives (before the 1/eps, 1/sigma factors) of the shifted pair energy
+// (force_lj_neigh_impl.h:129-156) and of g_i . F_i, with g the loss gradient
+// dL/dF_i.  With lj1 = 48 eps sigma^12, lj2 = 24 eps sigma^6:
+//   eps d/deps   of e and fpair: e and fpair themselves
+//   sigma d/dsigma: lj1 -> 12 lj1, lj2 -> 6 lj2.
+// Block partial sums of the four values, in a fixed order.
+template <bool TWO_D>
+__global__ void __launch_bounds__(256) k_lj_adjoint(const double4_32a* __restrict__ x4, ListView L, double lj1,
+                                                    double lj2, double cutsq, int n, int packed,
+                                                    const double* __restrict__ g, int nblk,
+                                                    double* __restrict__ part) {
+  __shared__ double sh[8];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double a[4] = {0.0, 0.0, 0.0, 0.0};  // E_eps, E_sig, (gF)_eps, (gF)_sig
+  if (i < n) {
+    const double4_32a xi = x4[i];
+    const double gx = g[3 * i], gy = g[3 * i + 1], gz = g[3 * i + 2];
+    const double r2c = 1.0 / cutsq, r6c = r2c * r2c * r2c;
+    const Row<TWO_D> row(L, i);
+    for (int jj = 0; jj < row.n; ++jj) {
+      const int j = entry_j(row[jj], packed);
+      const double4_32a xj = x4[j];
+      const double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+      const double rsq = dx * dx + dy * dy + dz * dz;
+      if (rsq < cutsq) {
+        const double r2inv = 1.0 / rsq, r6inv = r2inv * r2inv * r2inv;
+        a[0] += 0.5 * (r6inv * (lj1 / 12.0 * r6inv - lj2 / 6.0) - r6c * (lj1 / 12.0 * r6c - lj2 / 6.0));
+        a[1] += 0.5 * (r6inv * (lj1 * r6inv - lj2) - r6c * (lj1 * r6c - lj2));
+        const double gd = gx * dx + gy * dy + gz * dz;
+        a[2] += gd * (r6inv * (lj1 * r6inv - lj2) * r2inv);
+        a[3] += gd * (r6inv * (12.0 * lj1 * r6inv - 6.0 * lj2) * r2inv);
+      }
+    }
+  }
+  for (int k = 0; k < 4; ++k) {
+    const double t = block_sum(a[k], sh);
+    if (threadIdx.x == 0) part[size_t(k) * nblk + blockIdx.x] = t;
+  }
+}
+
 ListView list_view(Ctx& c) {
   ListView L;
   // CSR rows live in neighs; column-major rows in neighs (Neighbor2D) or in
@@ -295,6 +339,48 @@ emd_status emd_lj_energy(emd_ctx* ctx, double* pe) {
     EMD_CHECK_LAUNCH();
   }
   *pe = device_sum(c, c.red2.p, grid);
+  EMD_API_END
+}
+
+emd_status emd_lj_adjoint(emd_ctx* ctx, const double* dL_dF, double dL_dE, double* grad) {
+  EMD_API_BEGIN
+  require(grad != nullptr && (dL_dF != nullptr || c.N_local == 0), EMD_ERR_ARG, "emd_lj_adjoint: null array");
+  require(c.lj_ready && c.neigh_ready && c.neigh_rows == c.N_local, EMD_ERR_STATE, "emd_lj_adjoint: not ready");
+  require(!c.lj_half && !c.half_neigh, EMD_ERR_STATE, "emd_lj_adjoint: needs the full-list force (NEIGH_FULL)");
+  const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
+  std::vector<double> hp(3 * nt2);
+  EMD_CUDA(cudaMemcpyAsync(hp.data(), c.lj_params.p, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  for (size_t k = 1; k < nt2; ++k)
+    require(hp[k] == hp[0] && hp[nt2 + k] == hp[nt2] && hp[2 * nt2 + k] == hp[2 * nt2], EMD_ERR_STATE,
+            "emd_lj_adjoint: every type pair must share one eps / sigma / cutoff");
+  const double lj1 = hp[0], lj2 = hp[nt2], cutsq = hp[2 * nt2];
+  require(lj1 > 0 && lj2 > 0, EMD_ERR_STATE, "emd_lj_adjoint: eps and sigma must be positive");
+  const double eps = lj2 * lj2 / (12.0 * lj1), sigma = std::pow(lj1 / (2.0 * lj2), 1.0 / 6.0);
+  const int n = c.N_local;
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  if (n > 0) {
+    const int grid = blocks_for(n, 256);
+    DevBuf<double> g;  // per call: the fitting harness calls this once per configuration and step
+    g.reserve(3 * size_t(n), c.stream);
+    EMD_CUDA(cudaMemcpyAsync(g.p, dL_dF, sizeof(double) * 3 * size_t(n), cudaMemcpyHostToDevice, c.stream));
+    c.red2.reserve(4 * size_t(grid), c.stream);
+    {
+      TimedLaunch t(c, "lj_adjoint");
+      const ListView L = list_view(c);
+      if (c.neigh_layout_2d)
+        k_lj_adjoint<true><<<grid, 256, 0, c.stream>>>(c.x4.p, L, lj1, lj2, cutsq, n, c.neigh_packed, g.p, grid,
+                                                       c.red2.p);
+      else
+        k_lj_adjoint<false><<<grid, 256, 0, c.stream>>>(c.x4.p, L, lj1, lj2, cutsq, n, c.neigh_packed, g.p, grid,
+                                                        c.red2.p);
+      EMD_CHECK_LAUNCH();
+    }
+    for (int k = 0; k < 4; ++k) s[k] = device_sum(c, c.red2.p + size_t(k) * grid, grid);
+    g.release();
+  }
+  grad[0] = (dL_dE * s[0] + s[2]) / eps;
+  grad[1] = (dL_dE * s[1] + s[3]) / sigma;
   EMD_API_END
 }
 

@@ -59,6 +59,7 @@ struct SnapDev {
   const double* cg;     // compact CG blocks (a+1) x (b+1)
   const float* cg_f;
   const int* jobs;      // njobs: (t << 8) | (ma << 4) | mb
+  const int* tjob_off;  // nfull + 1: the jobs of triple t are [tjob_off[t], tjob_off[t+1])
   const int* yred_off;  // nyh + 1
   const int* yred_job;  // njobs
   const double* cY;     // nelem x nfull
@@ -73,9 +74,14 @@ struct SnapDev {
 struct SnapHost {
   SnapDev d;
   int precision = EMD_PREC_FP64;
-  DevBuf<int> trip, cg_off, jobs, yred_off, yred_job, map;
+  DevBuf<int> trip, cg_off, jobs, tjob_off, yred_off, yred_job, map;
   DevBuf<double> cg, cY, rootpq, beta0, radelem, wjelem, eatom;
   DevBuf<float> cg_f, cY_f;
+  // adjoint: per-atom columns, their per-element sums, the loss gradient dL/dF
+  DevBuf<double> adj, adj_sum, adj_g;
+  // coefficient k's three dB/dr terms: full triples and factors (the cY fold)
+  std::vector<int> k_t1, k_t2, k_t3;
+  std::vector<double> k_f2, k_f3;
 };
 
 // ---- index helpers (device)
@@ -238,9 +244,16 @@ struct SnapArgs {
   int n_local, cap;
   double* eatom;  // energy variant
   unsigned* status;
+  // adjoint variant
+  const double* g;           // dL/dF of the owned atoms (n_local x 3)
+  const int* ghost_owner;    // owned atom behind every ghost
+  int newton;                // ghost forces fold back to their owners
+  double* adj;               // column-major per-atom outputs, (2 nfull + 1) x n_local
+  size_t work_bytes;         // size of the shared `work` region
 };
 
-template <typename R, bool ENERGY>
+// MODE 0: forces; 1: per-atom energy; 2: adjoint columns (FP64 only)
+template <typename R, int MODE>
 __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   const SnapDev& S = A.S;
   const int i = blockIdx.x;
@@ -437,7 +450,8 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   __syncthreads();
 
   // ---- C: Z jobs and Y = sum_t cY_t Z_t
-  Cplx<R>* zs = reinterpret_cast<Cplx<R>*>(work);
+  // (the adjoint keeps Z for its final contraction, beyond `work`)
+  Cplx<R>* zs = reinterpret_cast<Cplx<R>*>(MODE == 2 ? work + A.work_bytes : work);
   const R* cg = sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cg) : reinterpret_cast<const R*>(S.cg_f);
   for (int jb = tid; jb < S.njobs; jb += SNAP_THREADS) {
     const int code = S.jobs[jb];
@@ -469,7 +483,7 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   __syncthreads();
   const R* cY = (sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cY) : reinterpret_cast<const R*>(S.cY_f)) +
                 (size_t)ei * S.nfull;
-  for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
+  for (int e = tid; e < (MODE == 2 ? 0 : S.nyh); e += SNAP_THREADS) {
     R yr = 0, yi = 0;
     for (int k = S.yred_off[e]; k < S.yred_off[e + 1]; ++k) {
       const int jb = S.yred_job[k];
@@ -482,7 +496,7 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
   __syncthreads();
 
   // ---- energy (optional): beta_0 + (2/3) sum_j sum_half w Re(conj(U) Y) + pair terms
-  if (ENERGY) {
+  if constexpr (MODE == 1) {
     double acc = 0.0;
     for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
       int j = 0;
@@ -494,6 +508,108 @@ __global__ void __launch_bounds__(SNAP_THREADS) k_snap(SnapArgs A) {
     for (int nb = tid; nb < ninside; nb += SNAP_THREADS) acc += nd[ND_EP * A.cap + nb] * 1.5;  // x 2/3 below
     const double t = block_sum(acc, red);
     if (tid == 0) A.eatom[i] = S.beta0[ei] + (2.0 / 3.0) * t;
+    return;
+  }
+
+  // ---- adjoint: for every full triple t = (j1, j2, j), with Z_t kept from C,
+  //   P_t = 2 sum_half w Re(conj(U_j) Z_t)        (= B_k when t is idxj triple k)
+  //   Q_t = 2 sum_half w Re(conj(D_j) Z_t),  D = sum_nb dU'_nb . (g_i - g_j)
+  // so that d/dbeta_k [sum_atoms g . F] over this atom's pairs is
+  // Q_t1 + (j+1)/(j1+1) Q_t2 + (j+1)/(j2+1) Q_t3 (compute_dbidrj's three terms,
+  // sna_impl.hpp:330-570, contracted with the loss gradient before the sum
+  // over k instead of after it).
+  if constexpr (MODE == 2) {
+    Cplx<double>* dpart = reinterpret_cast<Cplx<double>*>(zs + S.njobs);  // SNAP_WARPS x nyh
+    Cplx<double>* dsum = dpart + SNAP_WARPS * S.nyh;                      // nyh
+    Cplx<double>* dp = dpart + warp * S.nyh;
+    for (int e = lane; e < S.nyh; e += 32) dp[e] = Cplx<double>{0.0, 0.0};
+    const double gix = A.g[3 * i], giy = A.g[3 * i + 1], giz = A.g[3 * i + 2];
+    Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
+    __syncwarp();
+    for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
+      const R* qr = ndr + nb;
+      const R Rar = qr[ND_AR * A.cap], Rai = qr[ND_AI * A.cap], Rbr = qr[ND_BR * A.cap], Rbi = qr[ND_BI * A.cap];
+      R Rdar[3], Rdai[3], Rdbr[3], Rdbi[3], Ruk[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        Rdar[k] = qr[(ND_DAR + k) * A.cap];
+        Rdai[k] = qr[(ND_DAI + k) * A.cap];
+        Rdbr[k] = qr[(ND_DBR + k) * A.cap];
+        Rdbi[k] = qr[(ND_DBI + k) * A.cap];
+        Ruk[k] = qr[(ND_UK + k) * A.cap];
+      }
+      const R Rsfac = qr[ND_SFAC * A.cap], Rdsfac = qr[ND_DSFAC * A.cap];
+      // the pair's reaction force lands on j's owner (newton) or nowhere
+      const int j = in_j[nb];
+      const int jo = j < A.n_local ? j : (A.newton ? A.ghost_owner[j - A.n_local] : -1);
+      const double gjx = jo >= 0 ? A.g[3 * jo] : 0.0, gjy = jo >= 0 ? A.g[3 * jo + 1] : 0.0,
+                   gjz = jo >= 0 ? A.g[3 * jo + 2] : 0.0;
+      const R dv[3] = {R(gix - gjx), R(giy - gjy), R(giz - gjz)};
+      Cplx<R>* P = wd;
+      Cplx<R>* C = wd + L2;
+      Cplx<R>* dP = wd + 2 * L2;
+      Cplx<R>* dC = wd + 5 * L2;
+      if (lane == 0) {
+        P[0] = Cplx<R>{R(1), R(0)};
+        for (int k = 0; k < 3; ++k) dP[k] = Cplx<R>{R(0), R(0)};
+        dp[0].r += Rdsfac * (Ruk[0] * dv[0] + Ruk[1] * dv[1] + Ruk[2] * dv[2]);
+      }
+      __syncwarp();
+      for (int jl = 1; jl <= S.twojmax; ++jl) {
+        du_layer<R>(jl, lane, rootpq_r, L1, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
+        const int nh = (jl + 1) * (jl / 2 + 1), yo = yoff(jl);
+        for (int e = lane; e < nh; e += 32) {
+          const int mb = e / (jl + 1), ma = e % (jl + 1);
+          const int o = ma * (jl + 1) + mb;
+          const Cplx<R> u = C[o];
+          R dr = 0, di = 0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const Cplx<R> du = dC[3 * o + k];
+            dr += dv[k] * (Rdsfac * u.r * Ruk[k] + Rsfac * du.r);
+            di += dv[k] * (Rdsfac * u.i * Ruk[k] + Rsfac * du.i);
+          }
+          dp[yo + e].r += dr;
+          dp[yo + e].i += di;
+        }
+        __syncwarp();
+        Cplx<R>* t = P;
+        P = C;
+        C = t;
+        t = dP;
+        dP = dC;
+        dC = t;
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
+      double sr = 0.0, si = 0.0;
+      for (int w = 0; w < SNAP_WARPS; ++w) {
+        sr += dpart[w * S.nyh + e].r;
+        si += dpart[w * S.nyh + e].i;
+      }
+      dsum[e] = Cplx<double>{sr, si};
+    }
+    __syncthreads();
+    const size_t n = size_t(A.n_local);
+    for (int t = tid; t < S.nfull; t += SNAP_THREADS) {
+      const int jt = S.trip[3 * t + 2];
+      double p = 0.0, q = 0.0;
+      for (int jb = S.tjob_off[t]; jb < S.tjob_off[t + 1]; ++jb) {
+        const int code = S.jobs[jb];
+        const int ma = (code >> 4) & 15, mb = code & 15;
+        const double w = hw(jt, ma, mb);
+        if (w == 0.0) continue;
+        const Cplx<double> u = utot[uoff(jt) + ma * (jt + 1) + mb];
+        const Cplx<double> d = dsum[yoff(jt) + mb * (jt + 1) + ma];
+        const double zr = double(zs[jb].r), zi = double(zs[jb].i);
+        p += w * (u.r * zr + u.i * zi);
+        q += w * (d.r * zr + d.i * zi);
+      }
+      A.adj[size_t(t) * n + i] = 2.0 * p;
+      A.adj[size_t(S.nfull + t) * n + i] = 2.0 * q;
+    }
+    if (tid == 0) A.adj[size_t(2 * S.nfull) * n + i] = 1.0;  // atom count column (beta_0)
     return;
   }
 
@@ -619,8 +735,23 @@ double clebsch_gordan(int j1, int j2, int j, int m1, int m2) {
                    factorial((j2 - bb2) / 2) * factorial((j + cc2) / 2) * factorial((j - cc2) / 2) * (j + 1));
 }
 
+// bytes of the `work` region: per-warp U layers + partials (B), Z jobs (C),
+// per-warp U and dU layers (D)
+size_t snap_work_bytes(const SnapDev& S, int real_bytes) {
+  const int L2 = S.L * S.L;
+  const size_t wB = 2 * sizeof(double) * size_t(SNAP_WARPS) * (2 * L2 + S.nyh);
+  const size_t wC = 2 * size_t(real_bytes) * size_t(S.njobs);
+  const size_t wD = 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 8 * L2;
+  return (std::max(wB, std::max(wC, wD)) + 15) & ~size_t(15);
+}
+
+// the adjoint's extra shared memory after `work`: kept Z, per-warp D partials, D
+size_t snap_adjoint_bytes(const SnapDev& S) {
+  return 2 * sizeof(double) * (size_t(S.njobs) + size_t(SNAP_WARPS + 1) * S.nyh);
+}
+
 size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes) {
-  const int L = S.L, L2 = L * L, L1 = L + 1;
+  const int L1 = S.L + 1;
   size_t b = 0;
   b += sizeof(double) * size_t(L1 * L1);                 // rootpq (FP64)
   b += sizeof(double) * 5 * size_t(cap);                 // r, w, rcut
@@ -632,11 +763,22 @@ size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes) {
   b += sizeof(double) * 4 * SNAP_WARPS;                  // reductions
   b += sizeof(double) * ND_FIELDS * size_t(cap);         // per-neighbour scalars
   if (real_bytes != int(sizeof(double))) b += sizeof(double) * ((ND_FIELDS * size_t(cap) + 1) / 2);  // FP32 copy
-  const size_t wB = 2 * sizeof(double) * size_t(SNAP_WARPS) * (2 * L2 + S.nyh);
-  const size_t wC = 2 * size_t(real_bytes) * size_t(S.njobs);
-  const size_t wD = 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 8 * L2;
-  b += std::max(wB, std::max(wC, wD));
+  b += snap_work_bytes(S, real_bytes);
   return b + 64;
+}
+
+// per-element column sums of the adjoint's per-atom outputs (fixed order)
+__global__ void __launch_bounds__(256) k_adj_reduce(const double* __restrict__ adj, int n, int ncols,
+                                                    const int* __restrict__ type, const int* __restrict__ map,
+                                                    double* __restrict__ out) {
+  __shared__ double sh[8];
+  const int col = blockIdx.x, e = blockIdx.y;
+  const double* a = adj + size_t(col) * n;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += 256)
+    if (map[type[i]] == e) acc += a[i];
+  const double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) out[size_t(e) * ncols + col] = t;
 }
 
 }  // namespace
@@ -644,8 +786,10 @@ size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes) {
 void free_snap(Ctx& c) {
   if (!c.snap) return;
   SnapHost* h = static_cast<SnapHost*>(c.snap);
-  for (auto* b : {&h->trip, &h->cg_off, &h->jobs, &h->yred_off, &h->yred_job, &h->map}) b->release();
-  for (auto* b : {&h->cg, &h->cY, &h->rootpq, &h->beta0, &h->radelem, &h->wjelem, &h->eatom}) b->release();
+  for (auto* b : {&h->trip, &h->cg_off, &h->jobs, &h->tjob_off, &h->yred_off, &h->yred_job, &h->map}) b->release();
+  for (auto* b : {&h->cg, &h->cY, &h->rootpq, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
+                  &h->adj_g})
+    b->release();
   h->cg_f.release();
   h->cY_f.release();
   delete h;
@@ -684,10 +828,15 @@ static void snap_launch(Ctx& c, bool energy) {
   const bool fp64 = h->precision == EMD_PREC_FP64 || energy;
   const size_t smem = snap_smem_bytes(h->d, A.cap, fp64 ? 8 : 4);
   require(smem <= 227 * 1024, EMD_ERR_ARG, "SNAP: neighbour rows too long for one atom's shared memory");
+  A.g = nullptr;
+  A.ghost_owner = nullptr;
+  A.newton = 0;
+  A.adj = nullptr;
+  A.work_bytes = snap_work_bytes(h->d, fp64 ? 8 : 4);
   if (energy) {
     h->eatom.reserve(size_t(n), c.stream);
     A.eatom = h->eatom.p;
-    auto k = k_snap<double, true>;
+    auto k = k_snap<double, 1>;
     EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     TimedLaunch t(c, "snap_energy");
     k<<<n, SNAP_THREADS, smem, c.stream>>>(A);
@@ -695,12 +844,12 @@ static void snap_launch(Ctx& c, bool energy) {
     return;
   }
   if (fp64) {
-    auto k = k_snap<double, false>;
+    auto k = k_snap<double, 0>;
     EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     TimedLaunch t(c, "snap_fp64");
     k<<<n, SNAP_THREADS, smem, c.stream>>>(A);
   } else {
-    auto k = k_snap<float, false>;
+    auto k = k_snap<float, 0>;
     EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     TimedLaunch t(c, "snap_mixed");
     k<<<n, SNAP_THREADS, smem, c.stream>>>(A);
@@ -708,11 +857,76 @@ static void snap_launch(Ctx& c, bool energy) {
   EMD_CHECK_LAUNCH();
 }
 
+// d/dbeta of (dL_dE * E + sum_i dL_dF_i . F_i) for a loss L(E, F) of the
+// total SNAP energy and the owned atoms' forces (host arrays)
+static void snap_adjoint(Ctx& c, const double* dL_dF, double dL_dE, double* grad) {
+  SnapHost* h = static_cast<SnapHost*>(c.snap);
+  require(h != nullptr, EMD_ERR_STATE, "SNAP not initialised");
+  require(c.neigh_ready && c.neigh_rows == c.N_local && !c.half_neigh && !c.neigh_packed, EMD_ERR_STATE,
+          "emd_snap_adjoint needs a current full neighbour list");
+  const SnapDev& S = h->d;
+  const int n = c.N_local, nelem = S.nelem, ncols = 2 * S.nfull + 1;
+  std::vector<double> sums(size_t(nelem) * ncols, 0.0);
+  if (n > 0) {
+    h->adj_g.reserve(3 * size_t(n), c.stream);
+    EMD_CUDA(cudaMemcpyAsync(h->adj_g.p, dL_dF, sizeof(double) * 3 * size_t(n), cudaMemcpyHostToDevice, c.stream));
+    h->adj.reserve(size_t(ncols) * n, c.stream);
+    h->adj_sum.reserve(size_t(nelem) * ncols, c.stream);
+    SnapArgs A;
+    A.S = S;
+    A.x4 = c.x4.p;
+    A.type = c.type.p;
+    A.f = nullptr;
+    A.L = list_view(c);
+    A.n_local = n;
+    A.cap = std::max(1, c.neigh_maxrow);
+    A.status = c.d_status;
+    A.eatom = nullptr;
+    A.g = h->adj_g.p;
+    A.ghost_owner = c.ghost_owner.p;
+    A.newton = c.comm_newton;
+    A.adj = h->adj.p;
+    A.work_bytes = snap_work_bytes(S, 8);
+    const size_t smem = snap_smem_bytes(S, A.cap, 8) + snap_adjoint_bytes(S);
+    require(smem <= 227 * 1024, EMD_ERR_ARG, "SNAP adjoint: neighbour rows too long for shared memory");
+    auto k = k_snap<double, 2>;
+    EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    {
+      TimedLaunch t(c, "snap_adjoint");
+      k<<<n, SNAP_THREADS, smem, c.stream>>>(A);
+      EMD_CHECK_LAUNCH();
+    }
+    {
+      TimedLaunch t(c, "snap_adjoint_reduce");
+      k_adj_reduce<<<dim3(ncols, nelem), 256, 0, c.stream>>>(h->adj.p, n, ncols, c.type.p, S.map, h->adj_sum.p);
+      EMD_CHECK_LAUNCH();
+    }
+    EMD_CUDA(cudaMemcpyAsync(sums.data(), h->adj_sum.p, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
+                             c.stream));
+    EMD_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  for (int e = 0; e < nelem; ++e) {
+    const double* P = &sums[size_t(e) * ncols];
+    const double* Q = P + S.nfull;
+    double* g = grad + size_t(e) * S.ncoeffall;
+    g[0] = dL_dE * P[2 * S.nfull];  // E = sum_i (beta_0 + ...)
+    for (int k = 0; k < S.ncoeff; ++k)
+      g[k + 1] = dL_dE * P[h->k_t1[k]] + Q[h->k_t1[k]] + h->k_f2[k] * Q[h->k_t2[k]] + h->k_f3[k] * Q[h->k_t3[k]];
+  }
+}
+
 }  // namespace emd
 
 using namespace emd;
 
 extern "C" {
+
+emd_status emd_snap_adjoint(emd_ctx* ctx, const double* dL_dF, double dL_dE, double* grad_beta) {
+  EMD_API_BEGIN
+  require(grad_beta != nullptr && (dL_dF != nullptr || c.N_local == 0), EMD_ERR_ARG, "emd_snap_adjoint: null array");
+  snap_adjoint(c, dL_dF, dL_dE, grad_beta);
+  EMD_API_END
+}
 
 emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, int switchflag, double rcutfac,
                          int nelem, const double* radelem, const double* wjelem, const double* beta, int ncoeffall,
@@ -775,9 +989,10 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.nyh = yoff_h(L);
   S.nuf = L * (L + 1) * (2 * L + 1) / 6;
   std::vector<std::vector<int>> by_y(static_cast<size_t>(S.nyh));
-  std::vector<int> jobs;
+  std::vector<int> jobs, tjob_off;
   for (int t = 0; t < S.nfull; ++t) {
     const int cc = trip[3 * t + 2];
+    tjob_off.push_back(int(jobs.size()));
     for (int mb = 0; 2 * mb <= cc; ++mb)
       for (int ma = 0; ma <= cc; ++ma) {
         by_y[size_t(yoff_h(cc) + mb * (cc + 1) + ma)].push_back(int(jobs.size()));
@@ -785,6 +1000,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
       }
   }
   S.njobs = int(jobs.size());
+  tjob_off.push_back(S.njobs);
   std::vector<int> yred_off(size_t(S.nyh) + 1, 0), yred_job;
   for (int e = 0; e < S.nyh; ++e) {
     yred_off[size_t(e)] = int(yred_job.size());
@@ -805,6 +1021,14 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
       ce[find_full(std::max(j1, j), std::min(j1, j), j2)] += bk * (j + 1) / (j2 + 1.0);
     }
   }
+  for (int k = 0; k < S.ncoeff; ++k) {
+    const int j1 = idx3[3 * k], j2 = idx3[3 * k + 1], j = idx3[3 * k + 2];
+    h->k_t1.push_back(find_full(j1, j2, j));
+    h->k_t2.push_back(find_full(std::max(j, j2), std::min(j, j2), j1));
+    h->k_t3.push_back(find_full(std::max(j1, j), std::min(j1, j), j2));
+    h->k_f2.push_back((j + 1) / (j1 + 1.0));
+    h->k_f3.push_back((j + 1) / (j2 + 1.0));
+  }
   std::vector<double> rootpq(size_t(L + 1) * (L + 1), 0.0);
   for (int p = 1; p <= twojmax; p++)
     for (int q = 1; q <= twojmax; q++) rootpq[size_t(p) * (L + 1) + q] = std::sqrt(static_cast<double>(p) / q);
@@ -824,6 +1048,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   std::vector<float> cgf(cg.begin(), cg.end()), cYf(cY.begin(), cY.end());
   upload(c, h->cg_f, cgf);
   upload_i(c, h->jobs, jobs);
+  upload_i(c, h->tjob_off, tjob_off);
   upload_i(c, h->yred_off, yred_off);
   upload_i(c, h->yred_job, yred_job);
   upload(c, h->cY, cY);
@@ -839,6 +1064,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.cg = h->cg.p;
   S.cg_f = h->cg_f.p;
   S.jobs = h->jobs.p;
+  S.tjob_off = h->tjob_off.p;
   S.yred_off = h->yred_off.p;
   S.yred_job = h->yred_job.p;
   S.cY = h->cY.p;

@@ -74,6 +74,7 @@ emd_status emd_md_info(emd_md* md, int* n_global, int* n_local, int* n_ghost, in
 
 emd_status emd_md_thermo(emd_md* md, double* T, double* pe, double* ke) {
   MD_BEGIN
+  if (md->app->thermo_stale) md->app->thermo(md->app->step_done, false, 0, 0);
   if (T) *T = md->app->last_T;
   if (pe) *pe = md->app->last_PE;
   if (ke) *ke = md->app->last_KE;

@@ -242,6 +242,7 @@ class ExaMiniMD {
   Comm* comm = nullptr;
   int step_done = 0;
   double last_T = 0, last_PE = 0, last_KE = 0;
+  bool thermo_stale = false;  // last_* predate the latest run() steps
   double time_total = 0;
   double time_force = 0, time_neigh = 0, time_comm = 0, time_other = 0;
 

@@ -140,6 +140,13 @@ emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double
 emd_status emd_lj_compute(emd_ctx* ctx);
 /* compute_energy(): shifted LJ potential energy (force_lj_neigh_impl.h:129-156, 259-343). */
 emd_status emd_lj_energy(emd_ctx* ctx, double* pe);
+/* Gradient of a loss L(E, F) with respect to the LJ eps and sigma, for
+ * fitting them (no counterpart in ExaMiniMD).  Every type pair must share one
+ * eps / sigma / cutoff (the cutoff is held fixed); full list (NEIGH_FULL)
+ * only.  E is emd_lj_energy's shifted energy, F the owned atoms' forces.
+ * Given dL_dE and dL_dF (N_local x 3, host, current atom order), writes
+ * grad[0] = dL/deps, grad[1] = dL/dsigma.  FP64. */
+emd_status emd_lj_adjoint(emd_ctx* ctx, const double* dL_dF, double dL_dE, double* grad);
 
 /* emd_lj_energy without any device allocation; no counterpart in the
  * reference.  For callers that must not let a library call allocate device
@@ -174,6 +181,17 @@ emd_status emd_snap_compute(emd_ctx* ctx);
 emd_status emd_snap_energy(emd_ctx* ctx, double* pe);
 /* Number of bispectrum components (55 at twojmax 8). */
 emd_status emd_snap_ncoeff(emd_ctx* ctx, int* ncoeff);
+/* Gradient of a loss L(E, F) with respect to the SNAP linear coefficients,
+ * for fitting them (no counterpart in ExaMiniMD, which only runs SNAP).  E is
+ * the total SNAP energy of the owned atoms (emd_snap_energy), F the forces on
+ * the owned atoms after emd_snap_compute (+ emd_comm_update_force with newton
+ * on).  Given dL_dE and dL_dF (N_local x 3, host, in the current atom order),
+ * writes grad_beta (nelem x ncoeffall, host): beta_0 gets dL_dE times the
+ * atom count of its element; beta_k (k >= 1) gets
+ *   dL_dE * sum_i B_ik + sum_i sum_j (dL_dF_i - dL_dF_owner(j)) . dB_ik/dr_ij
+ * (the reaction term only where j's force reaches an owned atom).  Needs the
+ * current full neighbour list of the forces; computed in FP64. */
+emd_status emd_snap_adjoint(emd_ctx* ctx, const double* dL_dF, double dL_dE, double* grad_beta);
 
 /* ------------------------------------------------------ Properties
  * Temperature / KinE (property_temperature.cpp:43-62, property_kine.cpp:43-61):
