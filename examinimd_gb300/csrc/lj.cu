@@ -275,7 +275,10 @@ emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double
   c.lj_half = half_neigh ? 1 : 0;
   c.lj_prec = precision;
   c.lj_ready = true;
-  c.neigh_ready = false;  // rows must be rebuilt in the format this form reads
+  // a list in another row format (packed for the mixed form, plain for
+  // FP64) or of the other half/full kind must be rebuilt before the force
+  if (c.neigh_ready && (c.neigh_packed != (precision == EMD_PREC_MIXED ? 1 : 0) || c.half_neigh != c.lj_half))
+    c.neigh_ready = false;
   if (precision == EMD_PREC_MIXED) lj_mixed_prepare(c);
   EMD_API_END
 }
