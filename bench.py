@@ -368,6 +368,8 @@ def run_gpu_arm(a, ws, rank, local):
         extra["accuracy"] = lj_accuracy(md, wl["cells"], a.drift_steps, local)
     if not a.no_snap and a.workload == "lj4m":
         extra["snap_w"] = snap_measure(local, a.snap_steps, max(2, a.snap_steps // 5), 3)
+    if not a.no_batch and a.workload == "lj4m":
+        extra["batched_lj"] = batch_measure(local, a.batch_steps, 8, 20)
     if rank == 0 and not a.no_cpu and not snap:
         try:
             r = cpu_sample(WORKLOADS["lj4m"]["cells"] if a.workload == "lj4m" else wl["cells"], a.cpu_steps, 1)
@@ -518,6 +520,91 @@ def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells
     return res
 
 
+def batch_ensemble(nsys=256, seed=20261204, rho=0.8442, temp=1.44):
+    """256 fcc LJ systems, N_k log-uniform in [500, 20000] realised as
+    round((N_k / 4)^(1/3)) cubic cells, lattice positions, Gaussian velocities
+    at temp with zero net momentum per system."""
+    import numpy as np
+    from examinimd_gb300 import fit
+    rng = np.random.default_rng(seed)
+    a = (4.0 / rho) ** (1.0 / 3.0)
+    target = np.exp(rng.uniform(np.log(500.0), np.log(20000.0), nsys))
+    cells = np.maximum(5, np.round((target / 4.0) ** (1.0 / 3.0)).astype(int))
+    xs, vs, boxes = [], [], []
+    for c in cells:
+        x = fit.lattice("fcc", a, int(c))
+        v = rng.normal(0.0, np.sqrt(temp), size=x.shape)
+        v -= v.mean(axis=0)
+        xs.append(x)
+        vs.append(v)
+        boxes.append([c * a] * 3)
+    return cells, np.array([len(x) for x in xs]), np.array(boxes), np.concatenate(xs), np.concatenate(vs)
+
+
+def batch_measure(local: int, steps: int, loop_sample: int, loop_steps: int) -> dict:
+    """The batched ensemble: tuned shape, `steps` steps in CUDA graphs, device-timed;
+    beside it the same systems looped one at a time through the FP64 drop-in
+    driver (a sample of `loop_sample` sizes, `loop_steps` steps each)."""
+    import numpy as np
+    import torch
+
+    from examinimd_gb300 import MD, Batch
+    cells, ns, boxes, x, v = batch_ensemble()
+    t0 = time.perf_counter()
+    b = Batch(ns, boxes, x, v)
+    t_create = time.perf_counter() - t0
+    threads, spl = b.tune(40)
+    stream = torch.cuda.ExternalStream(b.stream, device=local)
+    mv2, pe = b.thermo()
+    e0 = 0.5 * mv2 + pe
+    e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e_a.record(stream)
+    b.run(steps)
+    e_b.record(stream)
+    torch.cuda.synchronize()
+    ms = e_a.elapsed_time(e_b)
+    mv2, pe = b.thermo()
+    e1 = 0.5 * mv2 + pe
+    drift = np.abs(e1 - e0) / np.abs(e0) * 1000.0 / steps
+    b.close()
+    total = int(ns.sum())
+    value = total * steps / (ms * 1e-3)
+    # looping the FP64 single-system drop-in over a spread of the same sizes
+    tmp = tempfile.mkdtemp(prefix="emdloop_")
+    pick = np.unique(np.quantile(cells, np.linspace(0, 1, loop_sample), method="nearest"))
+    loop_atoms, loop_ms = 0, 0.0
+    for c in pick:
+        deck = os.path.join(tmp, f"in.lj{c}")
+        with open(deck, "w") as fp:
+            fp.write(deck_text(int(c), loop_steps))
+        md = MD(["-il", deck, "--quiet", "--precision", "fp64", "--device", str(local)])
+        s = torch.cuda.ExternalStream(md.ctx.stream, device=local)
+        md.run(3)
+        md.ctx.synchronize()
+        a1, a2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t1 = time.perf_counter()
+        a1.record(s)
+        md.run(loop_steps)
+        a2.record(s)
+        md.ctx.synchronize()
+        wall = (time.perf_counter() - t1) * 1e3
+        loop_ms += max(wall, a1.elapsed_time(a2))
+        loop_atoms += md.info()["N"] * loop_steps
+        md.close()
+    loop_rate = loop_atoms / (loop_ms * 1e-3)
+    return {"value": value, "unit": METRIC, "systems": int(len(ns)), "atoms": total, "steps": steps,
+            "ms": ms, "atoms_min": int(ns.min()), "atoms_max": int(ns.max()),
+            "shape": {"threads_per_cta": threads, "steps_per_launch": spl, "chosen_by": "emd_batch_tune (40 steps)"},
+            "create_s": t_create, "energy_drift_rel_per_1000_max": float(drift.max()),
+            "looped_fp64": {"value": loop_rate, "unit": METRIC, "sizes_cells": [int(c) for c in pick],
+                            "steps_each": loop_steps,
+                            "how": "ExaMiniMD driver, FP64 drop-in, one system at a time (wall time incl. launches)"},
+            "speedup_vs_looped_fp64": value / loop_rate,
+            "config": "256 fcc LJ systems, rho* 0.8442, N log-uniform in [500, 20000] (seed 20261204), T* 1.44 "
+                      "Gaussian velocities, rc 2.5, skin 0.3, every 20, mixed form, CUDA-graph step loop"}
+
+
 def md_row_mean(ctx, nl) -> float:
     """Mean CSR row length from the list's own row counts."""
     import numpy as np
@@ -545,6 +632,8 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--no-snap", action="store_true", help="skip the SNAP-W measurement")
     ap.add_argument("--snap-steps", type=int, default=20)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--batch-steps", type=int, default=500)
     a = ap.parse_args()
     if a.warmup < 3:
         sys.exit("--warmup must be >= 3")

@@ -7,8 +7,8 @@ ctypes; there is no Python or CPU fallback for any kernel.
 """
 from __future__ import annotations
 
-from ._lib import (EMD_NEIGH_2D, EMD_NEIGH_CSR, EMD_PREC_FP64, EMD_PREC_MIXED, Context, EmdError, MD,
+from ._lib import (EMD_NEIGH_2D, EMD_NEIGH_CSR, EMD_PREC_FP64, EMD_PREC_MIXED, Batch, Context, EmdError, MD,
                    library_path, load_library)
 
-__all__ = ["Context", "MD", "EmdError", "load_library", "library_path", "EMD_PREC_FP64", "EMD_PREC_MIXED",
+__all__ = ["Batch", "Context", "MD", "EmdError", "load_library", "library_path", "EMD_PREC_FP64", "EMD_PREC_MIXED",
            "EMD_NEIGH_CSR", "EMD_NEIGH_2D"]

@@ -64,6 +64,16 @@ _SIGS = {
     "emd_lj_energy": ([_P, _DP], _I),
     "emd_lj_energy_noalloc": ([_P, _DP], _I),
     "emd_lj_adjoint": ([_P, _DP, _D, _DP], _I),
+    "emd_batch_create": ([C.POINTER(_P), _I, _I, _IP, _DP, _DP, _DP, _D, _D, _D, _D, _D, _D, _I, _I, _D], _I),
+    "emd_batch_destroy": ([_P], None),
+    "emd_batch_last_error": ([_P], C.c_char_p),
+    "emd_batch_run": ([_P, _I], _I),
+    "emd_batch_set_shape": ([_P, _I, _I], _I),
+    "emd_batch_tune": ([_P, _I, _IP, _IP], _I),
+    "emd_batch_get": ([_P, _DP, _DP, _DP], _I),
+    "emd_batch_thermo": ([_P, _DP, _DP], _I),
+    "emd_batch_info": ([_P, _LLP, _IP, _IP, _LLP], _I),
+    "emd_batch_stream": ([_P], _P),
     "emd_snap_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_snap_init": ([_P, _I, _D, _D, _I, _D, _I, _DP, _DP, _DP, _I, _I, _IP, _I], _I),
     "emd_snap_compute": ([_P], _I),
@@ -391,3 +401,75 @@ class MD:
         out = np.zeros(5)
         self._ok(self.lib.emd_md_timers(self.h, _dp(out)), "emd_md_timers")
         return dict(zip(("force", "neigh", "comm", "other", "total"), out.tolist()))
+
+
+class Batch:
+    """A batched LJ ensemble (emd_batch.h): independent periodic systems of
+    uneven size advanced together in the mixed-precision form."""
+
+    def __init__(self, natoms, boxes, x, v, mass=1.0, dt=0.005, eps=1.0, sigma=1.0, cut=2.5, skin=0.3, every=20,
+                 max_neigh=128, ghost_factor=1.5, device=0):
+        self.lib = load_library()
+        self.h = None
+        natoms = _i32(natoms)
+        boxes = _f64(boxes, (-1, 3))
+        x, v = _f64(x, (-1, 3)), _f64(v, (-1, 3))
+        if x.shape[0] != int(natoms.sum()) or v.shape != x.shape or boxes.shape[0] != natoms.shape[0]:
+            raise EmdError("Batch: natoms, boxes, x and v do not agree")
+        h = _P()
+        st = self.lib.emd_batch_create(C.byref(h), device, len(natoms), _ip(natoms), _dp(boxes), _dp(x), _dp(v),
+                                       mass, dt, eps, sigma, cut, skin, every, max_neigh, ghost_factor)
+        if st != 0:
+            raise EmdError(f"emd_batch_create: {self.lib.emd_status_string(st).decode()} (see stderr)")
+        self.h = h
+        self.nsys = len(natoms)
+        self.natoms = natoms
+        self.n = int(natoms.sum())
+
+    def _ok(self, st, what):
+        if st != 0:
+            raise EmdError(f"{what}: {self.lib.emd_status_string(st).decode()} "
+                           f"({self.lib.emd_batch_last_error(self.h).decode()})")
+
+    def close(self):
+        if self.h:
+            self.lib.emd_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return self.lib.emd_batch_stream(self.h) or 0
+
+    def run(self, nsteps: int):
+        self._ok(self.lib.emd_batch_run(self.h, nsteps), "emd_batch_run")
+
+    def set_shape(self, threads: int, steps_per_launch: int):
+        self._ok(self.lib.emd_batch_set_shape(self.h, threads, steps_per_launch), "emd_batch_set_shape")
+
+    def tune(self, trial_steps: int):
+        t, s = _I(), _I()
+        self._ok(self.lib.emd_batch_tune(self.h, trial_steps, C.byref(t), C.byref(s)), "emd_batch_tune")
+        return t.value, s.value
+
+    def get(self):
+        x, v, f = (np.empty((self.n, 3)) for _ in range(3))
+        self._ok(self.lib.emd_batch_get(self.h, _dp(x), _dp(v), _dp(f)), "emd_batch_get")
+        return x, v, f
+
+    def thermo(self):
+        """Per system (sum m v^2, shifted LJ potential energy)."""
+        a, b = np.empty(self.nsys), np.empty(self.nsys)
+        self._ok(self.lib.emd_batch_thermo(self.h, _dp(a), _dp(b)), "emd_batch_thermo")
+        return a, b
+
+    def info(self) -> dict:
+        at, th, sp, sd = C.c_longlong(), _I(), _I(), C.c_longlong()
+        self._ok(self.lib.emd_batch_info(self.h, C.byref(at), C.byref(th), C.byref(sp), C.byref(sd)),
+                 "emd_batch_info")
+        return {"atoms": at.value, "threads": th.value, "steps_per_launch": sp.value, "steps_done": sd.value}

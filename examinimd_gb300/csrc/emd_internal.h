@@ -21,11 +21,16 @@ struct Error : std::runtime_error {
   Error(emd_status c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
-#define EMD_CUDA(expr)                                                                      \
-  do {                                                                                      \
-    cudaError_t e__ = (expr);                                                               \
-    if (e__ != cudaSuccess)                                                                 \
-      throw ::emd::Error(EMD_ERR_CUDA, std::string(#expr " -> ") + cudaGetErrorString(e__)); \
+// On failure the thread's last-error state is read back so that a
+// non-sticky error (an invalid argument) is not reported again by the next
+// launch check of an unrelated call.
+#define EMD_CUDA(expr)                                                                        \
+  do {                                                                                        \
+    cudaError_t e__ = (expr);                                                                 \
+    if (e__ != cudaSuccess) {                                                                 \
+      (void)cudaGetLastError();                                                               \
+      throw ::emd::Error(EMD_ERR_CUDA, std::string(#expr " -> ") + cudaGetErrorString(e__));   \
+    }                                                                                         \
   } while (0)
 
 #define EMD_CHECK_LAUNCH() EMD_CUDA(cudaGetLastError())

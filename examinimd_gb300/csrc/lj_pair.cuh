@@ -1,0 +1,115 @@
+// Mixed-precision LJ pair arithmetic shared by the single-system force
+// (lj_mixed.cu) and the batched ensemble (batch.cu): FP32 pair math on
+// bin-relative FP32 positions with packed f32x2 operations, Kahan-compensated
+// FP32 sums, and an out-of-line FP64 decision for pairs on the cutoff.
+#pragma once
+#include "emd_device.cuh"
+#include "emd_internal.h"
+
+namespace emd {
+namespace {
+
+// half width of the FP32 cutoff band (relative to cutsq) inside which a pair
+// is re-tested in FP64; the FP32 r^2 of a listed pair is within ~3e-7 of the
+// exact value (bin-relative inputs below 1.5 in magnitude)
+constexpr float LJ_BAND = 4e-6f;
+
+struct LJParamsF {
+  const float* lj1;
+  const float* lj2;
+  const float* cutsq;
+  const double* cutsq_d;
+  int ntypes;
+  float lj1_0, lj2_0, cutsq_0;  // single-type values
+  double cutsq_d0;
+};
+
+// Exact FP64 cutoff test of a pair whose FP32 r^2 fell inside the guard
+// band.  Out of line on purpose: inlined, the compiler predicates it into the
+// pair loop and every warp then issues its FP64 instructions (64 cycles each
+// on this part) for every pair.
+__device__ __noinline__ bool cut_fp64(const double4_32a* __restrict__ x4, int i, int j, double cutsq) {
+  const double4_32a pi = x4[i], pj = x4[j];
+  const double ddx = pi.x - pj.x, ddy = pi.y - pj.y, ddz = pi.z - pj.z;
+  return (ddx * ddx + ddy * ddy + ddz * ddz) < cutsq;
+}
+
+// Kahan-compensated running sum; (x, y) as one packed f32x2 value, z scalar.
+// a - b is formed as fma(b, -1, a), which rounds exactly like a subtraction.
+struct Acc {
+  float2 sxy = {0.f, 0.f}, cxy = {0.f, 0.f};
+  float sz = 0.f, cz = 0.f;
+  __device__ __forceinline__ void add(float2 vxy, float vz) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 y = __ffma2_rn(cxy, m1, vxy);
+    const float2 t = __fadd2_rn(sxy, y);
+    cxy = __ffma2_rn(y, m1, __ffma2_rn(sxy, m1, t));
+    sxy = t;
+    const float yz = __fsub_rn(vz, cz);
+    const float tz = __fadd_rn(sz, yz);
+    cz = __fsub_rn(__fsub_rn(tz, sz), yz);
+    sz = tz;
+  }
+};
+
+struct PairCtx {
+  float4 xi;
+  int i, ti;
+  const float4* shift;  // shared: (1 - k) w per stencil code
+  const double4_32a* x4;
+};
+
+// One pair: returns its force on i, (x, y) packed and z, or zero outside the
+// cutoff.  x_i - x_j = (xl_i - xl_j) + (1 - k) w per dimension.
+template <bool SINGLE>
+__device__ __forceinline__ void lj_pair(const PairCtx& C, int e, const float4& xj, const LJParamsF& P, float2& fxy,
+                                        float& fz) {
+  const float4 sh = C.shift[e & 63];
+  float2 dxy = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
+  dxy = __fadd2_rn(dxy, make_float2(sh.x, sh.y));
+  const float dz = __fadd_rn(__fsub_rn(C.xi.z, xj.z), sh.z);
+  const float2 sq = __fmul2_rn(dxy, dxy);
+  const float rsq = __fmaf_rn(dz, dz, __fadd_rn(sq.x, sq.y));
+  float lj1, lj2, cutsq, lo, hi;
+  double cutsq_d;
+  if (SINGLE) {
+    lj1 = P.lj1_0;
+    lj2 = P.lj2_0;
+    cutsq = P.cutsq_0;
+    cutsq_d = P.cutsq_d0;
+  } else {
+    const int tp = C.ti * P.ntypes + __float_as_int(xj.w);
+    lj1 = __ldg(P.lj1 + tp);
+    lj2 = __ldg(P.lj2 + tp);
+    cutsq = __ldg(P.cutsq + tp);
+    cutsq_d = __ldg(P.cutsq_d + tp);
+  }
+  lo = cutsq * (1.0f - LJ_BAND);
+  hi = cutsq * (1.0f + LJ_BAND);
+  bool in = rsq < cutsq;
+  if (rsq > lo && rsq < hi) in = cut_fp64(C.x4, C.i, e >> 6, cutsq_d);  // borderline: decide as FP64 does
+  const float r2inv = in ? __fdividef(1.0f, rsq) : 0.0f;
+  const float r6inv = r2inv * r2inv * r2inv;
+  const float fpair = (r6inv * __fmaf_rn(lj1, r6inv, -lj2)) * r2inv;
+  fxy = __fmul2_rn(dxy, make_float2(fpair, fpair));
+  fz = dz * fpair;
+}
+
+// Four entries of one int4 granule, summed in FP32 and then added to the
+// compensated accumulator.
+template <bool SINGLE>
+__device__ __forceinline__ void lj_quad(const PairCtx& C, const int4& e, const float4* __restrict__ xl,
+                                        const LJParamsF& P, Acc& acc) {
+  const float4 x0 = xl[e.x >> 6], x1 = xl[e.y >> 6], x2 = xl[e.z >> 6], x3 = xl[e.w >> 6];
+  float2 a0, a1, a2, a3;
+  float z0, z1, z2, z3;
+  lj_pair<SINGLE>(C, e.x, x0, P, a0, z0);
+  lj_pair<SINGLE>(C, e.y, x1, P, a1, z1);
+  lj_pair<SINGLE>(C, e.z, x2, P, a2, z2);
+  lj_pair<SINGLE>(C, e.w, x3, P, a3, z3);
+  acc.add(__fadd2_rn(__fadd2_rn(a0, a1), __fadd2_rn(a2, a3)), __fadd_rn(__fadd_rn(z0, z1), __fadd_rn(z2, z3)));
+}
+
+
+}  // namespace
+}  // namespace emd

@@ -13,7 +13,7 @@ import pytest
 
 from tests.conftest import ROOT, gpu_available
 
-HEADERS = [os.path.join(ROOT, "include", f) for f in ("emd_gpu.h", "emd_driver.h")]
+HEADERS = [os.path.join(ROOT, "include", f) for f in ("emd_gpu.h", "emd_driver.h", "emd_batch.h")]
 
 
 def declared_functions():
