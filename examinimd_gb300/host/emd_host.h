@@ -220,6 +220,8 @@ class Input {
   bool dumpbinaryflag = false, correctnessflag = false;
   std::string dumpbinary_path, reference_path, correctness_file;
   bool quiet = false;
+  std::string restart_file;  // --restart: a --dumpbinary file to start from
+  int restart_step = -1;     // its step (-1: from the file name)
 
   explicit Input(System* s) : system(s) {}
   void read_command_line_args(int argc, const char* const* argv);
@@ -228,6 +230,9 @@ class Input {
   void check_lammps_command(int line);
   // Builds the lattice and velocities on the host and uploads them.
   void create_lattice(Comm* comm);
+  // Loads the owned atoms of a --dumpbinary file (id, type, q, x, v; forces
+  // are recomputed) and returns the step it was written at.
+  int read_restart(Comm* comm);
 };
 
 // ExaMiniMD driver (examinimd.h:49-71, examinimd.cpp:47-488)
@@ -243,6 +248,7 @@ class ExaMiniMD {
   int step_done = 0;
   double last_T = 0, last_PE = 0, last_KE = 0;
   bool thermo_stale = false;  // last_* predate the latest run() steps
+  bool thermo_header_done = false;
   double time_total = 0;
   double time_force = 0, time_neigh = 0, time_comm = 0, time_other = 0;
 

@@ -127,7 +127,9 @@ void ExaMiniMD::init(int argc, const char* const* argv) {
   if (system->do_print && !input->quiet)
     printf("Using: %s %s %s %s\n", force->name(), neighbor->name(), comm->name(), binning->name());
 
-  if (system->N == 0) input->create_lattice(comm);
+  int start_step = 0;
+  if (!input->restart_file.empty()) start_step = input->read_restart(comm);
+  else if (system->N == 0) input->create_lattice(comm);
 
   comm->exchange();
   const double neigh_cutoff = input->force_cutoff + input->neighbor_skin;
@@ -140,10 +142,10 @@ void ExaMiniMD::init(int argc, const char* const* argv) {
   force->compute(system, binning, neighbor);
   if (input->comm_newton) comm->update_force();
 
-  step_done = 0;
-  if (input->thermo_rate > 0) thermo(0, system->do_print, 0.0, 0.0);
-  if (input->dumpbinaryflag) dump_binary(0);
-  if (input->correctnessflag) check_correctness(0);
+  step_done = start_step;
+  if (input->thermo_rate > 0) thermo(step_done, system->do_print, 0.0, 0.0);
+  if (input->dumpbinaryflag) dump_binary(step_done);
+  if (input->correctnessflag) check_correctness(step_done);
 }
 
 // Temperature / PotE / KinE (property_*.cpp) and the thermo line
@@ -156,7 +158,8 @@ void ExaMiniMD::thermo(int step, bool print, double elapsed, double rate) {
   last_KE = mv2 * (0.5 * system->mvv2e) / system->N;
   thermo_stale = false;
   if (!print) return;
-  if (step == 0) {
+  if (!thermo_header_done) {
+    thermo_header_done = true;
     printf("\n#Timestep Temperature PotE ETot Time Atomsteps/s\n");
     printf("%i %lf %lf %lf %lf %e\n", step, last_T, last_PE, last_PE + last_KE, 0.0, 0.0);
   } else {

@@ -84,6 +84,8 @@ void Input::read_command_line_args(int argc, const char* const* argv) {
       printf("  --device [N]:               CUDA device\n");
       printf("  --dumpbinary [N] [PATH]:    binary output PATH/output* every N steps\n");
       printf("  --correctness [N] [PATH] [FILE]: compare against PATH/output* every N steps\n");
+      printf("  --restart [FILE]:           start from a --dumpbinary file (atoms and step)\n");
+      printf("  --restart-step [N]:         its step, when the file name does not give it\n");
     } else if (a == "-il" || a == "--input-lammps") {
       input_file = next(1);
       have_input = true;
@@ -127,6 +129,12 @@ void Input::read_command_line_args(int argc, const char* const* argv) {
       correctness_file = next(3);
       correctnessflag = true;
       i += 3;
+    } else if (a == "--restart") {
+      restart_file = next(1);
+      ++i;
+    } else if (a == "--restart-step") {
+      restart_step = atoi(next(1).c_str());
+      ++i;
     } else if (a.find("--kokkos-") == std::string::npos) {
       throw HostError("Unknown command line argument: " + a);
     }
@@ -371,6 +379,50 @@ void Input::create_lattice(Comm* comm) {
   check(emd_system_set_local(s.ctx, n, x.data(), v.data(), nullptr, type.data(), id.data(), q.data()), s.ctx,
         "emd_system_set_local");
   s.refresh_counts();
+}
+
+// Restart from a dump in the --dumpbinary layout (examinimd.cpp:296-346):
+// int n, int id[n], int type[n], double q[n], double x[3n], v[3n], f[3n].
+// The deck still sets units, box, masses and the force field; the dump
+// replaces create_atoms / velocity.  The step is the one in the name
+// output.<step>.<rank> unless --restart-step gives it.
+int Input::read_restart(Comm* comm) {
+  // the deck's lattice and region still define the box (as in create_lattice)
+  system->domain_x = lattice_constant * lattice_nx;
+  system->domain_y = lattice_constant * lattice_ny;
+  system->domain_z = lattice_constant * lattice_nz;
+  comm->create_domain_decomposition();
+  FILE* fp = fopen(restart_file.c_str(), "rb");
+  if (!fp) throw HostError("Cannot open restart file " + restart_file);
+  int n = 0;
+  bool ok = fread(&n, sizeof(int), 1, fp) == 1 && n > 0;
+  std::vector<int> id(ok ? size_t(n) : 0), type(ok ? size_t(n) : 0);
+  std::vector<double> q(ok ? size_t(n) : 0), x(ok ? 3 * size_t(n) : 0), v(ok ? 3 * size_t(n) : 0);
+  ok = ok && fread(id.data(), sizeof(int), size_t(n), fp) == size_t(n) &&
+       fread(type.data(), sizeof(int), size_t(n), fp) == size_t(n) &&
+       fread(q.data(), sizeof(double), size_t(n), fp) == size_t(n) &&
+       fread(x.data(), sizeof(double), 3 * size_t(n), fp) == 3 * size_t(n) &&
+       fread(v.data(), sizeof(double), 3 * size_t(n), fp) == 3 * size_t(n);
+  fclose(fp);
+  if (!ok) throw HostError("Restart file " + restart_file + " is truncated or empty");
+  System& s = *system;
+  for (int t : type)
+    if (t < 0 || t >= s.ntypes) throw HostError("Restart file " + restart_file + ": atom type outside the deck's types");
+  int step = restart_step;
+  if (step < 0) {
+    const size_t k = restart_file.rfind("output.");
+    if (k == std::string::npos || k + 17 > restart_file.size())
+      throw HostError("--restart: give --restart-step, the file name has no output.<step>.<rank>");
+    step = atoi(restart_file.substr(k + 7, 10).c_str());
+  }
+  s.N = n;
+  s.N_local = n;
+  if (s.do_print && !quiet) printf("Atoms: %i %i (restart from step %i)\n", s.N, s.N_local, step);
+  s.sync_params();
+  check(emd_system_set_local(s.ctx, n, x.data(), v.data(), nullptr, type.data(), id.data(), q.data()), s.ctx,
+        "emd_system_set_local");
+  s.refresh_counts();
+  return step;
 }
 
 }  // namespace emdhost
