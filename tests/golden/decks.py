@@ -16,12 +16,12 @@ atom_style atomic
 newton {newton}
 lattice fcc 0.8442
 region box block 0 {n} 0 {n} 0 {n}
-create_box 1 box
+create_box {ntypes} box
 create_atoms 1 box
-mass 1 {mass}
+{mass_lines}
 velocity all create {temp} 87287 loop geom
 pair_style lj/cut 2.5
-pair_coeff 1 1 1.0 1.0 2.5
+{coeff_lines}
 neighbor 0.3 bin
 neigh_modify delay 0 every {every} check no
 fix 1 all nve
@@ -64,16 +64,33 @@ CASES = {
                                    args=["--neigh-type", "2D", "--force-iteration", "NEIGH_HALF",
                                          "--comm-type", "SERIAL"],
                                    dump_every=10, keep_steps=[0, 10, 30]),
+    # LJ with two types of different mass (types drawn by the reference's rand()),
+    # three pair_coeff lines of which the last one holds (stack parameters)
+    "lj_fcc4_2types_full_csr": dict(kind="lj", n=4, mass=1.0, masses=[1.0, 2.5], temp=1.44, newton="off", every=10,
+                                    coeffs=[(1, 1, 1.0, 1.0, 2.5), (1, 2, 1.3, 1.05, 2.5), (2, 2, 0.8, 0.95, 2.5)],
+                                    thermo=10, steps=30,
+                                    args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL",
+                                          "--comm-type", "SERIAL"],
+                                    dump_every=10, keep_steps=[0, 10, 30]),
     # SNAP W, the shipped in.snap.W geometry (sc 4x8x8 = 256 atoms)
     "snap_W_sc": dict(kind="snap", a=3.1803, nx=4, ny=8, nz=8, mass=183.84, elem="W", every=1, thermo=5, steps=5,
                       coeff="W.snapcoeff", param="W.snapparam",
                       args=["--neigh-type", "CSR", "--comm-type", "SERIAL"], dump_every=5, keep_steps=[0, 5]),
+    # SNAP Ta, the shipped in.snap.Ta06A geometry (sc 4^3 = 64 atoms, twojmax 6), 2D list
+    "snap_Ta_sc": dict(kind="snap", a=3.316, nx=4, ny=4, nz=4, mass=180.88, elem="Ta", every=1, thermo=5, steps=10,
+                       coeff="Ta06A.snapcoeff", param="Ta06A.snapparam",
+                       args=["--neigh-type", "2D", "--comm-type", "SERIAL"], dump_every=5, keep_steps=[0, 5, 10]),
 }
 
 
 def deck_text(case: dict) -> str:
     if case["kind"] == "lj":
-        return LJ.format(**case)
+        masses = case.get("masses", [case["mass"]])
+        coeffs = case.get("coeffs", [(1, 1, 1.0, 1.0, 2.5)])
+        return LJ.format(ntypes=len(masses),
+                         mass_lines="\n".join(f"mass {t + 1} {m}" for t, m in enumerate(masses)),
+                         coeff_lines="\n".join(f"pair_coeff {a} {b} {e} {s} {c}" for a, b, e, s, c in coeffs),
+                         **case)
     return SNAP.format(**case)
 
 

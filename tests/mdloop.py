@@ -23,6 +23,7 @@ class Setup:
         self.newton, self.half, self.kind = newton, half, kind
         self.a, self.dt = a, dt
         self.neigh_cut = cut + skin
+        self.masses = [mass]  # per type
 
     @property
     def domain(self):
@@ -42,11 +43,23 @@ class LJSetup(Setup):
     """fcc LJ deck (in.lj style; lattice constant (4/rho)^(1/3), input.cpp:311-323)."""
 
     def __init__(self, n, mass=1.0, temp=1.44, seed=87287, cut=2.5, skin=0.3, every=20, newton=False, half=False,
-                 kind=0, rho=0.8442, dt=0.005):
+                 kind=0, rho=0.8442, dt=0.005, masses=None, coeffs=None):
         super().__init__(n, mass, temp, seed, cut, skin, every, newton, half, kind, math.pow(4.0 / rho, 1.0 / 3.0), dt)
-        self.lj1 = np.array([48.0 * 1.0 * math.pow(1.0, 12.0)])
-        self.lj2 = np.array([24.0 * 1.0 * math.pow(1.0, 6.0)])
-        self.cutsq = np.array([cut * cut])
+        self.masses = list(masses) if masses else [mass]
+        nt = len(self.masses)
+        # pair_coeff lines (t1, t2, eps, sigma, cut); with at most 12 types
+        # ForceLJNeigh keeps stack parameters and every pair_coeff line
+        # overwrites all pairs, so the last line holds (force_lj_neigh_impl.h:67-74)
+        coeffs = coeffs or [(1, 1, 1.0, 1.0, cut)]
+        lj1, lj2, cutsq = np.zeros((nt, nt)), np.zeros((nt, nt)), np.zeros((nt, nt))
+        for t1, t2, eps, sig, c in coeffs:
+            if nt <= 12:
+                lj1[:], lj2[:], cutsq[:] = 48.0 * eps * math.pow(sig, 12.0), 24.0 * eps * math.pow(sig, 6.0), c * c
+            else:
+                lj1[t1 - 1, t2 - 1] = lj1[t2 - 1, t1 - 1] = 48.0 * eps * math.pow(sig, 12.0)
+                lj2[t1 - 1, t2 - 1] = lj2[t2 - 1, t1 - 1] = 24.0 * eps * math.pow(sig, 6.0)
+                cutsq[t1 - 1, t2 - 1] = cutsq[t2 - 1, t1 - 1] = c * c
+        self.lj1, self.lj2, self.cutsq = lj1.ravel(), lj2.ravel(), cutsq.ravel()
 
     def force_init(self, b, precision=0):
         b.lj_init(self.lj1, self.lj2, self.cutsq, half=self.half, precision=precision)
@@ -63,8 +76,10 @@ class SnapSetup(Setup):
     boltz, mvv2e = 8.617343e-5, 1.0364269e-4
 
     def __init__(self, nx, ny, nz, snap: dict, a=3.1803, mass=183.84, temp=300.0, seed=4928459, skin=1.0, every=1,
-                 lattice_style=0, dt=0.001):
-        super().__init__(nx, mass, temp, seed, 4.73442, skin, every, True, False, 0, a, dt, ny, nz)
+                 lattice_style=0, dt=0.001, kind=0):
+        # force cutoff: 2 radelem rcutfac of the single element (force_snap_neigh_impl.h:327-333)
+        cut = 2.0 * float(snap["radius"]) * float(snap["params"]["rcutfac"])
+        super().__init__(nx, mass, temp, seed, cut, skin, every, True, False, kind, a, dt, ny, nz)
         self.lattice_style = lattice_style
         self.snap = snap
         p = snap["params"]
@@ -89,14 +104,14 @@ def make_lattice(setup: Setup, threads=1):
     """Initial owned particles from the oracle's Input::create_lattice restatement."""
     from oracle.orc import Oracle
     o = Oracle(threads)
-    o.system_init([setup.mass], setup.boltz, setup.mvv2e, setup.dt, setup.domain)
+    o.system_init(setup.masses, setup.boltz, setup.mvv2e, setup.dt, setup.domain)
     o.create_lattice(setup.lattice_style, setup.a, setup.nx, setup.ny, setup.nz, setup.temp, setup.seed)
     return o.get()
 
 
 def init(b, setup: Setup, state: dict, precision=0):
     """ExaMiniMD::init from the lattice on (examinimd.cpp:120-144)."""
-    b.system_init([setup.mass], setup.boltz, setup.mvv2e, setup.dt, setup.domain)
+    b.system_init(setup.masses, setup.boltz, setup.mvv2e, setup.dt, setup.domain)
     b.set_local(state["x"], state["type"], state["id"], v=state["v"], q=state.get("q"))
     setup.force_init(b, precision)
     b.comm_init(setup.neigh_cut)
@@ -164,6 +179,6 @@ def setup_for_case(name: str, case: dict, g=None) -> Setup:
     if case["kind"] == "lj":
         return LJSetup(case["n"], mass=case["mass"], temp=case["temp"], every=case["every"],
                        newton=case["newton"] == "on", half="NEIGH_HALF" in case["args"],
-                       kind=1 if "2D" in case["args"] else 0)
+                       kind=1 if "2D" in case["args"] else 0, masses=case.get("masses"), coeffs=case.get("coeffs"))
     return SnapSetup(case["nx"], case["ny"], case["nz"], golden_snap(g), a=case["a"], mass=case["mass"],
-                     every=case["every"])
+                     every=case["every"], kind=1 if "2D" in case["args"] else 0)

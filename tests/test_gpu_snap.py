@@ -35,9 +35,14 @@ def _snap_setup(golden, nx=None, ny=None, nz=None, lattice_style=0, a=3.1803):
                             lattice_style=lattice_style), g
 
 
-def test_snap_modules_vs_oracle(golden):
+SNAP_CASES = [k for k, v in CASES.items() if v["kind"] == "snap"]
+
+
+@pytest.mark.parametrize("name", SNAP_CASES)
+def test_snap_modules_vs_oracle(name, golden):
     from oracle.orc import Oracle
-    setup, g = _snap_setup(golden)
+    g = golden(name)
+    setup = mdloop.setup_for_case(name, CASES[name], g)
     state = mdloop.make_lattice(setup)
     gpu, orc = _ctx(), Oracle()
     mdloop.init(gpu, setup, state)
@@ -58,11 +63,12 @@ def test_snap_modules_vs_oracle(golden):
     assert abs(eg - eo) <= 1e-11 * abs(eo)
 
 
-def test_snap_driver_vs_reference_dumps(golden, tmp_path, monkeypatch):
+@pytest.mark.parametrize("name", SNAP_CASES)
+def test_snap_driver_vs_reference_dumps(name, golden, tmp_path, monkeypatch):
     from examinimd_gb300 import MD
     monkeypatch.chdir(tmp_path)  # the deck names its SNAP files relative to the working directory
-    g = golden("snap_W_sc")
-    case = CASES["snap_W_sc"]
+    g = golden(name)
+    case = CASES[name]
     deck, args = write_case(case, str(tmp_path), mdloop.golden_snap(g))
     md = MD(["-il", deck, "--quiet"] + args)
     done = 0
