@@ -595,14 +595,16 @@ def batch_measure(local: int, steps: int, loop_sample: int, loop_steps: int) -> 
     loop_rate = loop_atoms / (loop_ms * 1e-3)
     return {"value": value, "unit": METRIC, "systems": int(len(ns)), "atoms": total, "steps": steps,
             "ms": ms, "atoms_min": int(ns.min()), "atoms_max": int(ns.max()),
-            "shape": {"threads_per_cta": threads, "steps_per_launch": spl, "chosen_by": "emd_batch_tune (40 steps)"},
+            "shape": {"form": "phased (one launch per phase over all systems)" if spl == 0 else
+                      "persistent (one CTA per system)", "threads_per_cta": threads, "steps_per_launch": spl,
+                      "chosen_by": "emd_batch_tune (40 steps)"},
             "create_s": t_create, "energy_drift_rel_per_1000_max": float(drift.max()),
             "looped_fp64": {"value": loop_rate, "unit": METRIC, "sizes_cells": [int(c) for c in pick],
                             "steps_each": loop_steps,
                             "how": "ExaMiniMD driver, FP64 drop-in, one system at a time (wall time incl. launches)"},
             "speedup_vs_looped_fp64": value / loop_rate,
             "config": "256 fcc LJ systems, rho* 0.8442, N log-uniform in [500, 20000] (seed 20261204), T* 1.44 "
-                      "Gaussian velocities, rc 2.5, skin 0.3, every 20, mixed form, CUDA-graph step loop"}
+                      "Gaussian velocities, rc 2.5, skin 0.3, every 20, mixed form, CUDA-graph step loop, tuned form"}
 
 
 def md_row_mean(ctx, nl) -> float:

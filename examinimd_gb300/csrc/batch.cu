@@ -17,8 +17,16 @@
 //
 // Systems are ordered largest first, so their CTAs start first.  The host
 // captures a run's launches (`steps_per_launch` steps each) in a CUDA graph.
-// The CTA size and steps per launch are chosen by timing the candidates on
-// the ensemble itself (emd_batch_tune).
+//
+// A second, phased form keeps the per-system rebuild (wrap, halo, binning)
+// on one CTA per system.  It runs every other phase (NVE, neighbour rows,
+// halo refresh, force) as one launch over 128-atom chunks of all systems,
+// so one large system no longer sets the time of a step.  All of a run's
+// launches again go into one CUDA graph.  Both forms do the same per-atom
+// arithmetic in the same order.
+//
+// emd_batch_tune picks the form, the CTA size and the steps per launch by
+// timing the candidates on the ensemble itself.
 //
 // Differences from the single-system path:
 //   - halo image order (sweeps instead of the six CommSerial phases);
@@ -74,7 +82,8 @@ struct BArgs {
   float nb_lo, nb_hi;  // FP32 decision band of the neighbour test
   LJParamsF P;
   int every;
-  int step0, nsteps;   // steps step0+1 .. step0+nsteps; nsteps == 0: initial build + force
+  int step0, nsteps;   // steps step0+1 .. step0+nsteps
+  int mode;            // k_batch: 0 timesteps, 1 initial build + force, 2 wrap / halo / binning only
 };
 
 // inclusive scan within a warp
@@ -125,6 +134,46 @@ __device__ __noinline__ bool nb_fp64(const double4_32a* __restrict__ x, int i, i
   const double4_32a a = x[i], b = x[j];
   const double dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
   return dx * dx + dy * dy + dz * dz <= cutsq;
+}
+
+// neighbour row of owned atom i (system-local), stencil bins x slowest,
+// each bin in ascending index
+__device__ void build_row(const BArgs& A, const BSys& S, int i) {
+  const double4_32a* x = A.x + S.base;
+  const float4* xl = A.xl + S.base;
+  const int* binof = A.binof + S.base;
+  const int* perm = A.perm + S.base;
+  const int* bstart = A.binstart + S.bin_base;
+  int* rows = A.rows + S.row_base;
+  const int n = S.n;
+  const float wx = float(S.w[0]), wy = float(S.w[1]), wz = float(S.w[2]);
+  const float4 xi = xl[i];
+  int bx, by, bz;
+  bin_coords(S, binof[i], bx, by, bz);
+  int cnt = 0;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int bj = ((bx + dx) * (S.nb[1] + 2) + (by + dy)) * (S.nb[2] + 2) + (bz + dz);
+        const float sx = -dx * wx, sy = -dy * wy, sz = -dz * wz;
+        const int code = ((dx + 1) << 4) | ((dy + 1) << 2) | (dz + 1);
+        const int e1 = bstart[bj + 1];
+        for (int k = bstart[bj]; k < e1; ++k) {
+          const int j = perm[k];
+          if (j == i) continue;
+          const float4 xj = xl[j];
+          const float ddx = (xi.x - xj.x) + sx, ddy = (xi.y - xj.y) + sy, ddz = (xi.z - xj.z) + sz;
+          const float rsq = ddx * ddx + ddy * ddy + ddz * ddz;
+          bool in = rsq < A.nb_lo;
+          if (!in && rsq <= A.nb_hi) in = nb_fp64(x, i, j, A.cutsq_nb);
+          if (in) {
+            if (cnt < A.K) rows[quad_index(i, cnt, n)] = (j << 6) | code;
+            ++cnt;
+          }
+        }
+      }
+  A.num[S.base + i] = cnt;
+  if (cnt > A.K) latch_status(A.status, ST_NEIGH);
 }
 
 __device__ void rebuild(const BArgs& A, const BSys& S, int* sh, int* hist) {
@@ -239,131 +288,116 @@ __device__ void rebuild(const BArgs& A, const BSys& S, int* sh, int* hist) {
   }
   for (int p = tid; p < np; p += T) xl[p] = rel_to_bin(S, x[p], binof[p]);
   __syncthreads();
-  // full neighbour list, one owned atom per thread, stencil bins x slowest
-  int* rows = A.rows + S.row_base;
-  int* num = A.num + S.base;
-  const float wx = float(S.w[0]), wy = float(S.w[1]), wz = float(S.w[2]);
-  for (int i = tid; i < n; i += T) {
-    const float4 xi = xl[i];
-    int bx, by, bz;
-    bin_coords(S, binof[i], bx, by, bz);
-    int cnt = 0;
-    for (int dx = -1; dx <= 1; ++dx)
-      for (int dy = -1; dy <= 1; ++dy)
-        for (int dz = -1; dz <= 1; ++dz) {
-          const int bj = ((bx + dx) * (S.nb[1] + 2) + (by + dy)) * (S.nb[2] + 2) + (bz + dz);
-          const float sx = -dx * wx, sy = -dy * wy, sz = -dz * wz;
-          const int code = ((dx + 1) << 4) | ((dy + 1) << 2) | (dz + 1);
-          const int e1 = bstart[bj + 1];
-          for (int k = bstart[bj]; k < e1; ++k) {
-            const int j = perm[k];
-            if (j == i) continue;
-            const float4 xj = xl[j];
-            const float ddx = (xi.x - xj.x) + sx, ddy = (xi.y - xj.y) + sy, ddz = (xi.z - xj.z) + sz;
-            const float rsq = ddx * ddx + ddy * ddy + ddz * ddz;
-            bool in = rsq < A.nb_lo;
-            if (!in && rsq <= A.nb_hi) in = nb_fp64(x, i, j, A.cutsq_nb);
-            if (in) {
-              if (cnt < A.K) rows[quad_index(i, cnt, n)] = (j << 6) | code;
-              ++cnt;
-            }
-          }
-        }
-    num[i] = cnt;
-    if (cnt > A.K) latch_status(A.status, ST_NEIGH);
-  }
+  // full neighbour list, one owned atom per thread
+  if (A.mode != 2)
+    for (int i = tid; i < n; i += T) build_row(A, S, i);
   __syncthreads();
 }
 
-__device__ void halo_refresh(const BArgs& A, const BSys& S, int ng) {
+__device__ __forceinline__ void halo_ghost(const BArgs& A, const BSys& S, int g) {
   double4_32a* x = A.x + S.base;
-  float4* xl = A.xl + S.base;
-  const int* owner = A.owner + S.base;
-  const int* img = A.img + S.base;
-  const int* binof = A.binof + S.base;
-  for (int g = S.n + threadIdx.x; g < S.n + ng; g += blockDim.x) {
-    double4_32a p = x[owner[g]];
-    const int im = img[g];
-    p.x += ((im & 3) - 1) * S.L[0];
-    p.y += (((im >> 2) & 3) - 1) * S.L[1];
-    p.z += (((im >> 4) & 3) - 1) * S.L[2];
-    x[g] = p;
-    xl[g] = rel_to_bin(S, p, binof[g]);
+  double4_32a p = x[A.owner[S.base + g]];
+  const int im = A.img[S.base + g];
+  p.x += ((im & 3) - 1) * S.L[0];
+  p.y += (((im >> 2) & 3) - 1) * S.L[1];
+  p.z += (((im >> 4) & 3) - 1) * S.L[2];
+  x[g] = p;
+  A.xl[S.base + g] = rel_to_bin(S, p, A.binof[S.base + g]);
+}
+
+__device__ void halo_refresh(const BArgs& A, const BSys& S, int ng) {
+  for (int g = S.n + threadIdx.x; g < S.n + ng; g += blockDim.x) halo_ghost(A, S, g);
+}
+
+__device__ __forceinline__ void force_atom(const BArgs& A, const BSys& S, const float4* shift, int i) {
+  const float4* xl = A.xl + S.base;
+  const int4* rows4 = reinterpret_cast<const int4*>(A.rows + S.row_base);
+  double* f = A.f + 3 * size_t(S.base);
+  PairCtx C;
+  C.xi = xl[i];
+  C.i = i;
+  C.ti = 0;
+  C.shift = shift;
+  C.x4 = A.x + S.base;
+  const int cnt = min(A.num[S.base + i], A.K);
+  const int4* q = rows4 + i;
+  const int nfull = cnt >> 2;
+  Acc acc;
+  for (int kq = 0; kq < nfull; ++kq) lj_quad<true>(C, __ldg(q + size_t(kq) * S.n), xl, A.P, acc);
+  const int rem = cnt & 3;
+  if (rem) {
+    int4 t = __ldg(q + size_t(nfull) * S.n);
+    const int self = (i << 6) | 0x3f;
+    if (rem < 2) t.y = self;
+    if (rem < 3) t.z = self;
+    t.w = self;
+    lj_quad<true>(C, t, xl, A.P, acc);
   }
+  f[3 * i] = double(acc.sxy.x) - double(acc.cxy.x);
+  f[3 * i + 1] = double(acc.sxy.y) - double(acc.cxy.y);
+  f[3 * i + 2] = double(acc.sz) - double(acc.cz);
 }
 
 __device__ void force(const BArgs& A, const BSys& S, const float4* shift) {
-  const float4* xl = A.xl + S.base;
-  const int4* rows4 = reinterpret_cast<const int4*>(A.rows + S.row_base);
-  const int* num = A.num + S.base;
-  double* f = A.f + 3 * size_t(S.base);
-  for (int i = threadIdx.x; i < S.n; i += blockDim.x) {
-    PairCtx C;
-    C.xi = xl[i];
-    C.i = i;
-    C.ti = 0;
-    C.shift = shift;
-    C.x4 = A.x + S.base;
-    const int cnt = min(num[i], A.K);
-    const int4* q = rows4 + i;
-    const int nfull = cnt >> 2;
-    Acc acc;
-    for (int kq = 0; kq < nfull; ++kq) lj_quad<true>(C, __ldg(q + size_t(kq) * S.n), xl, A.P, acc);
-    const int rem = cnt & 3;
-    if (rem) {
-      int4 t = __ldg(q + size_t(nfull) * S.n);
-      const int self = (i << 6) | 0x3f;
-      if (rem < 2) t.y = self;
-      if (rem < 3) t.z = self;
-      t.w = self;
-      lj_quad<true>(C, t, xl, A.P, acc);
-    }
-    f[3 * i] = double(acc.sxy.x) - double(acc.cxy.x);
-    f[3 * i + 1] = double(acc.sxy.y) - double(acc.cxy.y);
-    f[3 * i + 2] = double(acc.sz) - double(acc.cz);
-  }
+  for (int i = threadIdx.x; i < S.n; i += blockDim.x) force_atom(A, S, shift, i);
 }
 
-__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch(BArgs A) {
-  extern __shared__ int hist[];
-  __shared__ int sh[33];
-  __shared__ float4 shift[64];
-  const BSys S = A.sys[blockIdx.x];
+// IntegratorNVE::initial_integrate, with the FP32 bin-relative copy
+__device__ __forceinline__ void nve_initial_atom(const BArgs& A, const BSys& S, int i) {
+  double* v = A.v + 3 * size_t(S.base);
+  const double* f = A.f + 3 * size_t(S.base);
+  double4_32a* x = A.x + S.base;
+  const double vx = fma(A.dtf, f[3 * i], v[3 * i]);
+  const double vy = fma(A.dtf, f[3 * i + 1], v[3 * i + 1]);
+  const double vz = fma(A.dtf, f[3 * i + 2], v[3 * i + 2]);
+  v[3 * i] = vx;
+  v[3 * i + 1] = vy;
+  v[3 * i + 2] = vz;
+  double4_32a p = x[i];
+  p.x = fma(A.dt, vx, p.x);
+  p.y = fma(A.dt, vy, p.y);
+  p.z = fma(A.dt, vz, p.z);
+  x[i] = p;
+  A.xl[S.base + i] = rel_to_bin(S, p, A.binof[S.base + i]);
+}
+
+// IntegratorNVE::final_integrate
+__device__ __forceinline__ void nve_final_atom(const BArgs& A, const BSys& S, int i) {
+  double* v = A.v + 3 * size_t(S.base);
+  const double* f = A.f + 3 * size_t(S.base);
+  v[3 * i] = fma(A.dtf, f[3 * i], v[3 * i]);
+  v[3 * i + 1] = fma(A.dtf, f[3 * i + 1], v[3 * i + 1]);
+  v[3 * i + 2] = fma(A.dtf, f[3 * i + 2], v[3 * i + 2]);
+}
+
+__device__ __forceinline__ void fill_shift(const BSys& S, float4* shift) {
   if (threadIdx.x < 64) {
     const int t = threadIdx.x, kx = (t >> 4) & 3, ky = (t >> 2) & 3, kz = t & 3;
     shift[t] = make_float4(kx == 3 ? 1.0e4f : float(1 - kx) * float(S.w[0]),
                            ky == 3 ? 1.0e4f : float(1 - ky) * float(S.w[1]),
                            kz == 3 ? 1.0e4f : float(1 - kz) * float(S.w[2]), 0.f);
   }
+}
+
+// Persistent form: one CTA advances one system.  mode 1: initial build +
+// force; mode 2: wrap, halo and binning only (the phased form's rebuild);
+// mode 0: nsteps timesteps.
+__global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch(BArgs A) {
+  extern __shared__ int hist[];
+  __shared__ int sh[33];
+  __shared__ float4 shift[64];
+  const BSys S = A.sys[blockIdx.x];
+  fill_shift(S, shift);
   __syncthreads();
-  double4_32a* x = A.x + S.base;
-  float4* xl = A.xl + S.base;
-  double* v = A.v + 3 * size_t(S.base);
-  double* f = A.f + 3 * size_t(S.base);
-  const int* binof = A.binof + S.base;
-  if (A.nsteps == 0) {
+  if (A.mode != 0) {
     rebuild(A, S, sh, hist);
-    force(A, S, shift);
+    if (A.mode == 1) force(A, S, shift);
     return;
   }
   int ng = A.nghost[blockIdx.x];
   for (int s = 1; s <= A.nsteps; ++s) {
     const int step = A.step0 + s;
-    // IntegratorNVE::initial_integrate
-    for (int i = threadIdx.x; i < S.n; i += blockDim.x) {
-      const double vx = fma(A.dtf, f[3 * i], v[3 * i]);
-      const double vy = fma(A.dtf, f[3 * i + 1], v[3 * i + 1]);
-      const double vz = fma(A.dtf, f[3 * i + 2], v[3 * i + 2]);
-      v[3 * i] = vx;
-      v[3 * i + 1] = vy;
-      v[3 * i + 2] = vz;
-      double4_32a p = x[i];
-      p.x = fma(A.dt, vx, p.x);
-      p.y = fma(A.dt, vy, p.y);
-      p.z = fma(A.dt, vz, p.z);
-      x[i] = p;
-      xl[i] = rel_to_bin(S, p, binof[i]);
-    }
+    for (int i = threadIdx.x; i < S.n; i += blockDim.x) nve_initial_atom(A, S, i);
     __syncthreads();
     if (step % A.every == 0) {
       rebuild(A, S, sh, hist);
@@ -373,14 +407,40 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch(BArgs A) {
       __syncthreads();
     }
     force(A, S, shift);
-    // IntegratorNVE::final_integrate (each thread its own atoms, as above)
-    for (int i = threadIdx.x; i < S.n; i += blockDim.x) {
-      v[3 * i] = fma(A.dtf, f[3 * i], v[3 * i]);
-      v[3 * i + 1] = fma(A.dtf, f[3 * i + 1], v[3 * i + 1]);
-      v[3 * i + 2] = fma(A.dtf, f[3 * i + 2], v[3 * i + 2]);
-    }
+    // each thread integrates the atoms it computed the force of
+    for (int i = threadIdx.x; i < S.n; i += blockDim.x) nve_final_atom(A, S, i);
     __syncthreads();
   }
+}
+
+// Phased form: one launch per phase over every system, 128-atom chunks of
+// one system per CTA (chunk table: system, first atom; ghosts relative to
+// the first ghost slot).
+constexpr int BP_THREADS = 128;
+struct BChunk {
+  int sys, first;
+};
+enum { BP_NVE_INITIAL = 0, BP_NEIGH = 1, BP_FORCE = 2, BP_NVE_FINAL = 3, BP_HALO = 4 };
+
+__global__ void __launch_bounds__(BP_THREADS) k_batch_phase(BArgs A, const BChunk* __restrict__ chunks, int phase) {
+  __shared__ float4 shift[64];
+  const BChunk ch = chunks[blockIdx.x];
+  const BSys& S = A.sys[ch.sys];
+  if (phase == BP_FORCE) {
+    fill_shift(S, shift);
+    __syncthreads();
+  }
+  const int k = ch.first + threadIdx.x;
+  if (phase == BP_HALO) {
+    const int ng = min(A.nghost[ch.sys], S.cap - S.n);
+    if (k < ng) halo_ghost(A, S, S.n + k);
+    return;
+  }
+  if (k >= S.n) return;
+  if (phase == BP_NVE_INITIAL) nve_initial_atom(A, S, k);
+  else if (phase == BP_NEIGH) build_row(A, S, k);
+  else if (phase == BP_FORCE) force_atom(A, S, shift, k);
+  else nve_final_atom(A, S, k);
 }
 
 // per system: sum m v^2 over owned atoms and the shifted LJ energy (FP64,
@@ -445,6 +505,11 @@ struct emd_batch {
   size_t smem = 0;
   long long steps_done = 0;
   size_t slots = 0;  // particle slots over all systems (owned + ghost capacity)
+  // phased form: chunk tables of the owned atoms and of the ghost capacity
+  bool phased = false;
+  BChunk* d_chunks = nullptr;
+  BChunk* d_gchunks = nullptr;
+  int n_chunks = 0, n_gchunks = 0;
 };
 
 namespace {
@@ -473,21 +538,49 @@ void batch_check(emd_batch* b) {
   if (st) throw Error(EMD_ERR_BOUNDS, "batch: device status " + std::to_string(st));
 }
 
-void batch_launch(emd_batch* b, int step0, int nsteps, int threads) {
+// persistent launch: nsteps timesteps, or (nsteps == 0) the initial build and force
+void batch_launch(emd_batch* b, int step0, int nsteps, int threads, int mode = -1) {
   BArgs a = b->a;
   a.step0 = step0;
   a.nsteps = nsteps;
+  a.mode = mode >= 0 ? mode : (nsteps == 0 ? 1 : 0);
   k_batch<<<b->nsys, threads, b->smem, b->stream>>>(a);
   EMD_CHECK_LAUNCH();
 }
 
-// runs nsteps as ceil(nsteps / spl) launches captured in one CUDA graph
-void batch_run(emd_batch* b, int nsteps, int threads, int spl) {
+void batch_phase(emd_batch* b, int phase) {
+  const bool ghosts = phase == BP_HALO;
+  k_batch_phase<<<ghosts ? b->n_gchunks : b->n_chunks, BP_THREADS, 0, b->stream>>>(
+      b->a, ghosts ? b->d_gchunks : b->d_chunks, phase);
+  EMD_CHECK_LAUNCH();
+}
+
+// one timestep of the phased form
+void batch_phased_step(emd_batch* b, long long step, int threads) {
+  batch_phase(b, BP_NVE_INITIAL);
+  if (step % b->a.every == 0) {
+    batch_launch(b, 0, 0, threads, 2);  // per system: wrap, halo, binning
+    batch_phase(b, BP_NEIGH);
+  } else {
+    batch_phase(b, BP_HALO);
+  }
+  batch_phase(b, BP_FORCE);
+  batch_phase(b, BP_NVE_FINAL);
+}
+
+// runs nsteps in one CUDA graph: ceil(nsteps / spl) persistent launches, or
+// the phased form's launches per step
+void batch_run(emd_batch* b, int nsteps, int threads, int spl, bool phased) {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   EMD_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   try {
-    for (int s = 0; s < nsteps; s += spl) batch_launch(b, int(b->steps_done + s), std::min(spl, nsteps - s), threads);
+    if (phased) {
+      for (int s = 1; s <= nsteps; ++s) batch_phased_step(b, b->steps_done + s, threads);
+    } else {
+      for (int s = 0; s < nsteps; s += spl)
+        batch_launch(b, int(b->steps_done + s), std::min(spl, nsteps - s), threads);
+    }
   } catch (...) {
     cudaStreamEndCapture(b->stream, &graph);
     if (graph) cudaGraphDestroy(graph);
@@ -590,6 +683,22 @@ emd_status emd_batch_create(emd_batch** out, int device, int nsys, const int* na
   b->thermo.reserve(2 * size_t(nsys), b->stream);
   EMD_CUDA(cudaMalloc(&b->d_sys, sizeof(BSys) * size_t(nsys)));
   EMD_CUDA(cudaMemcpyAsync(b->d_sys, b->sys.data(), sizeof(BSys) * size_t(nsys), cudaMemcpyHostToDevice, b->stream));
+  {
+    std::vector<BChunk> ch, gch;
+    for (int s = 0; s < nsys; ++s) {
+      const BSys& S = b->sys[size_t(s)];
+      for (int f0 = 0; f0 < S.n; f0 += BP_THREADS) ch.push_back(BChunk{s, f0});
+      for (int f0 = 0; f0 < S.cap - S.n; f0 += BP_THREADS) gch.push_back(BChunk{s, f0});
+    }
+    b->n_chunks = int(ch.size());
+    b->n_gchunks = int(gch.size());
+    EMD_CUDA(cudaMalloc(&b->d_chunks, sizeof(BChunk) * ch.size()));
+    EMD_CUDA(cudaMalloc(&b->d_gchunks, sizeof(BChunk) * gch.size()));
+    EMD_CUDA(cudaMemcpyAsync(b->d_chunks, ch.data(), sizeof(BChunk) * ch.size(), cudaMemcpyHostToDevice, b->stream));
+    EMD_CUDA(cudaMemcpyAsync(b->d_gchunks, gch.data(), sizeof(BChunk) * gch.size(), cudaMemcpyHostToDevice,
+                             b->stream));
+    EMD_CUDA(cudaStreamSynchronize(b->stream));
+  }
   // positions / velocities into the device slots (owned atoms keep the caller's order)
   std::vector<double4_32a> hx(ns, make_double4_32a(0, 0, 0, 0));
   std::vector<double> hv(3 * ns, 0.0);
@@ -665,6 +774,8 @@ void emd_batch_destroy(emd_batch* b) {
   b->f.release();
   b->thermo.release();
   if (b->d_sys) cudaFree(b->d_sys);
+  if (b->d_chunks) cudaFree(b->d_chunks);
+  if (b->d_gchunks) cudaFree(b->d_gchunks);
   if (b->d_status) cudaFree(b->d_status);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -676,7 +787,7 @@ emd_status emd_batch_run(emd_batch* b, int nsteps) {
   BATCH_BEGIN
   require(nsteps >= 0, EMD_ERR_ARG, "emd_batch_run: nsteps");
   if (nsteps == 0) return EMD_OK;
-  batch_run(b, nsteps, b->threads, b->steps_per_launch);
+  batch_run(b, nsteps, b->threads, b->steps_per_launch, b->phased);
   batch_check(b);
   BATCH_END
 }
@@ -685,9 +796,10 @@ emd_status emd_batch_set_shape(emd_batch* b, int threads, int steps_per_launch) 
   BATCH_BEGIN
   require(threads >= 64 && threads <= BATCH_MAX_THREADS && threads % 32 == 0, EMD_ERR_ARG,
           "emd_batch_set_shape: threads must be a multiple of 32 in [64, 1024]");
-  require(steps_per_launch >= 1, EMD_ERR_ARG, "emd_batch_set_shape: steps_per_launch");
+  require(steps_per_launch >= 0, EMD_ERR_ARG, "emd_batch_set_shape: steps_per_launch");
   b->threads = threads;
-  b->steps_per_launch = steps_per_launch;
+  b->phased = steps_per_launch == 0;
+  if (!b->phased) b->steps_per_launch = steps_per_launch;
   BATCH_END
 }
 
@@ -710,9 +822,11 @@ emd_status emd_batch_tune(emd_batch* b, int trial_steps, int* threads_out, int* 
   EMD_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
   int bt = b->threads, bs = b->steps_per_launch;
+  bool bp = b->phased;
   const int every = b->a.every;
   for (int threads : {256, 512, 1024}) {
-    for (int spl : {every, 5 * every, trial_steps}) {
+    // steps per launch; 0 = the phased form (its per-system rebuild on `threads`)
+    for (int spl : {0, every, 5 * every, trial_steps}) {
       if (spl > trial_steps) continue;
       // state of the trial's start (a rebuild step boundary)
       EMD_CUDA(cudaMemcpyAsync(b->x.p, x0.p, sizeof(double4_32a) * ns, cudaMemcpyDeviceToDevice, b->stream));
@@ -721,7 +835,7 @@ emd_status emd_batch_tune(emd_batch* b, int trial_steps, int* threads_out, int* 
       b->steps_done = saved_steps;
       batch_launch(b, 0, 0, threads);  // rebuild from the restored positions
       EMD_CUDA(cudaEventRecord(e0, b->stream));
-      batch_run(b, trial_steps, threads, spl);
+      batch_run(b, trial_steps, threads, std::max(spl, 1), spl == 0);
       EMD_CUDA(cudaEventRecord(e1, b->stream));
       EMD_CUDA(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -729,7 +843,8 @@ emd_status emd_batch_tune(emd_batch* b, int trial_steps, int* threads_out, int* 
       if (ms < best) {
         best = ms;
         bt = threads;
-        bs = spl;
+        bp = spl == 0;
+        if (!bp) bs = spl;
       }
     }
   }
@@ -746,8 +861,9 @@ emd_status emd_batch_tune(emd_batch* b, int trial_steps, int* threads_out, int* 
   f0.release();
   b->threads = bt;
   b->steps_per_launch = bs;
+  b->phased = bp;
   if (threads_out) *threads_out = bt;
-  if (spl_out) *spl_out = bs;
+  if (spl_out) *spl_out = bp ? 0 : bs;
   BATCH_END
 }
 
@@ -798,7 +914,7 @@ emd_status emd_batch_info(emd_batch* b, long long* atoms, int* threads, int* ste
   BATCH_BEGIN
   if (atoms) *atoms = b->atoms;
   if (threads) *threads = b->threads;
-  if (steps_per_launch) *steps_per_launch = b->steps_per_launch;
+  if (steps_per_launch) *steps_per_launch = b->phased ? 0 : b->steps_per_launch;
   if (steps_done) *steps_done = b->steps_done;
   BATCH_END
 }

@@ -36,10 +36,13 @@ const char* emd_batch_last_error(const emd_batch* b);
 /* Advances every system nsteps (one CUDA graph of ceil(nsteps /
  * steps_per_launch) launches). */
 emd_status emd_batch_run(emd_batch* b, int nsteps);
-/* CTA size (multiple of 32, 64..1024) and steps per launch. */
+/* CTA size (multiple of 32, 64..1024) and steps per persistent launch; 0
+ * steps per launch selects the phased form: one launch per phase over every
+ * system (128-atom chunks), the per-system rebuild on `threads`-thread CTAs. */
 emd_status emd_batch_set_shape(emd_batch* b, int threads, int steps_per_launch);
-/* Times every candidate shape on trial_steps steps from the current state
- * (restored after each trial), keeps the fastest and reports it. */
+/* Times every candidate shape (persistent and phased) on trial_steps steps
+ * from the current state (restored after each trial), keeps the fastest and
+ * reports it (steps per launch 0: phased). */
 emd_status emd_batch_tune(emd_batch* b, int trial_steps, int* threads, int* steps_per_launch);
 /* Owned atoms' x, v, f in the caller's order (any pointer may be NULL). */
 emd_status emd_batch_get(emd_batch* b, double* x, double* v, double* f);
