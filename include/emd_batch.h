@@ -5,9 +5,11 @@
  *
  * Each system is an orthorhombic box [0, L) with one atom type, LJ eps /
  * sigma with a fixed cutoff, and NVE velocity-Verlet.  Every `every` steps
- * its halo and full neighbour list (cutoff + skin) are rebuilt.  One CTA
- * advances one system for a whole launch, a run's launches are captured in a
- * CUDA graph, and emd_batch_tune times CTA sizes and steps per launch on the
+ * its halo and full neighbour list (cutoff + skin) are rebuilt.  Two forms:
+ * persistent (one CTA advances one system for a whole launch) and phased
+ * (one launch per phase over all systems; the per-system rebuild on one CTA
+ * each).  A run's launches are captured in one CUDA graph, and
+ * emd_batch_tune times the forms, CTA sizes and steps per launch on the
  * ensemble itself.
  *
  * Atom arrays are concatenated over the systems in the caller's order
