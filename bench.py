@@ -367,7 +367,8 @@ def run_gpu_arm(a, ws, rank, local):
     if not a.no_accuracy and a.workload.startswith("lj") and a.precision == "mixed":
         extra["accuracy"] = lj_accuracy(md, wl["cells"], a.drift_steps, local)
     if not a.no_snap and a.workload == "lj4m":
-        extra["snap_w"] = snap_measure(local, a.snap_steps, max(2, a.snap_steps // 5), 3)
+        extra["snap_w"] = snap_measure(local, a.snap_steps, max(2, a.snap_steps // 5), 3,
+                                       with_cpu=(rank == 0 and not a.no_cpu))
     if not a.no_batch and a.workload == "lj4m":
         extra["batched_lj"] = batch_measure(local, a.batch_steps, 8, 20)
     if rank == 0 and not a.no_cpu and not snap:
@@ -474,7 +475,29 @@ def snap_accuracy(md, device: int, cells: int, coeff: str, param: str, steps_don
     return out
 
 
-def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells: int = 40) -> dict:
+def snap_cpu_sample(coeff: str, param: str, cells: int = 10, steps: int = 2) -> dict:
+    """The CPU oracle's SNAP (the reference formulation, serial) on a bcc
+    cells^3 sample of the SNAP-W workload, timed per atom-step."""
+    from oracle.orc import Oracle
+    from tests import mdloop
+    from tests.golden.decks import read_snap_files
+    setup = mdloop.SnapSetup(cells, cells, cells, read_snap_files(coeff, param), a=3.1803, mass=183.84,
+                             lattice_style=2, dt=0.0005)
+    state = mdloop.make_lattice(setup)
+    o = Oracle(1)
+    mdloop.init(o, setup, state)
+    n = o.info()[0]
+    t0 = time.perf_counter()
+    for s_ in range(1, steps + 1):
+        mdloop.step(o, setup, s_)
+    dt = time.perf_counter() - t0
+    return {"value": n * steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"CPU oracle (ExaMiniMD's SNAP formulation, serial), bcc {cells}^3 = {n} atoms of the SNAP-W "
+                      f"workload, {steps} steps (neighbour rebuild every step)"}
+
+
+def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells: int = 40,
+                 with_cpu: bool = True) -> dict:
     """SNAP-W through the driver in both forms: device-timed atom-steps/s, the
     SNAP kernel's share, and the mixed-form force error at step 0."""
     import torch
@@ -516,6 +539,8 @@ def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells
         md.close()
     res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
     res["accuracy"] = acc
+    if with_cpu:
+        res["cpu_baseline"] = snap_cpu_sample(coeff, param)
     res["config"] = SNAP_DESC
     return res
 
