@@ -317,7 +317,7 @@ __device__ __forceinline__ void force_atom(const BArgs& A, const BSys& S, const 
   C.xi = xl[i];
   C.i = i;
   C.ti = 0;
-  C.shift = shift;
+  C.shift = shift + (threadIdx.x & 7);
   C.x4 = A.x + S.base;
   const int cnt = min(A.num[S.base + i], A.K);
   const int4* q = rows4 + i;
@@ -370,10 +370,11 @@ __device__ __forceinline__ void nve_final_atom(const BArgs& A, const BSys& S, in
   v[3 * i + 2] = fma(A.dtf, f[3 * i + 2], v[3 * i + 2]);
 }
 
+// the 64 bin shifts in the eight interleaved copies lj_pair reads
 __device__ __forceinline__ void fill_shift(const BSys& S, float4* shift) {
-  if (threadIdx.x < 64) {
-    const int t = threadIdx.x, kx = (t >> 4) & 3, ky = (t >> 2) & 3, kz = t & 3;
-    shift[t] = make_float4(kx == 3 ? 1.0e4f : float(1 - kx) * float(S.w[0]),
+  for (int u = threadIdx.x; u < 64 * 8; u += blockDim.x) {
+    const int t = u >> 3, kx = (t >> 4) & 3, ky = (t >> 2) & 3, kz = t & 3;
+    shift[u] = make_float4(kx == 3 ? 1.0e4f : float(1 - kx) * float(S.w[0]),
                            ky == 3 ? 1.0e4f : float(1 - ky) * float(S.w[1]),
                            kz == 3 ? 1.0e4f : float(1 - kz) * float(S.w[2]), 0.f);
   }
@@ -385,7 +386,7 @@ __device__ __forceinline__ void fill_shift(const BSys& S, float4* shift) {
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch(BArgs A) {
   extern __shared__ int hist[];
   __shared__ int sh[33];
-  __shared__ float4 shift[64];
+  __shared__ float4 shift[64 * 8];
   const BSys S = A.sys[blockIdx.x];
   fill_shift(S, shift);
   __syncthreads();
@@ -423,7 +424,7 @@ struct BChunk {
 enum { BP_NVE_INITIAL = 0, BP_NEIGH = 1, BP_FORCE = 2, BP_NVE_FINAL = 3, BP_HALO = 4 };
 
 __global__ void __launch_bounds__(BP_THREADS) k_batch_phase(BArgs A, const BChunk* __restrict__ chunks, int phase) {
-  __shared__ float4 shift[64];
+  __shared__ float4 shift[64 * 8];
   const BChunk ch = chunks[blockIdx.x];
   const BSys& S = A.sys[ch.sys];
   if (phase == BP_FORCE) {

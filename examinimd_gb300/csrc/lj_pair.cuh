@@ -55,7 +55,7 @@ struct Acc {
 struct PairCtx {
   float4 xi;
   int i, ti;
-  const float4* shift;  // shared: (1 - k) w per stencil code
+  const float4* shift;  // shared: (1 - k) w per stencil code, copy (lane % 8) of 8 interleaved copies
   const double4_32a* x4;
 };
 
@@ -64,7 +64,7 @@ struct PairCtx {
 template <bool SINGLE>
 __device__ __forceinline__ void lj_pair(const PairCtx& C, int e, const float4& xj, const LJParamsF& P, float2& fxy,
                                         float& fz) {
-  const float4 sh = C.shift[e & 63];
+  const float4 sh = C.shift[(e & 63) << 3];
   float2 dxy = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
   dxy = __fadd2_rn(dxy, make_float2(sh.x, sh.y));
   const float dz = __fadd_rn(__fsub_rn(C.xi.z, xj.z), sh.z);
