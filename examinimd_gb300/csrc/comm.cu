@@ -218,6 +218,7 @@ emd_status emd_comm_update_force(emd_ctx* ctx) {
     pack_off[p] = acc;
     acc += c.num_ghost[p];
   }
+  materialize_kick(c);  // owned forces are about to change
   materialize_zero(c, true, true);
   for (int phase = 5; phase >= 0; --phase) {
     const int count = c.num_ghost[phase];

@@ -189,6 +189,7 @@ void materialize_zero(Ctx& c, bool locals, bool ghosts) {
   const int want = (locals ? 1 : 0) | (ghosts ? 2 : 0);
   const int todo = c.f_zero_pending & want;
   if (!todo) return;
+  materialize_kick(c);
   TimedLaunch t(c, "zero_forces");
   if (todo == 3) {
     EMD_CUDA(cudaMemsetAsync(c.f.p, 0, sizeof(double) * 3 * size_t(c.N_max), c.stream));
@@ -351,6 +352,7 @@ void* emd_stream(emd_ctx* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
 
 emd_status emd_synchronize(emd_ctx* ctx) {
   EMD_API_BEGIN
+  materialize_kick(c);
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   EMD_API_END
 }
@@ -399,6 +401,7 @@ emd_status emd_system_grow(emd_ctx* ctx, int n_max) {
 emd_status emd_system_set_local(emd_ctx* ctx, int n, const double* x, const double* v, const double* f,
                                 const int* type, const int* id, const double* q) {
   EMD_API_BEGIN
+  c.v_kick_pending = false;  // v and f are replaced
   require(n >= 0 && (n == 0 || (x && type && id)), EMD_ERR_ARG, "emd_system_set_local: x, type, id required");
   for (int i = 0; i < n; ++i)
     require(type[i] >= 0 && type[i] < c.ntypes, EMD_ERR_ARG, "emd_system_set_local: type out of range");
@@ -435,6 +438,7 @@ emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x
   EMD_API_BEGIN
   require(first >= 0 && count >= 0 && first + count <= c.N_local, EMD_ERR_ARG, "emd_system_update: range");
   if (count == 0) return EMD_OK;
+  materialize_kick(c);
   if (f) materialize_zero(c, true, false);
   if (x) {
     c.xl_ok &= ~1;
@@ -455,6 +459,7 @@ emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double*
   const int total = c.N_local + c.N_ghost;
   require(first >= 0 && count >= 0 && first + count <= total, EMD_ERR_ARG, "emd_system_get: range");
   if (count == 0) return EMD_OK;
+  materialize_kick(c);
   if (f) materialize_zero(c, first < c.N_local, first + count > c.N_local);
   if (x) {
     c.stage_d.reserve(3 * size_t(count), c.stream);
@@ -492,6 +497,7 @@ emd_status emd_zero_forces(emd_ctx* ctx) {
 emd_status emd_thermo_mv2(emd_ctx* ctx, double* sum_mv2) {
   EMD_API_BEGIN
   require(sum_mv2 != nullptr, EMD_ERR_ARG, "emd_thermo_mv2: null output");
+  materialize_kick(c);
   c.red2.reserve(304, c.stream);
   {
     TimedLaunch t(c, "thermo_mv2");

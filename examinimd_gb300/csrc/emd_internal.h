@@ -165,6 +165,10 @@ struct Ctx {
   // deep_copy(f, 0) not yet applied to owned (1) / ghost (2) rows; the full-list
   // LJ kernels fold it into their stores, every other reader applies it first
   int f_zero_pending = 0;
+  // IntegratorNVE::final_integrate recorded but not applied: the next
+  // initial_integrate applies both half kicks in one pass; any other reader
+  // or writer of v or f applies it first (materialize_kick)
+  bool v_kick_pending = false;
   DevBuf<double> dtfm_d;  // dtf / mass per type (integrator_nve.cpp:66)
   DevBuf<double> red, red2;  // reduction partials
 
@@ -210,12 +214,15 @@ constexpr int kSumScratchDoubles = 305;
 void device_sum_launch(Ctx& c, const double* d_vals, int n, double* scratch);
 
 unsigned read_status(Ctx& c, bool clear);
-// applies a pending deep_copy(f, 0) to owned and/or ghost rows
+// applies a pending deep_copy(f, 0) to owned and/or ghost rows (after any
+// pending final half kick, which still needs the forces)
 void materialize_zero(Ctx& c, bool locals, bool ghosts);
+// applies a pending final half kick (integrate.cu)
+void materialize_kick(Ctx& c);
 // mixed-form hooks (lj_mixed.cu)
 bool mixed_xl_active(const Ctx& c);
 void lj_mixed_after_build(Ctx& c);
-void nve_initial_mixed(Ctx& c);
+void nve_initial_mixed(Ctx& c, bool kick_first);
 void nve_final_mixed(Ctx& c);
 
 }  // namespace emd

@@ -285,6 +285,7 @@ emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double
 
 emd_status emd_lj_compute(emd_ctx* ctx) {
   EMD_API_BEGIN
+  materialize_kick(c);  // the forces are about to be overwritten
   require(c.lj_ready, EMD_ERR_STATE, "emd_lj_compute: emd_lj_init not called");
   require(c.neigh_ready && c.neigh_rows == c.N_local, EMD_ERR_STATE, "emd_lj_compute: no current neighbour list");
   require(c.half_neigh == c.lj_half, EMD_ERR_STATE, "emd_lj_compute: list fullness does not match the force");

@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restric
 
 // IntegratorNVE::initial_integrate (integrator_nve.cpp:64-73) with FMA, plus
 // the FP32 bin-relative copy of the new position
+template <bool KICK>
 __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restrict__ x4, double* __restrict__ v,
                                                            const double* __restrict__ f, const int* __restrict__ type,
                                                            const double* __restrict__ dtfm_t, double dtv,
@@ -64,9 +65,16 @@ __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restri
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double dtfm = dtfm_t[type[i]];
-  const double vx = fma(dtfm, f[3 * i], v[3 * i]);
-  const double vy = fma(dtfm, f[3 * i + 1], v[3 * i + 1]);
-  const double vz = fma(dtfm, f[3 * i + 2], v[3 * i + 2]);
+  const double fx = f[3 * i], fy = f[3 * i + 1], fz = f[3 * i + 2];
+  double vx = v[3 * i], vy = v[3 * i + 1], vz = v[3 * i + 2];
+  if (KICK) {  // the previous step's final half kick, then this one
+    vx = fma(dtfm, fx, vx);
+    vy = fma(dtfm, fy, vy);
+    vz = fma(dtfm, fz, vz);
+  }
+  vx = fma(dtfm, fx, vx);
+  vy = fma(dtfm, fy, vy);
+  vz = fma(dtfm, fz, vz);
   v[3 * i] = vx;
   v[3 * i + 1] = vy;
   v[3 * i + 2] = vz;
@@ -183,12 +191,13 @@ bool mixed_xl_active(const Ctx& c) {
   return c.lj_ready && c.lj_prec == EMD_PREC_MIXED && c.neigh_ready && c.neigh_packed;
 }
 
-void nve_initial_mixed(Ctx& c) {
+void nve_initial_mixed(Ctx& c, bool kick_first) {
   const bool live = mixed_xl_active(c);
-  TimedLaunch t(c, "nve_initial");
-  k_nve_initial_mixed<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(
-      c.x4.p, c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.dt, live ? c.bin_ctr.p : nullptr, live ? c.xl.p : nullptr,
-      c.N_local);
+  TimedLaunch t(c, kick_first ? "nve_final_initial" : "nve_initial");
+  auto k = kick_first ? k_nve_initial_mixed<true> : k_nve_initial_mixed<false>;
+  k<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.dt,
+                                                       live ? c.bin_ctr.p : nullptr, live ? c.xl.p : nullptr,
+                                                       c.N_local);
   EMD_CHECK_LAUNCH();
   if (!live) c.xl_ok &= ~1;
 }
@@ -200,6 +209,7 @@ void nve_final_mixed(Ctx& c) {
 }
 
 void lj_mixed_compute(Ctx& c) {
+  materialize_kick(c);
   const int n_all = c.N_local + c.N_ghost;
   const BinFrame F = frame(c);
   if (c.xl_ok != 3) {

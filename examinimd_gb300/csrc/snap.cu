@@ -814,7 +814,10 @@ static void snap_launch(Ctx& c, bool energy) {
   require(!c.neigh_packed, EMD_ERR_STATE, "SNAP reads plain neighbour rows");
   const int n = c.N_local;
   if (n == 0) return;
-  if (!energy) materialize_zero(c, true, true);
+  if (!energy) {
+    materialize_kick(c);  // the forces are about to be overwritten
+    materialize_zero(c, true, true);
+  }
   SnapArgs A;
   A.S = h->d;
   A.x4 = c.x4.p;
