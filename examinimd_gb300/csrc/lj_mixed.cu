@@ -99,6 +99,15 @@ __global__ void __launch_bounds__(256) k_nve_final_mixed(double* __restrict__ v,
 
 // One thread per owned atom; four list entries per coalesced int4 load, the
 // next granule prefetched while the current four pairs are evaluated.
+// a granule of the neighbour list: read once, so it bypasses L1 and leaves
+// the L1 lines to the gathered neighbour positions
+__device__ __forceinline__ int4 ld_list(const int4* p) {
+  int4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+  return r;
+}
+
 template <bool SINGLE, bool ZERO>
 __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict__ xl,
                                                        const double4_32a* __restrict__ x4, double* __restrict__ f,
@@ -127,9 +136,9 @@ __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict_
   const int4* q = rows4 + i;
   const int nfull = cnt >> 2;
   Acc acc;
-  int4 e = nfull > 0 ? __ldg(q) : make_int4(0, 0, 0, 0);
+  int4 e = nfull > 0 ? ld_list(q) : make_int4(0, 0, 0, 0);
   for (int kq = 0; kq < nfull; ++kq) {
-    const int4 en = (kq + 1 < nfull) ? __ldg(q + (size_t)(kq + 1) * stride) : e;
+    const int4 en = (kq + 1 < nfull) ? ld_list(q + (size_t)(kq + 1) * stride) : e;
     lj_quad<SINGLE>(C, e, xl, P, acc);
     e = en;
   }
@@ -137,7 +146,7 @@ __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict_
   if (rem) {
     // unused slots of the last granule become padding: i itself with the
     // code k = (3, 3, 3), far outside the cutoff, so they add nothing
-    int4 t = __ldg(q + (size_t)nfull * stride);
+    int4 t = ld_list(q + (size_t)nfull * stride);
     const int self = (i << 6) | 0x3f;
     if (rem < 2) t.y = self;
     if (rem < 3) t.z = self;
