@@ -141,16 +141,25 @@ void ForceSNAP_GB300::init_coeff(int narg, char** arg) {
   std::vector<std::string> elements;
   for (int i = 0; i < nelements; i++) elements.push_back(arg[4 + i]);
   SnapFiles sf = read_snap_files(arg[3], arg[4 + nelements], elements);
-  std::vector<int> map(size_t(ntypes), -1);
+  // ExaMiniMD fills map[1..ntypes] with the element named for each 1-based
+  // type, in a view of nelements + 1 entries whose entry 0 stays zero, and
+  // then reads map[type] with the 0-based atom type (force_snap_neigh_impl.h:
+  // 247, 294-306, 598, 623): type 0 takes element 0 and type t >= 1 the
+  // element named for type t.  The same lookup is handed to the device.
+  std::vector<int> named(size_t(ntypes) + 1, 0);
   for (int i = 1; i <= ntypes; i++) {
     const std::string e = arg[5 + nelements + i - 1];
     int jelem = 0;
     for (; jelem < nelements; jelem++)
       if (e == elements[size_t(jelem)]) break;
-    if (jelem < nelements) map[size_t(i - 1)] = jelem;
-    else if (e == "NULL") map[size_t(i - 1)] = -1;
+    if (jelem < nelements) named[size_t(i)] = jelem;
+    else if (e == "NULL") named[size_t(i)] = -1;
     else throw HostError("Incorrect args for pair coefficients");
   }
+  if (ntypes > nelements + 1)
+    throw HostError("SNAP: more atom types than the reference's element map holds (nelements + 1)");
+  std::vector<int> map(size_t(ntypes), 0);
+  for (int t = 1; t < ntypes; t++) map[size_t(t)] = named[size_t(t)];
   rcutmax = 0.0;
   for (int e = 0; e < nelements; e++) rcutmax = std::max(2.0 * sf.radelem[size_t(e)] * sf.rcutfac, rcutmax);
   check(emd_snap_init(system_->ctx, sf.twojmax, sf.rfac0, sf.rmin0, sf.switchflag, sf.rcutfac, nelements,

@@ -33,11 +33,11 @@ SNAP = """units metal
 newton on
 lattice sc {a}
 region box block 0 {nx} 0 {ny} 0 {nz}
-create_box 1 box
+create_box {ntypes} box
 create_atoms 1 box
-mass 1 {mass}
+{mass_lines}
 pair_style snap
-pair_coeff * * {coeff} {elem} {param} {elem}
+pair_coeff * * {coeff} {elem_names} {param} {type_elems}
 thermo {thermo}
 neighbor 1.0 bin
 neigh_modify once no every {every} delay 0 check yes
@@ -76,6 +76,15 @@ CASES = {
     "snap_W_sc": dict(kind="snap", a=3.1803, nx=4, ny=8, nz=8, mass=183.84, elem="W", every=1, thermo=5, steps=5,
                       coeff="W.snapcoeff", param="W.snapparam",
                       args=["--neigh-type", "CSR", "--comm-type", "SERIAL"], dump_every=5, keep_steps=[0, 5]),
+    # two SNAP elements on two types (Ta06A parameters, synthetic second
+    # element): type 1 names B, type 2 names A.  ExaMiniMD reads the element
+    # of 0-based type t from map[t], which it filled at 1-based indices, so
+    # type 0 takes element 0 (A) and type 1 the element named first (B).
+    "snap_AB_sc": dict(kind="snap", a=3.316, nx=4, ny=4, nz=4, mass=180.88, masses=[180.88, 150.0],
+                       elem="A", elems=["A", "B"], type_elems=["B", "A"], every=1, thermo=5, steps=10,
+                       coeff="AB.snapcoeff", param="Ta06A.snapparam", synthetic_second=dict(radius=0.46, weight=0.85,
+                                                                                           scale=0.9, seed=11),
+                       args=["--neigh-type", "CSR", "--comm-type", "SERIAL"], dump_every=5, keep_steps=[0, 5, 10]),
     # SNAP Ta, the shipped in.snap.Ta06A geometry (sc 4^3 = 64 atoms, twojmax 6), 2D list
     "snap_Ta_sc": dict(kind="snap", a=3.316, nx=4, ny=4, nz=4, mass=180.88, elem="Ta", every=1, thermo=5, steps=10,
                        coeff="Ta06A.snapcoeff", param="Ta06A.snapparam",
@@ -83,7 +92,23 @@ CASES = {
 }
 
 
+def snap_elements(snap: dict) -> list[dict]:
+    """The element records of a SNAP number set (one-element sets keep the
+    flat elem / radius / weight / beta keys)."""
+    if "elements" in snap:
+        return snap["elements"]
+    return [dict(name=snap["elem"], radius=snap["radius"], weight=snap["weight"], beta=snap["beta"])]
+
+
 def deck_text(case: dict) -> str:
+    if case["kind"] == "snap":
+        masses = case.get("masses", [case["mass"]])
+        elems = case.get("elems", [case["elem"]])
+        fields = {k: v for k, v in case.items() if k not in ("type_elems", "elems", "masses")}
+        return SNAP.format(ntypes=len(masses),
+                           mass_lines="\n".join(f"mass {t + 1} {m}" for t, m in enumerate(masses)),
+                           elem_names=" ".join(elems),
+                           type_elems=" ".join(case.get("type_elems", [case["elem"]] * len(masses))), **fields)
     if case["kind"] == "lj":
         masses = case.get("masses", [case["mass"]])
         coeffs = case.get("coeffs", [(1, 1, 1.0, 1.0, 2.5)])
@@ -95,11 +120,15 @@ def deck_text(case: dict) -> str:
 
 
 def write_snap_files(work: str, case: dict, snap: dict) -> None:
-    """snap: elem, radius, weight, beta (ncoeffall floats), params {key: value}."""
+    """snap: elem, radius, weight, beta (ncoeffall floats) -- or a list of
+    such records under "elements" -- and params {key: value}."""
+    elems = snap_elements(snap)
     with open(os.path.join(work, case["coeff"]), "w") as fp:
-        fp.write(f"1 {len(snap['beta'])}\n{snap['elem']} {snap['radius']!r} {snap['weight']!r}\n")
-        for b in snap["beta"]:
-            fp.write(f"{float(b)!r}\n")
+        fp.write(f"{len(elems)} {len(elems[0]['beta'])}\n")
+        for e in elems:
+            fp.write(f"{e['name']} {float(e['radius'])!r} {float(e['weight'])!r}\n")
+            for b in e["beta"]:
+                fp.write(f"{float(b)!r}\n")
     with open(os.path.join(work, case["param"]), "w") as fp:
         for k, v in snap["params"].items():
             fp.write(f"{k} {v}\n")

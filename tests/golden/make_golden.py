@@ -29,7 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from tests.golden.decks import CASES, read_snap_files, write_case  # noqa: E402
+from tests.golden.decks import CASES, read_snap_files, snap_elements, write_case  # noqa: E402
 
 
 def read_probe(path: str) -> dict:
@@ -96,7 +96,18 @@ def main() -> None:
             snap = None
             if case["kind"] == "snap":
                 sd = os.path.join(a.ref, "input", "snap")
-                snap = read_snap_files(os.path.join(sd, case["coeff"]), os.path.join(sd, case["param"]))
+                if "synthetic_second" in case:
+                    # the shipped Ta06A numbers as element A, a seeded variant as element B
+                    base = read_snap_files(os.path.join(sd, "Ta06A.snapcoeff"), os.path.join(sd, case["param"]))
+                    sp = case["synthetic_second"]
+                    rng = np.random.default_rng(sp["seed"])
+                    beta_b = [b * sp["scale"] + float(rng.normal(0.0, 0.01)) for b in base["beta"]]
+                    snap = dict(elements=[dict(name="A", radius=base["radius"], weight=base["weight"],
+                                               beta=base["beta"]),
+                                          dict(name="B", radius=sp["radius"], weight=sp["weight"], beta=beta_b)],
+                                params=base["params"])
+                else:
+                    snap = read_snap_files(os.path.join(sd, case["coeff"]), os.path.join(sd, case["param"]))
             deck, args = write_case(case, work, snap)
             dump_dir = os.path.join(work, "dump")
             os.makedirs(dump_dir)
@@ -114,10 +125,15 @@ def main() -> None:
                     data[f"s{step}_{k}"] = v
             data["keep_steps"] = np.array(case["keep_steps"], np.int32)
             if snap is not None:
-                data["snap_elem"] = np.array(snap["elem"])
-                data["snap_radius"] = np.array(snap["radius"])
-                data["snap_weight"] = np.array(snap["weight"])
-                data["snap_beta"] = np.array(snap["beta"])
+                elems = snap_elements(snap)
+                data["snap_elem"] = np.array(elems[0]["name"])
+                data["snap_radius"] = np.array(elems[0]["radius"])
+                data["snap_weight"] = np.array(elems[0]["weight"])
+                data["snap_beta"] = np.array(elems[0]["beta"])
+                data["snap_elems"] = np.array([e["name"] for e in elems])
+                data["snap_radii"] = np.array([e["radius"] for e in elems])
+                data["snap_weights"] = np.array([e["weight"] for e in elems])
+                data["snap_betas"] = np.array([e["beta"] for e in elems])
                 data["snap_param_keys"] = np.array(list(snap["params"].keys()))
                 data["snap_param_vals"] = np.array(list(snap["params"].values()))
             out = os.path.join(HERE, f"{name}.npz")

@@ -76,10 +76,25 @@ class SnapSetup(Setup):
     boltz, mvv2e = 8.617343e-5, 1.0364269e-4
 
     def __init__(self, nx, ny, nz, snap: dict, a=3.1803, mass=183.84, temp=300.0, seed=4928459, skin=1.0, every=1,
-                 lattice_style=0, dt=0.001, kind=0):
-        # force cutoff: 2 radelem rcutfac of the single element (force_snap_neigh_impl.h:327-333)
-        cut = 2.0 * float(snap["radius"]) * float(snap["params"]["rcutfac"])
+                 lattice_style=0, dt=0.001, kind=0, masses=None, type_elems=None):
+        elems = snap["elements"] if "elements" in snap else [
+            dict(name=snap["elem"], radius=snap["radius"], weight=snap["weight"], beta=snap["beta"])]
+        # ExaMiniMD's read_files deep-copies each element's radius and weight
+        # into the whole radelem / wjelem views (force_snap_neigh_impl.h:458-461):
+        # every element ends with the values of the last one read
+        elems = [dict(e, radius=elems[-1]["radius"], weight=elems[-1]["weight"]) for e in elems]
+        # force cutoff: the largest 2 radelem rcutfac (force_snap_neigh_impl.h:327-333)
+        cut = max(2.0 * float(e["radius"]) * float(snap["params"]["rcutfac"]) for e in elems)
         super().__init__(nx, mass, temp, seed, cut, skin, every, True, False, kind, a, dt, ny, nz)
+        self.elements = elems
+        self.masses = list(masses) if masses else [mass]
+        names = [e["name"] for e in elems]
+        nt = len(self.masses)
+        type_elems = type_elems or [names[0]] * nt
+        # ExaMiniMD fills map[1..ntypes] from the element names and reads
+        # map[type] with 0-based types (force_snap_neigh_impl.h:294-306, 598):
+        # type 0 gets element 0, type t >= 1 the element named for type t
+        self.type_map = [0] + [names.index(type_elems[t - 1]) for t in range(1, nt)]
         self.lattice_style = lattice_style
         self.snap = snap
         p = snap["params"]
@@ -90,8 +105,10 @@ class SnapSetup(Setup):
         self.switchflag = int(p.get("switchflag", 1))
 
     def force_init(self, b, precision=0):
-        b.snap_init(self.twojmax, self.rfac0, self.rmin0, self.switchflag, self.rcutfac, [self.snap["radius"]],
-                    [self.snap["weight"]], np.asarray(self.snap["beta"], float)[None, :], [0], precision=precision)
+        elems = self.elements
+        b.snap_init(self.twojmax, self.rfac0, self.rmin0, self.switchflag, self.rcutfac,
+                    [e["radius"] for e in elems], [e["weight"] for e in elems],
+                    np.asarray([e["beta"] for e in elems], float), self.type_map, precision=precision)
 
     def force_compute(self, b):
         b.snap_compute()
@@ -170,9 +187,14 @@ def rows(num, ent):
 
 def golden_snap(g) -> dict:
     """SNAP file numbers stored in a golden fixture."""
-    return dict(elem=str(g["snap_elem"]), radius=float(g["snap_radius"]), weight=float(g["snap_weight"]),
-                beta=list(g["snap_beta"]), params=dict(zip([str(k) for k in g["snap_param_keys"]],
-                                                           [str(v) for v in g["snap_param_vals"]])))
+    out = dict(elem=str(g["snap_elem"]), radius=float(g["snap_radius"]), weight=float(g["snap_weight"]),
+               beta=list(g["snap_beta"]), params=dict(zip([str(k) for k in g["snap_param_keys"]],
+                                                          [str(v) for v in g["snap_param_vals"]])))
+    if "snap_elems" in g.files and len(g["snap_elems"]) > 1:
+        out["elements"] = [dict(name=str(n), radius=float(r), weight=float(w), beta=list(b))
+                           for n, r, w, b in zip(g["snap_elems"], g["snap_radii"], g["snap_weights"],
+                                                 g["snap_betas"])]
+    return out
 
 
 def setup_for_case(name: str, case: dict, g=None) -> Setup:
@@ -181,4 +203,5 @@ def setup_for_case(name: str, case: dict, g=None) -> Setup:
                        newton=case["newton"] == "on", half="NEIGH_HALF" in case["args"],
                        kind=1 if "2D" in case["args"] else 0, masses=case.get("masses"), coeffs=case.get("coeffs"))
     return SnapSetup(case["nx"], case["ny"], case["nz"], golden_snap(g), a=case["a"], mass=case["mass"],
-                     every=case["every"], kind=1 if "2D" in case["args"] else 0)
+                     every=case["every"], kind=1 if "2D" in case["args"] else 0, masses=case.get("masses"),
+                     type_elems=case.get("type_elems"))
