@@ -156,6 +156,8 @@ struct Ctx {
   bool lj_ready = false;
   DevBuf<double> lj_params;  // lj1 | lj2 | cutsq, ntypes^2 each
   DevBuf<float> lj_params_f; // FP32 copy for the mixed form
+  DevBuf<double> lj_intensity;  // lj/cut/idial repeat counts per type pair
+  bool lj_idial = false;
   bool lj_uniform = false;   // every type pair has the same parameters
   float lj_single[3] = {0, 0, 0};
   double lj_single_cutsq_d = 0;

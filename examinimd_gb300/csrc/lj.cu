@@ -23,13 +23,33 @@ struct LJParams {
   const double* lj2;
   const double* cutsq;
   int ntypes;
+  const double* intensity;  // lj/cut/idial: repeat count per type pair (as doubles)
 };
+
+// pair force over r: the plain LJ term, or (IDIAL) ForceLJIDialNeigh's
+// repeated evaluation, each repeat adding 1/intensity of the term
+// (force_lj_idial_neigh_impl.h:137-149)
+template <bool IDIAL>
+__device__ __forceinline__ double lj_fpair(double rsq, double lj1, double lj2, double inten) {
+  if (!IDIAL) {
+    const double r2inv = 1.0 / rsq;
+    const double r6inv = r2inv * r2inv * r2inv;
+    return (r6inv * (lj1 * r6inv - lj2)) * r2inv;
+  }
+  double fpair = 0.0;
+  for (int repeat = 0; repeat < inten; repeat++) {
+    const double r2inv = 1.0 / rsq;
+    const double r6inv = r2inv * r2inv * r2inv;
+    fpair += (r6inv * (lj1 * r6inv - lj2)) * r2inv / inten;
+  }
+  return fpair;
+}
 
 __device__ __forceinline__ int entry_j(int e, bool packed) { return packed ? (e >> 6) : e; }
 
 // TagFullNeigh (force_lj_neigh_impl.h:164-206).  ZERO folds the pending
 // deep_copy(f, 0) into the store as 0.0 + sum, the reference's exact result.
-template <bool TWO_D, bool ZERO>
+template <bool TWO_D, bool ZERO, bool IDIAL = false>
 __global__ void __launch_bounds__(128) k_lj_full_fp64(const double4_32a* __restrict__ x4, double* __restrict__ f,
                                                       ListView L, LJParams P, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -49,11 +69,8 @@ __global__ void __launch_bounds__(128) k_lj_full_fp64(const double4_32a* __restr
     const int tp = ti * P.ntypes + tj;
     const double cutsq_ij = __ldg(P.cutsq + tp);
     if (rsq < cutsq_ij) {
-      const double lj1_ij = __ldg(P.lj1 + tp);
-      const double lj2_ij = __ldg(P.lj2 + tp);
-      const double r2inv = 1.0 / rsq;
-      const double r6inv = r2inv * r2inv * r2inv;
-      const double fpair = (r6inv * (lj1_ij * r6inv - lj2_ij)) * r2inv;
+      const double fpair = lj_fpair<IDIAL>(rsq, __ldg(P.lj1 + tp), __ldg(P.lj2 + tp),
+                                           IDIAL ? __ldg(P.intensity + tp) : 1.0);
       fxi += dx * fpair;
       fyi += dy * fpair;
       fzi += dz * fpair;
@@ -71,7 +88,9 @@ __global__ void __launch_bounds__(128) k_lj_full_fp64(const double4_32a* __restr
 }
 
 // TagHalfNeigh (force_lj_neigh_impl.h:211-254)
-template <bool TWO_D>
+// IDIAL: ForceLJIDialNeigh's half form scatters to owned partners only
+// (force_lj_idial_neigh_impl.h:199-203)
+template <bool TWO_D, bool IDIAL = false>
 __global__ void __launch_bounds__(128) k_lj_half_fp64(const double4_32a* __restrict__ x4, double* __restrict__ f,
                                                       ListView L, LJParams P, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -90,15 +109,16 @@ __global__ void __launch_bounds__(128) k_lj_half_fp64(const double4_32a* __restr
     const double rsq = dx * dx + dy * dy + dz * dz;
     const int tp = ti * P.ntypes + tj;
     if (rsq < __ldg(P.cutsq + tp)) {
-      const double r2inv = 1.0 / rsq;
-      const double r6inv = r2inv * r2inv * r2inv;
-      const double fpair = (r6inv * (__ldg(P.lj1 + tp) * r6inv - __ldg(P.lj2 + tp))) * r2inv;
+      const double fpair = lj_fpair<IDIAL>(rsq, __ldg(P.lj1 + tp), __ldg(P.lj2 + tp),
+                                           IDIAL ? __ldg(P.intensity + tp) : 1.0);
       fxi += dx * fpair;
       fyi += dy * fpair;
       fzi += dz * fpair;
-      atomicAdd(f + 3 * j, -(dx * fpair));
-      atomicAdd(f + 3 * j + 1, -(dy * fpair));
-      atomicAdd(f + 3 * j + 2, -(dz * fpair));
+      if (!IDIAL || j < n) {
+        atomicAdd(f + 3 * j, -(dx * fpair));
+        atomicAdd(f + 3 * j + 1, -(dy * fpair));
+        atomicAdd(f + 3 * j + 2, -(dz * fpair));
+      }
     }
   }
   atomicAdd(f + 3 * i, fxi);
@@ -211,7 +231,8 @@ ListView list_view(Ctx& c) {
 
 static LJParams lj_params(Ctx& c) {
   const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
-  return LJParams{c.lj_params.p, c.lj_params.p + nt2, c.lj_params.p + 2 * nt2, c.lj_ntypes};
+  return LJParams{c.lj_params.p, c.lj_params.p + nt2, c.lj_params.p + 2 * nt2, c.lj_ntypes,
+                  c.lj_idial ? c.lj_intensity.p : nullptr};
 }
 
 // ---- scratch of emd_lj_energy_noalloc
@@ -272,6 +293,7 @@ emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double
   EMD_CUDA(cudaMemcpyAsync(c.lj_params.p, h.data(), sizeof(double) * 3 * nt2, cudaMemcpyHostToDevice, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   c.lj_ntypes = ntypes;
+  c.lj_idial = false;  // emd_lj_set_intensity after this call selects lj/cut/idial
   c.lj_half = half_neigh ? 1 : 0;
   c.lj_prec = precision;
   c.lj_ready = true;
@@ -306,18 +328,49 @@ emd_status emd_lj_compute(emd_ctx* ctx) {
   TimedLaunch t(c, c.lj_half ? "lj_half_fp64" : "lj_full_fp64");
   if (!c.lj_half) {
     if (two_d) {
-      if (zero) k_lj_full_fp64<true, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
-      else k_lj_full_fp64<true, false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      if (c.lj_idial) {
+        if (zero) k_lj_full_fp64<true, true, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+        else k_lj_full_fp64<true, false, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      } else {
+        if (zero) k_lj_full_fp64<true, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+        else k_lj_full_fp64<true, false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      }
     } else {
-      if (zero) k_lj_full_fp64<false, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
-      else k_lj_full_fp64<false, false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      if (c.lj_idial) {
+        if (zero) k_lj_full_fp64<false, true, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+        else k_lj_full_fp64<false, false, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      } else {
+        if (zero) k_lj_full_fp64<false, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+        else k_lj_full_fp64<false, false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      }
     }
     c.f_zero_pending &= ~1;
   } else {
-    if (two_d) k_lj_half_fp64<true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
-    else k_lj_half_fp64<false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    if (c.lj_idial) {
+      if (two_d) k_lj_half_fp64<true, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      else k_lj_half_fp64<false, true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    } else {
+      if (two_d) k_lj_half_fp64<true><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+      else k_lj_half_fp64<false><<<grid, 128, 0, c.stream>>>(c.x4.p, c.f.p, L, P, n);
+    }
   }
   EMD_CHECK_LAUNCH();
+  EMD_API_END
+}
+
+emd_status emd_lj_set_intensity(emd_ctx* ctx, const double* intensity) {
+  EMD_API_BEGIN
+  require(c.lj_ready, EMD_ERR_STATE, "emd_lj_set_intensity: emd_lj_init first");
+  if (!intensity) {
+    c.lj_idial = false;
+    return EMD_OK;
+  }
+  require(c.lj_prec == EMD_PREC_FP64, EMD_ERR_ARG, "emd_lj_set_intensity: the FP64 form only");
+  const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
+  c.lj_intensity.reserve(nt2, c.stream);
+  EMD_CUDA(cudaMemcpyAsync(c.lj_intensity.p, intensity, sizeof(double) * nt2, cudaMemcpyHostToDevice, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  c.lj_idial = true;
   EMD_API_END
 }
 

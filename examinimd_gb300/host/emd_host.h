@@ -18,7 +18,7 @@ namespace emdhost {
 
 enum { UNITS_REAL, UNITS_LJ, UNITS_METAL };
 enum { LATTICE_SC, LATTICE_FCC, LATTICE_BCC };
-enum { FORCE_LJ, FORCE_SNAP };
+enum { FORCE_LJ, FORCE_SNAP, FORCE_LJ_IDIAL };
 enum { FORCE_ITER_NEIGH_FULL, FORCE_ITER_NEIGH_HALF };
 enum { NEIGH_CSR, NEIGH_2D };
 enum { COMM_SERIAL };
@@ -144,14 +144,18 @@ class ForceLJNeigh_GB300 : public Force {
   System* system_;
   int ntypes_;
   int precision_;
-  std::vector<double> lj1_, lj2_, cutsq_;
+  bool idial_;  // pair_style lj/cut/idial (ForceLJIDialNeigh)
+  std::vector<double> lj1_, lj2_, cutsq_, intensity_;
 
  public:
-  ForceLJNeigh_GB300(System* system, bool half, int precision);
+  ForceLJNeigh_GB300(System* system, bool half, int precision, bool idial = false);
   void init_coeff(int nargs, char** args) override;
   void compute(System* system, Binning*, Neighbor*) override;
   double compute_energy(System* system, Binning*, Neighbor*) override;
-  const char* name() override { return half_neigh ? "ForceLJNeighHalf_GB300" : "ForceLJNeighFull_GB300"; }
+  const char* name() override {
+    if (idial_) return half_neigh ? "ForceLJIDialNeighHalf_GB300" : "ForceLJIDialNeighFull_GB300";
+    return half_neigh ? "ForceLJNeighHalf_GB300" : "ForceLJNeighFull_GB300";
+  }
 };
 
 // ForceSNAP (force_snap_neigh.h, force_snap_neigh_impl.h:228-587)

@@ -109,6 +109,8 @@ void ExaMiniMD::init(int argc, const char* const* argv) {
 
   const bool half_neigh = input->force_iteration_type == FORCE_ITER_NEIGH_HALF;
   if (input->force_type == FORCE_LJ) force = new ForceLJNeigh_GB300(system, half_neigh, input->precision);
+  else if (input->force_type == FORCE_LJ_IDIAL)
+    force = new ForceLJNeigh_GB300(system, half_neigh, input->precision, true);
   else force = new ForceSNAP_GB300(system, half_neigh, input->precision);
   if (input->force_line < 0) throw HostError("Invalid ForceType: no pair_style line");
   for (int line : input->force_coeff_lines) {

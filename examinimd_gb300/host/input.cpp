@@ -79,7 +79,7 @@ void Input::read_command_line_args(int argc, const char* const* argv) {
       printf("  -il [file] / --input-lammps [FILE]: Provide LAMMPS input file\n");
       printf("  --force-iteration [TYPE]:   NEIGH_FULL, NEIGH_HALF\n");
       printf("  --comm-type [TYPE]:         SERIAL (SERIAL_GB300)\n");
-      printf("  --neigh-type [TYPE]:        2D, CSR (2D_GB300, CSR_GB300)\n");
+      printf("  --neigh-type [TYPE]:        2D, CSR, CSR_MAPCONSTR (2D_GB300, CSR_GB300)\n");
       printf("  --precision [fp64|mixed]:   force arithmetic form\n");
       printf("  --device [N]:               CUDA device\n");
       printf("  --dumpbinary [N] [PATH]:    binary output PATH/output* every N steps\n");
@@ -103,7 +103,11 @@ void Input::read_command_line_args(int argc, const char* const* argv) {
       ++i;
     } else if (a == "--neigh-type") {
       const std::string v = next(1);
-      if (v == "CSR" || v == "CSR_GB300") neighbor_type = NEIGH_CSR;
+      // CSR_MAPCONSTR (neighbor_csr_map_constr.h) builds the same CSR pair
+      // set through a hash map; its row order is the map's slot order, so the
+      // stencil-order CSR rows stand in for it (same pairs, forces equal to
+      // rounding)
+      if (v == "CSR" || v == "CSR_GB300" || v == "CSR_MAPCONSTR") neighbor_type = NEIGH_CSR;
       else if (v == "2D" || v == "2D_GB300") neighbor_type = NEIGH_2D;
       else throw HostError("unsupported --neigh-type " + v);
       ++i;
@@ -245,6 +249,10 @@ void Input::check_lammps_command(int line) {
     const std::string& s = word(L, 1);
     if (s == "lj/cut") {
       force_type = FORCE_LJ;
+      force_cutoff = num(2);
+      force_line = line;
+    } else if (s == "lj/cut/idial") {
+      force_type = FORCE_LJ_IDIAL;
       force_cutoff = num(2);
       force_line = line;
     } else if (s == "snap") {

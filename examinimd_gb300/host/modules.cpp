@@ -81,23 +81,42 @@ void NeighborGB300::create_neigh_list(System* system, Binning*, bool half_neigh,
 }
 
 // ---------------------------------------------------------------- LJ
-ForceLJNeigh_GB300::ForceLJNeigh_GB300(System* system, bool half, int precision)
-    : Force(system, half), system_(system), ntypes_(system->ntypes), precision_(precision) {
+ForceLJNeigh_GB300::ForceLJNeigh_GB300(System* system, bool half, int precision, bool idial)
+    : Force(system, half), system_(system), ntypes_(system->ntypes), precision_(precision), idial_(idial) {
   const size_t nt2 = size_t(ntypes_) * ntypes_;
   lj1_.assign(nt2, 0.0);
   lj2_.assign(nt2, 0.0);
   cutsq_.assign(nt2, 0.0);
+  intensity_.assign(nt2, 0.0);
+  if (idial && precision != EMD_PREC_FP64) throw HostError("lj/cut/idial runs in the FP64 form only");
 }
 
 // force_lj_neigh_impl.h:57-98.  With ntypes <= 12 the reference stores
 // "stack params" and every pair_coeff line overwrites ALL type pairs; above
 // 12 only the named pair (and its mirror) is set.
 void ForceLJNeigh_GB300::init_coeff(int nargs, char** args) {
-  if (nargs < 6) throw HostError("pair_coeff for lj/cut needs: i j eps sigma cut");
+  if (nargs < (idial_ ? 7 : 6))
+    throw HostError(idial_ ? "pair_coeff for lj/cut/idial needs: i j eps sigma cut nrepeat"
+                           : "pair_coeff for lj/cut needs: i j eps sigma cut");
   const int t1 = atoi(args[1]) - 1, t2 = atoi(args[2]) - 1;
   const double eps = atof(args[3]), sigma = atof(args[4]), cut = atof(args[5]);
   const double v1 = 48.0 * eps * std::pow(sigma, 12.0);
   const double v2 = 24.0 * eps * std::pow(sigma, 6.0);
+  if (idial_) {
+    // ForceLJIDialNeigh::init_coeff (force_lj_idial_neigh_impl.h:48-84):
+    // always the named pair and its mirror, plus the repeat count
+    if (t1 < 0 || t2 < 0 || t1 >= ntypes_ || t2 >= ntypes_) throw HostError("pair_coeff type out of range");
+    const double nrepeat = double(atoi(args[6]));
+    lj1_[size_t(t1) * ntypes_ + t2] = lj1_[size_t(t2) * ntypes_ + t1] = v1;
+    lj2_[size_t(t1) * ntypes_ + t2] = lj2_[size_t(t2) * ntypes_ + t1] = v2;
+    cutsq_[size_t(t1) * ntypes_ + t2] = cutsq_[size_t(t2) * ntypes_ + t1] = cut * cut;
+    intensity_[size_t(t1) * ntypes_ + t2] = intensity_[size_t(t2) * ntypes_ + t1] = nrepeat;
+    check(emd_lj_init(system_->ctx, ntypes_, lj1_.data(), lj2_.data(), cutsq_.data(), half_neigh ? 1 : 0,
+                      precision_),
+          system_->ctx, "emd_lj_init");
+    check(emd_lj_set_intensity(system_->ctx, intensity_.data()), system_->ctx, "emd_lj_set_intensity");
+    return;
+  }
   if (ntypes_ <= 12) {
     for (int i = 0; i < ntypes_; i++)
       for (int j = 0; j < ntypes_; j++) {
@@ -120,6 +139,7 @@ void ForceLJNeigh_GB300::compute(System* system, Binning*, Neighbor*) {
 }
 
 double ForceLJNeigh_GB300::compute_energy(System* system, Binning*, Neighbor*) {
+  if (idial_) return 0.0;  // ForceLJIDialNeigh keeps Force's default (force.h:54)
   double pe = 0.0;
   check(emd_lj_energy(system->ctx, &pe), system->ctx, "emd_lj_energy");
   return pe;

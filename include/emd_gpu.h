@@ -138,6 +138,13 @@ emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double
                        const double* cutsq, int half_neigh, int precision);
 /* compute(): f += pair forces over the current neighbour list. */
 emd_status emd_lj_compute(emd_ctx* ctx);
+/* ForceLJIDialNeigh (pair_style lj/cut/idial, force_lj_idial_neigh_impl.h:
+ * 48-219): after emd_lj_init (FP64), a repeat count per type pair
+ * (ntypes*ntypes doubles) turns emd_lj_compute into the intensity-dial force:
+ * each pair force is evaluated `intensity` times, 1/intensity of it each time,
+ * and the half form scatters to owned partners only.  NULL returns to lj/cut.
+ * The intensity-dial style has no energy (thermo PE 0). */
+emd_status emd_lj_set_intensity(emd_ctx* ctx, const double* intensity);
 /* compute_energy(): shifted LJ potential energy (force_lj_neigh_impl.h:129-156, 259-343). */
 emd_status emd_lj_energy(emd_ctx* ctx, double* pe);
 /* Gradient of a loss L(E, F) with respect to the LJ eps and sigma, for

@@ -20,7 +20,7 @@ create_box {ntypes} box
 create_atoms 1 box
 {mass_lines}
 velocity all create {temp} 87287 loop geom
-pair_style lj/cut 2.5
+pair_style {style} 2.5
 {coeff_lines}
 neighbor 0.3 bin
 neigh_modify delay 0 every {every} check no
@@ -72,6 +72,18 @@ CASES = {
                                     args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL",
                                           "--comm-type", "SERIAL"],
                                     dump_every=10, keep_steps=[0, 10, 30]),
+    # LJ intensity dial (pair_style lj/cut/idial: each pair force evaluated 3
+    # times at a third), full CSR and half CSR lists
+    "lj_idial_fcc4_full_csr": dict(kind="lj_idial", n=4, mass=1.0, temp=1.44, newton="off", every=10,
+                                   coeffs=[(1, 1, 1.0, 1.0, 2.5, 3)], thermo=10, steps=30,
+                                   args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL",
+                                         "--comm-type", "SERIAL"],
+                                   dump_every=10, keep_steps=[0, 10, 30]),
+    "lj_idial_fcc4_half_csr": dict(kind="lj_idial", n=4, mass=1.0, temp=1.44, newton="off", every=10,
+                                   coeffs=[(1, 1, 1.0, 1.0, 2.5, 3)], thermo=10, steps=30,
+                                   args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_HALF",
+                                         "--comm-type", "SERIAL"],
+                                   dump_every=10, keep_steps=[0, 10, 30]),
     # SNAP W, the shipped in.snap.W geometry (sc 4x8x8 = 256 atoms)
     "snap_W_sc": dict(kind="snap", a=3.1803, nx=4, ny=8, nz=8, mass=183.84, elem="W", every=1, thermo=5, steps=5,
                       coeff="W.snapcoeff", param="W.snapparam",
@@ -109,12 +121,13 @@ def deck_text(case: dict) -> str:
                            mass_lines="\n".join(f"mass {t + 1} {m}" for t, m in enumerate(masses)),
                            elem_names=" ".join(elems),
                            type_elems=" ".join(case.get("type_elems", [case["elem"]] * len(masses))), **fields)
-    if case["kind"] == "lj":
+    if case["kind"] in ("lj", "lj_idial"):
         masses = case.get("masses", [case["mass"]])
         coeffs = case.get("coeffs", [(1, 1, 1.0, 1.0, 2.5)])
-        return LJ.format(ntypes=len(masses),
+        style = "lj/cut/idial" if case["kind"] == "lj_idial" else "lj/cut"
+        return LJ.format(ntypes=len(masses), style=style,
                          mass_lines="\n".join(f"mass {t + 1} {m}" for t, m in enumerate(masses)),
-                         coeff_lines="\n".join(f"pair_coeff {a} {b} {e} {s} {c}" for a, b, e, s, c in coeffs),
+                         coeff_lines="\n".join("pair_coeff " + " ".join(str(v) for v in c) for c in coeffs),
                          **case)
     return SNAP.format(**case)
 

@@ -15,6 +15,7 @@ from tests.golden.decks import CASES
 pytestmark = pytest.mark.gpu
 
 LJ_CASES = [k for k, v in CASES.items() if v["kind"] == "lj"]
+IDIAL_CASES = [k for k, v in CASES.items() if v["kind"] == "lj_idial"]
 
 
 def _ctx():
@@ -83,7 +84,7 @@ def test_lj_modules_vs_oracle(name, golden):
     assert abs(gpu.thermo_mv2() - orc.thermo_mv2()) <= 1e-12 * orc.thermo_mv2()
 
 
-@pytest.mark.parametrize("name", LJ_CASES)
+@pytest.mark.parametrize("name", LJ_CASES + IDIAL_CASES)
 def test_lj_driver_vs_reference_dumps(name, golden, tmp_path):
     """The re-hosted ExaMiniMD driver (emd_gb300 modules) on the golden deck
     against ExaMiniMD's own --dumpbinary output."""

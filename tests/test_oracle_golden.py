@@ -13,8 +13,12 @@ from oracle.orc import Oracle
 from tests import mdloop
 from tests.golden.decks import CASES
 
+# the intensity-dial LJ style has no oracle restatement: its fixtures pin the
+# GB300 driver directly (tests/test_gpu_lj.py)
+ORACLE_CASES = [k for k, v in CASES.items() if v["kind"] != "lj_idial"]
 
-@pytest.mark.parametrize("name", list(CASES))
+
+@pytest.mark.parametrize("name", ORACLE_CASES)
 def test_oracle_matches_reference_init(name, golden):
     g = golden(name)
     case = CASES[name]
@@ -47,7 +51,7 @@ def test_oracle_matches_reference_init(name, golden):
     np.testing.assert_array_equal(allp["f"][:nl].ravel(), g["probe_f"][:3 * nl])
 
 
-@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("name", ORACLE_CASES)
 def test_oracle_matches_reference_run(name, golden):
     g = golden(name)
     case = CASES[name]
