@@ -233,7 +233,7 @@ def run_reference_arm(a, ws, rank):
         return
     wl = WORKLOADS[a.workload]
     steps = max(1, min(a.steps, 20))
-    warm = max(0, min(a.warmup, 2))
+    warm = min(a.warmup, 5)
     r = cpu_sample(wl["cells"], steps, warm)
     sample = (f"{wl['desc']}; CPU oracle port of ExaMiniMD's serial algorithm, {r['threads']} OpenMP threads; "
               f"{warm} warm-up + {steps} timed steps of the full {r['n']}-atom system (bounded sample), init "
@@ -247,7 +247,7 @@ def run_reference_arm(a, ws, rank):
             "cpu_baseline": {"value": r["value"], "unit": METRIC, "cores": r["threads"], "kind": "port",
                              "sample": sample},
             "e2e": {"value": r["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    emit(line)
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -395,7 +395,7 @@ def run_gpu_arm(a, ws, rank, local):
                 "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "thermo_end": {"T": T, "PE_per_atom": pe, "KE_per_atom": ke}, "kernels": kernels}
         line.update(extra)
-        print(json.dumps(line), flush=True)
+        emit(line)
     md.close()
     if dist is not None:
         dist.destroy_process_group()
@@ -643,7 +643,21 @@ def md_row_mean(ctx, nl) -> float:
     return float(num[:nl].mean())
 
 
+_JSON_FD = None
+
+
+def emit(line: dict) -> None:
+    """The one JSON line, on the process's original stdout."""
+    os.write(_JSON_FD if _JSON_FD is not None else 1, (json.dumps(line) + "\n").encode())
+
+
 def main():
+    global _JSON_FD
+    # anything else written to stdout (the library's own prints, buffered C
+    # stdio flushed at exit) goes to stderr, so stdout carries one JSON line
+    sys.stdout.flush()
+    _JSON_FD = os.dup(1)
+    os.dup2(2, 1)
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)

@@ -1,0 +1,885 @@
+// ForceSNAP on the device (force_snap_neigh_impl.h:160-724, sna_impl.hpp).
+//
+// One CTA per owned atom i, 8 warps, U / Y in shared memory:
+//   A. inside list: warp 0 compacts the neighbours with r^2 < rcutmax^2 in
+//      row order (ballot + popc), keeping r_ij = x_j - x_i, w_j, rcut_ij;
+//   B. U_tot = wself*I + sum_j sfac*w_j*U_j by the Cayley-Klein layer
+//      recursion (compute_uarray, sna_impl.hpp:642-720), in FP64 in both
+//      forms.  FP64 form: each warp runs its neighbours one at a time, lanes
+//      over the (ma, mb) half layer, into a private half-grid partial; the
+//      partials are summed in a fixed order and mirrored to the full
+//      matrices.  Mixed form: the rescaled recursion (no square-root
+//      factors, b_stage_mixed), lanes over (neighbour, element) pairs of four
+//      neighbours per warp, one fixed-order block sum per layer;
+//   C. adjoint contraction: Z_t(ma,mb) for the 125 (j1>=j2, j) triples
+//      (compute_zi, sna_impl.hpp:197-283) and Y_j = sum_t cY_t Z_t, where
+//      cY folds the linear coefficients with the (j+1)/(j1+1), (j+1)/(j2+1)
+//      weights of the three terms of compute_dbidrj (sna_impl.hpp:330-539);
+//   D. per inside neighbour (a warp each): U and dU/dr by the differentiated
+//      recursion (compute_duarray, sna_impl.hpp:729-893) and
+//      F_ij = sum_j 2 sum_half w Re(conj(dU'_j) Y_j) + (-1.5e6/r^14) r_ij,
+//      which equals sum_k beta_k dB_k/dr_ij of the reference; f_i += F_ij,
+//      f_j -= F_ij with FP64 atomics (j may be a ghost; update_force follows).
+// The energy variant adds E_i = beta_0 + (2/3) sum_j sum_half w Re(conj(U_j) Y_j)
+// (B is cubic in U, so <U, dB/dU> = 3B) plus 1.25e5/r^12 per inside pair.
+//
+// Precision forms: FP64 (the drop-in; snap.cu, -fmad=false) and mixed
+// (snap_mixed.cu, contraction allowed), where U_tot stays FP64 (phase B) and
+// phases C/D run in FP32 with FP64 force sums.
+#pragma once
+#include <algorithm>
+#include <cmath>
+
+#include "emd_device.cuh"
+#include "emd_internal.h"
+#include "neigh_rows.cuh"
+
+namespace emd {
+
+ListView list_view(Ctx& c);
+
+namespace snapk {
+
+constexpr double MY_PI = 3.14159265358979323846;
+constexpr int SNAP_THREADS = 256;
+constexpr int SNAP_WARPS = SNAP_THREADS / 32;
+// per-neighbour scalar fields (structure of arrays, `cap` entries each)
+enum {
+  ND_AR_U, ND_AI_U, ND_BR_U, ND_BI_U,  // Cayley-Klein a, b of compute_uarray
+  ND_AR, ND_AI, ND_BR, ND_BI,          // a, b of compute_duarray
+  ND_DAR, ND_DAI = ND_DAR + 3, ND_DBR = ND_DAI + 3, ND_DBI = ND_DBR + 3, ND_UK = ND_DBI + 3,
+  ND_SFAC = ND_UK + 3, ND_DSFAC, ND_FP, ND_EP = ND_FP + 3, ND_FIELDS
+};
+
+struct SnapDev {
+  int twojmax, L;         // L = twojmax + 1
+  int nfull, njobs, nyh;  // triples, Z jobs, half-grid Y size
+  int nuf;                // full U size
+  int ncoeff, ncoeffall, nelem, ntypes;
+  double rfac0, rmin0, rcutfac, cutsq, wself;
+  int switchflag;
+  const int* trip;      // nfull x 3
+  const int* cg_off;    // nfull
+  const double* cg;     // compact CG blocks (a+1) x (b+1)
+  const float* cg_f;
+  const int* jobs;      // njobs: (t << 8) | (ma << 4) | mb
+  const int* tjob_off;  // nfull + 1: the jobs of triple t are [tjob_off[t], tjob_off[t+1])
+  const int* yred_off;  // nyh + 1
+  const int* yred_job;  // njobs
+  const double* cY;     // nelem x nfull
+  const float* cY_f;
+  const double* rootpq;  // (L+1) x (L+1)
+  const double* beta0;   // nelem
+  const double* radelem;
+  const double* wjelem;
+  const int* map;  // ntypes
+  // rescaled recursion of the mixed form: V_j(ma, mb) = f_j(ma, mb) U_j(ma, mb),
+  // invf = 1 / f over the half grid (nyh); half-layer buffer sizes (even, odd j)
+  const double* invf;
+  const float* invf_f;
+  int bh_even, bh_odd;
+};
+
+
+// ---- index helpers (device)
+__device__ __forceinline__ int yoff(int j) {  // sum_{j'<j} (j'+1)(j'/2+1)
+  int s = 0;
+  for (int k = 0; k < j; ++k) s += (k + 1) * (k / 2 + 1);
+  return s;
+}
+__device__ __forceinline__ int uoff(int j) {  // sum_{j'<j} (j'+1)^2
+  return j * (j + 1) * (2 * j + 1) / 6;
+}
+
+template <typename R>
+struct Cplx {
+  R r, i;
+};
+
+// contraction weight of half-grid element (ma, mb) of layer j (sna_impl.hpp:384-413)
+__device__ __forceinline__ double hw(int j, int ma, int mb) {
+  if (2 * mb < j) return 1.0;
+  if (2 * ma < j) return 1.0;
+  if (2 * ma == j) return 0.5;
+  return 0.0;
+}
+
+template <typename R>
+__device__ __forceinline__ R warp_sum_r(R v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL_MASK, v, o);
+  return v;
+}
+
+// twice that weight, in the contraction type
+template <typename R>
+__device__ __forceinline__ R hw2(int j, int ma, int mb) {
+  return (2 * mb < j || 2 * ma < j) ? R(2) : (2 * ma == j ? R(1) : R(0));
+}
+
+__device__ __forceinline__ double sfac_of(const SnapDev& S, double r, double rcut) {
+  if (S.switchflag == 0) return 1.0;
+  if (r <= S.rmin0) return 1.0;
+  if (r > rcut) return 0.0;
+  return 0.5 * (cos((r - S.rmin0) * (MY_PI / (rcut - S.rmin0))) + 1.0);
+}
+__device__ __forceinline__ double dsfac_of(const SnapDev& S, double r, double rcut) {
+  if (S.switchflag == 0) return 0.0;
+  if (r <= S.rmin0) return 0.0;
+  if (r > rcut) return 0.0;
+  const double rcutfac = MY_PI / (rcut - S.rmin0);
+  return -0.5 * sin((r - S.rmin0) * rcutfac) * rcutfac;
+}
+
+// One layer of the U recursion, lanes over the half layer of j from the full
+// layer j-1 in P (index ma*j + mb), into C (index ma*(j+1) + mb), then the
+// inversion-symmetry mirror (sna_impl.hpp:660-719).
+template <typename R>
+__device__ __forceinline__ void u_layer(int j, int lane, const R* __restrict__ rootpq, int L1, R ar, R ai, R br,
+                                        R bi, const Cplx<R>* P, Cplx<R>* C) {
+  const int nh = (j + 1) * (j / 2 + 1);
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e % (j + 1);
+    R vr = 0, vi = 0;
+    if (ma > 0) {
+      const Cplx<R> u = P[(ma - 1) * j + mb];
+      const R rp = rootpq[ma * L1 + (j - mb)];
+      vr = -rp * (br * u.r + bi * u.i);
+      vi = -rp * (br * u.i - bi * u.r);
+    }
+    if (ma < j) {
+      const Cplx<R> u = P[ma * j + mb];
+      const R rp = rootpq[(j - ma) * L1 + (j - mb)];
+      vr += rp * (ar * u.r + ai * u.i);
+      vi += rp * (ar * u.i - ai * u.r);
+    }
+    C[ma * (j + 1) + mb] = Cplx<R>{vr, vi};
+  }
+  __syncwarp();
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e % (j + 1);
+    const bool even = ((ma + mb) & 1) == 0;
+    if (2 * mb < j || 2 * ma < j) {
+      const Cplx<R> u = C[ma * (j + 1) + mb];
+      C[(j - ma) * (j + 1) + (j - mb)] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
+    } else if (2 * ma == j) {
+      C[ma * (j + 1) + mb].i = -C[ma * (j + 1) + mb].i;  // centre: conj (the reference's in-place mirror)
+    }
+  }
+  __syncwarp();
+}
+
+// U and dU/dr (3 components) layer: dU arrays hold 3 consecutive Cplx per element.
+template <typename R>
+__device__ __forceinline__ void du_layer(int j, int lane, const R* __restrict__ rootpq, int L1, R ar, R ai, R br,
+                                         R bi, const R* dar, const R* dai, const R* dbr, const R* dbi,
+                                         const Cplx<R>* P, const Cplx<R>* dP, Cplx<R>* C, Cplx<R>* dC) {
+  const int nh = (j + 1) * (j / 2 + 1);
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e % (j + 1);
+    R vr = 0, vi = 0, dr[3] = {0, 0, 0}, di[3] = {0, 0, 0};
+    if (ma > 0) {
+      const int s = (ma - 1) * j + mb;
+      const Cplx<R> u = P[s];
+      const R rp = rootpq[ma * L1 + (j - mb)];
+      vr = -rp * (br * u.r + bi * u.i);
+      vi = -rp * (br * u.i - bi * u.r);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const Cplx<R> du = dP[3 * s + k];
+        dr[k] = -rp * (dbr[k] * u.r + dbi[k] * u.i + br * du.r + bi * du.i);
+        di[k] = -rp * (dbr[k] * u.i - dbi[k] * u.r + br * du.i - bi * du.r);
+      }
+    }
+    if (ma < j) {
+      const int s = ma * j + mb;
+      const Cplx<R> u = P[s];
+      const R rp = rootpq[(j - ma) * L1 + (j - mb)];
+      vr += rp * (ar * u.r + ai * u.i);
+      vi += rp * (ar * u.i - ai * u.r);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const Cplx<R> du = dP[3 * s + k];
+        dr[k] += rp * (dar[k] * u.r + dai[k] * u.i + ar * du.r + ai * du.i);
+        di[k] += rp * (dar[k] * u.i - dai[k] * u.r + ar * du.i - ai * du.r);
+      }
+    }
+    const int o = ma * (j + 1) + mb;
+    C[o] = Cplx<R>{vr, vi};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dC[3 * o + k] = Cplx<R>{dr[k], di[k]};
+  }
+  __syncwarp();
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e % (j + 1);
+    const bool even = ((ma + mb) & 1) == 0;
+    const int o = ma * (j + 1) + mb;
+    if (2 * mb < j || 2 * ma < j) {
+      const int t = (j - ma) * (j + 1) + (j - mb);
+      const Cplx<R> u = C[o];
+      C[t] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const Cplx<R> du = dC[3 * o + k];
+        dC[3 * t + k] = even ? Cplx<R>{du.r, -du.i} : Cplx<R>{-du.r, du.i};
+      }
+    } else if (2 * ma == j) {
+      C[o].i = -C[o].i;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dC[3 * o + k].i = -dC[3 * o + k].i;
+    }
+  }
+  __syncwarp();
+}
+
+// ---- rescaled recursion (mixed form)
+// With V_j(ma, mb) = f_j(ma, mb) U_j(ma, mb), f_j(ma, mb)^2 = (j-mb)! mb! / ((j-ma)! ma!),
+// compute_uarray's recursion (sna_impl.hpp:664-690)
+//   U_j(ma, mb) = rootpq(j-ma, j-mb) a U_{j-1}(ma, mb) - rootpq(ma, j-mb) b U_{j-1}(ma-1, mb)
+// becomes V_j(ma, mb) = a V_{j-1}(ma, mb) - b V_{j-1}(ma-1, mb), because
+// f_j(ma, mb) sqrt((j-ma)/(j-mb)) = f_{j-1}(ma, mb) and
+// f_j(ma, mb) sqrt(ma/(j-mb)) = f_{j-1}(ma-1, mb).  f_j(ma, mb) = f_j(j-ma, j-mb),
+// so the inversion mirror holds for V as for U.  U = V / f is restored once
+// per atom (on the U_tot sums, and folded into Y for the dU contraction).
+
+__device__ __forceinline__ double flip_if(double x, bool f) {
+  const unsigned long long sign = f ? 0x8000000000000000ull : 0ull;
+  return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(__double_as_longlong(x)) ^ sign));
+}
+
+// element (ma, mb) of half layer jp (index mb (jp + 1) + ma, 2 mb <= jp); the
+// column past the half by the mirror (-1)^(ma+mb) conj V(jp - ma, jp - mb)
+__device__ __forceinline__ Cplx<double> ld_half(const Cplx<double>* P, int jp, int ma, int mb) {
+  if (2 * mb <= jp) return P[mb * (jp + 1) + ma];
+  const Cplx<double> v = P[(jp - mb) * (jp + 1) + (jp - ma)];
+  const bool odd = (ma + mb) & 1;
+  return Cplx<double>{flip_if(v.r, odd), flip_if(v.i, !odd)};
+}
+
+// neighbour slots per warp in b_stage_mixed
+constexpr int BG = 4;
+
+// B of the mixed form: U_tot (FP64) and its FP32 copy.  Neighbours go in
+// rounds of SNAP_WARPS * BG; warp w holds neighbours w, w + SNAP_WARPS, ... of
+// the round, its lanes over (slot, half-layer element) pairs.  Layer 0 is
+// seeded with sfac * w_j, so each layer's sum over the neighbours is a plain
+// sum: one warp adds up layer j - 1 in neighbour order while the others run
+// layer j.  `work` holds SNAP_WARPS * BG slots of (bh_even + bh_odd) elements.
+__device__ __forceinline__ void b_stage_mixed(const SnapDev& S, const double* nd, int cap, int ninside,
+                                              Cplx<double>* work, Cplx<double>* utot, Cplx<float>* utot_r) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int sw = S.bh_even + S.bh_odd, per_round = SNAP_WARPS * BG;
+  Cplx<double>* mine = work + size_t(warp) * BG * sw;
+  const int rounds = max(1, (ninside + per_round - 1) / per_round);
+  for (int rd = 0; rd < rounds; ++rd) {
+    const int nb0 = rd * per_round;
+    const int nin = max(0, min(ninside - nb0, per_round));
+    const int gw = nin > warp ? (nin - warp + SNAP_WARPS - 1) / SNAP_WARPS : 0;  // this warp's slots
+    if (lane < gw) mine[lane * sw] = Cplx<double>{nd[ND_SFAC * cap + nb0 + lane * SNAP_WARPS + warp], 0.0};
+    __syncthreads();
+    for (int j = 1; j <= S.twojmax + 1; ++j) {
+      if (j <= S.twojmax) {
+        const int nh = (j + 1) * (j / 2 + 1);
+        const int po = ((j - 1) & 1) * S.bh_even, co = (j & 1) * S.bh_even;
+        for (int it = lane; it < gw * nh; it += 32) {
+          const int g = it / nh, e = it - g * nh;
+          const int mb = e / (j + 1), ma = e - mb * (j + 1);
+          const int nb = nb0 + g * SNAP_WARPS + warp;
+          const double ar = nd[ND_AR_U * cap + nb], ai = nd[ND_AI_U * cap + nb];
+          const double br = nd[ND_BR_U * cap + nb], bi = nd[ND_BI_U * cap + nb];
+          const Cplx<double>* P = mine + g * sw + po;
+          Cplx<double> u1{0.0, 0.0}, u2{0.0, 0.0};
+          if (ma > 0) u1 = ld_half(P, j - 1, ma - 1, mb);
+          if (ma < j) u2 = ld_half(P, j - 1, ma, mb);
+          const double vr = fma(ar, u2.r, fma(ai, u2.i, fma(-br, u1.r, -bi * u1.i)));
+          const double vi = fma(ar, u2.i, fma(-ai, u2.r, fma(-br, u1.i, bi * u1.r)));
+          // the centre element conjugated, as the reference's in-place mirror leaves it
+          mine[g * sw + co + e] = Cplx<double>{vr, flip_if(vi, 2 * ma == j && 2 * mb == j)};
+        }
+      }
+      const int jr = j - 1;
+      if (warp == jr % SNAP_WARPS) {
+        const int nh = (jr + 1) * (jr / 2 + 1), ro = (jr & 1) * S.bh_even, yo = yoff(jr), uo = uoff(jr);
+        for (int e = lane; e < nh; e += 32) {
+          double sr = 0.0, si = 0.0;
+          for (int k = 0; k < nin; ++k) {
+            const Cplx<double> v = work[size_t((k % SNAP_WARPS) * BG + k / SNAP_WARPS) * sw + ro + e];
+            sr += v.r;
+            si += v.i;
+          }
+          const int mb = e / (jr + 1), ma = e - mb * (jr + 1);
+          const double f = S.invf[yo + e];
+          Cplx<double>& t = utot[uo + ma * (jr + 1) + mb];
+          const double r0 = rd == 0 ? (ma == mb ? S.wself : 0.0) : t.r;
+          const double i0 = rd == 0 ? 0.0 : t.i;
+          t = Cplx<double>{fma(sr, f, r0), fma(si, f, i0)};
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // mirror to the full matrices, FP32 copy
+  for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
+    int j = 0;
+    while (yoff(j + 1) <= e) ++j;
+    const int q = e - yoff(j), mb = q / (j + 1), ma = q % (j + 1);
+    if (2 * mb == j && 2 * ma > j) continue;  // written as the mirror of (j - ma, mb)
+    const int uo = uoff(j);
+    const Cplx<double> u = utot[uo + ma * (j + 1) + mb];
+    utot_r[uo + ma * (j + 1) + mb] = Cplx<float>{float(u.r), float(u.i)};
+    if (2 * mb < j || 2 * ma < j) {
+      const bool odd = (ma + mb) & 1;
+      const Cplx<double> m{flip_if(u.r, odd), flip_if(u.i, !odd)};
+      const int t = uo + (j - ma) * (j + 1) + (j - mb);
+      utot[t] = m;
+      utot_r[t] = Cplx<float>{float(m.r), float(m.i)};
+    }
+  }
+  __syncthreads();
+}
+
+// U and dU/dr layer of the rescaled recursion (V = f U, no rootpq factors);
+// layout and mirror as du_layer
+template <typename R>
+__device__ __forceinline__ void du_layer_s(int j, int lane, R ar, R ai, R br, R bi, const R* dar, const R* dai,
+                                           const R* dbr, const R* dbi, const Cplx<R>* P, const Cplx<R>* dP,
+                                           Cplx<R>* C, Cplx<R>* dC) {
+  const int nh = (j + 1) * (j / 2 + 1);
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e % (j + 1);
+    Cplx<R> u1{0, 0}, u2{0, 0}, du1[3], du2[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) du1[k] = du2[k] = Cplx<R>{0, 0};
+    if (ma > 0) {
+      const int s = (ma - 1) * j + mb;
+      u1 = P[s];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) du1[k] = dP[3 * s + k];
+    }
+    if (ma < j) {
+      const int s = ma * j + mb;
+      u2 = P[s];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) du2[k] = dP[3 * s + k];
+    }
+    const int o = ma * (j + 1) + mb;
+    C[o] = Cplx<R>{ar * u2.r + ai * u2.i - br * u1.r - bi * u1.i, ar * u2.i - ai * u2.r - br * u1.i + bi * u1.r};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const R dr = dar[k] * u2.r + dai[k] * u2.i + ar * du2[k].r + ai * du2[k].i - dbr[k] * u1.r - dbi[k] * u1.i -
+                   br * du1[k].r - bi * du1[k].i;
+      const R di = dar[k] * u2.i - dai[k] * u2.r + ar * du2[k].i - ai * du2[k].r - dbr[k] * u1.i + dbi[k] * u1.r -
+                   br * du1[k].i + bi * du1[k].r;
+      dC[3 * o + k] = Cplx<R>{dr, di};
+    }
+  }
+  __syncwarp();
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e % (j + 1);
+    const bool even = ((ma + mb) & 1) == 0;
+    const int o = ma * (j + 1) + mb;
+    if (2 * mb < j || 2 * ma < j) {
+      const int t = (j - ma) * (j + 1) + (j - mb);
+      const Cplx<R> u = C[o];
+      C[t] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const Cplx<R> du = dC[3 * o + k];
+        dC[3 * t + k] = even ? Cplx<R>{du.r, -du.i} : Cplx<R>{-du.r, du.i};
+      }
+    } else if (2 * ma == j) {
+      C[o].i = -C[o].i;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dC[3 * o + k].i = -dC[3 * o + k].i;
+    }
+  }
+  __syncwarp();
+}
+
+struct SnapArgs {
+  SnapDev S;
+  const double4_32a* x4;
+  const int* type;
+  double* f;
+  ListView L;
+  int n_local, cap;
+  double* eatom;  // energy variant
+  unsigned* status;
+  // adjoint variant
+  const double* g;           // dL/dF of the owned atoms (n_local x 3)
+  const int* ghost_owner;    // owned atom behind every ghost
+  int newton;                // ghost forces fold back to their owners
+  double* adj;               // column-major per-atom outputs, (2 nfull + 1) x n_local
+  size_t work_bytes;         // size of the shared `work` region
+};
+
+// MODE 0: forces; 1: per-atom energy; 2: adjoint columns (FP64 only).
+// Minimum resident CTAs: three for the mixed form (<= 80 registers; its
+// shared memory fits three per SM), two for the FP64 forms.
+template <typename R, int MODE>
+__global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 : 2) k_snap(SnapArgs A) {
+  const SnapDev& S = A.S;
+  const int i = blockIdx.x;
+  if (i >= A.n_local) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int L = S.L, L2 = L * L, L1 = L + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // ---- shared memory carve-up
+  double* rootpq_d = reinterpret_cast<double*>(smem_raw);  // L1*L1
+  double* in_r = rootpq_d + L1 * L1;                       // 3*cap
+  double* in_w = in_r + 3 * A.cap;                         // cap
+  double* in_rc = in_w + A.cap;                            // cap
+  Cplx<double>* utot = reinterpret_cast<Cplx<double>*>(in_rc + A.cap);  // nuf
+  R* rootpq_r = reinterpret_cast<R*>(utot + S.nuf);                     // L1*L1
+  Cplx<R>* ytot = reinterpret_cast<Cplx<R>*>(rootpq_r + ((L1 * L1 + 1) & ~1));  // nyh
+  // U_tot in the contraction type: the FP64 array itself, or an FP32 copy
+  // made once per atom (converting inside the Z loops would put an FP64-pipe
+  // conversion on every Clebsch-Gordan term)
+  constexpr bool kF64 = sizeof(R) == sizeof(double);
+  Cplx<R>* utot_r = kF64 ? reinterpret_cast<Cplx<R>*>(utot) : ytot + S.nyh;      // nuf
+  int* in_j = reinterpret_cast<int*>(kF64 ? ytot + S.nyh : utot_r + S.nuf);     // cap
+  double* red = reinterpret_cast<double*>(in_j + ((A.cap + 3) & ~3));          // 4*SNAP_WARPS
+  double* nd = red + 4 * SNAP_WARPS;                                           // ND_FIELDS*cap
+  // the per-neighbour scalars in the contraction type (FP32 copy made once)
+  R* ndr = kF64 ? reinterpret_cast<R*>(nd) : reinterpret_cast<R*>(nd + ND_FIELDS * A.cap);
+  unsigned char* work = reinterpret_cast<unsigned char*>(kF64 ? nd + ND_FIELDS * A.cap
+                                                              : nd + ND_FIELDS * A.cap + (ND_FIELDS * A.cap + 1) / 2);
+  __shared__ int s_ninside;
+
+  for (int k = tid; k < L1 * L1; k += SNAP_THREADS) {
+    rootpq_d[k] = S.rootpq[k];
+    rootpq_r[k] = R(S.rootpq[k]);
+  }
+  // ---- A: inside list (force_snap_neigh_impl.h:612-656)
+  const double4_32a xi = A.x4[i];
+  const int ti = A.type[i];
+  const int ei = S.map[ti];
+  if (warp == 0) {
+    const double radi = S.radelem[ei];
+    const Row<false> rowc(A.L, i);
+    const Row<true> row2(A.L, i);
+    const bool two_d = A.L.stride != 0;
+    const int n = rowc.n;
+    const unsigned lt = (1u << lane) - 1u;
+    int cnt = 0;
+    for (int base = 0; base < n; base += 32) {
+      const int k = base + lane;
+      bool take = false;
+      int j = 0;
+      double dx = 0, dy = 0, dz = 0;
+      if (k < n) {
+        j = two_d ? row2[k] : rowc[k];
+        const double4_32a xj = A.x4[j];
+        dx = xj.x - xi.x;
+        dy = xj.y - xi.y;
+        dz = xj.z - xi.z;
+        take = (dx * dx + dy * dy + dz * dz) < S.cutsq;
+      }
+      const unsigned m = __ballot_sync(FULL_MASK, take);
+      const int pos = cnt + __popc(m & lt);
+      if (take && pos < A.cap) {
+        const int ej = S.map[A.type[j]];
+        in_j[pos] = j;
+        in_r[3 * pos] = dx;
+        in_r[3 * pos + 1] = dy;
+        in_r[3 * pos + 2] = dz;
+        in_w[pos] = S.wjelem[ej];
+        in_rc[pos] = (radi + S.radelem[ej]) * S.rcutfac;
+      }
+      cnt += __popc(m);
+    }
+    if (lane == 0) {
+      if (cnt > A.cap) latch_status(A.status, ST_BOUNDS);
+      s_ninside = min(cnt, A.cap);
+    }
+  }
+  // per-warp regions for phase B: 2 layers (L2 each) + half-grid partial (nyh)
+  Cplx<double>* wb = reinterpret_cast<Cplx<double>*>(work) + warp * (2 * L2 + S.nyh);
+  Cplx<double>* Pb = wb;
+  Cplx<double>* Cb = wb + L2;
+  Cplx<double>* part = wb + 2 * L2;
+  if constexpr (kF64) {
+    for (int e = lane; e < S.nyh; e += 32) part[e] = Cplx<double>{0.0, 0.0};
+  }
+  __syncthreads();
+  const int ninside = s_ninside;
+
+  // ---- per-neighbour scalars, one thread per neighbour (every lane of a
+  // warp would otherwise repeat the FP64 transcendentals)
+  for (int nb = tid; nb < ninside; nb += SNAP_THREADS) {
+    const double x = in_r[3 * nb], y = in_r[3 * nb + 1], z = in_r[3 * nb + 2];
+    const double rcut = in_rc[nb], wj = in_w[nb];
+    const double rsq = x * x + y * y + z * z;
+    const double r = sqrt(rsq);
+    double* q = nd + nb;
+    // compute_ui (sna_impl.hpp:174-187): a, b of compute_uarray
+    {
+      const double theta0 = (r - S.rmin0) * S.rfac0 * MY_PI / (rcut - S.rmin0);
+      const double z0 = r / tan(theta0);
+      const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
+      q[ND_AR_U * A.cap] = r0inv * z0;
+      q[ND_AI_U * A.cap] = -r0inv * z;
+      q[ND_BR_U * A.cap] = r0inv * y;
+      q[ND_BI_U * A.cap] = -r0inv * x;
+    }
+    // compute_duidrj + the prologue of compute_duarray (sna_impl.hpp:291-321, 729-778)
+    const double rscale0 = S.rfac0 * MY_PI / (rcut - S.rmin0);
+    const double theta0 = (r - S.rmin0) * rscale0;
+    const double cs = cos(theta0), sn = sin(theta0);
+    const double z0 = r * cs / sn;
+    const double dz0dr = z0 / r - (r * rscale0) * (rsq + z0 * z0) / rsq;
+    const double rinv = 1.0 / r;
+    const double uk[3] = {x * rinv, y * rinv, z * rinv};
+    const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
+    q[ND_AR * A.cap] = z0 * r0inv;
+    q[ND_AI * A.cap] = -z * r0inv;
+    q[ND_BR * A.cap] = y * r0inv;
+    q[ND_BI * A.cap] = -x * r0inv;
+    const double dr0invdr = -(r0inv * r0inv * r0inv) * (r + z0 * dz0dr);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double dr0inv = dr0invdr * uk[k];
+      const double dz0 = dz0dr * uk[k];
+      q[(ND_DAR + k) * A.cap] = dz0 * r0inv + z0 * dr0inv + 0.0;
+      q[(ND_DAI + k) * A.cap] = -z * dr0inv + (k == 2 ? -r0inv : 0.0);
+      q[(ND_DBR + k) * A.cap] = y * dr0inv + (k == 1 ? r0inv : 0.0);
+      q[(ND_DBI + k) * A.cap] = -x * dr0inv + (k == 0 ? -r0inv : 0.0);
+      q[(ND_UK + k) * A.cap] = uk[k];
+    }
+    q[ND_SFAC * A.cap] = sfac_of(S, r, rcut) * wj;
+    q[ND_DSFAC * A.cap] = dsfac_of(S, r, rcut) * wj;
+    // extra repulsion of the reference (force_snap_neigh_impl.h:705-711) and
+    // its energy 1.25e5 / r^12 per ordered pair
+    const double r2 = rsq * rsq, r4 = r2 * r2;
+    const double fdivr = -1.5e6 / (r4 * r2 * rsq);
+    q[ND_FP * A.cap] = x * fdivr;
+    q[(ND_FP + 1) * A.cap] = y * fdivr;
+    q[(ND_FP + 2) * A.cap] = z * fdivr;
+    q[ND_EP * A.cap] = 1.25e5 / (r4 * r2);
+  }
+  __syncthreads();
+  if (!kF64) {
+    for (int k = tid; k < ND_FIELDS * A.cap; k += SNAP_THREADS) ndr[k] = R(nd[k]);
+  }
+
+  // ---- B: U_tot (FP64)
+  if constexpr (kF64) {
+    for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
+      const double ar = nd[ND_AR_U * A.cap + nb], ai = nd[ND_AI_U * A.cap + nb];
+      const double br = nd[ND_BR_U * A.cap + nb], bi = nd[ND_BI_U * A.cap + nb];
+      const double sfac = nd[ND_SFAC * A.cap + nb];
+      if (lane == 0) {
+        Pb[0] = Cplx<double>{1.0, 0.0};
+        part[0].r += sfac * 1.0;
+      }
+      __syncwarp();
+      Cplx<double>* P = Pb;
+      Cplx<double>* C = Cb;
+      for (int j = 1; j <= S.twojmax; ++j) {
+        u_layer<double>(j, lane, rootpq_d, L1, ar, ai, br, bi, P, C);
+        const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j);
+        for (int e = lane; e < nh; e += 32) {
+          const int mb = e / (j + 1), ma = e % (j + 1);
+          const Cplx<double> u = C[ma * (j + 1) + mb];
+          part[yo + e].r += sfac * u.r;
+          part[yo + e].i += sfac * u.i;
+        }
+        __syncwarp();
+        Cplx<double>* t = P;
+        P = C;
+        C = t;
+      }
+    }
+    __syncthreads();
+    // sum partials (fixed order), add wself on the diagonal, mirror to full U_tot
+    for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
+      int j = 0;
+      while (yoff(j + 1) <= e) ++j;
+      const int q = e - yoff(j);
+      const int mb = q / (j + 1), ma = q % (j + 1);
+      double sr = (ma == mb) ? S.wself : 0.0, si = 0.0;
+      for (int w = 0; w < SNAP_WARPS; ++w) {
+        const Cplx<double>* pw = reinterpret_cast<Cplx<double>*>(work) + w * (2 * L2 + S.nyh) + 2 * L2;
+        sr += pw[e].r;
+        si += pw[e].i;
+      }
+      const int uo = uoff(j);
+      utot[uo + ma * (j + 1) + mb] = Cplx<double>{sr, si};
+      if (2 * mb < j || 2 * ma < j) {
+        const bool even = ((ma + mb) & 1) == 0;
+        const int t = uo + (j - ma) * (j + 1) + (j - mb);
+        utot[t] = even ? Cplx<double>{sr, -si} : Cplx<double>{-sr, si};
+      }
+    }
+    __syncthreads();
+  } else {
+    b_stage_mixed(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot,
+                  reinterpret_cast<Cplx<float>*>(utot_r));
+  }
+
+  // ---- C: Z jobs and Y = sum_t cY_t Z_t
+  // (the adjoint keeps Z for its final contraction, beyond `work`)
+  Cplx<R>* zs = reinterpret_cast<Cplx<R>*>(MODE == 2 ? work + A.work_bytes : work);
+  const R* cg = sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cg) : reinterpret_cast<const R*>(S.cg_f);
+  for (int jb = tid; jb < S.njobs; jb += SNAP_THREADS) {
+    const int code = S.jobs[jb];
+    const int t = code >> 8, ma = (code >> 4) & 15, mb = code & 15;
+    const int j1 = S.trip[3 * t], j2 = S.trip[3 * t + 1], j = S.trip[3 * t + 2];
+    const R* cgt = cg + S.cg_off[t];
+    const Cplx<R>* U1 = utot_r + uoff(j1);
+    const Cplx<R>* U2 = utot_r + uoff(j2);
+    R zr = 0, zi = 0;
+    const int ma1lo = max(0, (2 * ma - j - j2 + j1) / 2), ma1hi = min(j1, (2 * ma - j + j2 + j1) / 2);
+    const int mb1lo = max(0, (2 * mb - j - j2 + j1) / 2), mb1hi = min(j1, (2 * mb - j + j2 + j1) / 2);
+    for (int ma1 = ma1lo; ma1 <= ma1hi; ++ma1) {
+      const int ma2 = (2 * ma - j - (2 * ma1 - j1) + j2) / 2;
+      R sr = 0, si = 0;
+      for (int mb1 = mb1lo; mb1 <= mb1hi; ++mb1) {
+        const int mb2 = (2 * mb - j - (2 * mb1 - j1) + j2) / 2;
+        const R cga = cgt[mb1 * (j2 + 1) + mb2];
+        const Cplx<R> a = U1[ma1 * (j1 + 1) + mb1];
+        const Cplx<R> b = U2[ma2 * (j2 + 1) + mb2];
+        sr += cga * (a.r * b.r - a.i * b.i);
+        si += cga * (a.r * b.i + a.i * b.r);
+      }
+      const R cga = cgt[ma1 * (j2 + 1) + ma2];
+      zr += sr * cga;
+      zi += si * cga;
+    }
+    zs[jb] = Cplx<R>{zr, zi};
+  }
+  __syncthreads();
+  const R* cY = (sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cY) : reinterpret_cast<const R*>(S.cY_f)) +
+                (size_t)ei * S.nfull;
+  for (int e = tid; e < (MODE == 2 ? 0 : S.nyh); e += SNAP_THREADS) {
+    R yr = 0, yi = 0;
+    for (int k = S.yred_off[e]; k < S.yred_off[e + 1]; ++k) {
+      const int jb = S.yred_job[k];
+      const R cy = cY[S.jobs[jb] >> 8];
+      yr += cy * zs[jb].r;
+      yi += cy * zs[jb].i;
+    }
+    if constexpr (!kF64) {  // Y / f: the mixed form's dU recursion runs on V = f U
+      const R f = S.invf_f[e];
+      yr *= f;
+      yi *= f;
+    }
+    ytot[e] = Cplx<R>{yr, yi};
+  }
+  __syncthreads();
+
+  // ---- energy (optional): beta_0 + (2/3) sum_j sum_half w Re(conj(U) Y) + pair terms
+  if constexpr (MODE == 1) {
+    double acc = 0.0;
+    for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
+      int j = 0;
+      while (yoff(j + 1) <= e) ++j;
+      const int q = e - yoff(j), mb = q / (j + 1), ma = q % (j + 1);
+      const Cplx<double> u = utot[uoff(j) + ma * (j + 1) + mb];
+      acc += hw(j, ma, mb) * (u.r * double(ytot[e].r) + u.i * double(ytot[e].i));
+    }
+    for (int nb = tid; nb < ninside; nb += SNAP_THREADS) acc += nd[ND_EP * A.cap + nb] * 1.5;  // x 2/3 below
+    const double t = block_sum(acc, red);
+    if (tid == 0) A.eatom[i] = S.beta0[ei] + (2.0 / 3.0) * t;
+    return;
+  }
+
+  // ---- adjoint: for every full triple t = (j1, j2, j), with Z_t kept from C,
+  //   P_t = 2 sum_half w Re(conj(U_j) Z_t)        (= B_k when t is idxj triple k)
+  //   Q_t = 2 sum_half w Re(conj(D_j) Z_t),  D = sum_nb dU'_nb . (g_i - g_j)
+  // so that d/dbeta_k [sum_atoms g . F] over this atom's pairs is
+  // Q_t1 + (j+1)/(j1+1) Q_t2 + (j+1)/(j2+1) Q_t3 (compute_dbidrj's three terms,
+  // sna_impl.hpp:330-570, contracted with the loss gradient before the sum
+  // over k instead of after it).
+  if constexpr (MODE == 2) {
+    Cplx<double>* dpart = reinterpret_cast<Cplx<double>*>(zs + S.njobs);  // SNAP_WARPS x nyh
+    Cplx<double>* dsum = dpart + SNAP_WARPS * S.nyh;                      // nyh
+    Cplx<double>* dp = dpart + warp * S.nyh;
+    for (int e = lane; e < S.nyh; e += 32) dp[e] = Cplx<double>{0.0, 0.0};
+    const double gix = A.g[3 * i], giy = A.g[3 * i + 1], giz = A.g[3 * i + 2];
+    Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
+    __syncwarp();
+    for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
+      const R* qr = ndr + nb;
+      const R Rar = qr[ND_AR * A.cap], Rai = qr[ND_AI * A.cap], Rbr = qr[ND_BR * A.cap], Rbi = qr[ND_BI * A.cap];
+      R Rdar[3], Rdai[3], Rdbr[3], Rdbi[3], Ruk[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        Rdar[k] = qr[(ND_DAR + k) * A.cap];
+        Rdai[k] = qr[(ND_DAI + k) * A.cap];
+        Rdbr[k] = qr[(ND_DBR + k) * A.cap];
+        Rdbi[k] = qr[(ND_DBI + k) * A.cap];
+        Ruk[k] = qr[(ND_UK + k) * A.cap];
+      }
+      const R Rsfac = qr[ND_SFAC * A.cap], Rdsfac = qr[ND_DSFAC * A.cap];
+      // the pair's reaction force lands on j's owner (newton) or nowhere
+      const int j = in_j[nb];
+      const int jo = j < A.n_local ? j : (A.newton ? A.ghost_owner[j - A.n_local] : -1);
+      const double gjx = jo >= 0 ? A.g[3 * jo] : 0.0, gjy = jo >= 0 ? A.g[3 * jo + 1] : 0.0,
+                   gjz = jo >= 0 ? A.g[3 * jo + 2] : 0.0;
+      const R dv[3] = {R(gix - gjx), R(giy - gjy), R(giz - gjz)};
+      Cplx<R>* P = wd;
+      Cplx<R>* C = wd + L2;
+      Cplx<R>* dP = wd + 2 * L2;
+      Cplx<R>* dC = wd + 5 * L2;
+      if (lane == 0) {
+        P[0] = Cplx<R>{R(1), R(0)};
+        for (int k = 0; k < 3; ++k) dP[k] = Cplx<R>{R(0), R(0)};
+        dp[0].r += Rdsfac * (Ruk[0] * dv[0] + Ruk[1] * dv[1] + Ruk[2] * dv[2]);
+      }
+      __syncwarp();
+      for (int jl = 1; jl <= S.twojmax; ++jl) {
+        du_layer<R>(jl, lane, rootpq_r, L1, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
+        const int nh = (jl + 1) * (jl / 2 + 1), yo = yoff(jl);
+        for (int e = lane; e < nh; e += 32) {
+          const int mb = e / (jl + 1), ma = e % (jl + 1);
+          const int o = ma * (jl + 1) + mb;
+          const Cplx<R> u = C[o];
+          R dr = 0, di = 0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const Cplx<R> du = dC[3 * o + k];
+            dr += dv[k] * (Rdsfac * u.r * Ruk[k] + Rsfac * du.r);
+            di += dv[k] * (Rdsfac * u.i * Ruk[k] + Rsfac * du.i);
+          }
+          dp[yo + e].r += dr;
+          dp[yo + e].i += di;
+        }
+        __syncwarp();
+        Cplx<R>* t = P;
+        P = C;
+        C = t;
+        t = dP;
+        dP = dC;
+        dC = t;
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
+      double sr = 0.0, si = 0.0;
+      for (int w = 0; w < SNAP_WARPS; ++w) {
+        sr += dpart[w * S.nyh + e].r;
+        si += dpart[w * S.nyh + e].i;
+      }
+      dsum[e] = Cplx<double>{sr, si};
+    }
+    __syncthreads();
+    const size_t n = size_t(A.n_local);
+    for (int t = tid; t < S.nfull; t += SNAP_THREADS) {
+      const int jt = S.trip[3 * t + 2];
+      double p = 0.0, q = 0.0;
+      for (int jb = S.tjob_off[t]; jb < S.tjob_off[t + 1]; ++jb) {
+        const int code = S.jobs[jb];
+        const int ma = (code >> 4) & 15, mb = code & 15;
+        const double w = hw(jt, ma, mb);
+        if (w == 0.0) continue;
+        const Cplx<double> u = utot[uoff(jt) + ma * (jt + 1) + mb];
+        const Cplx<double> d = dsum[yoff(jt) + mb * (jt + 1) + ma];
+        const double zr = double(zs[jb].r), zi = double(zs[jb].i);
+        p += w * (u.r * zr + u.i * zi);
+        q += w * (d.r * zr + d.i * zi);
+      }
+      A.adj[size_t(t) * n + i] = 2.0 * p;
+      A.adj[size_t(S.nfull + t) * n + i] = 2.0 * q;
+    }
+    if (tid == 0) A.adj[size_t(2 * S.nfull) * n + i] = 1.0;  // atom count column (beta_0)
+    return;
+  }
+
+  // ---- D: per neighbour dU/dr and the force (FP64 or FP32)
+  Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
+  double fix = 0, fiy = 0, fiz = 0;
+  for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
+    const double* q = nd + nb;
+    const R* qr = ndr + nb;
+    const R Rar = qr[ND_AR * A.cap], Rai = qr[ND_AI * A.cap], Rbr = qr[ND_BR * A.cap], Rbi = qr[ND_BI * A.cap];
+    R Rdar[3], Rdai[3], Rdbr[3], Rdbi[3], Ruk[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      Rdar[k] = qr[(ND_DAR + k) * A.cap];
+      Rdai[k] = qr[(ND_DAI + k) * A.cap];
+      Rdbr[k] = qr[(ND_DBR + k) * A.cap];
+      Rdbi[k] = qr[(ND_DBI + k) * A.cap];
+      Ruk[k] = qr[(ND_UK + k) * A.cap];
+    }
+    const R Rsfac = qr[ND_SFAC * A.cap], Rdsfac = qr[ND_DSFAC * A.cap];
+    Cplx<R>* P = wd;
+    Cplx<R>* C = wd + L2;
+    Cplx<R>* dP = wd + 2 * L2;
+    Cplx<R>* dC = wd + 5 * L2;
+    // layer 0: U = 1, dU = 0; half grid is the centre (weight 1/2)
+    R fx = 0, fy = 0, fz = 0;
+    if (lane == 0) {
+      P[0] = Cplx<R>{R(1), R(0)};
+      for (int k = 0; k < 3; ++k) dP[k] = Cplx<R>{R(0), R(0)};
+      const R yr = ytot[0].r;
+      fx = Rdsfac * Ruk[0] * yr;
+      fy = Rdsfac * Ruk[1] * yr;
+      fz = Rdsfac * Ruk[2] * yr;
+    }
+    __syncwarp();
+    for (int j = 1; j <= S.twojmax; ++j) {
+      if constexpr (kF64)
+        du_layer<R>(j, lane, rootpq_r, L1, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
+      else
+        du_layer_s<R>(j, lane, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
+      const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j);
+      for (int e = lane; e < nh; e += 32) {
+        const int mb = e / (j + 1), ma = e % (j + 1);
+        const R w = hw2<R>(j, ma, mb);
+        if (w == R(0)) continue;
+        const int o = ma * (j + 1) + mb;
+        const Cplx<R> u = C[o];
+        const Cplx<R> yv = ytot[yo + e];
+        R g[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const Cplx<R> du = dC[3 * o + k];
+          const R dur = Rdsfac * u.r * Ruk[k] + Rsfac * du.r;
+          const R dui = Rdsfac * u.i * Ruk[k] + Rsfac * du.i;
+          g[k] = w * (dur * yv.r + dui * yv.i);
+        }
+        fx += g[0];
+        fy += g[1];
+        fz += g[2];
+      }
+      __syncwarp();
+      Cplx<R>* t = P;
+      P = C;
+      C = t;
+      t = dP;
+      dP = dC;
+      dC = t;
+    }
+    // the pair force summed over the lanes in the contraction type (an FP64
+    // shuffle tree would cost more FP64-pipe time than the FP32 layers)
+    double Fx = double(warp_sum_r(fx)), Fy = double(warp_sum_r(fy)), Fz = double(warp_sum_r(fz));
+    if (lane == 0) {
+      Fx += q[ND_FP * A.cap];
+      Fy += q[(ND_FP + 1) * A.cap];
+      Fz += q[(ND_FP + 2) * A.cap];
+      const int j = in_j[nb];
+      atomicAdd(A.f + 3 * j, -Fx);
+      atomicAdd(A.f + 3 * j + 1, -Fy);
+      atomicAdd(A.f + 3 * j + 2, -Fz);
+      fix += Fx;
+      fiy += Fy;
+      fiz += Fz;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    red[warp] = fix;
+    red[SNAP_WARPS + warp] = fiy;
+    red[2 * SNAP_WARPS + warp] = fiz;
+  }
+  __syncthreads();
+  if (tid < 3) {
+    double s = 0.0;
+    for (int w = 0; w < SNAP_WARPS; ++w) s += red[tid * SNAP_WARPS + w];
+    atomicAdd(A.f + 3 * i + tid, s);
+  }
+}
+
+}  // namespace snapk
+}  // namespace emd

@@ -347,7 +347,7 @@ void Input::create_lattice(Comm* comm) {
         }
   s.N_local = n;
   s.N = n;
-  if (s.do_print) printf("Atoms: %i %i\n", s.N, s.N_local);
+  if (s.do_print && !quiet) printf("Atoms: %i %i\n", s.N, s.N_local);
 
   // velocities (input.cpp:731-791): geom uniform draws, momentum zeroing,
   // rescale to the target temperature with a serial FP64 sum
