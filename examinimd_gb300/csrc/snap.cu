@@ -20,7 +20,7 @@ struct SnapHost {
   int precision = EMD_PREC_FP64;
   DevBuf<int> trip, cg_off, jobs, tjob_off, yred_off, yred_job, map;
   DevBuf<double> cg, cY, rootpq, beta0, radelem, wjelem, eatom, invf;
-  DevBuf<float> cg_f, cY_f, invf_f;
+  DevBuf<float> cg_f, cY_f, yscale_f;
   // adjoint: per-atom columns, their per-element sums, the loss gradient dL/dF
   DevBuf<double> adj, adj_sum, adj_g;
   // coefficient k's three dB/dr terms: full triples and factors (the cY fold)
@@ -61,14 +61,18 @@ double clebsch_gordan(int j1, int j2, int j, int m1, int m2) {
 
 // bytes of the `work` region: per-warp U layers + partials (FP64 form) or
 // the neighbour slots' half layers (mixed form) for B, Z jobs (C), per-warp
-// U and dU layers (D)
+// U and dU layers (FP64 form) or the forward layers and adjoints of
+// d_reverse (mixed form) for D
 size_t snap_work_bytes(const SnapDev& S, int real_bytes) {
   const int L2 = S.L * S.L;
   const size_t wB = real_bytes == int(sizeof(double))
                         ? 2 * sizeof(double) * size_t(SNAP_WARPS) * (2 * L2 + S.nyh)
                         : 2 * sizeof(double) * size_t(SNAP_WARPS) * BG * size_t(S.bh_even + S.bh_odd);
   const size_t wC = 2 * size_t(real_bytes) * size_t(S.njobs);
-  const size_t wD = 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 8 * L2;
+  const int J = S.twojmax;
+  const size_t wD = real_bytes == int(sizeof(double))
+                        ? 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 8 * L2
+                        : 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 2 * size_t(drev_words(J));
   return (std::max(wB, std::max(wC, wD)) + 15) & ~size_t(15);
 }
 
@@ -117,7 +121,7 @@ void free_snap(Ctx& c) {
   for (auto* b : {&h->cg, &h->cY, &h->rootpq, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
                   &h->adj_g, &h->invf})
     b->release();
-  for (auto* b : {&h->cg_f, &h->cY_f, &h->invf_f}) b->release();
+  for (auto* b : {&h->cg_f, &h->cY_f, &h->yscale_f}) b->release();
   delete h;
   c.snap = nullptr;
 }
@@ -359,17 +363,23 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   std::vector<double> rootpq(size_t(L + 1) * (L + 1), 0.0);
   for (int p = 1; p <= twojmax; p++)
     for (int q = 1; q <= twojmax; q++) rootpq[size_t(p) * (L + 1) + q] = std::sqrt(static_cast<double>(p) / q);
-  // 1 / f_j(ma, mb) of the rescaled recursion over the half grid, and the
-  // largest half layer of even and odd j
+  // over the half grid: 1 / f_j(ma, mb) of the rescaled recursion and the
+  // D contraction's Y scale (twice the half-grid weight over f); the largest
+  // half layer of even and odd j
   std::vector<double> invf(static_cast<size_t>(S.nyh));
+  std::vector<float> yscale(static_cast<size_t>(S.nyh));
   S.bh_even = S.bh_odd = 1;
   for (int j = 0; j <= twojmax; ++j) {
     const int nh = (j + 1) * (j / 2 + 1);
     (j & 1 ? S.bh_odd : S.bh_even) = std::max(j & 1 ? S.bh_odd : S.bh_even, nh);
     for (int mb = 0; 2 * mb <= j; ++mb)
-      for (int ma = 0; ma <= j; ++ma)
-        invf[size_t(yoff_h(j) + mb * (j + 1) + ma)] =
-            std::sqrt(factorial(j - ma) * factorial(ma) / (factorial(j - mb) * factorial(mb)));
+      for (int ma = 0; ma <= j; ++ma) {
+        const size_t e = size_t(yoff_h(j) + mb * (j + 1) + ma);
+        invf[e] = std::sqrt(factorial(j - ma) * factorial(ma) / (factorial(j - mb) * factorial(mb)));
+        // twice the half-grid contraction weight (sna_impl.hpp:384-413)
+        const double w2 = (2 * mb < j || 2 * ma < j) ? 2.0 : (2 * ma == j ? 1.0 : 0.0);
+        yscale[e] = float(w2 * invf[e]);
+      }
   }
   double rcutmax = 0.0;
   for (int e = 0; e < nelem; e++) rcutmax = std::max(2.0 * radelem[e] * rcutfac, rcutmax);
@@ -394,7 +404,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   upload(c, h->cY_f, cYf);
   upload(c, h->rootpq, rootpq);
   upload(c, h->invf, invf);
-  upload(c, h->invf_f, std::vector<float>(invf.begin(), invf.end()));
+  upload(c, h->yscale_f, yscale);
   upload(c, h->beta0, beta0);
   upload(c, h->radelem, std::vector<double>(radelem, radelem + nelem));
   upload(c, h->wjelem, std::vector<double>(wjelem, wjelem + nelem));
@@ -412,7 +422,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.cY_f = h->cY_f.p;
   S.rootpq = h->rootpq.p;
   S.invf = h->invf.p;
-  S.invf_f = h->invf_f.p;
+  S.yscale_f = h->yscale_f.p;
   S.beta0 = h->beta0.p;
   S.radelem = h->radelem.p;
   S.wjelem = h->wjelem.p;

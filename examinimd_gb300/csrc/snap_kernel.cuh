@@ -15,11 +15,13 @@
 //      (compute_zi, sna_impl.hpp:197-283) and Y_j = sum_t cY_t Z_t, where
 //      cY folds the linear coefficients with the (j+1)/(j1+1), (j+1)/(j2+1)
 //      weights of the three terms of compute_dbidrj (sna_impl.hpp:330-539);
-//   D. per inside neighbour (a warp each): U and dU/dr by the differentiated
-//      recursion (compute_duarray, sna_impl.hpp:729-893) and
+//   D. per inside neighbour (a warp each):
 //      F_ij = sum_j 2 sum_half w Re(conj(dU'_j) Y_j) + (-1.5e6/r^14) r_ij,
 //      which equals sum_k beta_k dB_k/dr_ij of the reference; f_i += F_ij,
 //      f_j -= F_ij with FP64 atomics (j may be a ghost; update_force follows).
+//      FP64 form: U and dU/dr by the differentiated recursion
+//      (compute_duarray, sna_impl.hpp:729-893).  Mixed form: one forward
+//      sweep of the rescaled U recursion and one adjoint sweep (d_reverse).
 // The energy variant adds E_i = beta_0 + (2/3) sum_j sum_half w Re(conj(U_j) Y_j)
 // (B is cubic in U, so <U, dB/dU> = 3B) plus 1.25e5/r^12 per inside pair.
 //
@@ -73,10 +75,11 @@ struct SnapDev {
   const double* radelem;
   const double* wjelem;
   const int* map;  // ntypes
-  // rescaled recursion of the mixed form: V_j(ma, mb) = f_j(ma, mb) U_j(ma, mb),
-  // invf = 1 / f over the half grid (nyh); half-layer buffer sizes (even, odd j)
+  // rescaled recursion of the mixed form: V_j(ma, mb) = f_j(ma, mb) U_j(ma, mb);
+  // over the half grid (nyh): invf = 1 / f, yscale_f = hw2 / f (the D
+  // contraction's weight folded into Y); half-layer buffer sizes (even, odd j)
   const double* invf;
-  const float* invf_f;
+  const float* yscale_f;
   int bh_even, bh_odd;
 };
 
@@ -338,62 +341,145 @@ __device__ __forceinline__ void b_stage_mixed(const SnapDev& S, const double* nd
   __syncthreads();
 }
 
-// U and dU/dr layer of the rescaled recursion (V = f U, no rootpq factors);
-// layout and mirror as du_layer
-template <typename R>
-__device__ __forceinline__ void du_layer_s(int j, int lane, R ar, R ai, R br, R bi, const R* dar, const R* dai,
-                                           const R* dbr, const R* dbi, const Cplx<R>* P, const Cplx<R>* dP,
-                                           Cplx<R>* C, Cplx<R>* dC) {
-  const int nh = (j + 1) * (j / 2 + 1);
-  for (int e = lane; e < nh; e += 32) {
-    const int mb = e / (j + 1), ma = e % (j + 1);
-    Cplx<R> u1{0, 0}, u2{0, 0}, du1[3], du2[3];
+// Phase D of the mixed form, in reverse mode, for NB neighbours at once (one
+// per register set, so each lane carries NB independent chains).  With
+// Phi = sum_j sum_half Re(conj(V_j) Y'_j), Y' = w Y / f (ytot of the mixed
+// form), the pair force needs only Phi and its gradient in a = (ar, ai),
+// b = (br, bi):  F_k = dsfac u_k Phi + sfac sum_p dPhi/dp dp/dr_k.  The
+// forward sweep runs the rescaled recursion and keeps layers 0..J-1 (full,
+// column-major, in F); the backward sweep carries the adjoint
+// lambda_j = dPhi/dV_j down the layers: from a mirrored element back to its
+// source (conjugated, with the mirror's sign), through the centre
+// conjugation, and through the recursion as
+//   lambda_{j-1}(ma, mb) = a lambda'_j(ma, mb) - b lambda'_j(ma + 1, mb),
+//   dPhi/d conj(a) += conj(V_{j-1}(ma, mb)) lambda'_j(ma, mb),
+//   dPhi/d conj(b) -= conj(V_{j-1}(ma - 1, mb)) lambda'_j(ma, mb).
+// One forward and one adjoint sweep replace the three dU/dr recursions of
+// compute_duarray (sna_impl.hpp:729-893) and their contraction with Y.
+// Outputs per-lane partials: phi, ga = sum conj(V) lambda' for a, gb for b
+// (dPhi/dar = ga.r, dPhi/dai = -ga.i, dPhi/dbr = -gb.r, dPhi/dbi = gb.i).
+// Neighbour n's buffers start at W + n * drev_words(J): F max(1, uoff(J)),
+// LA and LB max(1, J (J/2 + 1)) each, LP (J + 1)(J/2 + 1).
+struct DRevAB {
+  float ar, ai, br, bi;
+};
+__host__ __device__ __forceinline__ int drev_words(int J) {
+  return (J * (J + 1) * (2 * J + 1) / 6 > 1 ? J * (J + 1) * (2 * J + 1) / 6 : 1) +
+         2 * (J * (J / 2 + 1) > 1 ? J * (J / 2 + 1) : 1) + (J + 1) * (J / 2 + 1);
+}
+template <int NB>
+__device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB* ab, const Cplx<float>* __restrict__ ytot,
+                                          Cplx<float>* W, float* phi, Cplx<float>* ga, Cplx<float>* gb) {
+  using R = float;
+  const int nF = max(1, uoff(J)), nL = max(1, J * (J / 2 + 1)), stride = drev_words(J);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) du1[k] = du2[k] = Cplx<R>{0, 0};
-    if (ma > 0) {
-      const int s = (ma - 1) * j + mb;
-      u1 = P[s];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) du1[k] = dP[3 * s + k];
-    }
-    if (ma < j) {
-      const int s = ma * j + mb;
-      u2 = P[s];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) du2[k] = dP[3 * s + k];
-    }
-    const int o = ma * (j + 1) + mb;
-    C[o] = Cplx<R>{ar * u2.r + ai * u2.i - br * u1.r - bi * u1.i, ar * u2.i - ai * u2.r - br * u1.i + bi * u1.r};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const R dr = dar[k] * u2.r + dai[k] * u2.i + ar * du2[k].r + ai * du2[k].i - dbr[k] * u1.r - dbi[k] * u1.i -
-                   br * du1[k].r - bi * du1[k].i;
-      const R di = dar[k] * u2.i - dai[k] * u2.r + ar * du2[k].i - ai * du2[k].r - dbr[k] * u1.i + dbi[k] * u1.r -
-                   br * du1[k].i + bi * du1[k].r;
-      dC[3 * o + k] = Cplx<R>{dr, di};
-    }
+  for (int n = 0; n < NB; ++n) {
+    phi[n] = (lane == 0) ? ytot[0].r : R(0);
+    ga[n] = gb[n] = Cplx<R>{R(0), R(0)};
+    if (lane == 0) W[n * stride] = Cplx<R>{R(1), R(0)};
   }
   __syncwarp();
-  for (int e = lane; e < nh; e += 32) {
-    const int mb = e / (j + 1), ma = e % (j + 1);
-    const bool even = ((ma + mb) & 1) == 0;
-    const int o = ma * (j + 1) + mb;
-    if (2 * mb < j || 2 * ma < j) {
-      const int t = (j - ma) * (j + 1) + (j - mb);
-      const Cplx<R> u = C[o];
-      C[t] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
+  for (int j = 1; j <= J; ++j) {
+    const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j), po = uoff(j - 1), co = uoff(j);
+    for (int e = lane; e < nh; e += 32) {
+      const int mb = e / (j + 1), ma = e - mb * (j + 1);
+      const Cplx<R> y = ytot[yo + e];
+      const bool centre = 2 * ma == j && 2 * mb == j;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const Cplx<R> du = dC[3 * o + k];
-        dC[3 * t + k] = even ? Cplx<R>{du.r, -du.i} : Cplx<R>{-du.r, du.i};
+      for (int n = 0; n < NB; ++n) {
+        const Cplx<R>* P = W + n * stride + po;
+        Cplx<R> u1{R(0), R(0)}, u2{R(0), R(0)};
+        if (ma > 0) u1 = P[mb * j + ma - 1];
+        if (ma < j) u2 = P[mb * j + ma];
+        const R vr = ab[n].ar * u2.r + ab[n].ai * u2.i - ab[n].br * u1.r - ab[n].bi * u1.i;
+        R vi = ab[n].ar * u2.i - ab[n].ai * u2.r - ab[n].br * u1.i + ab[n].bi * u1.r;
+        if (centre) vi = -vi;
+        phi[n] += vr * y.r + vi * y.i;
+        if (j < J) W[n * stride + co + e] = Cplx<R>{vr, vi};
       }
-    } else if (2 * ma == j) {
-      C[o].i = -C[o].i;
+    }
+    __syncwarp();
+    if (j < J) {
+      for (int e = lane; e < nh; e += 32) {
+        const int mb = e / (j + 1), ma = e - mb * (j + 1);
+        if (2 * mb < j || 2 * ma < j) {
+          const bool even = ((ma + mb) & 1) == 0;
+          const int t = co + (j - mb) * (j + 1) + (j - ma);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) dC[3 * o + k].i = -dC[3 * o + k].i;
+          for (int n = 0; n < NB; ++n) {
+            const Cplx<R> u = W[n * stride + co + e];
+            W[n * stride + t] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
+          }
+        }
+      }
+      __syncwarp();
     }
   }
-  __syncwarp();
+  int lam = nF, nxt = nF + nL;  // offsets of the current and next adjoint layers
+  const int lp = nF + 2 * nL;
+  for (int j = J; j >= 1; --j) {
+    const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j), po = uoff(j - 1);
+    for (int e = lane; e < nh; e += 32) {
+      const int mb = e / (j + 1), ma = e - mb * (j + 1);
+      const bool dead = 2 * mb == j && 2 * ma > j;  // overwritten by the mirror: no adjoint
+      const bool mirrored = 2 * mb < j || 2 * ma < j;
+      // the mirror target (j - ma, j - mb) has an adjoint only where layer
+      // j + 1 read it (columns up to (j + 1) / 2)
+      const int tc = j - mb;
+      const bool from_t = mirrored && j < J && 2 * tc <= j + 1;
+      const bool even = ((ma + mb) & 1) == 0;
+      const Cplx<R> y = ytot[yo + e];
+#pragma unroll
+      for (int n = 0; n < NB; ++n) {
+        Cplx<float>* Wn = W + n * stride;
+        Cplx<R> l{R(0), R(0)};
+        if (!dead) {
+          l = (j == J) ? y : Wn[lam + e];
+          if (from_t) {
+            const Cplx<R> lt = Wn[lam + tc * (j + 1) + (j - ma)];
+            l.r += even ? lt.r : -lt.r;
+            l.i += even ? -lt.i : lt.i;
+          } else if (!mirrored && 2 * ma == j) {
+            l.i = -l.i;
+          }
+          if (ma < j) {
+            const Cplx<R> p = Wn[po + mb * j + ma];
+            ga[n].r += p.r * l.r + p.i * l.i;
+            ga[n].i += p.r * l.i - p.i * l.r;
+          }
+          if (ma > 0) {
+            const Cplx<R> p = Wn[po + mb * j + ma - 1];
+            gb[n].r += p.r * l.r + p.i * l.i;
+            gb[n].i += p.r * l.i - p.i * l.r;
+          }
+        }
+        Wn[lp + e] = l;
+      }
+    }
+    __syncwarp();
+    if (j > 1) {
+      // adjoint of layer j - 1 over the columns layer j reads (mb <= j / 2),
+      // plus its own Y' term on the half grid
+      const int n = j * (j / 2 + 1), nhp = j * ((j - 1) / 2 + 1), yop = yoff(j - 1);
+      for (int idx = lane; idx < n; idx += 32) {
+        const int mb = idx / j, mp = idx - mb * j;
+        Cplx<R> y{R(0), R(0)};
+        if (idx < nhp) y = ytot[yop + idx];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+          Cplx<float>* Wn = W + k * stride;
+          const Cplx<R> l1 = Wn[lp + mb * (j + 1) + mp], l0 = Wn[lp + mb * (j + 1) + mp + 1];
+          const DRevAB& q = ab[k];
+          Wn[nxt + idx] = Cplx<R>{q.ar * l1.r - q.ai * l1.i - (q.br * l0.r - q.bi * l0.i) + y.r,
+                                  q.ar * l1.i + q.ai * l1.r - (q.br * l0.i + q.bi * l0.r) + y.i};
+        }
+      }
+      __syncwarp();
+      const int t = lam;
+      lam = nxt;
+      nxt = t;
+    }
+  }
 }
 
 struct SnapArgs {
@@ -512,55 +598,113 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
     const double rsq = x * x + y * y + z * z;
     const double r = sqrt(rsq);
     double* q = nd + nb;
-    // compute_ui (sna_impl.hpp:174-187): a, b of compute_uarray
-    {
-      const double theta0 = (r - S.rmin0) * S.rfac0 * MY_PI / (rcut - S.rmin0);
-      const double z0 = r / tan(theta0);
+    if constexpr (kF64) {
+      // compute_ui (sna_impl.hpp:174-187): a, b of compute_uarray
+      {
+        const double theta0 = (r - S.rmin0) * S.rfac0 * MY_PI / (rcut - S.rmin0);
+        const double z0 = r / tan(theta0);
+        const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
+        q[ND_AR_U * A.cap] = r0inv * z0;
+        q[ND_AI_U * A.cap] = -r0inv * z;
+        q[ND_BR_U * A.cap] = r0inv * y;
+        q[ND_BI_U * A.cap] = -r0inv * x;
+      }
+      q[ND_SFAC * A.cap] = sfac_of(S, r, rcut) * wj;
+      // compute_duidrj + the prologue of compute_duarray (sna_impl.hpp:291-321, 729-778)
+      const double rscale0 = S.rfac0 * MY_PI / (rcut - S.rmin0);
+      const double theta0 = (r - S.rmin0) * rscale0;
+      const double cs = cos(theta0), sn = sin(theta0);
+      const double z0 = r * cs / sn;
+      const double dz0dr = z0 / r - (r * rscale0) * (rsq + z0 * z0) / rsq;
+      const double rinv = 1.0 / r;
+      const double uk[3] = {x * rinv, y * rinv, z * rinv};
       const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
-      q[ND_AR_U * A.cap] = r0inv * z0;
-      q[ND_AI_U * A.cap] = -r0inv * z;
-      q[ND_BR_U * A.cap] = r0inv * y;
-      q[ND_BI_U * A.cap] = -r0inv * x;
-    }
-    // compute_duidrj + the prologue of compute_duarray (sna_impl.hpp:291-321, 729-778)
-    const double rscale0 = S.rfac0 * MY_PI / (rcut - S.rmin0);
-    const double theta0 = (r - S.rmin0) * rscale0;
-    const double cs = cos(theta0), sn = sin(theta0);
-    const double z0 = r * cs / sn;
-    const double dz0dr = z0 / r - (r * rscale0) * (rsq + z0 * z0) / rsq;
-    const double rinv = 1.0 / r;
-    const double uk[3] = {x * rinv, y * rinv, z * rinv};
-    const double r0inv = 1.0 / sqrt(r * r + z0 * z0);
-    q[ND_AR * A.cap] = z0 * r0inv;
-    q[ND_AI * A.cap] = -z * r0inv;
-    q[ND_BR * A.cap] = y * r0inv;
-    q[ND_BI * A.cap] = -x * r0inv;
-    const double dr0invdr = -(r0inv * r0inv * r0inv) * (r + z0 * dz0dr);
+      q[ND_AR * A.cap] = z0 * r0inv;
+      q[ND_AI * A.cap] = -z * r0inv;
+      q[ND_BR * A.cap] = y * r0inv;
+      q[ND_BI * A.cap] = -x * r0inv;
+      const double dr0invdr = -(r0inv * r0inv * r0inv) * (r + z0 * dz0dr);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const double dr0inv = dr0invdr * uk[k];
-      const double dz0 = dz0dr * uk[k];
-      q[(ND_DAR + k) * A.cap] = dz0 * r0inv + z0 * dr0inv + 0.0;
-      q[(ND_DAI + k) * A.cap] = -z * dr0inv + (k == 2 ? -r0inv : 0.0);
-      q[(ND_DBR + k) * A.cap] = y * dr0inv + (k == 1 ? r0inv : 0.0);
-      q[(ND_DBI + k) * A.cap] = -x * dr0inv + (k == 0 ? -r0inv : 0.0);
-      q[(ND_UK + k) * A.cap] = uk[k];
+      for (int k = 0; k < 3; ++k) {
+        const double dr0inv = dr0invdr * uk[k];
+        const double dz0 = dz0dr * uk[k];
+        q[(ND_DAR + k) * A.cap] = dz0 * r0inv + z0 * dr0inv + 0.0;
+        q[(ND_DAI + k) * A.cap] = -z * dr0inv + (k == 2 ? -r0inv : 0.0);
+        q[(ND_DBR + k) * A.cap] = y * dr0inv + (k == 1 ? r0inv : 0.0);
+        q[(ND_DBI + k) * A.cap] = -x * dr0inv + (k == 0 ? -r0inv : 0.0);
+        q[(ND_UK + k) * A.cap] = uk[k];
+      }
+      q[ND_DSFAC * A.cap] = dsfac_of(S, r, rcut) * wj;
+      // extra repulsion of the reference (force_snap_neigh_impl.h:705-711) and
+      // its energy 1.25e5 / r^12 per ordered pair
+      const double r2 = rsq * rsq, r4 = r2 * r2;
+      const double fdivr = -1.5e6 / (r4 * r2 * rsq);
+      q[ND_FP * A.cap] = x * fdivr;
+      q[(ND_FP + 1) * A.cap] = y * fdivr;
+      q[(ND_FP + 2) * A.cap] = z * fdivr;
+      q[ND_EP * A.cap] = 1.25e5 / (r4 * r2);
+    } else {
+      // Mixed form: the same quantities in closed form, once, in FP64.  With
+      // s = sin(theta0), c = cos(theta0): z0 = r c / s, r0inv = s / r, so
+      //   a = c - i z s / r,  b = (y - i x) s / r  (compute_ui and
+      //   compute_duidrj give these twice, sna_impl.hpp:174-187, 291-321),
+      //   da/dr_k = -s rscale0 u_k,  d(s / r)/dr_k = g u_k,
+      //   g = (c rscale0 r - s) / r^2  (the prologue of compute_duarray,
+      //   sna_impl.hpp:729-778, in a form without its cancelling terms).
+      // a, b and sfac feed phase B in FP64; the rest is rounded once to FP32
+      // for phase D.
+      R* qf = ndr + nb;
+      const double rscale0 = S.rfac0 * MY_PI / (rcut - S.rmin0);
+      double sn, cs;
+      sincos((r - S.rmin0) * rscale0, &sn, &cs);
+      const double rinv = 1.0 / r;
+      const double r0inv = sn * rinv;
+      const double uk[3] = {x * rinv, y * rinv, z * rinv};
+      const double g = (cs * rscale0 * r - sn) * (rinv * rinv);
+      q[ND_AR_U * A.cap] = cs;
+      q[ND_AI_U * A.cap] = -z * r0inv;
+      q[ND_BR_U * A.cap] = y * r0inv;
+      q[ND_BI_U * A.cap] = -x * r0inv;
+      qf[ND_AR * A.cap] = R(cs);
+      qf[ND_AI * A.cap] = R(-z * r0inv);
+      qf[ND_BR * A.cap] = R(y * r0inv);
+      qf[ND_BI * A.cap] = R(-x * r0inv);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double dr0inv = g * uk[k];
+        qf[(ND_DAR + k) * A.cap] = R(-sn * rscale0 * uk[k]);
+        qf[(ND_DAI + k) * A.cap] = R(-z * dr0inv + (k == 2 ? -r0inv : 0.0));
+        qf[(ND_DBR + k) * A.cap] = R(y * dr0inv + (k == 1 ? r0inv : 0.0));
+        qf[(ND_DBI + k) * A.cap] = R(-x * dr0inv + (k == 0 ? -r0inv : 0.0));
+        qf[(ND_UK + k) * A.cap] = R(uk[k]);
+      }
+      // switching function and its derivative from one sincos (compute_sfac,
+      // compute_dsfac, sna_impl.hpp:1099-1128)
+      double sf = 1.0, dsf = 0.0;
+      if (S.switchflag != 0 && r > S.rmin0) {
+        if (r > rcut) {
+          sf = 0.0;
+        } else {
+          const double rcutfac = MY_PI / (rcut - S.rmin0);
+          double ss, cc;
+          sincos((r - S.rmin0) * rcutfac, &ss, &cc);
+          sf = 0.5 * (cc + 1.0);
+          dsf = -0.5 * ss * rcutfac;
+        }
+      }
+      q[ND_SFAC * A.cap] = sf * wj;
+      qf[ND_SFAC * A.cap] = R(sf * wj);
+      qf[ND_DSFAC * A.cap] = R(dsf * wj);
+      // the r^-12 repulsion's force stays FP64: its pair terms are of the size
+      // of the net force and cancel in the sum over neighbours
+      const double r2 = rsq * rsq, r4 = r2 * r2;
+      const double fdivr = -1.5e6 / (r4 * r2 * rsq);
+      q[ND_FP * A.cap] = x * fdivr;
+      q[(ND_FP + 1) * A.cap] = y * fdivr;
+      q[(ND_FP + 2) * A.cap] = z * fdivr;
     }
-    q[ND_SFAC * A.cap] = sfac_of(S, r, rcut) * wj;
-    q[ND_DSFAC * A.cap] = dsfac_of(S, r, rcut) * wj;
-    // extra repulsion of the reference (force_snap_neigh_impl.h:705-711) and
-    // its energy 1.25e5 / r^12 per ordered pair
-    const double r2 = rsq * rsq, r4 = r2 * r2;
-    const double fdivr = -1.5e6 / (r4 * r2 * rsq);
-    q[ND_FP * A.cap] = x * fdivr;
-    q[(ND_FP + 1) * A.cap] = y * fdivr;
-    q[(ND_FP + 2) * A.cap] = z * fdivr;
-    q[ND_EP * A.cap] = 1.25e5 / (r4 * r2);
   }
   __syncthreads();
-  if (!kF64) {
-    for (int k = tid; k < ND_FIELDS * A.cap; k += SNAP_THREADS) ndr[k] = R(nd[k]);
-  }
 
   // ---- B: U_tot (FP64)
   if constexpr (kF64) {
@@ -659,8 +803,8 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       yr += cy * zs[jb].r;
       yi += cy * zs[jb].i;
     }
-    if constexpr (!kF64) {  // Y / f: the mixed form's dU recursion runs on V = f U
-      const R f = S.invf_f[e];
+    if constexpr (!kF64) {  // w Y / f: the mixed form's dU recursion runs on V = f U
+      const R f = S.yscale_f[e];
       yr *= f;
       yi *= f;
     }
@@ -786,8 +930,74 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
     return;
   }
 
-  // ---- D: per neighbour dU/dr and the force (FP64 or FP32)
-  Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
+  // ---- D: the pair forces.  Mixed form: reverse mode (d_reverse), two
+  // neighbours per warp at a time; the FP64 part (repulsion, scatter to j,
+  // the sum for i) is done afterwards, one thread per neighbour.
+  if constexpr (!kF64) {
+    const int J = S.twojmax, stride = drev_words(J);
+    Cplx<float>* W = reinterpret_cast<Cplx<float>*>(work) + size_t(warp) * 2 * stride;
+    double* fpair = in_r;  // r_ij is not read after the per-neighbour scalars
+    for (int nb0 = warp; nb0 < ninside; nb0 += 2 * SNAP_WARPS) {
+      const int nb1 = nb0 + SNAP_WARPS;
+      const int nn = nb1 < ninside ? 2 : 1;
+      DRevAB ab[2];
+      for (int n = 0; n < 2; ++n) {
+        const R* qr = ndr + (n < nn ? (n ? nb1 : nb0) : nb0);
+        ab[n] = DRevAB{qr[ND_AR * A.cap], qr[ND_AI * A.cap], qr[ND_BR * A.cap], qr[ND_BI * A.cap]};
+      }
+      float phi[2];
+      Cplx<float> ga[2], gb[2];
+      if (nn == 2)
+        d_reverse<2>(J, lane, ab, ytot, W, phi, ga, gb);
+      else
+        d_reverse<1>(J, lane, ab, ytot, W, phi, ga, gb);
+      for (int n = 0; n < nn; ++n) {
+        const int nb = n ? nb1 : nb0;
+        const R* qr = ndr + nb;
+        const R sf = qr[ND_SFAC * A.cap], cp = qr[ND_DSFAC * A.cap] * phi[n];
+        R fk[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          fk[k] = cp * qr[(ND_UK + k) * A.cap] +
+                  sf * (ga[n].r * qr[(ND_DAR + k) * A.cap] - ga[n].i * qr[(ND_DAI + k) * A.cap] -
+                        gb[n].r * qr[(ND_DBR + k) * A.cap] + gb[n].i * qr[(ND_DBI + k) * A.cap]);
+        // summed over the lanes in FP32 (an FP64 shuffle tree would cost more
+        // FP64-pipe time than the FP32 sweeps)
+        const R sx = warp_sum_r(fk[0]), sy = warp_sum_r(fk[1]), sz = warp_sum_r(fk[2]);
+        if (lane == 0) {
+          fpair[3 * nb] = double(sx);
+          fpair[3 * nb + 1] = double(sy);
+          fpair[3 * nb + 2] = double(sz);
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    for (int nb = tid; nb < ninside; nb += SNAP_THREADS) {
+      const double Fx = fpair[3 * nb] + nd[ND_FP * A.cap + nb];
+      const double Fy = fpair[3 * nb + 1] + nd[(ND_FP + 1) * A.cap + nb];
+      const double Fz = fpair[3 * nb + 2] + nd[(ND_FP + 2) * A.cap + nb];
+      const int j = in_j[nb];
+      atomicAdd(A.f + 3 * j, -Fx);
+      atomicAdd(A.f + 3 * j + 1, -Fy);
+      atomicAdd(A.f + 3 * j + 2, -Fz);
+      fpair[3 * nb] = Fx;
+      fpair[3 * nb + 1] = Fy;
+      fpair[3 * nb + 2] = Fz;
+    }
+    __syncthreads();
+    if (warp == 0) {  // f_i += sum over the neighbours, in a fixed order
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double t = 0.0;
+        for (int nb = lane; nb < ninside; nb += 32) t += fpair[3 * nb + k];
+        t = warp_sum(t);
+        if (lane == 0) atomicAdd(A.f + 3 * i + k, t);
+      }
+    }
+    return;
+  }
+  // FP64 form: per neighbour (a warp each), U and dU/dr by the recursion
   double fix = 0, fiy = 0, fiz = 0;
   for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
     const double* q = nd + nb;
@@ -803,53 +1013,53 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       Ruk[k] = qr[(ND_UK + k) * A.cap];
     }
     const R Rsfac = qr[ND_SFAC * A.cap], Rdsfac = qr[ND_DSFAC * A.cap];
-    Cplx<R>* P = wd;
-    Cplx<R>* C = wd + L2;
-    Cplx<R>* dP = wd + 2 * L2;
-    Cplx<R>* dC = wd + 5 * L2;
-    // layer 0: U = 1, dU = 0; half grid is the centre (weight 1/2)
     R fx = 0, fy = 0, fz = 0;
-    if (lane == 0) {
-      P[0] = Cplx<R>{R(1), R(0)};
-      for (int k = 0; k < 3; ++k) dP[k] = Cplx<R>{R(0), R(0)};
-      const R yr = ytot[0].r;
-      fx = Rdsfac * Ruk[0] * yr;
-      fy = Rdsfac * Ruk[1] * yr;
-      fz = Rdsfac * Ruk[2] * yr;
-    }
-    __syncwarp();
-    for (int j = 1; j <= S.twojmax; ++j) {
-      if constexpr (kF64)
-        du_layer<R>(j, lane, rootpq_r, L1, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
-      else
-        du_layer_s<R>(j, lane, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
-      const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j);
-      for (int e = lane; e < nh; e += 32) {
-        const int mb = e / (j + 1), ma = e % (j + 1);
-        const R w = hw2<R>(j, ma, mb);
-        if (w == R(0)) continue;
-        const int o = ma * (j + 1) + mb;
-        const Cplx<R> u = C[o];
-        const Cplx<R> yv = ytot[yo + e];
-        R g[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const Cplx<R> du = dC[3 * o + k];
-          const R dur = Rdsfac * u.r * Ruk[k] + Rsfac * du.r;
-          const R dui = Rdsfac * u.i * Ruk[k] + Rsfac * du.i;
-          g[k] = w * (dur * yv.r + dui * yv.i);
-        }
-        fx += g[0];
-        fy += g[1];
-        fz += g[2];
+    if constexpr (kF64) {
+      Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
+      Cplx<R>* P = wd;
+      Cplx<R>* C = wd + L2;
+      Cplx<R>* dP = wd + 2 * L2;
+      Cplx<R>* dC = wd + 5 * L2;
+      // layer 0: U = 1, dU = 0; half grid is the centre (weight 1/2)
+      if (lane == 0) {
+        P[0] = Cplx<R>{R(1), R(0)};
+        for (int k = 0; k < 3; ++k) dP[k] = Cplx<R>{R(0), R(0)};
+        const R yr = ytot[0].r;
+        fx = Rdsfac * Ruk[0] * yr;
+        fy = Rdsfac * Ruk[1] * yr;
+        fz = Rdsfac * Ruk[2] * yr;
       }
       __syncwarp();
-      Cplx<R>* t = P;
-      P = C;
-      C = t;
-      t = dP;
-      dP = dC;
-      dC = t;
+      for (int j = 1; j <= S.twojmax; ++j) {
+        du_layer<R>(j, lane, rootpq_r, L1, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
+        const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j);
+        for (int e = lane; e < nh; e += 32) {
+          const int mb = e / (j + 1), ma = e % (j + 1);
+          const R w = hw2<R>(j, ma, mb);
+          if (w == R(0)) continue;
+          const int o = ma * (j + 1) + mb;
+          const Cplx<R> u = C[o];
+          const Cplx<R> yv = ytot[yo + e];
+          R g[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const Cplx<R> du = dC[3 * o + k];
+            const R dur = Rdsfac * u.r * Ruk[k] + Rsfac * du.r;
+            const R dui = Rdsfac * u.i * Ruk[k] + Rsfac * du.i;
+            g[k] = w * (dur * yv.r + dui * yv.i);
+          }
+          fx += g[0];
+          fy += g[1];
+          fz += g[2];
+        }
+        __syncwarp();
+        Cplx<R>* t = P;
+        P = C;
+        C = t;
+        t = dP;
+        dP = dC;
+        dC = t;
+      }
     }
     // the pair force summed over the lanes in the contraction type (an FP64
     // shuffle tree would cost more FP64-pipe time than the FP32 layers)
