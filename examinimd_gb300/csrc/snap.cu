@@ -19,6 +19,7 @@ struct SnapHost {
   SnapDev d;
   int precision = EMD_PREC_FP64;
   DevBuf<int> trip, cg_off, jobs, tjob_off, yred_off, yred_job, map;
+  DevBuf<int4> zord;
   DevBuf<double> cg, cY, rootpq, beta0, radelem, wjelem, eatom, invf;
   DevBuf<float> cg_f, cY_f, yscale_f;
   // adjoint: per-atom columns, their per-element sums, the loss gradient dL/dF
@@ -57,6 +58,46 @@ double clebsch_gordan(int j1, int j2, int j, int m1, int m2) {
   return sum * deltacg(j1, j2, j) *
          std::sqrt(factorial((j1 + aa2) / 2) * factorial((j1 - aa2) / 2) * factorial((j2 + bb2) / 2) *
                    factorial((j2 - bb2) / 2) * factorial((j + cc2) / 2) * factorial((j - cc2) / 2) * (j + 1));
+}
+
+// The mixed form's Z jobs as descriptors (see SnapDev::zord), ordered for
+// balance: sorted by inner-loop count, longest first, in chunks of 32 (a warp
+// gets jobs of one length); chunk c goes to round c / 8 and, alternating
+// direction from round to round, to warp c % 8 or 7 - c % 8.
+std::vector<int4> zjob_order(const std::vector<int>& trip, const std::vector<int>& cg_off, const std::vector<int>& jobs) {
+  const int nj = int(jobs.size());
+  std::vector<int4> desc(static_cast<size_t>(nj));
+  std::vector<int> cost(static_cast<size_t>(nj));
+  for (int jb = 0; jb < nj; ++jb) {
+    const int code = jobs[size_t(jb)], t = code >> 8, ma = (code >> 4) & 15, mb = code & 15;
+    const int j1 = trip[3 * size_t(t)], j2 = trip[3 * size_t(t) + 1], j = trip[3 * size_t(t) + 2];
+    const int ma1lo = std::max(0, (2 * ma - j - j2 + j1) / 2), ma1hi = std::min(j1, (2 * ma - j + j2 + j1) / 2);
+    const int mb1lo = std::max(0, (2 * mb - j - j2 + j1) / 2), mb1hi = std::min(j1, (2 * mb - j + j2 + j1) / 2);
+    int na = std::max(0, ma1hi - ma1lo + 1), nb = std::max(0, mb1hi - mb1lo + 1);
+    const int ma2 = (2 * ma - j - (2 * ma1lo - j1) + j2) / 2, mb2 = (2 * mb - j - (2 * mb1lo - j1) + j2) / 2;
+    const int uo1 = j1 * (j1 + 1) * (2 * j1 + 1) / 6, uo2 = j2 * (j2 + 1) * (2 * j2 + 1) / 6;
+    int u1 = uo1 + ma1lo * (j1 + 1) + mb1lo, u2 = uo2 + ma2 * (j2 + 1) + mb2;
+    int ci = cg_off[size_t(t)] + mb1lo * (j2 + 1) + mb2, co = cg_off[size_t(t)] + ma1lo * (j2 + 1) + ma2;
+    if (na == 0 || nb == 0) na = nb = u1 = u2 = ci = co = 0;  // Z = 0, nothing read
+    require(u1 >= 0 && u2 >= 0 && ci >= 0 && co >= 0 && u1 < 65536 && u2 < 65536 && ci < 65536 && co < 65536 &&
+                na < 256 && nb < 256,
+            EMD_ERR_ARG,
+            "SNAP: Z job tables exceed their packed fields");
+    desc[size_t(jb)] = int4{jb, int(unsigned(u1) | (unsigned(u2) << 16)), int(unsigned(ci) | (unsigned(co) << 16)),
+                            int(unsigned(na) | (unsigned(nb) << 8) | (unsigned(j1 + 1) << 16) | (unsigned(j2 + 1) << 24))};
+    cost[size_t(jb)] = na * (nb + 1);
+  }
+  std::vector<int> idx(static_cast<size_t>(nj));
+  for (int k = 0; k < nj; ++k) idx[size_t(k)] = k;
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return cost[size_t(x)] > cost[size_t(y)]; });
+  const int nchunk = (nj + 31) / 32, nround = (nchunk + SNAP_WARPS - 1) / SNAP_WARPS;
+  std::vector<int4> out(size_t(nround) * SNAP_THREADS, int4{-1, 0, 0, 0});
+  for (int c = 0; c < nchunk; ++c) {
+    const int r = c / SNAP_WARPS, p = c % SNAP_WARPS, w = (r & 1) ? SNAP_WARPS - 1 - p : p;
+    for (int l = 0; l < 32 && 32 * c + l < nj; ++l)
+      out[size_t(r) * SNAP_THREADS + 32 * size_t(w) + l] = desc[size_t(idx[size_t(32 * c + l)])];
+  }
+  return out;
 }
 
 // bytes of the `work` region: per-warp U layers + partials (FP64 form) or
@@ -118,6 +159,7 @@ void free_snap(Ctx& c) {
   if (!c.snap) return;
   SnapHost* h = static_cast<SnapHost*>(c.snap);
   for (auto* b : {&h->trip, &h->cg_off, &h->jobs, &h->tjob_off, &h->yred_off, &h->yred_job, &h->map}) b->release();
+  h->zord.release();
   for (auto* b : {&h->cg, &h->cY, &h->rootpq, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
                   &h->adj_g, &h->invf})
     b->release();
@@ -332,6 +374,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   }
   S.njobs = int(jobs.size());
   tjob_off.push_back(S.njobs);
+  const std::vector<int4> zord = zjob_order(trip, cg_off, jobs);
   std::vector<int> yred_off(size_t(S.nyh) + 1, 0), yred_job;
   for (int e = 0; e < S.nyh; ++e) {
     yred_off[size_t(e)] = int(yred_job.size());
@@ -397,6 +440,9 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   std::vector<float> cgf(cg.begin(), cg.end()), cYf(cY.begin(), cY.end());
   upload(c, h->cg_f, cgf);
   upload_i(c, h->jobs, jobs);
+  h->zord.reserve(zord.size(), c.stream);
+  EMD_CUDA(cudaMemcpyAsync(h->zord.p, zord.data(), sizeof(int4) * zord.size(), cudaMemcpyHostToDevice, c.stream));
+  S.nzo = int(zord.size());
   upload_i(c, h->tjob_off, tjob_off);
   upload_i(c, h->yred_off, yred_off);
   upload_i(c, h->yred_job, yred_job);
@@ -415,6 +461,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.cg = h->cg.p;
   S.cg_f = h->cg_f.p;
   S.jobs = h->jobs.p;
+  S.zord = h->zord.p;
   S.tjob_off = h->tjob_off.p;
   S.yred_off = h->yred_off.p;
   S.yred_job = h->yred_job.p;

@@ -81,6 +81,11 @@ struct SnapDev {
   const double* invf;
   const float* yscale_f;
   int bh_even, bh_odd;
+  // the mixed form's Z jobs as descriptors, longest first, in the order
+  // thread (warp w, lane l) takes them in round r: zord[r * SNAP_THREADS +
+  // 32 w + l] (x < 0: no job); see zjob_order in snap.cu
+  const int4* zord;
+  int nzo;
 };
 
 
@@ -266,7 +271,7 @@ constexpr int BG = 4;
 // rounds of SNAP_WARPS * BG; warp w holds neighbours w, w + SNAP_WARPS, ... of
 // the round, its lanes over (slot, half-layer element) pairs.  Layer 0 is
 // seeded with sfac * w_j, so each layer's sum over the neighbours is a plain
-// sum: one warp adds up layer j - 1 in neighbour order while the others run
+// sum: one warp adds up layer j - 1 (in a fixed order) while the others run
 // layer j.  `work` holds SNAP_WARPS * BG slots of (bh_even + bh_odd) elements.
 __device__ __forceinline__ void b_stage_mixed(const SnapDev& S, const double* nd, int cap, int ninside,
                                               Cplx<double>* work, Cplx<double>* utot, Cplx<float>* utot_r) {
@@ -302,20 +307,41 @@ __device__ __forceinline__ void b_stage_mixed(const SnapDev& S, const double* nd
       }
       const int jr = j - 1;
       if (warp == jr % SNAP_WARPS) {
+        // elements in chunks of up to 32; a chunk of m elements spreads the
+        // neighbours over G = 32 / m (a power of two) lane groups, each summing
+        // a contiguous share, then the groups are added pairwise (fixed order)
         const int nh = (jr + 1) * (jr / 2 + 1), ro = (jr & 1) * S.bh_even, yo = yoff(jr), uo = uoff(jr);
-        for (int e = lane; e < nh; e += 32) {
+        for (int c0 = 0; c0 < nh; c0 += 32) {
+          const int m = min(32, nh - c0);
+          int G = 1;
+          while (4 * G * m <= 64) G *= 2;
+          const int g = lane / m, e = c0 + lane - g * m;
+          const int per = (nin + G - 1) / G;
           double sr = 0.0, si = 0.0;
-          for (int k = 0; k < nin; ++k) {
-            const Cplx<double> v = work[size_t((k % SNAP_WARPS) * BG + k / SNAP_WARPS) * sw + ro + e];
-            sr += v.r;
-            si += v.i;
+          if (g < G) {
+            const int k1 = min(nin, (g + 1) * per);
+            for (int k = g * per; k < k1; ++k) {
+              const Cplx<double> v = work[size_t((k % SNAP_WARPS) * BG + k / SNAP_WARPS) * sw + ro + e];
+              sr += v.r;
+              si += v.i;
+            }
           }
-          const int mb = e / (jr + 1), ma = e - mb * (jr + 1);
-          const double f = S.invf[yo + e];
-          Cplx<double>& t = utot[uo + ma * (jr + 1) + mb];
-          const double r0 = rd == 0 ? (ma == mb ? S.wself : 0.0) : t.r;
-          const double i0 = rd == 0 ? 0.0 : t.i;
-          t = Cplx<double>{fma(sr, f, r0), fma(si, f, i0)};
+          for (int h = G / 2; h >= 1; h /= 2) {
+            const double ur = __shfl_down_sync(FULL_MASK, sr, h * m);
+            const double ui = __shfl_down_sync(FULL_MASK, si, h * m);
+            if (g < h) {
+              sr += ur;
+              si += ui;
+            }
+          }
+          if (g == 0) {
+            const int mb = e / (jr + 1), ma = e - mb * (jr + 1);
+            const double f = S.invf[yo + e];
+            Cplx<double>& t = utot[uo + ma * (jr + 1) + mb];
+            const double r0 = rd == 0 ? (ma == mb ? S.wself : 0.0) : t.r;
+            const double i0 = rd == 0 ? 0.0 : t.i;
+            t = Cplx<double>{fma(sr, f, r0), fma(si, f, i0)};
+          }
         }
       }
       __syncthreads();
@@ -765,32 +791,65 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
   // (the adjoint keeps Z for its final contraction, beyond `work`)
   Cplx<R>* zs = reinterpret_cast<Cplx<R>*>(MODE == 2 ? work + A.work_bytes : work);
   const R* cg = sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cg) : reinterpret_cast<const R*>(S.cg_f);
-  for (int jb = tid; jb < S.njobs; jb += SNAP_THREADS) {
-    const int code = S.jobs[jb];
-    const int t = code >> 8, ma = (code >> 4) & 15, mb = code & 15;
-    const int j1 = S.trip[3 * t], j2 = S.trip[3 * t + 1], j = S.trip[3 * t + 2];
-    const R* cgt = cg + S.cg_off[t];
-    const Cplx<R>* U1 = utot_r + uoff(j1);
-    const Cplx<R>* U2 = utot_r + uoff(j2);
-    R zr = 0, zi = 0;
-    const int ma1lo = max(0, (2 * ma - j - j2 + j1) / 2), ma1hi = min(j1, (2 * ma - j + j2 + j1) / 2);
-    const int mb1lo = max(0, (2 * mb - j - j2 + j1) / 2), mb1hi = min(j1, (2 * mb - j + j2 + j1) / 2);
-    for (int ma1 = ma1lo; ma1 <= ma1hi; ++ma1) {
-      const int ma2 = (2 * ma - j - (2 * ma1 - j1) + j2) / 2;
-      R sr = 0, si = 0;
-      for (int mb1 = mb1lo; mb1 <= mb1hi; ++mb1) {
-        const int mb2 = (2 * mb - j - (2 * mb1 - j1) + j2) / 2;
-        const R cga = cgt[mb1 * (j2 + 1) + mb2];
-        const Cplx<R> a = U1[ma1 * (j1 + 1) + mb1];
-        const Cplx<R> b = U2[ma2 * (j2 + 1) + mb2];
-        sr += cga * (a.r * b.r - a.i * b.i);
-        si += cga * (a.r * b.i + a.i * b.r);
+  if constexpr (kF64) {
+    for (int jb = tid; jb < S.njobs; jb += SNAP_THREADS) {
+      const int code = S.jobs[jb];
+      const int t = code >> 8, ma = (code >> 4) & 15, mb = code & 15;
+      const int j1 = S.trip[3 * t], j2 = S.trip[3 * t + 1], j = S.trip[3 * t + 2];
+      const R* cgt = cg + S.cg_off[t];
+      const Cplx<R>* U1 = utot_r + uoff(j1);
+      const Cplx<R>* U2 = utot_r + uoff(j2);
+      R zr = 0, zi = 0;
+      const int ma1lo = max(0, (2 * ma - j - j2 + j1) / 2), ma1hi = min(j1, (2 * ma - j + j2 + j1) / 2);
+      const int mb1lo = max(0, (2 * mb - j - j2 + j1) / 2), mb1hi = min(j1, (2 * mb - j + j2 + j1) / 2);
+      for (int ma1 = ma1lo; ma1 <= ma1hi; ++ma1) {
+        const int ma2 = (2 * ma - j - (2 * ma1 - j1) + j2) / 2;
+        R sr = 0, si = 0;
+        for (int mb1 = mb1lo; mb1 <= mb1hi; ++mb1) {
+          const int mb2 = (2 * mb - j - (2 * mb1 - j1) + j2) / 2;
+          const R cga = cgt[mb1 * (j2 + 1) + mb2];
+          const Cplx<R> a = U1[ma1 * (j1 + 1) + mb1];
+          const Cplx<R> b = U2[ma2 * (j2 + 1) + mb2];
+          sr += cga * (a.r * b.r - a.i * b.i);
+          si += cga * (a.r * b.i + a.i * b.r);
+        }
+        const R cga = cgt[ma1 * (j2 + 1) + ma2];
+        zr += sr * cga;
+        zi += si * cga;
       }
-      const R cga = cgt[ma1 * (j2 + 1) + ma2];
-      zr += sr * cga;
-      zi += si * cga;
+      zs[jb] = Cplx<R>{zr, zi};
     }
-    zs[jb] = Cplx<R>{zr, zi};
+  } else {
+    // descriptor: x the job, y the U_tot offsets of the first U1 and U2
+    // terms, z the first inner and outer Clebsch-Gordan offsets, w the counts
+    // (ma1, mb1) and the row strides j1 + 1, j2 + 1.  Along mb1 the U1 index
+    // rises by 1, the U2 index falls by 1 and the CG index rises by j2; along
+    // ma1 the rows move by +(j1 + 1) and -(j2 + 1) (compute_zi,
+    // sna_impl.hpp:197-283).
+    for (int k = tid; k < S.nzo; k += SNAP_THREADS) {
+      const int4 d = S.zord[k];
+      if (d.x < 0) continue;
+      const int u1 = d.y & 0xffff, u2 = int(unsigned(d.y) >> 16);
+      const int ci = d.z & 0xffff, co = int(unsigned(d.z) >> 16);
+      const int na = d.w & 0xff, nbb = (d.w >> 8) & 0xff, s1 = (d.w >> 16) & 0xff, s2 = int(unsigned(d.w) >> 24);
+      const int cs = s2 - 1;
+      R zr = 0, zi = 0;
+      for (int a = 0; a < na; ++a) {
+        const Cplx<R>* A1 = utot_r + u1 + a * s1;
+        const Cplx<R>* B2 = utot_r + u2 - a * s2;
+        R sr = 0, si = 0;
+        for (int b = 0; b < nbb; ++b) {
+          const R c = cg[ci + b * cs];
+          const Cplx<R> x = A1[b], y = B2[-b];
+          sr += c * (x.r * y.r - x.i * y.i);
+          si += c * (x.r * y.i + x.i * y.r);
+        }
+        const R c = cg[co + a * cs];
+        zr += sr * c;
+        zi += si * c;
+      }
+      zs[d.x] = Cplx<R>{zr, zi};
+    }
   }
   __syncthreads();
   const R* cY = (sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cY) : reinterpret_cast<const R*>(S.cY_f)) +
