@@ -20,7 +20,7 @@ struct SnapHost {
   int precision = EMD_PREC_FP64;
   DevBuf<int> trip, cg_off, jobs, tjob_off, yred_off, yred_job, map;
   DevBuf<int4> zord;
-  DevBuf<double> cg, cY, rootpq, beta0, radelem, wjelem, eatom, invf;
+  DevBuf<double> cg, cY, rootpq, beta0, radelem, wjelem, eatom, invf, yscale;
   DevBuf<float> cg_f, cY_f, yscale_f;
   // adjoint: per-atom columns, their per-element sums, the loss gradient dL/dF
   DevBuf<double> adj, adj_sum, adj_g;
@@ -60,7 +60,7 @@ double clebsch_gordan(int j1, int j2, int j, int m1, int m2) {
                    factorial((j2 - bb2) / 2) * factorial((j + cc2) / 2) * factorial((j - cc2) / 2) * (j + 1));
 }
 
-// The mixed form's Z jobs as descriptors (see SnapDev::zord), ordered for
+// The Z jobs as descriptors (see SnapDev::zord), ordered for
 // balance: sorted by inner-loop count, longest first, in chunks of 32 (a warp
 // gets jobs of one length); chunk c goes to round c / 8 and, alternating
 // direction from round to round, to warp c % 8 or 7 - c % 8.
@@ -100,20 +100,16 @@ std::vector<int4> zjob_order(const std::vector<int>& trip, const std::vector<int
   return out;
 }
 
-// bytes of the `work` region: per-warp U layers + partials (FP64 form) or
-// the neighbour slots' half layers (mixed form) for B, Z jobs (C), per-warp
-// U and dU layers (FP64 form) or the forward layers and adjoints of
-// d_reverse (mixed form) for D
+// bytes of the `work` region: the neighbour slots' half layers (B), Z jobs
+// (C), the forward layers and adjoints of d_reverse (D), or the fitting
+// adjoint's per-warp U and dU layers
 size_t snap_work_bytes(const SnapDev& S, int real_bytes) {
-  const int L2 = S.L * S.L;
-  const size_t wB = real_bytes == int(sizeof(double))
-                        ? 2 * sizeof(double) * size_t(SNAP_WARPS) * (2 * L2 + S.nyh)
-                        : 2 * sizeof(double) * size_t(SNAP_WARPS) * BG * size_t(S.bh_even + S.bh_odd);
+  const int L2 = S.L * S.L, J = S.twojmax;
+  const size_t wB = 2 * sizeof(double) * size_t(SNAP_WARPS) * BG * size_t(S.bh_even + S.bh_odd);
   const size_t wC = 2 * size_t(real_bytes) * size_t(S.njobs);
-  const int J = S.twojmax;
-  const size_t wD = real_bytes == int(sizeof(double))
-                        ? 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 8 * L2
-                        : 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 2 * size_t(drev_words(J));
+  size_t wD = 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 2 * size_t(drev_words(J));
+  if (real_bytes == int(sizeof(double)))  // the fitting adjoint's dU/dr layers
+    wD = std::max(wD, 2 * sizeof(double) * size_t(SNAP_WARPS) * 8 * L2);
   return (std::max(wB, std::max(wC, wD)) + 15) & ~size_t(15);
 }
 
@@ -161,7 +157,7 @@ void free_snap(Ctx& c) {
   for (auto* b : {&h->trip, &h->cg_off, &h->jobs, &h->tjob_off, &h->yred_off, &h->yred_job, &h->map}) b->release();
   h->zord.release();
   for (auto* b : {&h->cg, &h->cY, &h->rootpq, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
-                  &h->adj_g, &h->invf})
+                  &h->adj_g, &h->invf, &h->yscale})
     b->release();
   for (auto* b : {&h->cg_f, &h->cY_f, &h->yscale_f}) b->release();
   delete h;
@@ -410,7 +406,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   // D contraction's Y scale (twice the half-grid weight over f); the largest
   // half layer of even and odd j
   std::vector<double> invf(static_cast<size_t>(S.nyh));
-  std::vector<float> yscale(static_cast<size_t>(S.nyh));
+  std::vector<double> yscale(static_cast<size_t>(S.nyh));
   S.bh_even = S.bh_odd = 1;
   for (int j = 0; j <= twojmax; ++j) {
     const int nh = (j + 1) * (j / 2 + 1);
@@ -421,7 +417,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
         invf[e] = std::sqrt(factorial(j - ma) * factorial(ma) / (factorial(j - mb) * factorial(mb)));
         // twice the half-grid contraction weight (sna_impl.hpp:384-413)
         const double w2 = (2 * mb < j || 2 * ma < j) ? 2.0 : (2 * ma == j ? 1.0 : 0.0);
-        yscale[e] = float(w2 * invf[e]);
+        yscale[e] = w2 * invf[e];
       }
   }
   double rcutmax = 0.0;
@@ -450,7 +446,8 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   upload(c, h->cY_f, cYf);
   upload(c, h->rootpq, rootpq);
   upload(c, h->invf, invf);
-  upload(c, h->yscale_f, yscale);
+  upload(c, h->yscale, yscale);
+  upload(c, h->yscale_f, std::vector<float>(yscale.begin(), yscale.end()));
   upload(c, h->beta0, beta0);
   upload(c, h->radelem, std::vector<double>(radelem, radelem + nelem));
   upload(c, h->wjelem, std::vector<double>(wjelem, wjelem + nelem));
@@ -469,6 +466,7 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.cY_f = h->cY_f.p;
   S.rootpq = h->rootpq.p;
   S.invf = h->invf.p;
+  S.yscale = h->yscale.p;
   S.yscale_f = h->yscale_f.p;
   S.beta0 = h->beta0.p;
   S.radelem = h->radelem.p;

@@ -5,12 +5,9 @@
 //      row order (ballot + popc), keeping r_ij = x_j - x_i, w_j, rcut_ij;
 //   B. U_tot = wself*I + sum_j sfac*w_j*U_j by the Cayley-Klein layer
 //      recursion (compute_uarray, sna_impl.hpp:642-720), in FP64 in both
-//      forms.  FP64 form: each warp runs its neighbours one at a time, lanes
-//      over the (ma, mb) half layer, into a private half-grid partial; the
-//      partials are summed in a fixed order and mirrored to the full
-//      matrices.  Mixed form: the rescaled recursion (no square-root
-//      factors, b_stage_mixed), lanes over (neighbour, element) pairs of four
-//      neighbours per warp, one fixed-order block sum per layer;
+//      forms: the rescaled recursion (no square-root factors, b_stage), lanes
+//      over (neighbour, element) pairs of four neighbours per warp, one
+//      fixed-order block sum per layer, mirrored to the full matrices;
 //   C. adjoint contraction: Z_t(ma,mb) for the 125 (j1>=j2, j) triples
 //      (compute_zi, sna_impl.hpp:197-283) and Y_j = sum_t cY_t Z_t, where
 //      cY folds the linear coefficients with the (j+1)/(j1+1), (j+1)/(j2+1)
@@ -19,9 +16,10 @@
 //      F_ij = sum_j 2 sum_half w Re(conj(dU'_j) Y_j) + (-1.5e6/r^14) r_ij,
 //      which equals sum_k beta_k dB_k/dr_ij of the reference; f_i += F_ij,
 //      f_j -= F_ij with FP64 atomics (j may be a ghost; update_force follows).
-//      FP64 form: U and dU/dr by the differentiated recursion
-//      (compute_duarray, sna_impl.hpp:729-893).  Mixed form: one forward
-//      sweep of the rescaled U recursion and one adjoint sweep (d_reverse).
+//      One forward sweep of the rescaled U recursion and one adjoint sweep
+//      per neighbour (d_reverse) in place of the dU/dr recursion of
+//      compute_duarray (sna_impl.hpp:729-893).  The fitting adjoint (MODE 2)
+//      runs that dU/dr recursion (du_layer).
 // The energy variant adds E_i = beta_0 + (2/3) sum_j sum_half w Re(conj(U_j) Y_j)
 // (B is cubic in U, so <U, dB/dU> = 3B) plus 1.25e5/r^12 per inside pair.
 //
@@ -75,13 +73,14 @@ struct SnapDev {
   const double* radelem;
   const double* wjelem;
   const int* map;  // ntypes
-  // rescaled recursion of the mixed form: V_j(ma, mb) = f_j(ma, mb) U_j(ma, mb);
-  // over the half grid (nyh): invf = 1 / f, yscale_f = hw2 / f (the D
-  // contraction's weight folded into Y); half-layer buffer sizes (even, odd j)
+  // rescaled recursion: V_j(ma, mb) = f_j(ma, mb) U_j(ma, mb); over the half
+  // grid (nyh): invf = 1 / f, yscale = hw2 / f (the force contraction's
+  // weight folded into Y; FP64 and FP32); half-layer buffer sizes (even, odd j)
   const double* invf;
+  const double* yscale;
   const float* yscale_f;
   int bh_even, bh_odd;
-  // the mixed form's Z jobs as descriptors, longest first, in the order
+  // the Z jobs as descriptors, longest first, in the order
   // thread (warp w, lane l) takes them in round r: zord[r * SNAP_THREADS +
   // 32 w + l] (x < 0: no job); see zjob_order in snap.cu
   const int4* zord;
@@ -137,44 +136,6 @@ __device__ __forceinline__ double dsfac_of(const SnapDev& S, double r, double rc
   if (r > rcut) return 0.0;
   const double rcutfac = MY_PI / (rcut - S.rmin0);
   return -0.5 * sin((r - S.rmin0) * rcutfac) * rcutfac;
-}
-
-// One layer of the U recursion, lanes over the half layer of j from the full
-// layer j-1 in P (index ma*j + mb), into C (index ma*(j+1) + mb), then the
-// inversion-symmetry mirror (sna_impl.hpp:660-719).
-template <typename R>
-__device__ __forceinline__ void u_layer(int j, int lane, const R* __restrict__ rootpq, int L1, R ar, R ai, R br,
-                                        R bi, const Cplx<R>* P, Cplx<R>* C) {
-  const int nh = (j + 1) * (j / 2 + 1);
-  for (int e = lane; e < nh; e += 32) {
-    const int mb = e / (j + 1), ma = e % (j + 1);
-    R vr = 0, vi = 0;
-    if (ma > 0) {
-      const Cplx<R> u = P[(ma - 1) * j + mb];
-      const R rp = rootpq[ma * L1 + (j - mb)];
-      vr = -rp * (br * u.r + bi * u.i);
-      vi = -rp * (br * u.i - bi * u.r);
-    }
-    if (ma < j) {
-      const Cplx<R> u = P[ma * j + mb];
-      const R rp = rootpq[(j - ma) * L1 + (j - mb)];
-      vr += rp * (ar * u.r + ai * u.i);
-      vi += rp * (ar * u.i - ai * u.r);
-    }
-    C[ma * (j + 1) + mb] = Cplx<R>{vr, vi};
-  }
-  __syncwarp();
-  for (int e = lane; e < nh; e += 32) {
-    const int mb = e / (j + 1), ma = e % (j + 1);
-    const bool even = ((ma + mb) & 1) == 0;
-    if (2 * mb < j || 2 * ma < j) {
-      const Cplx<R> u = C[ma * (j + 1) + mb];
-      C[(j - ma) * (j + 1) + (j - mb)] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
-    } else if (2 * ma == j) {
-      C[ma * (j + 1) + mb].i = -C[ma * (j + 1) + mb].i;  // centre: conj (the reference's in-place mirror)
-    }
-  }
-  __syncwarp();
 }
 
 // U and dU/dr (3 components) layer: dU arrays hold 3 consecutive Cplx per element.
@@ -264,17 +225,19 @@ __device__ __forceinline__ Cplx<double> ld_half(const Cplx<double>* P, int jp, i
   return Cplx<double>{flip_if(v.r, odd), flip_if(v.i, !odd)};
 }
 
-// neighbour slots per warp in b_stage_mixed
+// neighbour slots per warp in b_stage
 constexpr int BG = 4;
 
-// B of the mixed form: U_tot (FP64) and its FP32 copy.  Neighbours go in
+// B: U_tot (FP64) and, for R = float, its FP32 copy.  Neighbours go in
 // rounds of SNAP_WARPS * BG; warp w holds neighbours w, w + SNAP_WARPS, ... of
 // the round, its lanes over (slot, half-layer element) pairs.  Layer 0 is
 // seeded with sfac * w_j, so each layer's sum over the neighbours is a plain
 // sum: one warp adds up layer j - 1 (in a fixed order) while the others run
 // layer j.  `work` holds SNAP_WARPS * BG slots of (bh_even + bh_odd) elements.
-__device__ __forceinline__ void b_stage_mixed(const SnapDev& S, const double* nd, int cap, int ninside,
-                                              Cplx<double>* work, Cplx<double>* utot, Cplx<float>* utot_r) {
+template <typename R>
+__device__ __forceinline__ void b_stage(const SnapDev& S, const double* nd, int cap, int ninside, Cplx<double>* work,
+                                        Cplx<double>* utot, Cplx<R>* utot_r) {
+  constexpr bool kCopy = sizeof(R) != sizeof(double);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int sw = S.bh_even + S.bh_odd, per_round = SNAP_WARPS * BG;
   Cplx<double>* mine = work + size_t(warp) * BG * sw;
@@ -355,22 +318,22 @@ __device__ __forceinline__ void b_stage_mixed(const SnapDev& S, const double* nd
     if (2 * mb == j && 2 * ma > j) continue;  // written as the mirror of (j - ma, mb)
     const int uo = uoff(j);
     const Cplx<double> u = utot[uo + ma * (j + 1) + mb];
-    utot_r[uo + ma * (j + 1) + mb] = Cplx<float>{float(u.r), float(u.i)};
+    if constexpr (kCopy) utot_r[uo + ma * (j + 1) + mb] = Cplx<R>{R(u.r), R(u.i)};
     if (2 * mb < j || 2 * ma < j) {
       const bool odd = (ma + mb) & 1;
       const Cplx<double> m{flip_if(u.r, odd), flip_if(u.i, !odd)};
       const int t = uo + (j - ma) * (j + 1) + (j - mb);
       utot[t] = m;
-      utot_r[t] = Cplx<float>{float(m.r), float(m.i)};
+      if constexpr (kCopy) utot_r[t] = Cplx<R>{R(m.r), R(m.i)};
     }
   }
   __syncthreads();
 }
 
-// Phase D of the mixed form, in reverse mode, for NB neighbours at once (one
-// per register set, so each lane carries NB independent chains).  With
-// Phi = sum_j sum_half Re(conj(V_j) Y'_j), Y' = w Y / f (ytot of the mixed
-// form), the pair force needs only Phi and its gradient in a = (ar, ai),
+// Phase D of the force, in reverse mode, for NB neighbours at once (one per
+// register set, so each lane carries NB independent chains).  With
+// Phi = sum_j sum_half Re(conj(V_j) Y'_j), Y' = w Y / f (ytot of the force
+// kernel), the pair force needs only Phi and its gradient in a = (ar, ai),
 // b = (br, bi):  F_k = dsfac u_k Phi + sfac sum_p dPhi/dp dp/dr_k.  The
 // forward sweep runs the rescaled recursion and keeps layers 0..J-1 (full,
 // column-major, in F); the backward sweep carries the adjoint
@@ -386,17 +349,17 @@ __device__ __forceinline__ void b_stage_mixed(const SnapDev& S, const double* nd
 // (dPhi/dar = ga.r, dPhi/dai = -ga.i, dPhi/dbr = -gb.r, dPhi/dbi = gb.i).
 // Neighbour n's buffers start at W + n * drev_words(J): F max(1, uoff(J)),
 // LA and LB max(1, J (J/2 + 1)) each, LP (J + 1)(J/2 + 1).
+template <typename R>
 struct DRevAB {
-  float ar, ai, br, bi;
+  R ar, ai, br, bi;
 };
 __host__ __device__ __forceinline__ int drev_words(int J) {
   return (J * (J + 1) * (2 * J + 1) / 6 > 1 ? J * (J + 1) * (2 * J + 1) / 6 : 1) +
          2 * (J * (J / 2 + 1) > 1 ? J * (J / 2 + 1) : 1) + (J + 1) * (J / 2 + 1);
 }
-template <int NB>
-__device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB* ab, const Cplx<float>* __restrict__ ytot,
-                                          Cplx<float>* W, float* phi, Cplx<float>* ga, Cplx<float>* gb) {
-  using R = float;
+template <typename R, int NB>
+__device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, const Cplx<R>* __restrict__ ytot,
+                                          Cplx<R>* W, R* phi, Cplx<R>* ga, Cplx<R>* gb) {
   const int nF = max(1, uoff(J)), nL = max(1, J * (J / 2 + 1)), stride = drev_words(J);
 #pragma unroll
   for (int n = 0; n < NB; ++n) {
@@ -457,7 +420,7 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB* ab, con
       const Cplx<R> y = ytot[yo + e];
 #pragma unroll
       for (int n = 0; n < NB; ++n) {
-        Cplx<float>* Wn = W + n * stride;
+        Cplx<R>* Wn = W + n * stride;
         Cplx<R> l{R(0), R(0)};
         if (!dead) {
           l = (j == J) ? y : Wn[lam + e];
@@ -493,9 +456,9 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB* ab, con
         if (idx < nhp) y = ytot[yop + idx];
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
-          Cplx<float>* Wn = W + k * stride;
+          Cplx<R>* Wn = W + k * stride;
           const Cplx<R> l1 = Wn[lp + mb * (j + 1) + mp], l0 = Wn[lp + mb * (j + 1) + mp + 1];
-          const DRevAB& q = ab[k];
+          const DRevAB<R>& q = ab[k];
           Wn[nxt + idx] = Cplx<R>{q.ar * l1.r - q.ai * l1.i - (q.br * l0.r - q.bi * l0.i) + y.r,
                                   q.ar * l1.i + q.ai * l1.r - (q.br * l0.i + q.bi * l0.r) + y.i};
         }
@@ -604,14 +567,6 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       if (cnt > A.cap) latch_status(A.status, ST_BOUNDS);
       s_ninside = min(cnt, A.cap);
     }
-  }
-  // per-warp regions for phase B: 2 layers (L2 each) + half-grid partial (nyh)
-  Cplx<double>* wb = reinterpret_cast<Cplx<double>*>(work) + warp * (2 * L2 + S.nyh);
-  Cplx<double>* Pb = wb;
-  Cplx<double>* Cb = wb + L2;
-  Cplx<double>* part = wb + 2 * L2;
-  if constexpr (kF64) {
-    for (int e = lane; e < S.nyh; e += 32) part[e] = Cplx<double>{0.0, 0.0};
   }
   __syncthreads();
   const int ninside = s_ninside;
@@ -732,124 +687,42 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
   }
   __syncthreads();
 
-  // ---- B: U_tot (FP64)
-  if constexpr (kF64) {
-    for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
-      const double ar = nd[ND_AR_U * A.cap + nb], ai = nd[ND_AI_U * A.cap + nb];
-      const double br = nd[ND_BR_U * A.cap + nb], bi = nd[ND_BI_U * A.cap + nb];
-      const double sfac = nd[ND_SFAC * A.cap + nb];
-      if (lane == 0) {
-        Pb[0] = Cplx<double>{1.0, 0.0};
-        part[0].r += sfac * 1.0;
-      }
-      __syncwarp();
-      Cplx<double>* P = Pb;
-      Cplx<double>* C = Cb;
-      for (int j = 1; j <= S.twojmax; ++j) {
-        u_layer<double>(j, lane, rootpq_d, L1, ar, ai, br, bi, P, C);
-        const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j);
-        for (int e = lane; e < nh; e += 32) {
-          const int mb = e / (j + 1), ma = e % (j + 1);
-          const Cplx<double> u = C[ma * (j + 1) + mb];
-          part[yo + e].r += sfac * u.r;
-          part[yo + e].i += sfac * u.i;
-        }
-        __syncwarp();
-        Cplx<double>* t = P;
-        P = C;
-        C = t;
-      }
-    }
-    __syncthreads();
-    // sum partials (fixed order), add wself on the diagonal, mirror to full U_tot
-    for (int e = tid; e < S.nyh; e += SNAP_THREADS) {
-      int j = 0;
-      while (yoff(j + 1) <= e) ++j;
-      const int q = e - yoff(j);
-      const int mb = q / (j + 1), ma = q % (j + 1);
-      double sr = (ma == mb) ? S.wself : 0.0, si = 0.0;
-      for (int w = 0; w < SNAP_WARPS; ++w) {
-        const Cplx<double>* pw = reinterpret_cast<Cplx<double>*>(work) + w * (2 * L2 + S.nyh) + 2 * L2;
-        sr += pw[e].r;
-        si += pw[e].i;
-      }
-      const int uo = uoff(j);
-      utot[uo + ma * (j + 1) + mb] = Cplx<double>{sr, si};
-      if (2 * mb < j || 2 * ma < j) {
-        const bool even = ((ma + mb) & 1) == 0;
-        const int t = uo + (j - ma) * (j + 1) + (j - mb);
-        utot[t] = even ? Cplx<double>{sr, -si} : Cplx<double>{-sr, si};
-      }
-    }
-    __syncthreads();
-  } else {
-    b_stage_mixed(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot,
-                  reinterpret_cast<Cplx<float>*>(utot_r));
-  }
+  // ---- B: U_tot (FP64, both forms)
+  b_stage<R>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
 
   // ---- C: Z jobs and Y = sum_t cY_t Z_t
   // (the adjoint keeps Z for its final contraction, beyond `work`)
   Cplx<R>* zs = reinterpret_cast<Cplx<R>*>(MODE == 2 ? work + A.work_bytes : work);
   const R* cg = sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cg) : reinterpret_cast<const R*>(S.cg_f);
-  if constexpr (kF64) {
-    for (int jb = tid; jb < S.njobs; jb += SNAP_THREADS) {
-      const int code = S.jobs[jb];
-      const int t = code >> 8, ma = (code >> 4) & 15, mb = code & 15;
-      const int j1 = S.trip[3 * t], j2 = S.trip[3 * t + 1], j = S.trip[3 * t + 2];
-      const R* cgt = cg + S.cg_off[t];
-      const Cplx<R>* U1 = utot_r + uoff(j1);
-      const Cplx<R>* U2 = utot_r + uoff(j2);
-      R zr = 0, zi = 0;
-      const int ma1lo = max(0, (2 * ma - j - j2 + j1) / 2), ma1hi = min(j1, (2 * ma - j + j2 + j1) / 2);
-      const int mb1lo = max(0, (2 * mb - j - j2 + j1) / 2), mb1hi = min(j1, (2 * mb - j + j2 + j1) / 2);
-      for (int ma1 = ma1lo; ma1 <= ma1hi; ++ma1) {
-        const int ma2 = (2 * ma - j - (2 * ma1 - j1) + j2) / 2;
-        R sr = 0, si = 0;
-        for (int mb1 = mb1lo; mb1 <= mb1hi; ++mb1) {
-          const int mb2 = (2 * mb - j - (2 * mb1 - j1) + j2) / 2;
-          const R cga = cgt[mb1 * (j2 + 1) + mb2];
-          const Cplx<R> a = U1[ma1 * (j1 + 1) + mb1];
-          const Cplx<R> b = U2[ma2 * (j2 + 1) + mb2];
-          sr += cga * (a.r * b.r - a.i * b.i);
-          si += cga * (a.r * b.i + a.i * b.r);
-        }
-        const R cga = cgt[ma1 * (j2 + 1) + ma2];
-        zr += sr * cga;
-        zi += si * cga;
+  // descriptor: x the job, y the U_tot offsets of the first U1 and U2
+  // terms, z the first inner and outer Clebsch-Gordan offsets, w the counts
+  // (ma1, mb1) and the row strides j1 + 1, j2 + 1.  Along mb1 the U1 index
+  // rises by 1, the U2 index falls by 1 and the CG index rises by j2; along
+  // ma1 the rows move by +(j1 + 1) and -(j2 + 1) (compute_zi,
+  // sna_impl.hpp:197-283).
+  for (int k = tid; k < S.nzo; k += SNAP_THREADS) {
+    const int4 d = S.zord[k];
+    if (d.x < 0) continue;
+    const int u1 = d.y & 0xffff, u2 = int(unsigned(d.y) >> 16);
+    const int ci = d.z & 0xffff, co = int(unsigned(d.z) >> 16);
+    const int na = d.w & 0xff, nbb = (d.w >> 8) & 0xff, s1 = (d.w >> 16) & 0xff, s2 = int(unsigned(d.w) >> 24);
+    const int cs = s2 - 1;
+    R zr = 0, zi = 0;
+    for (int a = 0; a < na; ++a) {
+      const Cplx<R>* A1 = utot_r + u1 + a * s1;
+      const Cplx<R>* B2 = utot_r + u2 - a * s2;
+      R sr = 0, si = 0;
+      for (int b = 0; b < nbb; ++b) {
+        const R c = cg[ci + b * cs];
+        const Cplx<R> x = A1[b], y = B2[-b];
+        sr += c * (x.r * y.r - x.i * y.i);
+        si += c * (x.r * y.i + x.i * y.r);
       }
-      zs[jb] = Cplx<R>{zr, zi};
+      const R c = cg[co + a * cs];
+      zr += sr * c;
+      zi += si * c;
     }
-  } else {
-    // descriptor: x the job, y the U_tot offsets of the first U1 and U2
-    // terms, z the first inner and outer Clebsch-Gordan offsets, w the counts
-    // (ma1, mb1) and the row strides j1 + 1, j2 + 1.  Along mb1 the U1 index
-    // rises by 1, the U2 index falls by 1 and the CG index rises by j2; along
-    // ma1 the rows move by +(j1 + 1) and -(j2 + 1) (compute_zi,
-    // sna_impl.hpp:197-283).
-    for (int k = tid; k < S.nzo; k += SNAP_THREADS) {
-      const int4 d = S.zord[k];
-      if (d.x < 0) continue;
-      const int u1 = d.y & 0xffff, u2 = int(unsigned(d.y) >> 16);
-      const int ci = d.z & 0xffff, co = int(unsigned(d.z) >> 16);
-      const int na = d.w & 0xff, nbb = (d.w >> 8) & 0xff, s1 = (d.w >> 16) & 0xff, s2 = int(unsigned(d.w) >> 24);
-      const int cs = s2 - 1;
-      R zr = 0, zi = 0;
-      for (int a = 0; a < na; ++a) {
-        const Cplx<R>* A1 = utot_r + u1 + a * s1;
-        const Cplx<R>* B2 = utot_r + u2 - a * s2;
-        R sr = 0, si = 0;
-        for (int b = 0; b < nbb; ++b) {
-          const R c = cg[ci + b * cs];
-          const Cplx<R> x = A1[b], y = B2[-b];
-          sr += c * (x.r * y.r - x.i * y.i);
-          si += c * (x.r * y.i + x.i * y.r);
-        }
-        const R c = cg[co + a * cs];
-        zr += sr * c;
-        zi += si * c;
-      }
-      zs[d.x] = Cplx<R>{zr, zi};
-    }
+    zs[d.x] = Cplx<R>{zr, zi};
   }
   __syncthreads();
   const R* cY = (sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cY) : reinterpret_cast<const R*>(S.cY_f)) +
@@ -862,8 +735,8 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       yr += cy * zs[jb].r;
       yi += cy * zs[jb].i;
     }
-    if constexpr (!kF64) {  // w Y / f: the mixed form's dU recursion runs on V = f U
-      const R f = S.yscale_f[e];
+    if constexpr (MODE == 0) {  // w Y / f: the force runs on V = f U (d_reverse)
+      const R f = sizeof(R) == sizeof(double) ? R(S.yscale[e]) : R(S.yscale_f[e]);
       yr *= f;
       yi *= f;
     }
@@ -989,27 +862,27 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
     return;
   }
 
-  // ---- D: the pair forces.  Mixed form: reverse mode (d_reverse), two
-  // neighbours per warp at a time; the FP64 part (repulsion, scatter to j,
-  // the sum for i) is done afterwards, one thread per neighbour.
-  if constexpr (!kF64) {
+  // ---- D: the pair forces in reverse mode (d_reverse), two neighbours per
+  // warp at a time; the FP64 part (repulsion, scatter to j, the sum for i) is
+  // done afterwards, one thread per neighbour.
+  {
     const int J = S.twojmax, stride = drev_words(J);
-    Cplx<float>* W = reinterpret_cast<Cplx<float>*>(work) + size_t(warp) * 2 * stride;
+    Cplx<R>* W = reinterpret_cast<Cplx<R>*>(work) + size_t(warp) * 2 * stride;
     double* fpair = in_r;  // r_ij is not read after the per-neighbour scalars
     for (int nb0 = warp; nb0 < ninside; nb0 += 2 * SNAP_WARPS) {
       const int nb1 = nb0 + SNAP_WARPS;
       const int nn = nb1 < ninside ? 2 : 1;
-      DRevAB ab[2];
+      DRevAB<R> ab[2];
       for (int n = 0; n < 2; ++n) {
         const R* qr = ndr + (n < nn ? (n ? nb1 : nb0) : nb0);
-        ab[n] = DRevAB{qr[ND_AR * A.cap], qr[ND_AI * A.cap], qr[ND_BR * A.cap], qr[ND_BI * A.cap]};
+        ab[n] = DRevAB<R>{qr[ND_AR * A.cap], qr[ND_AI * A.cap], qr[ND_BR * A.cap], qr[ND_BI * A.cap]};
       }
-      float phi[2];
-      Cplx<float> ga[2], gb[2];
+      R phi[2];
+      Cplx<R> ga[2], gb[2];
       if (nn == 2)
-        d_reverse<2>(J, lane, ab, ytot, W, phi, ga, gb);
+        d_reverse<R, 2>(J, lane, ab, ytot, W, phi, ga, gb);
       else
-        d_reverse<1>(J, lane, ab, ytot, W, phi, ga, gb);
+        d_reverse<R, 1>(J, lane, ab, ytot, W, phi, ga, gb);
       for (int n = 0; n < nn; ++n) {
         const int nb = n ? nb1 : nb0;
         const R* qr = ndr + nb;
@@ -1020,8 +893,8 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
           fk[k] = cp * qr[(ND_UK + k) * A.cap] +
                   sf * (ga[n].r * qr[(ND_DAR + k) * A.cap] - ga[n].i * qr[(ND_DAI + k) * A.cap] -
                         gb[n].r * qr[(ND_DBR + k) * A.cap] + gb[n].i * qr[(ND_DBI + k) * A.cap]);
-        // summed over the lanes in FP32 (an FP64 shuffle tree would cost more
-        // FP64-pipe time than the FP32 sweeps)
+        // summed over the lanes in the contraction type (an FP64 shuffle tree
+        // would cost the mixed form more FP64-pipe time than its FP32 sweeps)
         const R sx = warp_sum_r(fk[0]), sy = warp_sum_r(fk[1]), sz = warp_sum_r(fk[2]);
         if (lane == 0) {
           fpair[3 * nb] = double(sx);
@@ -1054,99 +927,6 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
         if (lane == 0) atomicAdd(A.f + 3 * i + k, t);
       }
     }
-    return;
-  }
-  // FP64 form: per neighbour (a warp each), U and dU/dr by the recursion
-  double fix = 0, fiy = 0, fiz = 0;
-  for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
-    const double* q = nd + nb;
-    const R* qr = ndr + nb;
-    const R Rar = qr[ND_AR * A.cap], Rai = qr[ND_AI * A.cap], Rbr = qr[ND_BR * A.cap], Rbi = qr[ND_BI * A.cap];
-    R Rdar[3], Rdai[3], Rdbr[3], Rdbi[3], Ruk[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      Rdar[k] = qr[(ND_DAR + k) * A.cap];
-      Rdai[k] = qr[(ND_DAI + k) * A.cap];
-      Rdbr[k] = qr[(ND_DBR + k) * A.cap];
-      Rdbi[k] = qr[(ND_DBI + k) * A.cap];
-      Ruk[k] = qr[(ND_UK + k) * A.cap];
-    }
-    const R Rsfac = qr[ND_SFAC * A.cap], Rdsfac = qr[ND_DSFAC * A.cap];
-    R fx = 0, fy = 0, fz = 0;
-    if constexpr (kF64) {
-      Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
-      Cplx<R>* P = wd;
-      Cplx<R>* C = wd + L2;
-      Cplx<R>* dP = wd + 2 * L2;
-      Cplx<R>* dC = wd + 5 * L2;
-      // layer 0: U = 1, dU = 0; half grid is the centre (weight 1/2)
-      if (lane == 0) {
-        P[0] = Cplx<R>{R(1), R(0)};
-        for (int k = 0; k < 3; ++k) dP[k] = Cplx<R>{R(0), R(0)};
-        const R yr = ytot[0].r;
-        fx = Rdsfac * Ruk[0] * yr;
-        fy = Rdsfac * Ruk[1] * yr;
-        fz = Rdsfac * Ruk[2] * yr;
-      }
-      __syncwarp();
-      for (int j = 1; j <= S.twojmax; ++j) {
-        du_layer<R>(j, lane, rootpq_r, L1, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
-        const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j);
-        for (int e = lane; e < nh; e += 32) {
-          const int mb = e / (j + 1), ma = e % (j + 1);
-          const R w = hw2<R>(j, ma, mb);
-          if (w == R(0)) continue;
-          const int o = ma * (j + 1) + mb;
-          const Cplx<R> u = C[o];
-          const Cplx<R> yv = ytot[yo + e];
-          R g[3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            const Cplx<R> du = dC[3 * o + k];
-            const R dur = Rdsfac * u.r * Ruk[k] + Rsfac * du.r;
-            const R dui = Rdsfac * u.i * Ruk[k] + Rsfac * du.i;
-            g[k] = w * (dur * yv.r + dui * yv.i);
-          }
-          fx += g[0];
-          fy += g[1];
-          fz += g[2];
-        }
-        __syncwarp();
-        Cplx<R>* t = P;
-        P = C;
-        C = t;
-        t = dP;
-        dP = dC;
-        dC = t;
-      }
-    }
-    // the pair force summed over the lanes in the contraction type (an FP64
-    // shuffle tree would cost more FP64-pipe time than the FP32 layers)
-    double Fx = double(warp_sum_r(fx)), Fy = double(warp_sum_r(fy)), Fz = double(warp_sum_r(fz));
-    if (lane == 0) {
-      Fx += q[ND_FP * A.cap];
-      Fy += q[(ND_FP + 1) * A.cap];
-      Fz += q[(ND_FP + 2) * A.cap];
-      const int j = in_j[nb];
-      atomicAdd(A.f + 3 * j, -Fx);
-      atomicAdd(A.f + 3 * j + 1, -Fy);
-      atomicAdd(A.f + 3 * j + 2, -Fz);
-      fix += Fx;
-      fiy += Fy;
-      fiz += Fz;
-    }
-    __syncwarp();
-  }
-  if (lane == 0) {
-    red[warp] = fix;
-    red[SNAP_WARPS + warp] = fiy;
-    red[2 * SNAP_WARPS + warp] = fiz;
-  }
-  __syncthreads();
-  if (tid < 3) {
-    double s = 0.0;
-    for (int w = 0; w < SNAP_WARPS; ++w) s += red[tid * SNAP_WARPS + w];
-    atomicAdd(A.f + 3 * i + tid, s);
   }
 }
 
