@@ -25,7 +25,8 @@
 //
 // Precision forms: FP64 (the drop-in; snap.cu, -fmad=false) and mixed
 // (snap_mixed.cu, contraction allowed), where U_tot stays FP64 (phase B) and
-// phases C/D run in FP32 with FP64 force sums.
+// phases C/D run in FP32 with FP64 force sums.  The recursions and the Z
+// contraction use explicit fused multiply-adds in both forms.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -380,10 +381,10 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, 
         Cplx<R> u1{R(0), R(0)}, u2{R(0), R(0)};
         if (ma > 0) u1 = P[mb * j + ma - 1];
         if (ma < j) u2 = P[mb * j + ma];
-        const R vr = ab[n].ar * u2.r + ab[n].ai * u2.i - ab[n].br * u1.r - ab[n].bi * u1.i;
-        R vi = ab[n].ar * u2.i - ab[n].ai * u2.r - ab[n].br * u1.i + ab[n].bi * u1.r;
+        const R vr = fma(ab[n].ar, u2.r, fma(ab[n].ai, u2.i, fma(-ab[n].br, u1.r, -ab[n].bi * u1.i)));
+        R vi = fma(ab[n].ar, u2.i, fma(-ab[n].ai, u2.r, fma(-ab[n].br, u1.i, ab[n].bi * u1.r)));
         if (centre) vi = -vi;
-        phi[n] += vr * y.r + vi * y.i;
+        phi[n] = fma(vr, y.r, fma(vi, y.i, phi[n]));
         if (j < J) W[n * stride + co + e] = Cplx<R>{vr, vi};
       }
     }
@@ -433,13 +434,13 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, 
           }
           if (ma < j) {
             const Cplx<R> p = Wn[po + mb * j + ma];
-            ga[n].r += p.r * l.r + p.i * l.i;
-            ga[n].i += p.r * l.i - p.i * l.r;
+            ga[n].r = fma(p.r, l.r, fma(p.i, l.i, ga[n].r));
+            ga[n].i = fma(p.r, l.i, fma(-p.i, l.r, ga[n].i));
           }
           if (ma > 0) {
             const Cplx<R> p = Wn[po + mb * j + ma - 1];
-            gb[n].r += p.r * l.r + p.i * l.i;
-            gb[n].i += p.r * l.i - p.i * l.r;
+            gb[n].r = fma(p.r, l.r, fma(p.i, l.i, gb[n].r));
+            gb[n].i = fma(p.r, l.i, fma(-p.i, l.r, gb[n].i));
           }
         }
         Wn[lp + e] = l;
@@ -459,8 +460,8 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, 
           Cplx<R>* Wn = W + k * stride;
           const Cplx<R> l1 = Wn[lp + mb * (j + 1) + mp], l0 = Wn[lp + mb * (j + 1) + mp + 1];
           const DRevAB<R>& q = ab[k];
-          Wn[nxt + idx] = Cplx<R>{q.ar * l1.r - q.ai * l1.i - (q.br * l0.r - q.bi * l0.i) + y.r,
-                                  q.ar * l1.i + q.ai * l1.r - (q.br * l0.i + q.bi * l0.r) + y.i};
+          Wn[nxt + idx] = Cplx<R>{fma(q.ar, l1.r, fma(-q.ai, l1.i, fma(-q.br, l0.r, fma(q.bi, l0.i, y.r)))),
+                                  fma(q.ar, l1.i, fma(q.ai, l1.r, fma(-q.br, l0.i, fma(-q.bi, l0.r, y.i))))};
         }
       }
       __syncwarp();
@@ -715,12 +716,12 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       for (int b = 0; b < nbb; ++b) {
         const R c = cg[ci + b * cs];
         const Cplx<R> x = A1[b], y = B2[-b];
-        sr += c * (x.r * y.r - x.i * y.i);
-        si += c * (x.r * y.i + x.i * y.r);
+        sr = fma(c, fma(x.r, y.r, -x.i * y.i), sr);
+        si = fma(c, fma(x.r, y.i, x.i * y.r), si);
       }
       const R c = cg[co + a * cs];
-      zr += sr * c;
-      zi += si * c;
+      zr = fma(sr, c, zr);
+      zi = fma(si, c, zi);
     }
     zs[d.x] = Cplx<R>{zr, zi};
   }
