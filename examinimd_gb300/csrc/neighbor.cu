@@ -1,22 +1,23 @@
 // NeighborCSR / Neighbor2D on the device (neighbor_csr.h:176-435,
 // neighbor_2d.h:175-331).
 //
-// One CTA per interior bin.  The CTA stages the particles of its 27-bin
+// One warp per interior bin.  The warp stages the particles of its 27-bin
 // stencil in the reference order (bx_j slowest, bz_j fastest; inside a bin
 // in permutation order) into shared memory as FP32 positions relative to the
 // centre of ITS bin (exact bin-relative FP32 coordinates come from the
 // binning pass), so a candidate test is three FP32 subtractions and an FP32
 // r^2.  Only when r^2 lies within 4e-5 relative of the cutoff is the pair
 // re-tested with the FP64 positions, so every accept / reject equals the FP64
-// test `rsq <= neigh_cut^2` of the reference.  Each warp owns centre atoms
-// and walks the staged candidates 32 at a time; accepted candidates are
-// compacted with ballot + popc, so row i lists its neighbours in exactly the
-// order the serial reference appends them.
+// test `rsq <= neigh_cut^2` of the reference.  Each lane owns one centre atom
+// of the bin and walks the staged candidates in order (one broadcast
+// shared-memory read per candidate for the whole warp), appending the
+// accepted ones, so row i lists its neighbours in exactly the order the
+// serial reference appends them.
 //
 // One pass writes rows column-major in 16-byte granules (neigh_rows.cuh:
 // the LayoutLeft of the reference's Neighbor2D view on a GPU, four entries
-// per granule) with capacity K; the host grows K like Neighbor2D's regrow
-// loop (x1.2) when a row overflows.
+// per granule) with capacity K; the host grows K like
+// Neighbor2D's regrow loop (x1.2) when a row overflows.
 // NeighborCSR rows are then compacted behind an exclusive scan of the
 // counts.  Rows built for the mixed-precision force carry packed entries
 // (j << 6) | (kx << 4) | (ky << 2) | kz with k = (bin_j - bin_i) + 1 per
@@ -31,9 +32,8 @@
 namespace emd {
 namespace {
 
-constexpr int NB_THREADS = 128;
-constexpr int NB_WARPS = NB_THREADS / 32;
-constexpr int NB_CAP = 1024;  // staged candidates per chunk
+constexpr int NB_THREADS = 32;  // one warp per interior bin
+constexpr int NB_CAP = 384;     // staged candidates per chunk
 constexpr int NB_SLOTS = 64;  // spread slots for the longest-row reduction
 static_assert(1 + NB_SLOTS <= kHostInts, "read-back of the row-length slots exceeds the pinned scratch");
 
@@ -71,111 +71,129 @@ __device__ __forceinline__ long long okey(double v) {
   return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
+template <bool HALF, bool PACKED>
 __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
   __shared__ float4 cand[NB_CAP];
   __shared__ int pre[28];
   __shared__ int boff[27];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // interior bin of this CTA
+  const int lane = threadIdx.x;
+  // interior bin of this warp
   const int ix = a.nbx - 2 * a.nhalo, iy = a.nby - 2 * a.nhalo, iz = a.nbz - 2 * a.nhalo;
+  (void)ix;
   const int bx = blockIdx.x / (iy * iz) + a.nhalo;
   const int by = (blockIdx.x / iz) % iy + a.nhalo;
   const int bz = blockIdx.x % iz + a.nhalo;
   const int bc = (bx * a.nby + by) * a.nbz + bz;
-  if (tid < 27) {
-    const int dbx = tid / 9 - 1, dby = (tid / 3) % 3 - 1, dbz = tid % 3 - 1;
+  int cntb = 0, offb = 0;
+  if (lane < 27) {
+    const int dbx = lane / 9 - 1, dby = (lane / 3) % 3 - 1, dbz = lane % 3 - 1;
     const int b = ((bx + dbx) * a.nby + (by + dby)) * a.nbz + (bz + dbz);
-    pre[tid + 1] = a.bincount[b];
-    boff[tid] = a.binoffsets[b];
+    cntb = a.bincount[b];
+    offb = a.binoffsets[b];
   }
-  __syncthreads();
-  if (tid == 0) {
-    pre[0] = 0;
-    for (int s = 0; s < 27; ++s) pre[s + 1] += pre[s];
+  // inclusive scan of the 27 stencil counts over the lanes
+  int inc = cntb;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(FULL_MASK, inc, o);
+    if (lane >= o) inc += v;
   }
-  __syncthreads();
+  if (lane < 27) {
+    pre[lane + 1] = inc;
+    boff[lane] = offb;
+  }
+  if (lane == 0) pre[0] = 0;
+  __syncwarp();
   const int M = pre[27];
   const int nc = a.bincount[bc], oc = a.binoffsets[bc];
-  const unsigned lt = (1u << lane) - 1u;
-  for (int base = 0; base < M; base += NB_CAP) {
-    const int m = min(NB_CAP, M - base);
-    for (int t = tid; t < m; t += NB_THREADS) {
-      const int g = base + t;
-      int s = 0;
-      while (pre[s + 1] <= g) ++s;
-      const int j = a.permute[boff[s] + (g - pre[s])];
-      const float4 p = a.xl[j];
-      const float sx = float(s / 9 - 1) * a.wx, sy = float((s / 3) % 3 - 1) * a.wy, sz = float(s % 3 - 1) * a.wz;
-      const int code = ((s / 9) << 4) | (((s / 3) % 3) << 2) | (s % 3);
-      const int w = a.packed ? ((j << 6) | code) : j;
-      cand[t] = make_float4(p.x + sx, p.y + sy, p.z + sz, __int_as_float(w));
-    }
-    __syncthreads();
-    for (int bi = warp; bi < nc; bi += NB_WARPS) {
-      const int i = a.permute[oc + bi];
-      if (i >= a.n_local) continue;  // ghosts own no row
-      const float4 xi = a.xl[i];
-      double4_32a xd = make_double4_32a(0, 0, 0, 0);
-      long long kx = 0, ky = 0, kz = 0;
-      if (a.half) {
-        xd = a.x4[i];
+  int mx = 0;
+  for (int a0 = 0; a0 < nc; a0 += 32) {
+    // this lane's centre atom
+    const int bi = a0 + lane;
+    const int i = bi < nc ? a.permute[oc + bi] : -1;
+    const bool own = i >= 0 && i < a.n_local;  // ghosts own no row
+    float4 xi = make_float4(0.f, 0.f, 0.f, 0.f);
+    long long kx = 0, ky = 0, kz = 0;
+    // i's own entry: the centre bin's code (1, 1, 1) when packed
+    const int self = PACKED ? int((unsigned(i) << 6) | 0x15u) : i;
+    if (own) {
+      xi = a.xl[i];
+      if (HALF) {
+        const double4_32a xd = a.x4[i];
         kx = okey(xd.x);
         ky = okey(xd.y);
         kz = okey(xd.z);
       }
-      int cnt = base == 0 ? 0 : a.num_neighs[i];
-      for (int k0 = 0; k0 < m; k0 += 32) {
-        const int k = k0 + lane;
-        bool take = false;
-        int w = 0;
-        if (k < m) {
-          const float4 c = cand[k];
-          w = __float_as_int(c.w);
-          const int j = a.packed ? (w >> 6) : w;
-          const float dx = xi.x - c.x, dy = xi.y - c.y, dz = xi.z - c.z;
-          const float rsq = dx * dx + dy * dy + dz * dz;
-          bool in = rsq < a.cut_lo;
-          bool decided = in || rsq > a.cut_hi;
-          if (a.half) {
-            // neighbor_csr.h:287-291: skip unless j is "above" i
-            // lexicographically, or j is a ghost with newton off
-            const double4_32a xj = a.x4[j];
-            const long long jx = okey(xj.x), jy = okey(xj.y), jz = okey(xj.z);
-            const bool above = (jx > kx) || ((jx == kx) && ((jy > ky) || ((jy == ky) && (jz > kz))));
-            const bool skip = ((j == i) || (j < a.n_local || a.newton)) && !above;
-            if (!skip) {
-              if (!decided) in = retest_fp64(a.x4, i, j, a.cutsq);
-              take = in;
+    }
+    int cnt = 0;
+    // next slot of the row: +1 inside a 4-entry granule, then on to the
+    // row's next granule (4 stride - 3 ints further)
+    int* rp = a.rows + quad_index(own ? i : 0, 0, a.stride);
+    const int jump = 4 * a.stride - 3;
+    for (int base = 0; base < M; base += NB_CAP) {
+      const int m = min(NB_CAP, M - base), m4 = (m + 3) & ~3;
+      __syncwarp();
+      for (int t = lane; t < m; t += 32) {
+        const int g = base + t;
+        int s = 0;  // stencil bin of candidate g: binary search of the prefix
+#pragma unroll
+        for (int h = 16; h >= 1; h >>= 1)
+          if (s + h <= 27 && pre[s + h] <= g) s += h;
+        const int j = a.permute[boff[s] + (g - pre[s])];
+        const float4 p = a.xl[j];
+        const float sx = float(s / 9 - 1) * a.wx, sy = float((s / 3) % 3 - 1) * a.wy, sz = float(s % 3 - 1) * a.wz;
+        const int code = ((s / 9) << 4) | (((s / 3) % 3) << 2) | (s % 3);
+        const int w = PACKED ? ((j << 6) | code) : j;
+        cand[t] = make_float4(p.x + sx, p.y + sy, p.z + sz, __int_as_float(w));
+      }
+      __syncwarp();
+      // pad to a multiple of four with copies of the first candidate moved far
+      // outside the cutoff (a valid particle, never accepted)
+      if (lane < m4 - m) cand[m + lane] = make_float4(1.0e4f, 1.0e4f, 1.0e4f, cand[0].w);
+      __syncwarp();
+      if (own) {
+        for (int k = 0; k < m4; k += 4) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const float4 c = cand[k + u];
+            const int w = __float_as_int(c.w);
+            const float dx = xi.x - c.x, dy = xi.y - c.y, dz = xi.z - c.z;
+            const float rsq = dx * dx + dy * dy + dz * dz;
+            bool in = rsq < a.cut_lo;
+            const bool decided = in || rsq > a.cut_hi;
+            bool take;
+            if (HALF) {
+              // neighbor_csr.h:287-291: skip unless j is "above" i
+              // lexicographically, or j is a ghost with newton off
+              const int j = PACKED ? (w >> 6) : w;
+              const double4_32a xj = a.x4[j];
+              const long long jx = okey(xj.x), jy = okey(xj.y), jz = okey(xj.z);
+              const bool above = (jx > kx) || ((jx == kx) && ((jy > ky) || ((jy == ky) && (jz > kz))));
+              const bool skip = ((j == i) || (j < a.n_local || a.newton)) && !above;
+              if (!skip && !decided) in = retest_fp64(a.x4, i, j, a.cutsq);
+              take = !skip && in;
+            } else {
+              if (!decided) in = retest_fp64(a.x4, i, PACKED ? (w >> 6) : w, a.cutsq);
+              take = in && (w != self);
             }
-          } else {
-            if (!decided) in = retest_fp64(a.x4, i, j, a.cutsq);
-            take = in && (i != j);
+            if (take) {
+              if (cnt < a.K) *rp = w;
+              rp += (cnt & 3) == 3 ? jump : 1;
+              ++cnt;
+            }
           }
         }
-        const unsigned bal = __ballot_sync(FULL_MASK, take);
-        if (take) {
-          const int pos = cnt + __popc(bal & lt);
-          if (pos < a.K) a.rows[quad_index(i, pos, a.stride)] = w;
-        }
-        cnt += __popc(bal);
       }
-      if (lane == 0) a.num_neighs[i] = cnt;
     }
-    __syncthreads();
+    if (own) {
+      a.num_neighs[i] = cnt;
+      mx = max(mx, cnt);
+    }
   }
-  // overflow flag and longest row: one atomic per CTA into one of 64 slots
+  // overflow flag and longest row: one atomic per warp into one of 64 slots
   // (a single shared address would serialise millions of atomics in L2)
-  int mx = 0;
-  for (int bi = tid; bi < nc; bi += NB_THREADS) {
-    const int i = a.permute[oc + bi];
-    if (i < a.n_local) mx = max(mx, a.num_neighs[i]);
-  }
   mx = __reduce_max_sync(FULL_MASK, mx);
-  __shared__ int wmax[NB_WARPS];
-  if (lane == 0) wmax[warp] = mx;
-  __syncthreads();
-  if (tid == 0) {
-    for (int w = 1; w < NB_WARPS; ++w) mx = max(mx, wmax[w]);
+  if (lane == 0) {
     if (mx > 0) atomicMax(&a.flags[1 + (blockIdx.x & (NB_SLOTS - 1))], mx);
     if (mx > a.K) a.flags[0] = 1;
   }
@@ -277,7 +295,9 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
       }
       if (ibins > 0) {
         TimedLaunch t(c, "neigh_build");
-        k_neigh_bin<<<ibins, NB_THREADS, 0, c.stream>>>(a);
+        auto k = a.half ? (packed ? k_neigh_bin<true, true> : k_neigh_bin<true, false>)
+                        : (packed ? k_neigh_bin<false, true> : k_neigh_bin<false, false>);
+        k<<<ibins, NB_THREADS, 0, c.stream>>>(a);
         EMD_CHECK_LAUNCH();
       }
     }
