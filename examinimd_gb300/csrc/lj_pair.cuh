@@ -59,57 +59,77 @@ struct PairCtx {
   const double4_32a* x4;
 };
 
-// One pair: returns its force on i, (x, y) packed and z, or zero outside the
-// cutoff.  x_i - x_j = (xl_i - xl_j) + (1 - k) w per dimension.
-template <bool SINGLE>
-__device__ __forceinline__ void lj_pair(const PairCtx& C, int e, const float4& xj, const LJParamsF& P, float2& fxy,
-                                        float& fz) {
-  const float4 sh = C.shift[(e & 63) << 3];
-  float2 dxy = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
-  dxy = __fadd2_rn(dxy, make_float2(sh.x, sh.y));
-  const float dz = __fadd_rn(__fsub_rn(C.xi.z, xj.z), sh.z);
-  const float2 sq = __fmul2_rn(dxy, dxy);
-  const float rsq = __fmaf_rn(dz, dz, __fadd_rn(sq.x, sq.y));
-  float lj1, lj2, cutsq, lo, hi;
+// One pair's geometry and coefficients: x_i - x_j = (xl_i - xl_j) + (1 - k) w
+// per dimension, r^2, and the type pair's lj1, lj2, cutoffs.
+struct PairGeo {
+  float2 dxy;
+  float dz, rsq, lj1, lj2, cutsq;
   double cutsq_d;
+};
+
+template <bool SINGLE>
+__device__ __forceinline__ PairGeo lj_geo(const PairCtx& C, int e, const float4& xj, const LJParamsF& P) {
+  PairGeo g;
+  const float4 sh = C.shift[(e & 63) << 3];
+  g.dxy = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
+  g.dxy = __fadd2_rn(g.dxy, make_float2(sh.x, sh.y));
+  g.dz = __fadd_rn(__fsub_rn(C.xi.z, xj.z), sh.z);
+  const float2 sq = __fmul2_rn(g.dxy, g.dxy);
+  g.rsq = __fmaf_rn(g.dz, g.dz, __fadd_rn(sq.x, sq.y));
   if (SINGLE) {
-    lj1 = P.lj1_0;
-    lj2 = P.lj2_0;
-    cutsq = P.cutsq_0;
-    cutsq_d = P.cutsq_d0;
+    g.lj1 = P.lj1_0;
+    g.lj2 = P.lj2_0;
+    g.cutsq = P.cutsq_0;
+    g.cutsq_d = P.cutsq_d0;
   } else {
     const int tp = C.ti * P.ntypes + __float_as_int(xj.w);
-    lj1 = __ldg(P.lj1 + tp);
-    lj2 = __ldg(P.lj2 + tp);
-    cutsq = __ldg(P.cutsq + tp);
-    cutsq_d = __ldg(P.cutsq_d + tp);
+    g.lj1 = __ldg(P.lj1 + tp);
+    g.lj2 = __ldg(P.lj2 + tp);
+    g.cutsq = __ldg(P.cutsq + tp);
+    g.cutsq_d = __ldg(P.cutsq_d + tp);
   }
-  lo = cutsq * (1.0f - LJ_BAND);
-  hi = cutsq * (1.0f + LJ_BAND);
-  bool in = rsq < cutsq;
-  if (rsq > lo && rsq < hi) in = cut_fp64(C.x4, C.i, e >> 6, cutsq_d);  // borderline: decide as FP64 does
-  const float r2inv = in ? __fdividef(1.0f, rsq) : 0.0f;
+  return g;
+}
+
+__device__ __forceinline__ bool in_band(const PairGeo& g) {
+  return g.rsq > g.cutsq * (1.0f - LJ_BAND) && g.rsq < g.cutsq * (1.0f + LJ_BAND);
+}
+
+// The pair's force on i, (x, y) packed and z; zero unless `in`.
+__device__ __forceinline__ void lj_force(const PairGeo& g, bool in, float2& fxy, float& fz) {
+  const float r2inv = in ? __fdividef(1.0f, g.rsq) : 0.0f;
   const float r6inv = r2inv * r2inv * r2inv;
-  const float fpair = (r6inv * __fmaf_rn(lj1, r6inv, -lj2)) * r2inv;
-  fxy = __fmul2_rn(dxy, make_float2(fpair, fpair));
-  fz = dz * fpair;
+  const float fpair = (r6inv * __fmaf_rn(g.lj1, r6inv, -g.lj2)) * r2inv;
+  fxy = __fmul2_rn(g.dxy, make_float2(fpair, fpair));
+  fz = g.dz * fpair;
 }
 
 // Four entries of one int4 granule, summed in FP32 and then added to the
-// compensated accumulator.
+// compensated accumulator.  The FP32 cutoff test decides a pair unless its
+// r^2 lies in the guard band; one branch per granule re-tests such pairs in
+// FP64, as the reference decides them.
 template <bool SINGLE>
 __device__ __forceinline__ void lj_quad(const PairCtx& C, const int4& e, const float4* __restrict__ xl,
                                         const LJParamsF& P, Acc& acc) {
   const float4 x0 = xl[e.x >> 6], x1 = xl[e.y >> 6], x2 = xl[e.z >> 6], x3 = xl[e.w >> 6];
+  const PairGeo g0 = lj_geo<SINGLE>(C, e.x, x0, P), g1 = lj_geo<SINGLE>(C, e.y, x1, P);
+  const PairGeo g2 = lj_geo<SINGLE>(C, e.z, x2, P), g3 = lj_geo<SINGLE>(C, e.w, x3, P);
+  bool in0 = g0.rsq < g0.cutsq, in1 = g1.rsq < g1.cutsq, in2 = g2.rsq < g2.cutsq, in3 = g3.rsq < g3.cutsq;
+  const bool b0 = in_band(g0), b1 = in_band(g1), b2 = in_band(g2), b3 = in_band(g3);
+  if (b0 || b1 || b2 || b3) {  // borderline: decide as FP64 does
+    if (b0) in0 = cut_fp64(C.x4, C.i, e.x >> 6, g0.cutsq_d);
+    if (b1) in1 = cut_fp64(C.x4, C.i, e.y >> 6, g1.cutsq_d);
+    if (b2) in2 = cut_fp64(C.x4, C.i, e.z >> 6, g2.cutsq_d);
+    if (b3) in3 = cut_fp64(C.x4, C.i, e.w >> 6, g3.cutsq_d);
+  }
   float2 a0, a1, a2, a3;
   float z0, z1, z2, z3;
-  lj_pair<SINGLE>(C, e.x, x0, P, a0, z0);
-  lj_pair<SINGLE>(C, e.y, x1, P, a1, z1);
-  lj_pair<SINGLE>(C, e.z, x2, P, a2, z2);
-  lj_pair<SINGLE>(C, e.w, x3, P, a3, z3);
+  lj_force(g0, in0, a0, z0);
+  lj_force(g1, in1, a1, z1);
+  lj_force(g2, in2, a2, z2);
+  lj_force(g3, in3, a3, z3);
   acc.add(__fadd2_rn(__fadd2_rn(a0, a1), __fadd2_rn(a2, a3)), __fadd_rn(__fadd_rn(z0, z1), __fadd_rn(z2, z3)));
 }
-
 
 }  // namespace
 }  // namespace emd
