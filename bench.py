@@ -350,17 +350,16 @@ def run_gpu_arm(a, ws, rank, local):
     barrier(dist)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        n_now = md.info()["N_local"]
-        assert lib.emd_system_update(ctx.h, 0, n_now, _dp(hx), _dp(hv), _dp(hf)) == 0
-        md.run(1)
-        assert lib.emd_system_get(ctx.h, 0, n_now, _dp(hx), _dp(hv), _dp(hf), None, None, None) == 0
+    # every step: x, v, f uploaded from the pinned host arrays, one ExaMiniMD
+    # step, x, v, f read back into them (x's read-back overlaps the force)
+    md.run_host(e2e_steps, hx, hv, hf)
     ctx.synchronize()
     t_e2e = reduce_max(dist, time.perf_counter() - t0)
     barrier(dist)
     e2e = {"value": ws * N * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": int(nl * 72),
            "d2h_bytes_per_step": int(nl * 72), "steps": e2e_steps,
-           "path": "emd_system_update (x,v,f pinned H2D) + one ExaMiniMD step + emd_system_get (x,v,f D2H)"}
+           "path": "emd_md_run_host: per step x,v,f pinned H2D, one ExaMiniMD step, x,v,f D2H (x's read-back "
+                   "overlapping the force, f's the final integration)"}
     T, pe, ke = md.thermo(recompute=True)
 
     extra = {}

@@ -44,6 +44,8 @@ _SIGS = {
     "emd_system_update": ([_P, _I, _I, _DP, _DP, _DP], _I),
     "emd_system_get": ([_P, _I, _I, _DP, _DP, _DP, _IP, _IP, _DP], _I),
     "emd_system_info": ([_P, _IP, _IP, _IP], _I),
+    "emd_system_download": ([_P, _I, _DP], _I),
+    "emd_system_download_wait": ([_P], _I),
     "emd_zero_forces": ([_P], _I),
     "emd_nve_initial": ([_P], _I),
     "emd_nve_final": ([_P], _I),
@@ -86,6 +88,7 @@ _SIGS = {
     "emd_timing_get": ([_P, C.c_char_p, _DP, _LLP], _I),
     "emd_md_create": ([_I, C.POINTER(C.c_char_p), C.c_char_p, _I], _P),
     "emd_md_run": ([_P, _I], _I),
+    "emd_md_run_host": ([_P, _I, _DP, _DP, _DP], _I),
     "emd_md_destroy": ([_P], None),
     "emd_md_error": ([_P], C.c_char_p),
     "emd_md_ctx": ([_P], _P),
@@ -209,6 +212,13 @@ class Context:
             if a is not None:
                 out[k] = a
         return out
+
+    def update(self, first=0, x=None, v=None, f=None):
+        """emd_system_update: overwrites rows [first, first + len) of the owned
+        particles' x, v, f (None = unchanged)."""
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x, v, f)]
+        n = next((a.shape[0] for a in arrs if a is not None), 0)
+        self._ok(self.lib.emd_system_update(self.h, first, n, *[_dp(a) for a in arrs]), "emd_system_update")
 
     def zero_forces(self):
         self._ok(self.lib.emd_zero_forces(self.h), "emd_zero_forces")
@@ -385,6 +395,16 @@ class MD:
 
     def run(self, nsteps: int = -1):
         self._ok(self.lib.emd_md_run(self.h, nsteps), "emd_md_run")
+
+    def run_host(self, nsteps: int, x, v, f):
+        """run(nsteps) with the owned particles' x, v, f in host arrays
+        (float64, C-contiguous, N_local x 3, updated in place): uploaded before
+        every step and read back after it (emd_md_run_host)."""
+        n = self.info()["N_local"]
+        for a in (x, v, f):
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.shape != (n, 3):
+                raise EmdError(f"run_host: arrays must be float64, C-contiguous, shape ({n}, 3)")
+        self._ok(self.lib.emd_md_run_host(self.h, nsteps, _dp(x), _dp(v), _dp(f)), "emd_md_run_host")
 
     def info(self) -> dict:
         v = [_I() for _ in range(5)]

@@ -316,8 +316,9 @@ void emd_destroy(emd_ctx* ctx) {
   Ctx& c = ctx->c;
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
+  if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
   free_snap(c);
-  for (auto* b : {&c.v, &c.f, &c.q, &c.mass_d, &c.stage_d, &c.lj_params, &c.red, &c.red2}) b->release();
+  for (auto* b : {&c.v, &c.f, &c.q, &c.mass_d, &c.stage_d, &c.stage_dl, &c.lj_params, &c.red, &c.red2}) b->release();
   for (auto* b : {&c.type, &c.id, &c.stage_i, &c.pack, &c.ghost_owner, &c.ghost_img, &c.flags, &c.flags_scan,
                   &c.bincount, &c.binoffsets, &c.permute, &c.binof, &c.bin_cursor, &c.perm_tmp, &c.num_neighs,
                   &c.neigh_offsets, &c.neighs, &c.resize_flag, &c.abin})
@@ -342,6 +343,8 @@ void emd_destroy(emd_ctx* ctx) {
   if (c.h_scalar) cudaFreeHost(c.h_scalar);
   if (c.h_ll) cudaFreeHost(c.h_ll);
   if (c.h_int) cudaFreeHost(c.h_int);
+  if (c.copy_after) cudaEventDestroy(c.copy_after);
+  if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
   if (c.stream) cudaStreamDestroy(c.stream);
   delete ctx;
 }
@@ -474,6 +477,41 @@ emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double*
   if (id) EMD_CUDA(cudaMemcpyAsync(id, c.id.p + first, sizeof(int) * count, cudaMemcpyDeviceToHost, c.stream));
   if (q) EMD_CUDA(cudaMemcpyAsync(q, c.q.p + first, sizeof(double) * count, cudaMemcpyDeviceToHost, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));
+  EMD_API_END
+}
+
+// Read-back of x, v or f of the owned atoms on the copy stream, ordered after
+// everything issued so far on the context's stream: the copy overlaps the
+// work issued after it.
+emd_status emd_system_download(emd_ctx* ctx, int field, double* host) {
+  EMD_API_BEGIN
+  require(field >= 0 && field <= 2, EMD_ERR_ARG, "emd_system_download: field must be 0 (x), 1 (v) or 2 (f)");
+  const int n = c.N_local;
+  require(host != nullptr || n == 0, EMD_ERR_ARG, "emd_system_download: null host array");
+  if (n == 0) return EMD_OK;
+  if (field == 1) materialize_kick(c);
+  if (field == 2) materialize_zero(c, true, false);
+  if (!c.copy_stream) {
+    EMD_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+    EMD_CUDA(cudaEventCreateWithFlags(&c.copy_after, cudaEventDisableTiming));
+  }
+  EMD_CUDA(cudaEventRecord(c.copy_after, c.stream));
+  EMD_CUDA(cudaStreamWaitEvent(c.copy_stream, c.copy_after, 0));
+  const size_t bytes = sizeof(double) * 3 * size_t(n);
+  if (field == 0) {
+    c.stage_dl.reserve(3 * size_t(n), c.stream);
+    k_unpack_x4<<<blocks_for(n, 256), 256, 0, c.copy_stream>>>(c.x4.p, c.stage_dl.p, n);
+    EMD_CHECK_LAUNCH();
+    EMD_CUDA(cudaMemcpyAsync(host, c.stage_dl.p, bytes, cudaMemcpyDeviceToHost, c.copy_stream));
+  } else {
+    EMD_CUDA(cudaMemcpyAsync(host, field == 1 ? c.v.p : c.f.p, bytes, cudaMemcpyDeviceToHost, c.copy_stream));
+  }
+  EMD_API_END
+}
+
+emd_status emd_system_download_wait(emd_ctx* ctx) {
+  EMD_API_BEGIN
+  if (c.copy_stream) EMD_CUDA(cudaStreamSynchronize(c.copy_stream));
   EMD_API_END
 }
 

@@ -111,6 +111,11 @@ struct Ctx {
   DevBuf<double> mass_d;  // per type
   // staging for uploads / sorting gathers
   DevBuf<double> stage_d;
+  // asynchronous read-back (emd_system_download): its own stream, the event
+  // it waits on, and its own x staging
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_after = nullptr;
+  DevBuf<double> stage_dl;
   DevBuf<int> stage_i;
   DevBuf<double4_32a> stage_x4;
 

@@ -51,6 +51,13 @@ emd_status emd_md_run(emd_md* md, int nsteps) {
   MD_END
 }
 
+emd_status emd_md_run_host(emd_md* md, int nsteps, double* x, double* v, double* f) {
+  MD_BEGIN
+  if (!x || !v || !f) throw std::runtime_error("emd_md_run_host: x, v and f must all be given");
+  md->app->run_host(nsteps < 0 ? md->app->input->nsteps : nsteps, x, v, f);
+  MD_END
+}
+
 void emd_md_destroy(emd_md* md) {
   if (!md) return;
   delete md->app;

@@ -260,6 +260,9 @@ class ExaMiniMD {
   ~ExaMiniMD();
   void init(int argc, const char* const* argv);
   void run(int nsteps);
+  // run(nsteps) with x, v, f of the owned particles held in host arrays:
+  // uploaded before every step, read back after it (emd_md_run_host)
+  void run_host(int nsteps, double* hx, double* hv, double* hf);
   void thermo(int step, bool print, double elapsed, double rate);
   void dump_binary(int step);
   void check_correctness(int step);

@@ -169,17 +169,29 @@ void ExaMiniMD::thermo(int step, bool print, double elapsed, double rate) {
   }
 }
 
-void ExaMiniMD::run(int nsteps) {
+void ExaMiniMD::run(int nsteps) { run_host(nsteps, nullptr, nullptr, nullptr); }
+
+// The step loop of ExaMiniMD::run (examinimd.cpp:192-276).  With host arrays
+// (hx non-null) every step first uploads x, v, f of the owned particles and
+// reads them back as soon as each is final: x after the initial integration
+// (after the rebuild's re-sort on rebuild steps), overlapping the force; f
+// after the force, overlapping the final integration; v last.
+void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
+  emd_ctx* ctx = system->ctx;
+  const bool host = hx != nullptr;
   const double neigh_cutoff = input->force_cutoff + input->neighbor_skin;
   PhaseClock clk(emd_stream(system->ctx));
   const double t0 = wall();
   double last_time = 0.0;
   for (int step = step_done + 1; step <= step_done + nsteps; step++) {
+    const bool rebuild = step % input->comm_exchange_rate == 0 && step > 0;
+    if (host) check(emd_system_update(ctx, 0, system->N_local, hx, hv, hf), ctx, "emd_system_update");
     cudaEvent_t e = clk.begin();
     integrator->initial_integrate();
     clk.end(B_OTHER, e);
+    if (host && !rebuild) check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
 
-    if (step % input->comm_exchange_rate == 0 && step > 0) {
+    if (rebuild) {
       e = clk.begin();
       comm->exchange();
       clk.end(B_COMM, e);
@@ -193,6 +205,7 @@ void ExaMiniMD::run(int nsteps) {
       binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, true, false);
       neighbor->create_neigh_list(system, binning, force->half_neigh, false);
       clk.end(B_NEIGH, e);
+      if (host) check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
     } else {
       e = clk.begin();
       comm->update_halo();
@@ -210,9 +223,14 @@ void ExaMiniMD::run(int nsteps) {
       clk.end(B_COMM, e);
     }
 
+    if (host) check(emd_system_download(ctx, 2, hf), ctx, "emd_system_download");
     e = clk.begin();
     integrator->final_integrate();
     clk.end(B_OTHER, e);
+    if (host) {
+      check(emd_system_download(ctx, 1, hv), ctx, "emd_system_download");
+      check(emd_system_download_wait(ctx), ctx, "emd_system_download_wait");
+    }
 
     if (input->thermo_rate > 0 && step % input->thermo_rate == 0) {
       check(emd_synchronize(system->ctx), system->ctx, "emd_synchronize");

@@ -20,6 +20,11 @@ typedef struct emd_md emd_md;
 emd_md* emd_md_create(int argc, const char* const* argv, char* err, int err_len);
 /* ExaMiniMD::run (examinimd.cpp:176-294); nsteps < 0 runs the deck's `run` count. */
 emd_status emd_md_run(emd_md* md, int nsteps);
+/* run(nsteps) with the owned particles' x, v, f kept in host arrays (N_local
+ * x 3 doubles each, in the context's current order): every step uploads them
+ * before it starts and reads them back when it ends.  The read-back of x
+ * overlaps the force computation and that of f the final integration. */
+emd_status emd_md_run_host(emd_md* md, int nsteps, double* x, double* v, double* f);
 void emd_md_destroy(emd_md* md);
 const char* emd_md_error(const emd_md* md);
 emd_ctx* emd_md_ctx(emd_md* md);

@@ -80,6 +80,15 @@ emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x
 emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double* v, double* f,
                           int* type, int* id, double* q);
 emd_status emd_system_info(emd_ctx* ctx, int* n_local, int* n_ghost, int* n_max);
+/* Asynchronous read-back of one field of the owned particles, N_local x 3
+ * doubles (field 0 = x, 1 = v, 2 = f): ordered after every call already made
+ * on the context and copied on a second stream, so it overlaps the calls
+ * made after it.  Until emd_system_download_wait returns, the host array
+ * must not be read and the field must not be overwritten (emd_system_update,
+ * set_local, an integration step).  No reference counterpart: it serves
+ * callers that keep the particle state in host memory (emd_md_run_host). */
+emd_status emd_system_download(emd_ctx* ctx, int field, double* host);
+emd_status emd_system_download_wait(emd_ctx* ctx);
 /* Kokkos::deep_copy(system->f, 0.0) over all N_max rows (examinimd.cpp:232). */
 emd_status emd_zero_forces(emd_ctx* ctx);
 
