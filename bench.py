@@ -130,6 +130,55 @@ def load_peaks() -> dict:
     return dict(hbm_gbs=6800.0, src="fallback")
 
 
+def fp_pipe_peaks(device: int) -> dict:
+    """FP64 and FP32 (non-tensor) arithmetic peaks of this GPU, measured as
+    cuBLAS DGEMM and SGEMM (TF32 off) throughput, best of three, in GFLOP/s:
+    the denominators of the SNAP roofline (MEASURED_PEAKS.json holds HBM and
+    bf16 tensor figures only)."""
+    import torch
+    out = {}
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        for name, dt, n in (("fp64", torch.float64, 4096), ("fp32", torch.float32, 8192)):
+            a = torch.randn(n, n, dtype=dt, device=device)
+            b = torch.randn(n, n, dtype=dt, device=device)
+            torch.matmul(a, b)
+            torch.cuda.synchronize()
+            best = 1e30
+            for _ in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                torch.matmul(a, b)
+                e1.record()
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            out[name] = 2.0 * n ** 3 / (best * 1e-3) / 1e9
+            del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    out["how"] = "torch.matmul DGEMM 4096^3 and SGEMM 8192^3 (TF32 off), best of 3, CUDA events"
+    return out
+
+
+def snap_inside_mean(ctx, n_local: int, rcutsq: float) -> float:
+    """Mean number of neighbours inside the SNAP cutoff, from the device's
+    positions and full list."""
+    import numpy as np
+    nl_, ng_ = ctx.info()[:2]
+    st = ctx.get(0, nl_ + ng_, fields=("x",))
+    x = st["x"]
+    num = np.empty(max(n_local, 1), np.int32)
+    from examinimd_gb300._lib import _ip
+    assert ctx.lib.emd_neigh_get(ctx.h, _ip(num), None) == 0
+    total = int(num[:n_local].sum())
+    ent = np.empty(max(total, 1), np.int32)
+    assert ctx.lib.emd_neigh_get(ctx.h, None, _ip(ent)) == 0
+    i = np.repeat(np.arange(n_local), num[:n_local])
+    d = x[ent[:total]] - x[i]
+    return float(np.count_nonzero(np.einsum("ij,ij->i", d, d) < rcutsq)) / n_local
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -335,6 +384,17 @@ def run_gpu_arm(a, ws, rank, local):
                 "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "traffic": traffic,
                 "peak_source": peaks["src"], "bytes_per_launch": bytes_launch, "mean_row": mean_row,
                 "launch_ms": (kms / kn) if kn else None}
+        if a.precision == "fp64" and kn:
+            # the FP64 drop-in is bound by the FP64 pipe: 8 operations per listed
+            # pair (difference, r^2, test) and 13 more inside the cutoff (1/r^2,
+            # r^-6, the force, the sums); the inside fraction is the volume
+            # ratio (rc / (rc + skin))^3 of the two cutoffs
+            pk = fp_pipe_peaks(local)
+            inside = (2.5 / 2.8) ** 3
+            flops = nl * mean_row * (8.0 + 13.0 * inside)
+            got = flops / (kms / kn * 1e-3) / 1e9
+            roof["fp64_pipe"] = {"achieved": got, "peak": pk["fp64"], "unit": "GFLOP/s", "frac": got / pk["fp64"],
+                                 "flops_per_launch": flops, "peak_how": pk["how"]}
     kernels = {k: {"ms": v[0], "launches": v[1], "share": v[0] / max(1e-12, sum(x[0] for x in rep.values()))}
                for k, v in sorted(rep.items(), key=lambda kv: -kv[1][0])}
 
@@ -504,6 +564,7 @@ def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells
     from examinimd_gb300 import MD
     tmp = tempfile.mkdtemp(prefix="emdsnap_")
     coeff, param = snap_files(tmp)
+    peaks = fp_pipe_peaks(local)
     res, acc = {}, None
     for prec, steps in (("mixed", steps_mixed), ("fp64", steps_fp64)):
         deck = os.path.join(tmp, f"in.snap.{prec}")
@@ -535,6 +596,24 @@ def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells
                      "gpu_launches": sum(c for _, c in rep.values())}
         if prec == "mixed":
             acc = snap_accuracy(md, local, cells, coeff, param, warm + steps)
+        # roofline: operations of the kernel's own formulation (snap_flops)
+        # against the measured FP64 and FP32 pipe peaks
+        if kn:
+            from examinimd_gb300.snap_flops import snap_flops
+            rc = 2.0 * 0.5 * 4.73442  # 2 radius rcutfac of the synthetic W coefficients
+            nin = snap_inside_mean(ctx, md.info()["N_local"], rc * rc)
+            fl = snap_flops(8, nin)
+            t = kms / kn * 1e-3
+            n_loc = md.info()["N_local"]
+            f64, f32 = fl["fp64"][prec] * n_loc, fl["fp32"][prec] * n_loc
+            t_roof = max(f64 / (peaks["fp64"] * 1e9), f32 / (peaks["fp32"] * 1e9))
+            res[prec]["roofline"] = {
+                "bound": "fp64" if prec == "fp64" else "fp64+fp32 (max of the two pipe times)",
+                "flops_per_atom": fl["total"], "fp64_flops_per_atom": fl["fp64"][prec],
+                "fp32_flops_per_atom": fl["fp32"][prec], "ninside_mean": nin,
+                "achieved_gflops": fl["total"] * n_loc / t / 1e9, "peak_fp64_gflops": peaks["fp64"],
+                "peak_fp32_gflops": peaks["fp32"], "frac": t_roof / t,
+                "how": "examinimd_gb300/snap_flops.py counts the kernel's loops; peaks " + peaks["how"]}
         md.close()
     res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
     res["accuracy"] = acc
