@@ -142,7 +142,9 @@ emd_status emd_neigh_maxneighs(emd_ctx* ctx, int* maxneighs);
  * ForceLJNeigh (force_lj_neigh_impl.h:57-343).  Per-type tables are
  * ntypes*ntypes row-major: lj1 = 48 eps sigma^12, lj2 = 24 eps sigma^6,
  * cutsq = cut^2.  precision: EMD_PREC_FP64 (bit-compatible drop-in) or
- * EMD_PREC_MIXED (FP32 pair math, FP64 displacements and accumulation). */
+ * EMD_PREC_MIXED (FP32 pair math on FP32 bin-relative positions, compensated
+ * FP32 sums stored as FP64 forces; full lists only, EMD_ERR_ARG with
+ * half_neigh). */
 emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double* lj2,
                        const double* cutsq, int half_neigh, int precision);
 /* compute(): f += pair forces over the current neighbour list. */
