@@ -118,21 +118,45 @@ size_t snap_adjoint_bytes(const SnapDev& S) {
   return 2 * sizeof(double) * (size_t(S.njobs) + size_t(SNAP_WARPS + 1) * S.nyh);
 }
 
-size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes) {
+// the kernel's shared-memory carve-up (k_snap), for `cap` inside neighbours
+size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes, bool adjoint) {
   const int L1 = S.L + 1;
+  const bool f64 = real_bytes == int(sizeof(double));
+  const size_t nd = f64 ? size_t(ND_FIELDS) : size_t(ND_MIXED), nr = f64 ? 0 : size_t(NR_MIXED);
   size_t b = 0;
-  b += sizeof(double) * size_t(L1 * L1);                 // rootpq (FP64)
-  b += sizeof(double) * 5 * size_t(cap);                 // r, w, rcut
-  b += 2 * sizeof(double) * size_t(S.nuf);               // utot
-  b += size_t(real_bytes) * size_t((L1 * L1 + 1) & ~1);  // rootpq (R)
-  b += 2 * size_t(real_bytes) * size_t(S.nyh);           // ytot
-  if (real_bytes != int(sizeof(double))) b += 2 * size_t(real_bytes) * size_t(S.nuf);  // FP32 U_tot
-  b += sizeof(int) * size_t((cap + 3) & ~3);             // inside j
-  b += sizeof(double) * 4 * SNAP_WARPS;                  // reductions
-  b += sizeof(double) * ND_FIELDS * size_t(cap);         // per-neighbour scalars
-  if (real_bytes != int(sizeof(double))) b += sizeof(double) * ((ND_FIELDS * size_t(cap) + 1) / 2);  // FP32 copy
+  b += sizeof(double) * 5 * size_t(cap);                                // r, w, rcut
+  b += 2 * sizeof(double) * size_t(S.nuf);                              // utot
+  if (adjoint) b += size_t(real_bytes) * size_t((L1 * L1 + 1) & ~1);    // rootpq
+  b += 2 * size_t(real_bytes) * size_t(S.nyh);                          // ytot
+  if (!f64) b += 2 * size_t(real_bytes) * size_t(S.nuf);               // FP32 U_tot
+  b += sizeof(int) * size_t((cap + 3) & ~3);                            // inside j
+  b += sizeof(double) * 4 * SNAP_WARPS;                                 // reductions
+  b += sizeof(double) * nd * size_t(cap);                               // FP64 per-neighbour fields
+  b += sizeof(double) * ((nr * size_t(cap) + 1) / 2);                   // FP32 per-neighbour fields
   b += snap_work_bytes(S, real_bytes);
   return b + 64;
+}
+
+// the largest number of inside neighbours (r^2 < rcutmax^2) over the owned
+// atoms: the kernel's per-neighbour shared arrays are sized by it
+__global__ void __launch_bounds__(256) k_snap_inside_max(const double4_32a* __restrict__ x4, ListView L, int n,
+                                                         double cutsq, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int cnt = 0;
+  if (i < n) {
+    const double4_32a xi = x4[i];
+    const Row<false> rowc(L, i);
+    const Row<true> row2(L, i);
+    const bool two_d = L.stride != 0;
+    for (int k = 0; k < rowc.n; ++k) {
+      const int j = two_d ? row2[k] : rowc[k];
+      const double4_32a xj = x4[j];
+      const double dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+      cnt += (dx * dx + dy * dy + dz * dz) < cutsq;
+    }
+  }
+  cnt = __reduce_max_sync(FULL_MASK, cnt);
+  if ((threadIdx.x & 31) == 0 && cnt > 0) atomicMax(out, cnt);
 }
 
 // per-element column sums of the adjoint's per-atom outputs (fixed order)
@@ -174,6 +198,21 @@ static void upload(Ctx& c, DevBuf<T>& b, const std::vector<T>& v) {
   EMD_CUDA(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, c.stream));
 }
 
+// cap for the kernel's per-neighbour arrays: the largest inside count
+static int snap_cap(Ctx& c, const SnapDev& S) {
+  const int n = c.N_local;
+  c.resize_flag.reserve(1 + 64, c.stream);
+  EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, sizeof(int), c.stream));
+  {
+    TimedLaunch t(c, "snap_inside_max");
+    k_snap_inside_max<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p, list_view(c), n, S.cutsq, c.resize_flag.p);
+    EMD_CHECK_LAUNCH();
+  }
+  EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  return std::max(1, c.h_int[0]);
+}
+
 static void snap_launch(Ctx& c, bool energy) {
   SnapHost* h = static_cast<SnapHost*>(c.snap);
   require(h != nullptr, EMD_ERR_STATE, "SNAP not initialised");
@@ -193,11 +232,11 @@ static void snap_launch(Ctx& c, bool energy) {
   A.f = c.f.p;
   A.L = list_view(c);
   A.n_local = n;
-  A.cap = std::max(1, c.neigh_maxrow);
+  A.cap = snap_cap(c, h->d);
   A.status = c.d_status;
   A.eatom = nullptr;
   const bool fp64 = h->precision == EMD_PREC_FP64 || energy;
-  const size_t smem = snap_smem_bytes(h->d, A.cap, fp64 ? 8 : 4);
+  const size_t smem = snap_smem_bytes(h->d, A.cap, fp64 ? 8 : 4, false);
   require(smem <= 227 * 1024, EMD_ERR_ARG, "SNAP: neighbour rows too long for one atom's shared memory");
   A.g = nullptr;
   A.ghost_owner = nullptr;
@@ -248,7 +287,7 @@ static void snap_adjoint(Ctx& c, const double* dL_dF, double dL_dE, double* grad
     A.f = nullptr;
     A.L = list_view(c);
     A.n_local = n;
-    A.cap = std::max(1, c.neigh_maxrow);
+    A.cap = snap_cap(c, S);
     A.status = c.d_status;
     A.eatom = nullptr;
     A.g = h->adj_g.p;
@@ -256,7 +295,7 @@ static void snap_adjoint(Ctx& c, const double* dL_dF, double dL_dE, double* grad
     A.newton = c.comm_newton;
     A.adj = h->adj.p;
     A.work_bytes = snap_work_bytes(S, 8);
-    const size_t smem = snap_smem_bytes(S, A.cap, 8) + snap_adjoint_bytes(S);
+    const size_t smem = snap_smem_bytes(S, A.cap, 8, true) + snap_adjoint_bytes(S);
     require(smem <= 227 * 1024, EMD_ERR_ARG, "SNAP adjoint: neighbour rows too long for shared memory");
     auto k = k_snap<double, 2>;
     EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));

@@ -51,6 +51,20 @@ enum {
   ND_DAR, ND_DAI = ND_DAR + 3, ND_DBR = ND_DAI + 3, ND_DBI = ND_DBR + 3, ND_UK = ND_DBI + 3,
   ND_SFAC = ND_UK + 3, ND_DSFAC, ND_FP, ND_EP = ND_FP + 3, ND_FIELDS
 };
+// Slots of those fields.  The FP64 form keeps every field in nd (FP64).  The
+// mixed form keeps in nd only what phase B and the FP64 force tail read (a, b
+// of compute_uarray, sfac, the repulsion force) and the phase D inputs in ndr
+// (FP32, fields ND_AR .. ND_DSFAC).
+constexpr int ND_MIXED = 8;
+constexpr int NR_MIXED = ND_DSFAC + 1 - ND_AR;
+template <bool F64>
+__host__ __device__ constexpr int ndx(int f) {
+  return F64 ? f : (f < ND_AR ? f : (f == ND_SFAC ? 4 : 5 + (f - ND_FP)));
+}
+template <bool F64>
+__host__ __device__ constexpr int nrx(int f) {
+  return F64 ? f : f - ND_AR;
+}
 
 struct SnapDev {
   int twojmax, L;         // L = twojmax + 1
@@ -247,7 +261,7 @@ __device__ __forceinline__ void b_stage(const SnapDev& S, const double* nd, int 
     const int nb0 = rd * per_round;
     const int nin = max(0, min(ninside - nb0, per_round));
     const int gw = nin > warp ? (nin - warp + SNAP_WARPS - 1) / SNAP_WARPS : 0;  // this warp's slots
-    if (lane < gw) mine[lane * sw] = Cplx<double>{nd[ND_SFAC * cap + nb0 + lane * SNAP_WARPS + warp], 0.0};
+    if (lane < gw) mine[lane * sw] = Cplx<double>{nd[ndx<!kCopy>(ND_SFAC) * cap + nb0 + lane * SNAP_WARPS + warp], 0.0};
     __syncthreads();
     for (int j = 1; j <= S.twojmax + 1; ++j) {
       if (j <= S.twojmax) {
@@ -257,8 +271,8 @@ __device__ __forceinline__ void b_stage(const SnapDev& S, const double* nd, int 
           const int g = it / nh, e = it - g * nh;
           const int mb = e / (j + 1), ma = e - mb * (j + 1);
           const int nb = nb0 + g * SNAP_WARPS + warp;
-          const double ar = nd[ND_AR_U * cap + nb], ai = nd[ND_AI_U * cap + nb];
-          const double br = nd[ND_BR_U * cap + nb], bi = nd[ND_BI_U * cap + nb];
+          const double ar = nd[ndx<!kCopy>(ND_AR_U) * cap + nb], ai = nd[ndx<!kCopy>(ND_AI_U) * cap + nb];
+          const double br = nd[ndx<!kCopy>(ND_BR_U) * cap + nb], bi = nd[ndx<!kCopy>(ND_BI_U) * cap + nb];
           const Cplx<double>* P = mine + g * sw + po;
           Cplx<double> u1{0.0, 0.0}, u2{0.0, 0.0};
           if (ma > 0) u1 = ld_half(P, j - 1, ma - 1, mb);
@@ -490,42 +504,41 @@ struct SnapArgs {
 };
 
 // MODE 0: forces; 1: per-atom energy; 2: adjoint columns (FP64 only).
-// Minimum resident CTAs: three for the mixed form (<= 80 registers; its
-// shared memory fits three per SM), two for the FP64 forms.
+// Minimum resident CTAs: four for the mixed form (<= 64 registers; its
+// shared memory, sized by the largest inside count, fits four per SM up to
+// about 28 inside neighbours), two for the FP64 forms.
 template <typename R, int MODE>
-__global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 : 2) k_snap(SnapArgs A) {
+__global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 : 2) k_snap(SnapArgs A) {
   const SnapDev& S = A.S;
   const int i = blockIdx.x;
   if (i >= A.n_local) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = S.L, L2 = L * L, L1 = L + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // ---- shared memory carve-up
-  double* rootpq_d = reinterpret_cast<double*>(smem_raw);  // L1*L1
-  double* in_r = rootpq_d + L1 * L1;                       // 3*cap
+  // ---- shared memory carve-up (mirrored by snap_smem_bytes)
+  constexpr bool kF64 = sizeof(R) == sizeof(double);
+  constexpr int kNd = kF64 ? int(ND_FIELDS) : ND_MIXED, kNr = kF64 ? 0 : NR_MIXED;
+  const int nrp = MODE == 2 ? ((L1 * L1 + 1) & ~1) : 0;  // rootpq, for the fitting adjoint's dU/dr
+  double* in_r = reinterpret_cast<double*>(smem_raw);      // 3*cap
   double* in_w = in_r + 3 * A.cap;                         // cap
   double* in_rc = in_w + A.cap;                            // cap
   Cplx<double>* utot = reinterpret_cast<Cplx<double>*>(in_rc + A.cap);  // nuf
-  R* rootpq_r = reinterpret_cast<R*>(utot + S.nuf);                     // L1*L1
-  Cplx<R>* ytot = reinterpret_cast<Cplx<R>*>(rootpq_r + ((L1 * L1 + 1) & ~1));  // nyh
+  R* rootpq_r = reinterpret_cast<R*>(utot + S.nuf);                     // nrp
+  Cplx<R>* ytot = reinterpret_cast<Cplx<R>*>(rootpq_r + nrp);          // nyh
   // U_tot in the contraction type: the FP64 array itself, or an FP32 copy
   // made once per atom (converting inside the Z loops would put an FP64-pipe
   // conversion on every Clebsch-Gordan term)
-  constexpr bool kF64 = sizeof(R) == sizeof(double);
   Cplx<R>* utot_r = kF64 ? reinterpret_cast<Cplx<R>*>(utot) : ytot + S.nyh;      // nuf
   int* in_j = reinterpret_cast<int*>(kF64 ? ytot + S.nyh : utot_r + S.nuf);     // cap
   double* red = reinterpret_cast<double*>(in_j + ((A.cap + 3) & ~3));          // 4*SNAP_WARPS
-  double* nd = red + 4 * SNAP_WARPS;                                           // ND_FIELDS*cap
-  // the per-neighbour scalars in the contraction type (FP32 copy made once)
-  R* ndr = kF64 ? reinterpret_cast<R*>(nd) : reinterpret_cast<R*>(nd + ND_FIELDS * A.cap);
-  unsigned char* work = reinterpret_cast<unsigned char*>(kF64 ? nd + ND_FIELDS * A.cap
-                                                              : nd + ND_FIELDS * A.cap + (ND_FIELDS * A.cap + 1) / 2);
+  double* nd = red + 4 * SNAP_WARPS;                                           // kNd*cap
+  // the phase D inputs in the contraction type (mixed form: FP32 fields)
+  R* ndr = kF64 ? reinterpret_cast<R*>(nd) : reinterpret_cast<R*>(nd + kNd * A.cap);
+  unsigned char* work = reinterpret_cast<unsigned char*>(nd + kNd * A.cap + (kNr * A.cap + 1) / 2);
   __shared__ int s_ninside;
 
-  for (int k = tid; k < L1 * L1; k += SNAP_THREADS) {
-    rootpq_d[k] = S.rootpq[k];
-    rootpq_r[k] = R(S.rootpq[k]);
-  }
+  if constexpr (MODE == 2)
+    for (int k = tid; k < L1 * L1; k += SNAP_THREADS) rootpq_r[k] = R(S.rootpq[k]);
   // ---- A: inside list (force_snap_neigh_impl.h:612-656)
   const double4_32a xi = A.x4[i];
   const int ti = A.type[i];
@@ -643,22 +656,22 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       const double r0inv = sn * rinv;
       const double uk[3] = {x * rinv, y * rinv, z * rinv};
       const double g = (cs * rscale0 * r - sn) * (rinv * rinv);
-      q[ND_AR_U * A.cap] = cs;
-      q[ND_AI_U * A.cap] = -z * r0inv;
-      q[ND_BR_U * A.cap] = y * r0inv;
-      q[ND_BI_U * A.cap] = -x * r0inv;
-      qf[ND_AR * A.cap] = R(cs);
-      qf[ND_AI * A.cap] = R(-z * r0inv);
-      qf[ND_BR * A.cap] = R(y * r0inv);
-      qf[ND_BI * A.cap] = R(-x * r0inv);
+      q[ndx<false>(ND_AR_U) * A.cap] = cs;
+      q[ndx<false>(ND_AI_U) * A.cap] = -z * r0inv;
+      q[ndx<false>(ND_BR_U) * A.cap] = y * r0inv;
+      q[ndx<false>(ND_BI_U) * A.cap] = -x * r0inv;
+      qf[nrx<false>(ND_AR) * A.cap] = R(cs);
+      qf[nrx<false>(ND_AI) * A.cap] = R(-z * r0inv);
+      qf[nrx<false>(ND_BR) * A.cap] = R(y * r0inv);
+      qf[nrx<false>(ND_BI) * A.cap] = R(-x * r0inv);
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const double dr0inv = g * uk[k];
-        qf[(ND_DAR + k) * A.cap] = R(-sn * rscale0 * uk[k]);
-        qf[(ND_DAI + k) * A.cap] = R(-z * dr0inv + (k == 2 ? -r0inv : 0.0));
-        qf[(ND_DBR + k) * A.cap] = R(y * dr0inv + (k == 1 ? r0inv : 0.0));
-        qf[(ND_DBI + k) * A.cap] = R(-x * dr0inv + (k == 0 ? -r0inv : 0.0));
-        qf[(ND_UK + k) * A.cap] = R(uk[k]);
+        qf[nrx<false>(ND_DAR + k) * A.cap] = R(-sn * rscale0 * uk[k]);
+        qf[nrx<false>(ND_DAI + k) * A.cap] = R(-z * dr0inv + (k == 2 ? -r0inv : 0.0));
+        qf[nrx<false>(ND_DBR + k) * A.cap] = R(y * dr0inv + (k == 1 ? r0inv : 0.0));
+        qf[nrx<false>(ND_DBI + k) * A.cap] = R(-x * dr0inv + (k == 0 ? -r0inv : 0.0));
+        qf[nrx<false>(ND_UK + k) * A.cap] = R(uk[k]);
       }
       // switching function and its derivative from one sincos (compute_sfac,
       // compute_dsfac, sna_impl.hpp:1099-1128)
@@ -674,16 +687,16 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
           dsf = -0.5 * ss * rcutfac;
         }
       }
-      q[ND_SFAC * A.cap] = sf * wj;
-      qf[ND_SFAC * A.cap] = R(sf * wj);
-      qf[ND_DSFAC * A.cap] = R(dsf * wj);
+      q[ndx<false>(ND_SFAC) * A.cap] = sf * wj;
+      qf[nrx<false>(ND_SFAC) * A.cap] = R(sf * wj);
+      qf[nrx<false>(ND_DSFAC) * A.cap] = R(dsf * wj);
       // the r^-12 repulsion's force stays FP64: its pair terms are of the size
       // of the net force and cancel in the sum over neighbours
       const double r2 = rsq * rsq, r4 = r2 * r2;
       const double fdivr = -1.5e6 / (r4 * r2 * rsq);
-      q[ND_FP * A.cap] = x * fdivr;
-      q[(ND_FP + 1) * A.cap] = y * fdivr;
-      q[(ND_FP + 2) * A.cap] = z * fdivr;
+      q[ndx<false>(ND_FP) * A.cap] = x * fdivr;
+      q[ndx<false>(ND_FP + 1) * A.cap] = y * fdivr;
+      q[ndx<false>(ND_FP + 2) * A.cap] = z * fdivr;
     }
   }
   __syncthreads();
@@ -876,7 +889,7 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       DRevAB<R> ab[2];
       for (int n = 0; n < 2; ++n) {
         const R* qr = ndr + (n < nn ? (n ? nb1 : nb0) : nb0);
-        ab[n] = DRevAB<R>{qr[ND_AR * A.cap], qr[ND_AI * A.cap], qr[ND_BR * A.cap], qr[ND_BI * A.cap]};
+        ab[n] = DRevAB<R>{qr[nrx<kF64>(ND_AR) * A.cap], qr[nrx<kF64>(ND_AI) * A.cap], qr[nrx<kF64>(ND_BR) * A.cap], qr[nrx<kF64>(ND_BI) * A.cap]};
       }
       R phi[2];
       Cplx<R> ga[2], gb[2];
@@ -887,13 +900,13 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
       for (int n = 0; n < nn; ++n) {
         const int nb = n ? nb1 : nb0;
         const R* qr = ndr + nb;
-        const R sf = qr[ND_SFAC * A.cap], cp = qr[ND_DSFAC * A.cap] * phi[n];
+        const R sf = qr[nrx<kF64>(ND_SFAC) * A.cap], cp = qr[nrx<kF64>(ND_DSFAC) * A.cap] * phi[n];
         R fk[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
-          fk[k] = cp * qr[(ND_UK + k) * A.cap] +
-                  sf * (ga[n].r * qr[(ND_DAR + k) * A.cap] - ga[n].i * qr[(ND_DAI + k) * A.cap] -
-                        gb[n].r * qr[(ND_DBR + k) * A.cap] + gb[n].i * qr[(ND_DBI + k) * A.cap]);
+          fk[k] = cp * qr[nrx<kF64>(ND_UK + k) * A.cap] +
+                  sf * (ga[n].r * qr[nrx<kF64>(ND_DAR + k) * A.cap] - ga[n].i * qr[nrx<kF64>(ND_DAI + k) * A.cap] -
+                        gb[n].r * qr[nrx<kF64>(ND_DBR + k) * A.cap] + gb[n].i * qr[nrx<kF64>(ND_DBI + k) * A.cap]);
         // summed over the lanes in the contraction type (an FP64 shuffle tree
         // would cost the mixed form more FP64-pipe time than its FP32 sweeps)
         const R sx = warp_sum_r(fk[0]), sy = warp_sum_r(fk[1]), sz = warp_sum_r(fk[2]);
@@ -907,9 +920,9 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 3 :
     }
     __syncthreads();
     for (int nb = tid; nb < ninside; nb += SNAP_THREADS) {
-      const double Fx = fpair[3 * nb] + nd[ND_FP * A.cap + nb];
-      const double Fy = fpair[3 * nb + 1] + nd[(ND_FP + 1) * A.cap + nb];
-      const double Fz = fpair[3 * nb + 2] + nd[(ND_FP + 2) * A.cap + nb];
+      const double Fx = fpair[3 * nb] + nd[ndx<kF64>(ND_FP) * A.cap + nb];
+      const double Fy = fpair[3 * nb + 1] + nd[ndx<kF64>(ND_FP + 1) * A.cap + nb];
+      const double Fz = fpair[3 * nb + 2] + nd[ndx<kF64>(ND_FP + 2) * A.cap + nb];
       const int j = in_j[nb];
       atomicAdd(A.f + 3 * j, -Fx);
       atomicAdd(A.f + 3 * j + 1, -Fy);
