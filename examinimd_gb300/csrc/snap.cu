@@ -20,6 +20,7 @@ struct SnapHost {
   int precision = EMD_PREC_FP64;
   DevBuf<int> trip, cg_off, jobs, tjob_off, yred_off, yred_job, map;
   DevBuf<int4> zord;
+  DevBuf<int> inside_max;  // k_snap_inside_max's result
   DevBuf<double> cg, cY, rootpq, beta0, radelem, wjelem, eatom, invf, yscale;
   DevBuf<float> cg_f, cY_f, yscale_f;
   // adjoint: per-atom columns, their per-element sums, the loss gradient dL/dF
@@ -180,6 +181,7 @@ void free_snap(Ctx& c) {
   SnapHost* h = static_cast<SnapHost*>(c.snap);
   for (auto* b : {&h->trip, &h->cg_off, &h->jobs, &h->tjob_off, &h->yred_off, &h->yred_job, &h->map}) b->release();
   h->zord.release();
+  h->inside_max.release();
   for (auto* b : {&h->cg, &h->cY, &h->rootpq, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
                   &h->adj_g, &h->invf, &h->yscale})
     b->release();
@@ -199,16 +201,17 @@ static void upload(Ctx& c, DevBuf<T>& b, const std::vector<T>& v) {
 }
 
 // cap for the kernel's per-neighbour arrays: the largest inside count
-static int snap_cap(Ctx& c, const SnapDev& S) {
+static int snap_cap(Ctx& c, SnapHost* h) {
   const int n = c.N_local;
-  c.resize_flag.reserve(1 + 64, c.stream);
-  EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, sizeof(int), c.stream));
+  h->inside_max.reserve(1, c.stream);
+  EMD_CUDA(cudaMemsetAsync(h->inside_max.p, 0, sizeof(int), c.stream));
   {
     TimedLaunch t(c, "snap_inside_max");
-    k_snap_inside_max<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p, list_view(c), n, S.cutsq, c.resize_flag.p);
+    k_snap_inside_max<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p, list_view(c), n, h->d.cutsq,
+                                                                 h->inside_max.p);
     EMD_CHECK_LAUNCH();
   }
-  EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  EMD_CUDA(cudaMemcpyAsync(c.h_int, h->inside_max.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   return std::max(1, c.h_int[0]);
 }
@@ -232,7 +235,7 @@ static void snap_launch(Ctx& c, bool energy) {
   A.f = c.f.p;
   A.L = list_view(c);
   A.n_local = n;
-  A.cap = snap_cap(c, h->d);
+  A.cap = snap_cap(c, h);
   A.status = c.d_status;
   A.eatom = nullptr;
   const bool fp64 = h->precision == EMD_PREC_FP64 || energy;
@@ -287,7 +290,7 @@ static void snap_adjoint(Ctx& c, const double* dL_dF, double dL_dE, double* grad
     A.f = nullptr;
     A.L = list_view(c);
     A.n_local = n;
-    A.cap = snap_cap(c, S);
+    A.cap = snap_cap(c, h);
     A.status = c.d_status;
     A.eatom = nullptr;
     A.g = h->adj_g.p;
