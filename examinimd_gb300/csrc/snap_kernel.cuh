@@ -89,7 +89,7 @@ struct SnapDev {
   const double* wjelem;
   const int* map;  // ntypes
   // rescaled recursion: V_j(ma, mb) = f_j(ma, mb) U_j(ma, mb); over the half
-  // grid (nyh): invf = 1 / f, yscale = hw2 / f (the force contraction's
+  // grid (nyh): invf = 1 / f, yscale = 2 hw / f (the force contraction's
   // weight folded into Y; FP64 and FP32); half-layer buffer sizes (even, odd j)
   const double* invf;
   const double* yscale;
@@ -131,12 +131,6 @@ __device__ __forceinline__ R warp_sum_r(R v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL_MASK, v, o);
   return v;
-}
-
-// twice that weight, in the contraction type
-template <typename R>
-__device__ __forceinline__ R hw2(int j, int ma, int mb) {
-  return (2 * mb < j || 2 * ma < j) ? R(2) : (2 * ma == j ? R(1) : R(0));
 }
 
 __device__ __forceinline__ double sfac_of(const SnapDev& S, double r, double rcut) {
