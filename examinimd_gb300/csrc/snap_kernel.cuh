@@ -12,14 +12,15 @@
 //      (compute_zi, sna_impl.hpp:197-283) and Y_j = sum_t cY_t Z_t, where
 //      cY folds the linear coefficients with the (j+1)/(j1+1), (j+1)/(j2+1)
 //      weights of the three terms of compute_dbidrj (sna_impl.hpp:330-539);
-//   D. per inside neighbour (a warp each):
+//   D. per inside neighbour (two per warp at a time):
 //      F_ij = sum_j 2 sum_half w Re(conj(dU'_j) Y_j) + (-1.5e6/r^14) r_ij,
-//      which equals sum_k beta_k dB_k/dr_ij of the reference; f_i += F_ij,
-//      f_j -= F_ij with FP64 atomics (j may be a ghost; update_force follows).
-//      One forward sweep of the rescaled U recursion and one adjoint sweep
-//      per neighbour (d_reverse) in place of the dU/dr recursion of
-//      compute_duarray (sna_impl.hpp:729-893).  The fitting adjoint (MODE 2)
-//      runs that dU/dr recursion (du_layer).
+//      which equals sum_k beta_k dB_k/dr_ij of the reference, from one
+//      forward sweep of the rescaled U recursion and one adjoint sweep
+//      (d_reverse) in place of the dU/dr recursion of compute_duarray
+//      (sna_impl.hpp:729-893); then, one thread per neighbour, f_j -= F_ij
+//      with FP64 atomics (j may be a ghost; update_force follows) and
+//      f_i += sum_j F_ij in a fixed order.  The fitting adjoint (MODE 2) runs
+//      the dU/dr recursion (du_layer).
 // The energy variant adds E_i = beta_0 + (2/3) sum_j sum_half w Re(conj(U_j) Y_j)
 // (B is cubic in U, so <U, dB/dU> = 3B) plus 1.25e5/r^12 per inside pair.
 //
