@@ -430,6 +430,8 @@ def run_gpu_arm(a, ws, rank, local):
                                        with_cpu=(rank == 0 and not a.no_cpu))
     if not a.no_batch and a.workload == "lj4m":
         extra["batched_lj"] = batch_measure(local, a.batch_steps, 8, 20)
+    if not a.no_fit and a.workload == "lj4m":
+        extra["fit_gradients"] = fit_measure(local, a.fit_evals)
     if rank == 0 and not a.no_cpu and not snap:
         try:
             r = cpu_sample(WORKLOADS["lj4m"]["cells"] if a.workload == "lj4m" else wl["cells"], a.cpu_steps, 1)
@@ -623,6 +625,46 @@ def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells
     return res
 
 
+def fit_measure(local: int, evals: int) -> dict:
+    """Force-matching gradient throughput: the 64 bcc W configurations (16 to
+    1,024 atoms) with targets from a hidden beta*, and the 16 fcc LJ
+    configurations with hidden (eps, sigma); one evaluation is the loss and its
+    gradient (FP64 forward of every configuration, then the adjoint kernels)
+    through the torch harness."""
+    import numpy as np
+    import torch
+    from examinimd_gb300 import fit
+    ncoef = fit.ncoeffall_for(8)
+    scfg = [fit.SnapConfig(x, box, fit.W_PARAMS, device=local) for x, box in fit.snap_config_set(64)]
+    lcfg = [fit.LJConfig(x, box, device=local) for x, box in fit.lj_config_set(16)]
+    with torch.no_grad():
+        Es, Fs = fit.SnapEnergyForces.apply(torch.tensor(fit.synthetic_beta(20261203, ncoef)), scfg)
+        El, Fl = fit.LJEnergyForces.apply(torch.tensor([1.05, 0.98], dtype=torch.float64), lcfg)
+    out = {}
+    for name, cfgs, p0, fn, Er, Fr, wE in (
+            ("snap", scfg, fit.synthetic_beta(7, ncoef), fit.SnapEnergyForces, Es, Fs, 1e-2),
+            ("lj", lcfg, np.array([1.0, 1.0]), fit.LJEnergyForces, El, Fl, 1e-3)):
+        def step():
+            p = torch.tensor(p0, dtype=torch.float64, requires_grad=True)
+            E, F = fn.apply(p, cfgs)
+            fit.loss_fn(E, F, Er, Fr, w_E=wE, w_F=1.0).backward()
+            return p.grad
+        step()  # warm-up (contexts, tables, lists)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(evals):
+            g = step()
+        t = time.perf_counter() - t0
+        atoms = sum(c.n for c in cfgs)
+        out[name] = {"gradient_evals_per_s": evals / t, "configs": len(cfgs), "atoms": atoms,
+                     "atom_evals_per_s": atoms * evals / t, "grad_norm": float(g.norm()),
+                     "how": "wall time of loss + backward through torch.autograd (FP64 forward of every "
+                            "configuration, then the adjoint), each configuration on its own context"}
+    for c in scfg + lcfg:
+        c.close()
+    return out
+
+
 def batch_ensemble(nsys=256, seed=20261204, rho=0.8442, temp=1.44):
     """256 fcc LJ systems, N_k log-uniform in [500, 20000] realised as
     round((N_k / 4)^(1/3)) cubic cells, lattice positions, Gaussian velocities
@@ -753,6 +795,8 @@ def main():
     ap.add_argument("--snap-steps", type=int, default=20)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--no-fit", action="store_true", help="skip the fitting-gradient measurement")
+    ap.add_argument("--fit-evals", type=int, default=5)
     a = ap.parse_args()
     if a.warmup < 3:
         sys.exit("--warmup must be >= 3")

@@ -78,6 +78,7 @@ _SIGS = {
     "emd_batch_stream": ([_P], _P),
     "emd_snap_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_snap_init": ([_P, _I, _D, _D, _I, _D, _I, _DP, _DP, _DP, _I, _I, _IP, _I], _I),
+    "emd_snap_set_beta": ([_P, _DP], _I),
     "emd_snap_compute": ([_P], _I),
     "emd_snap_energy": ([_P, _DP], _I),
     "emd_snap_ncoeff": ([_P, _IP], _I),
@@ -331,6 +332,11 @@ class Context:
         self._ok(self.lib.emd_snap_init(self.h, twojmax, rfac0, rmin0, switchflag, rcutfac, len(radelem),
                                         _dp(radelem), _dp(wjelem), _dp(beta), beta.shape[1], len(tmap), _ip(tmap),
                                         precision), "emd_snap_init")
+
+    def snap_set_beta(self, beta):
+        """emd_snap_set_beta: new linear coefficients (nelem x ncoeffall), same tables."""
+        b = np.ascontiguousarray(beta, dtype=np.float64)
+        self._ok(self.lib.emd_snap_set_beta(self.h, _dp(b)), "emd_snap_set_beta")
 
     def snap_compute(self):
         self._ok(self.lib.emd_snap_compute(self.h), "emd_snap_compute")

@@ -21,13 +21,14 @@ struct SnapHost {
   DevBuf<int> trip, cg_off, jobs, tjob_off, yred_off, yred_job, map;
   DevBuf<int4> zord;
   DevBuf<int> inside_max;  // k_snap_inside_max's result
-  DevBuf<double> cg, cY, rootpq, beta0, radelem, wjelem, eatom, invf, yscale;
+  DevBuf<double> cg, cY, beta0, radelem, wjelem, eatom, invf, yscale;
   DevBuf<float> cg_f, cY_f, yscale_f;
   // adjoint: per-atom columns, their per-element sums, the loss gradient dL/dF
   DevBuf<double> adj, adj_sum, adj_g;
   // coefficient k's three dB/dr terms: full triples and factors (the cY fold)
   std::vector<int> k_t1, k_t2, k_t3;
   std::vector<double> k_f2, k_f3;
+  std::vector<int> k_j;  // (j1, j2, j) of coefficient k
 };
 
 
@@ -109,8 +110,8 @@ size_t snap_work_bytes(const SnapDev& S, int real_bytes) {
   const size_t wB = 2 * sizeof(double) * size_t(SNAP_WARPS) * BG * size_t(S.bh_even + S.bh_odd);
   const size_t wC = 2 * size_t(real_bytes) * size_t(S.njobs);
   size_t wD = 2 * size_t(real_bytes) * size_t(SNAP_WARPS) * 2 * size_t(drev_words(J));
-  if (real_bytes == int(sizeof(double)))  // the fitting adjoint's dU/dr layers
-    wD = std::max(wD, 2 * sizeof(double) * size_t(SNAP_WARPS) * 8 * L2);
+  if (real_bytes == int(sizeof(double)))  // the fitting adjoint's U and tangent layers
+    wD = std::max(wD, 2 * sizeof(double) * size_t(SNAP_WARPS) * 4 * L2);
   return (std::max(wB, std::max(wC, wD)) + 15) & ~size_t(15);
 }
 
@@ -120,14 +121,12 @@ size_t snap_adjoint_bytes(const SnapDev& S) {
 }
 
 // the kernel's shared-memory carve-up (k_snap), for `cap` inside neighbours
-size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes, bool adjoint) {
-  const int L1 = S.L + 1;
+size_t snap_smem_bytes(const SnapDev& S, int cap, int real_bytes) {
   const bool f64 = real_bytes == int(sizeof(double));
   const size_t nd = f64 ? size_t(ND_FIELDS) : size_t(ND_MIXED), nr = f64 ? 0 : size_t(NR_MIXED);
   size_t b = 0;
   b += sizeof(double) * 5 * size_t(cap);                                // r, w, rcut
   b += 2 * sizeof(double) * size_t(S.nuf);                              // utot
-  if (adjoint) b += size_t(real_bytes) * size_t((L1 * L1 + 1) & ~1);    // rootpq
   b += 2 * size_t(real_bytes) * size_t(S.nyh);                          // ytot
   if (!f64) b += 2 * size_t(real_bytes) * size_t(S.nuf);               // FP32 U_tot
   b += sizeof(int) * size_t((cap + 3) & ~3);                            // inside j
@@ -182,7 +181,7 @@ void free_snap(Ctx& c) {
   for (auto* b : {&h->trip, &h->cg_off, &h->jobs, &h->tjob_off, &h->yred_off, &h->yred_job, &h->map}) b->release();
   h->zord.release();
   h->inside_max.release();
-  for (auto* b : {&h->cg, &h->cY, &h->rootpq, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
+  for (auto* b : {&h->cg, &h->cY, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
                   &h->adj_g, &h->invf, &h->yscale})
     b->release();
   for (auto* b : {&h->cg_f, &h->cY_f, &h->yscale_f}) b->release();
@@ -198,6 +197,26 @@ template <class T>
 static void upload(Ctx& c, DevBuf<T>& b, const std::vector<T>& v) {
   b.reserve(v.size() + 1, c.stream);
   EMD_CUDA(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, c.stream));
+}
+
+// Y's coefficients: beta_k folded onto the full triples of compute_dbidrj's
+// three terms (sna_impl.hpp:330-570), per element, with beta_0 apart
+void snap_fold_beta(const SnapHost& h, int nfull, int nelem, int ncoeffall, const double* beta,
+                    std::vector<double>& cY, std::vector<double>& beta0) {
+  cY.assign(size_t(nelem) * nfull, 0.0);
+  beta0.assign(static_cast<size_t>(nelem), 0.0);
+  for (int e = 0; e < nelem; ++e) {
+    const double* be = beta + size_t(e) * ncoeffall;
+    beta0[size_t(e)] = be[0];
+    double* ce = &cY[size_t(e) * nfull];
+    for (size_t k = 0; k < h.k_t1.size(); ++k) {
+      const int j1 = h.k_j[3 * k], j2 = h.k_j[3 * k + 1], j = h.k_j[3 * k + 2];
+      const double bk = be[k + 1];
+      ce[h.k_t1[k]] += bk;
+      ce[h.k_t2[k]] += bk * (j + 1) / (j1 + 1.0);
+      ce[h.k_t3[k]] += bk * (j + 1) / (j2 + 1.0);
+    }
+  }
 }
 
 // cap for the kernel's per-neighbour arrays: the largest inside count
@@ -239,7 +258,7 @@ static void snap_launch(Ctx& c, bool energy) {
   A.status = c.d_status;
   A.eatom = nullptr;
   const bool fp64 = h->precision == EMD_PREC_FP64 || energy;
-  const size_t smem = snap_smem_bytes(h->d, A.cap, fp64 ? 8 : 4, false);
+  const size_t smem = snap_smem_bytes(h->d, A.cap, fp64 ? 8 : 4);
   require(smem <= 227 * 1024, EMD_ERR_ARG, "SNAP: neighbour rows too long for one atom's shared memory");
   A.g = nullptr;
   A.ghost_owner = nullptr;
@@ -298,7 +317,7 @@ static void snap_adjoint(Ctx& c, const double* dL_dF, double dL_dE, double* grad
     A.newton = c.comm_newton;
     A.adj = h->adj.p;
     A.work_bytes = snap_work_bytes(S, 8);
-    const size_t smem = snap_smem_bytes(S, A.cap, 8, true) + snap_adjoint_bytes(S);
+    const size_t smem = snap_smem_bytes(S, A.cap, 8) + snap_adjoint_bytes(S);
     require(smem <= 227 * 1024, EMD_ERR_ARG, "SNAP adjoint: neighbour rows too long for shared memory");
     auto k = k_snap<double, 2>;
     EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
@@ -419,20 +438,6 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
     for (int jb : by_y[size_t(e)]) yred_job.push_back(jb);
   }
   yred_off[size_t(S.nyh)] = int(yred_job.size());
-  // adjoint coefficients: fold beta_k and the three dB terms per element
-  std::vector<double> cY(size_t(nelem) * S.nfull, 0.0), beta0(static_cast<size_t>(nelem));
-  for (int e = 0; e < nelem; ++e) {
-    const double* be = beta + size_t(e) * ncoeffall;
-    beta0[size_t(e)] = be[0];
-    double* ce = &cY[size_t(e) * S.nfull];
-    for (int k = 0; k < S.ncoeff; ++k) {
-      const int j1 = idx3[3 * k], j2 = idx3[3 * k + 1], j = idx3[3 * k + 2];
-      const double bk = be[k + 1];
-      ce[find_full(j1, j2, j)] += bk;
-      ce[find_full(std::max(j, j2), std::min(j, j2), j1)] += bk * (j + 1) / (j1 + 1.0);
-      ce[find_full(std::max(j1, j), std::min(j1, j), j2)] += bk * (j + 1) / (j2 + 1.0);
-    }
-  }
   for (int k = 0; k < S.ncoeff; ++k) {
     const int j1 = idx3[3 * k], j2 = idx3[3 * k + 1], j = idx3[3 * k + 2];
     h->k_t1.push_back(find_full(j1, j2, j));
@@ -440,10 +445,10 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
     h->k_t3.push_back(find_full(std::max(j1, j), std::min(j1, j), j2));
     h->k_f2.push_back((j + 1) / (j1 + 1.0));
     h->k_f3.push_back((j + 1) / (j2 + 1.0));
+    h->k_j.insert(h->k_j.end(), {j1, j2, j});
   }
-  std::vector<double> rootpq(size_t(L + 1) * (L + 1), 0.0);
-  for (int p = 1; p <= twojmax; p++)
-    for (int q = 1; q <= twojmax; q++) rootpq[size_t(p) * (L + 1) + q] = std::sqrt(static_cast<double>(p) / q);
+  std::vector<double> cY, beta0;
+  snap_fold_beta(*h, S.nfull, nelem, ncoeffall, beta, cY, beta0);
   // over the half grid: 1 / f_j(ma, mb) of the rescaled recursion and the
   // D contraction's Y scale (twice the half-grid weight over f); the largest
   // half layer of even and odd j
@@ -486,7 +491,6 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   upload_i(c, h->yred_job, yred_job);
   upload(c, h->cY, cY);
   upload(c, h->cY_f, cYf);
-  upload(c, h->rootpq, rootpq);
   upload(c, h->invf, invf);
   upload(c, h->yscale, yscale);
   upload(c, h->yscale_f, std::vector<float>(yscale.begin(), yscale.end()));
@@ -506,7 +510,6 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.yred_job = h->yred_job.p;
   S.cY = h->cY.p;
   S.cY_f = h->cY_f.p;
-  S.rootpq = h->rootpq.p;
   S.invf = h->invf.p;
   S.yscale = h->yscale.p;
   S.yscale_f = h->yscale_f.p;
@@ -514,6 +517,22 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.radelem = h->radelem.p;
   S.wjelem = h->wjelem.p;
   S.map = h->map.p;
+  EMD_API_END
+}
+
+emd_status emd_snap_set_beta(emd_ctx* ctx, const double* beta) {
+  EMD_API_BEGIN
+  SnapHost* h = static_cast<SnapHost*>(c.snap);
+  require(h != nullptr, EMD_ERR_STATE, "emd_snap_set_beta: SNAP not initialised");
+  require(beta != nullptr, EMD_ERR_ARG, "emd_snap_set_beta: null beta");
+  std::vector<double> cY, beta0;
+  snap_fold_beta(*h, h->d.nfull, h->d.nelem, h->d.ncoeffall, beta, cY, beta0);
+  std::vector<float> cYf(cY.begin(), cY.end());
+  EMD_CUDA(cudaMemcpyAsync(h->cY.p, cY.data(), sizeof(double) * cY.size(), cudaMemcpyHostToDevice, c.stream));
+  EMD_CUDA(cudaMemcpyAsync(h->cY_f.p, cYf.data(), sizeof(float) * cYf.size(), cudaMemcpyHostToDevice, c.stream));
+  EMD_CUDA(cudaMemcpyAsync(h->beta0.p, beta0.data(), sizeof(double) * beta0.size(), cudaMemcpyHostToDevice,
+                           c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
   EMD_API_END
 }
 

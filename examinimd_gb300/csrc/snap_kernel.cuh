@@ -19,8 +19,9 @@
 //      (d_reverse) in place of the dU/dr recursion of compute_duarray
 //      (sna_impl.hpp:729-893); then, one thread per neighbour, f_j -= F_ij
 //      with FP64 atomics (j may be a ghost; update_force follows) and
-//      f_i += sum_j F_ij in a fixed order.  The fitting adjoint (MODE 2) runs
-//      the dU/dr recursion (du_layer).
+//      f_i += sum_j F_ij in a fixed order.  The fitting adjoint (MODE 2)
+//      carries one directional derivative of the rescaled recursion per
+//      neighbour (dt_layer).
 // The energy variant adds E_i = beta_0 + (2/3) sum_j sum_half w Re(conj(U_j) Y_j)
 // (B is cubic in U, so <U, dB/dU> = 3B) plus 1.25e5/r^12 per inside pair.
 //
@@ -84,7 +85,6 @@ struct SnapDev {
   const int* yred_job;  // njobs
   const double* cY;     // nelem x nfull
   const float* cY_f;
-  const double* rootpq;  // (L+1) x (L+1)
   const double* beta0;   // nelem
   const double* radelem;
   const double* wjelem;
@@ -146,69 +146,6 @@ __device__ __forceinline__ double dsfac_of(const SnapDev& S, double r, double rc
   if (r > rcut) return 0.0;
   const double rcutfac = MY_PI / (rcut - S.rmin0);
   return -0.5 * sin((r - S.rmin0) * rcutfac) * rcutfac;
-}
-
-// U and dU/dr (3 components) layer: dU arrays hold 3 consecutive Cplx per element.
-template <typename R>
-__device__ __forceinline__ void du_layer(int j, int lane, const R* __restrict__ rootpq, int L1, R ar, R ai, R br,
-                                         R bi, const R* dar, const R* dai, const R* dbr, const R* dbi,
-                                         const Cplx<R>* P, const Cplx<R>* dP, Cplx<R>* C, Cplx<R>* dC) {
-  const int nh = (j + 1) * (j / 2 + 1);
-  for (int e = lane; e < nh; e += 32) {
-    const int mb = e / (j + 1), ma = e % (j + 1);
-    R vr = 0, vi = 0, dr[3] = {0, 0, 0}, di[3] = {0, 0, 0};
-    if (ma > 0) {
-      const int s = (ma - 1) * j + mb;
-      const Cplx<R> u = P[s];
-      const R rp = rootpq[ma * L1 + (j - mb)];
-      vr = -rp * (br * u.r + bi * u.i);
-      vi = -rp * (br * u.i - bi * u.r);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const Cplx<R> du = dP[3 * s + k];
-        dr[k] = -rp * (dbr[k] * u.r + dbi[k] * u.i + br * du.r + bi * du.i);
-        di[k] = -rp * (dbr[k] * u.i - dbi[k] * u.r + br * du.i - bi * du.r);
-      }
-    }
-    if (ma < j) {
-      const int s = ma * j + mb;
-      const Cplx<R> u = P[s];
-      const R rp = rootpq[(j - ma) * L1 + (j - mb)];
-      vr += rp * (ar * u.r + ai * u.i);
-      vi += rp * (ar * u.i - ai * u.r);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const Cplx<R> du = dP[3 * s + k];
-        dr[k] += rp * (dar[k] * u.r + dai[k] * u.i + ar * du.r + ai * du.i);
-        di[k] += rp * (dar[k] * u.i - dai[k] * u.r + ar * du.i - ai * du.r);
-      }
-    }
-    const int o = ma * (j + 1) + mb;
-    C[o] = Cplx<R>{vr, vi};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) dC[3 * o + k] = Cplx<R>{dr[k], di[k]};
-  }
-  __syncwarp();
-  for (int e = lane; e < nh; e += 32) {
-    const int mb = e / (j + 1), ma = e % (j + 1);
-    const bool even = ((ma + mb) & 1) == 0;
-    const int o = ma * (j + 1) + mb;
-    if (2 * mb < j || 2 * ma < j) {
-      const int t = (j - ma) * (j + 1) + (j - mb);
-      const Cplx<R> u = C[o];
-      C[t] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const Cplx<R> du = dC[3 * o + k];
-        dC[3 * t + k] = even ? Cplx<R>{du.r, -du.i} : Cplx<R>{-du.r, du.i};
-      }
-    } else if (2 * ma == j) {
-      C[o].i = -C[o].i;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) dC[3 * o + k].i = -dC[3 * o + k].i;
-    }
-  }
-  __syncwarp();
 }
 
 // ---- rescaled recursion (mixed form)
@@ -481,6 +418,52 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, 
   }
 }
 
+// Layer j of the rescaled recursion and of its derivative along one
+// direction (the fitting adjoint's g_i - g_j):
+//   V_j = conj(a) V_{j-1}(ma) - conj(b) V_{j-1}(ma - 1),
+//   T_j = conj(ta) V_{j-1}(ma) + conj(a) T_{j-1}(ma) - conj(tb) V_{j-1}(ma - 1) - conj(b) T_{j-1}(ma - 1),
+// with du_layer's inversion mirror and centre conjugation.  Full layers,
+// column-major (element (ma, mb) at mb (j + 1) + ma).
+template <typename R>
+__device__ __forceinline__ void dt_layer(int j, int lane, R ar, R ai, R br, R bi, R tar, R tai, R tbr, R tbi,
+                                         const Cplx<R>* P, const Cplx<R>* TP, Cplx<R>* C, Cplx<R>* TC) {
+  const int nh = (j + 1) * (j / 2 + 1);
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e - mb * (j + 1);
+    Cplx<R> u1{0, 0}, u2{0, 0}, t1{0, 0}, t2{0, 0};
+    if (ma > 0) {
+      u1 = P[mb * j + ma - 1];
+      t1 = TP[mb * j + ma - 1];
+    }
+    if (ma < j) {
+      u2 = P[mb * j + ma];
+      t2 = TP[mb * j + ma];
+    }
+    C[e] = Cplx<R>{fma(ar, u2.r, fma(ai, u2.i, fma(-br, u1.r, -bi * u1.i))),
+                   fma(ar, u2.i, fma(-ai, u2.r, fma(-br, u1.i, bi * u1.r)))};
+    const R tr = fma(tar, u2.r, fma(tai, u2.i, fma(ar, t2.r, fma(ai, t2.i,
+                 fma(-tbr, u1.r, fma(-tbi, u1.i, fma(-br, t1.r, -bi * t1.i)))))));
+    const R ti = fma(tar, u2.i, fma(-tai, u2.r, fma(ar, t2.i, fma(-ai, t2.r,
+                 fma(-tbr, u1.i, fma(tbi, u1.r, fma(-br, t1.i, bi * t1.r)))))));
+    TC[e] = Cplx<R>{tr, ti};
+  }
+  __syncwarp();
+  for (int e = lane; e < nh; e += 32) {
+    const int mb = e / (j + 1), ma = e - mb * (j + 1);
+    const bool even = ((ma + mb) & 1) == 0;
+    if (2 * mb < j || 2 * ma < j) {
+      const int t = (j - mb) * (j + 1) + (j - ma);
+      const Cplx<R> u = C[e], w = TC[e];
+      C[t] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
+      TC[t] = even ? Cplx<R>{w.r, -w.i} : Cplx<R>{-w.r, w.i};
+    } else if (2 * ma == j) {
+      C[e].i = -C[e].i;
+      TC[e].i = -TC[e].i;
+    }
+  }
+  __syncwarp();
+}
+
 struct SnapArgs {
   SnapDev S;
   const double4_32a* x4;
@@ -508,18 +491,16 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
   const int i = blockIdx.x;
   if (i >= A.n_local) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int L = S.L, L2 = L * L, L1 = L + 1;
+  const int L = S.L, L2 = L * L;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // ---- shared memory carve-up (mirrored by snap_smem_bytes)
   constexpr bool kF64 = sizeof(R) == sizeof(double);
   constexpr int kNd = kF64 ? int(ND_FIELDS) : ND_MIXED, kNr = kF64 ? 0 : NR_MIXED;
-  const int nrp = MODE == 2 ? ((L1 * L1 + 1) & ~1) : 0;  // rootpq, for the fitting adjoint's dU/dr
   double* in_r = reinterpret_cast<double*>(smem_raw);      // 3*cap
   double* in_w = in_r + 3 * A.cap;                         // cap
   double* in_rc = in_w + A.cap;                            // cap
   Cplx<double>* utot = reinterpret_cast<Cplx<double>*>(in_rc + A.cap);  // nuf
-  R* rootpq_r = reinterpret_cast<R*>(utot + S.nuf);                     // nrp
-  Cplx<R>* ytot = reinterpret_cast<Cplx<R>*>(rootpq_r + nrp);          // nyh
+  Cplx<R>* ytot = reinterpret_cast<Cplx<R>*>(utot + S.nuf);            // nyh
   // U_tot in the contraction type: the FP64 array itself, or an FP32 copy
   // made once per atom (converting inside the Z loops would put an FP64-pipe
   // conversion on every Clebsch-Gordan term)
@@ -532,8 +513,6 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
   unsigned char* work = reinterpret_cast<unsigned char*>(nd + kNd * A.cap + (kNr * A.cap + 1) / 2);
   __shared__ int s_ninside;
 
-  if constexpr (MODE == 2)
-    for (int k = tid; k < L1 * L1; k += SNAP_THREADS) rootpq_r[k] = R(S.rootpq[k]);
   // ---- A: inside list (force_snap_neigh_impl.h:612-656)
   const double4_32a xi = A.x4[i];
   const int ti = A.type[i];
@@ -782,61 +761,52 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
     Cplx<double>* dp = dpart + warp * S.nyh;
     for (int e = lane; e < S.nyh; e += 32) dp[e] = Cplx<double>{0.0, 0.0};
     const double gix = A.g[3 * i], giy = A.g[3 * i + 1], giz = A.g[3 * i + 2];
-    Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (8 * L2);
+    Cplx<R>* wd = reinterpret_cast<Cplx<R>*>(work) + warp * (4 * L2);
     __syncwarp();
     for (int nb = warp; nb < ninside; nb += SNAP_WARPS) {
       const R* qr = ndr + nb;
       const R Rar = qr[ND_AR * A.cap], Rai = qr[ND_AI * A.cap], Rbr = qr[ND_BR * A.cap], Rbi = qr[ND_BI * A.cap];
-      R Rdar[3], Rdai[3], Rdbr[3], Rdbi[3], Ruk[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        Rdar[k] = qr[(ND_DAR + k) * A.cap];
-        Rdai[k] = qr[(ND_DAI + k) * A.cap];
-        Rdbr[k] = qr[(ND_DBR + k) * A.cap];
-        Rdbi[k] = qr[(ND_DBI + k) * A.cap];
-        Ruk[k] = qr[(ND_UK + k) * A.cap];
-      }
-      const R Rsfac = qr[ND_SFAC * A.cap], Rdsfac = qr[ND_DSFAC * A.cap];
       // the pair's reaction force lands on j's owner (newton) or nowhere
       const int j = in_j[nb];
       const int jo = j < A.n_local ? j : (A.newton ? A.ghost_owner[j - A.n_local] : -1);
       const double gjx = jo >= 0 ? A.g[3 * jo] : 0.0, gjy = jo >= 0 ? A.g[3 * jo + 1] : 0.0,
                    gjz = jo >= 0 ? A.g[3 * jo + 2] : 0.0;
       const R dv[3] = {R(gix - gjx), R(giy - gjy), R(giz - gjz)};
+      // derivatives of a, b, sfac along dv
+      R tar = 0, tai = 0, tbr = 0, tbi = 0, tu = 0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        tar += qr[(ND_DAR + k) * A.cap] * dv[k];
+        tai += qr[(ND_DAI + k) * A.cap] * dv[k];
+        tbr += qr[(ND_DBR + k) * A.cap] * dv[k];
+        tbi += qr[(ND_DBI + k) * A.cap] * dv[k];
+        tu += qr[(ND_UK + k) * A.cap] * dv[k];
+      }
+      const R Rsfac = qr[ND_SFAC * A.cap], sv = qr[ND_DSFAC * A.cap] * tu;
       Cplx<R>* P = wd;
       Cplx<R>* C = wd + L2;
-      Cplx<R>* dP = wd + 2 * L2;
-      Cplx<R>* dC = wd + 5 * L2;
+      Cplx<R>* TP = wd + 2 * L2;
+      Cplx<R>* TC = wd + 3 * L2;
       if (lane == 0) {
         P[0] = Cplx<R>{R(1), R(0)};
-        for (int k = 0; k < 3; ++k) dP[k] = Cplx<R>{R(0), R(0)};
-        dp[0].r += Rdsfac * (Ruk[0] * dv[0] + Ruk[1] * dv[1] + Ruk[2] * dv[2]);
+        TP[0] = Cplx<R>{R(0), R(0)};
+        dp[0].r += sv;
       }
       __syncwarp();
       for (int jl = 1; jl <= S.twojmax; ++jl) {
-        du_layer<R>(jl, lane, rootpq_r, L1, Rar, Rai, Rbr, Rbi, Rdar, Rdai, Rdbr, Rdbi, P, dP, C, dC);
+        dt_layer<R>(jl, lane, Rar, Rai, Rbr, Rbi, tar, tai, tbr, tbi, P, TP, C, TC);
         const int nh = (jl + 1) * (jl / 2 + 1), yo = yoff(jl);
-        for (int e = lane; e < nh; e += 32) {
-          const int mb = e / (jl + 1), ma = e % (jl + 1);
-          const int o = ma * (jl + 1) + mb;
-          const Cplx<R> u = C[o];
-          R dr = 0, di = 0;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            const Cplx<R> du = dC[3 * o + k];
-            dr += dv[k] * (Rdsfac * u.r * Ruk[k] + Rsfac * du.r);
-            di += dv[k] * (Rdsfac * u.i * Ruk[k] + Rsfac * du.i);
-          }
-          dp[yo + e].r += dr;
-          dp[yo + e].i += di;
+        for (int e = lane; e < nh; e += 32) {  // rescaled: D = sum (sv V + sfac T), times 1/f below
+          dp[yo + e].r += sv * C[e].r + Rsfac * TC[e].r;
+          dp[yo + e].i += sv * C[e].i + Rsfac * TC[e].i;
         }
         __syncwarp();
         Cplx<R>* t = P;
         P = C;
         C = t;
-        t = dP;
-        dP = dC;
-        dC = t;
+        t = TP;
+        TP = TC;
+        TC = t;
       }
     }
     __syncthreads();
@@ -846,7 +816,7 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
         sr += dpart[w * S.nyh + e].r;
         si += dpart[w * S.nyh + e].i;
       }
-      dsum[e] = Cplx<double>{sr, si};
+      dsum[e] = Cplx<double>{sr * S.invf[e], si * S.invf[e]};
     }
     __syncthreads();
     const size_t n = size_t(A.n_local);

@@ -22,6 +22,8 @@ simulation path does not use it.
 """
 from __future__ import annotations
 
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 import torch
 
@@ -121,12 +123,14 @@ class SnapConfig(_Config):
         super().__init__(x, box, 2.0 * radius * float(params["rcutfac"]), True, device)
 
     def set_beta(self, beta):
+        if self._built:  # tables and list in place: only the coefficients change
+            self.ctx.snap_set_beta(np.asarray(beta, float)[None, :])
+            return
         p = self.params
         self.ctx.snap_init(int(p["twojmax"]), float(p.get("rfac0", 0.99363)), float(p.get("rmin0", 0.0)),
                            int(p.get("switchflag", 1)), float(p["rcutfac"]), [self.radius], [self.weight],
                            np.asarray(beta, float)[None, :], [0], precision=EMD_PREC_FP64)
-        if not self._built:
-            self.build()
+        self.build()
 
     def _compute(self):
         self.ctx.snap_compute()
@@ -163,6 +167,17 @@ class LJConfig(_Config):
 
 # ---------------------------------------------------------------- autograd functions
 
+# Configurations are small (tens to thousands of atoms), so one alone fills a
+# few SMs.  Each lives on its own context and stream; running their calls from
+# a pool of host threads (the C calls release the GIL) keeps many of them on
+# the GPU at once.  Results are gathered in configuration order.
+_POOL = ThreadPoolExecutor(max_workers=16)
+
+
+def _each(fn, items):
+    return list(_POOL.map(fn, items))
+
+
 
 class SnapEnergyForces(torch.autograd.Function):
     """beta (ncoeffall,) -> (E (n_cfg,), F (sum N, 3)) over SnapConfigs."""
@@ -170,11 +185,13 @@ class SnapEnergyForces(torch.autograd.Function):
     @staticmethod
     def forward(ctx, beta, configs):
         b = beta.detach().cpu().numpy().astype(np.float64)
-        es, fs = [], []
-        for cfg in configs:
+
+        def one(cfg):
             cfg.set_beta(b)
-            fs.append(cfg.forces())
-            es.append(cfg.energy())
+            return cfg.forces(), cfg.energy()
+
+        res = _each(one, configs)
+        fs, es = [r[0] for r in res], [r[1] for r in res]
         ctx.configs = configs
         ctx.ncoeffall = b.shape[0]
         return (torch.tensor(es, dtype=torch.float64), torch.tensor(np.concatenate(fs), dtype=torch.float64))
@@ -183,11 +200,12 @@ class SnapEnergyForces(torch.autograd.Function):
     def backward(ctx, gE, gF):
         gE = gE.detach().cpu().numpy()
         gF = gF.detach().cpu().numpy()
+        offs = np.cumsum([0] + [cfg.n for cfg in ctx.configs])
+        parts = _each(lambda k: ctx.configs[k].adjoint(gF[offs[k]:offs[k + 1]], float(gE[k]), ctx.ncoeffall),
+                      range(len(ctx.configs)))
         grad = np.zeros(ctx.ncoeffall)
-        o = 0
-        for k, cfg in enumerate(ctx.configs):
-            grad += cfg.adjoint(gF[o:o + cfg.n], float(gE[k]), ctx.ncoeffall)
-            o += cfg.n
+        for g in parts:  # summed in configuration order
+            grad += g
         return torch.tensor(grad, dtype=torch.float64), None
 
 
@@ -197,11 +215,13 @@ class LJEnergyForces(torch.autograd.Function):
     @staticmethod
     def forward(ctx, params, configs):
         eps, sigma = (float(v) for v in params.detach().cpu().numpy())
-        es, fs = [], []
-        for cfg in configs:
+
+        def one(cfg):
             cfg.set_params(eps, sigma)
-            fs.append(cfg.forces())
-            es.append(cfg.energy())
+            return cfg.forces(), cfg.energy()
+
+        res = _each(one, configs)
+        fs, es = [r[0] for r in res], [r[1] for r in res]
         ctx.configs = configs
         return (torch.tensor(es, dtype=torch.float64), torch.tensor(np.concatenate(fs), dtype=torch.float64))
 
@@ -209,11 +229,12 @@ class LJEnergyForces(torch.autograd.Function):
     def backward(ctx, gE, gF):
         gE = gE.detach().cpu().numpy()
         gF = gF.detach().cpu().numpy()
+        offs = np.cumsum([0] + [cfg.n for cfg in ctx.configs])
+        parts = _each(lambda k: ctx.configs[k].adjoint(gF[offs[k]:offs[k + 1]], float(gE[k])),
+                      range(len(ctx.configs)))
         grad = np.zeros(2)
-        o = 0
-        for k, cfg in enumerate(ctx.configs):
-            grad += cfg.adjoint(gF[o:o + cfg.n], float(gE[k]))
-            o += cfg.n
+        for g in parts:  # summed in configuration order
+            grad += g
         return torch.tensor(grad, dtype=torch.float64), None
 
 
