@@ -64,17 +64,17 @@ __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restri
                                                            float4* __restrict__ xl, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double dtfm = dtfm_t[type[i]];
+  const int ti = type[i];
+  const double dtfm = dtfm_t[ti];
   const double fx = f[3 * i], fy = f[3 * i + 1], fz = f[3 * i + 2];
   double vx = v[3 * i], vy = v[3 * i + 1], vz = v[3 * i + 2];
-  if (KICK) {  // the previous step's final half kick, then this one
-    vx = fma(dtfm, fx, vx);
-    vy = fma(dtfm, fy, vy);
-    vz = fma(dtfm, fz, vz);
-  }
-  vx = fma(dtfm, fx, vx);
-  vy = fma(dtfm, fy, vy);
-  vz = fma(dtfm, fz, vz);
+  // KICK: the previous step's final half kick and this step's first, with
+  // the same forces, as one kick of 2 dtfm (one rounding; the FP64 drop-in
+  // keeps the reference's two)
+  const double k = KICK ? 2.0 * dtfm : dtfm;
+  vx = fma(k, fx, vx);
+  vy = fma(k, fy, vy);
+  vz = fma(k, fz, vz);
   v[3 * i] = vx;
   v[3 * i + 1] = vy;
   v[3 * i + 2] = vz;
@@ -83,7 +83,10 @@ __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restri
   p.y = fma(dtv, vy, p.y);
   p.z = fma(dtv, vz, p.z);
   x4[i] = p;
-  if (xl) xl[i] = rel(p, ctr[i]);
+  if (xl) {  // the type from the int array: converting x4.w would cost an FP64-pipe instruction
+    const double4_32a o = ctr[i];
+    xl[i] = make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(ti));
+  }
 }
 
 __global__ void __launch_bounds__(256) k_nve_final_mixed(double* __restrict__ v, const double* __restrict__ f,
