@@ -124,3 +124,27 @@ def test_snap_mixed_force_error(golden):
     scale = np.sqrt(np.mean(np.linalg.norm(a, axis=1) ** 2))
     assert np.sqrt(np.mean(err ** 2)) / scale <= 1e-5
     assert err.max() / scale <= 1e-4
+
+
+@pytest.mark.parametrize("name", SNAP_CASES)
+def test_snap_mixed_force_error_on_golden_decks(name, golden):
+    """The mixed form against the FP64 form on every SNAP golden deck
+    (one and two elements), at displaced positions."""
+    from examinimd_gb300 import EMD_PREC_MIXED
+    g = golden(name)
+    setup = mdloop.setup_for_case(name, CASES[name], g)
+    state = mdloop.make_lattice(setup)
+    rng = np.random.default_rng(5)
+    state["x"] = state["x"] + rng.normal(0, 0.05, state["x"].shape)
+    ref, mix = _ctx(), _ctx()
+    mdloop.init(ref, setup, state)
+    mdloop.init(mix, setup, state, precision=EMD_PREC_MIXED)
+    nl = ref.info()[0]
+    a, b = ref.get(0, nl), mix.get(0, nl)
+    np.testing.assert_array_equal(a["id"], b["id"])
+    err = np.linalg.norm(b["f"] - a["f"], axis=1)
+    scale = np.sqrt(np.mean(np.linalg.norm(a["f"], axis=1) ** 2))
+    assert np.sqrt(np.mean(err ** 2)) / scale <= 1e-5, (name, np.sqrt(np.mean(err ** 2)) / scale)
+    assert err.max() / scale <= 1e-4
+    ref.close()
+    mix.close()
