@@ -107,6 +107,14 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
   const int M = pre[27];
   const int nc = a.bincount[bc], oc = a.binoffsets[bc];
   int mx = 0;
+  // Candidates farther than the cutoff from every centre atom of the chunk
+  // are dropped while staging, once per warp: the FP32 r^2 of a centre atom
+  // to a candidate is at least the candidate's squared FP32 distance to the
+  // bounding box of the chunk's centre atoms (rounding is monotone), and a
+  // dropped candidate's exceeds cut_hi by a 1e-5 margin, so no lane would
+  // accept the pair or re-test it in FP64.  Rows keep their order.
+  const float prune_sq = a.cut_hi * 1.00001f;
+  const unsigned lt = (1u << lane) - 1u;
   for (int a0 = 0; a0 < nc; a0 += 32) {
     // this lane's centre atom
     const int bi = a0 + lane;
@@ -125,27 +133,52 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
         kz = okey(xd.z);
       }
     }
+    // bounding box of the chunk's centre atoms that own rows
+    float lox = own ? xi.x : 3.0e38f, loy = own ? xi.y : 3.0e38f, loz = own ? xi.z : 3.0e38f;
+    float hix = own ? xi.x : -3.0e38f, hiy = own ? xi.y : -3.0e38f, hiz = own ? xi.z : -3.0e38f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lox = fminf(lox, __shfl_xor_sync(FULL_MASK, lox, o));
+      loy = fminf(loy, __shfl_xor_sync(FULL_MASK, loy, o));
+      loz = fminf(loz, __shfl_xor_sync(FULL_MASK, loz, o));
+      hix = fmaxf(hix, __shfl_xor_sync(FULL_MASK, hix, o));
+      hiy = fmaxf(hiy, __shfl_xor_sync(FULL_MASK, hiy, o));
+      hiz = fmaxf(hiz, __shfl_xor_sync(FULL_MASK, hiz, o));
+    }
     int cnt = 0;
     // next slot of the row: +1 inside a 4-entry granule, then on to the
     // row's next granule (4 stride - 3 ints further)
     int* rp = a.rows + quad_index(own ? i : 0, 0, a.stride);
     const int jump = 4 * a.stride - 3;
     for (int base = 0; base < M; base += NB_CAP) {
-      const int m = min(NB_CAP, M - base), m4 = (m + 3) & ~3;
+      const int mc = min(NB_CAP, M - base);
+      int m = 0;  // candidates kept
       __syncwarp();
-      for (int t = lane; t < m; t += 32) {
-        const int g = base + t;
-        int s = 0;  // stencil bin of candidate g: binary search of the prefix
+      for (int t0 = 0; t0 < mc; t0 += 32) {
+        const int t = t0 + lane;
+        bool keep = false;
+        float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (t < mc) {
+          const int g = base + t;
+          int s = 0;  // stencil bin of candidate g: binary search of the prefix
 #pragma unroll
-        for (int h = 16; h >= 1; h >>= 1)
-          if (s + h <= 27 && pre[s + h] <= g) s += h;
-        const int j = a.permute[boff[s] + (g - pre[s])];
-        const float4 p = a.xl[j];
-        const float sx = float(s / 9 - 1) * a.wx, sy = float((s / 3) % 3 - 1) * a.wy, sz = float(s % 3 - 1) * a.wz;
-        const int code = ((s / 9) << 4) | (((s / 3) % 3) << 2) | (s % 3);
-        const int w = PACKED ? ((j << 6) | code) : j;
-        cand[t] = make_float4(p.x + sx, p.y + sy, p.z + sz, __int_as_float(w));
+          for (int h = 16; h >= 1; h >>= 1)
+            if (s + h <= 27 && pre[s + h] <= g) s += h;
+          const int j = a.permute[boff[s] + (g - pre[s])];
+          const float4 p = a.xl[j];
+          const float sx = float(s / 9 - 1) * a.wx, sy = float((s / 3) % 3 - 1) * a.wy, sz = float(s % 3 - 1) * a.wz;
+          const int code = ((s / 9) << 4) | (((s / 3) % 3) << 2) | (s % 3);
+          const int w = PACKED ? ((j << 6) | code) : j;
+          c = make_float4(p.x + sx, p.y + sy, p.z + sz, __int_as_float(w));
+          const float bx = fmaxf(fmaxf(lox - c.x, c.x - hix), 0.f), by = fmaxf(fmaxf(loy - c.y, c.y - hiy), 0.f),
+                      bz = fmaxf(fmaxf(loz - c.z, c.z - hiz), 0.f);
+          keep = bx * bx + by * by + bz * bz <= prune_sq;
+        }
+        const unsigned bal = __ballot_sync(FULL_MASK, keep);
+        if (keep) cand[m + __popc(bal & lt)] = c;
+        m += __popc(bal);
       }
+      const int m4 = (m + 3) & ~3;
       __syncwarp();
       // pad to a multiple of four with copies of the first candidate moved far
       // outside the cutoff (a valid particle, never accepted)
