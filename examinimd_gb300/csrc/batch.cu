@@ -309,7 +309,7 @@ __device__ void halo_refresh(const BArgs& A, const BSys& S, int ng) {
   for (int g = S.n + threadIdx.x; g < S.n + ng; g += blockDim.x) halo_ghost(A, S, g);
 }
 
-__device__ __forceinline__ void force_atom(const BArgs& A, const BSys& S, const float4* shift, int i) {
+__device__ __forceinline__ void force_atom(const BArgs& A, const BSys& S, int i) {
   const float4* xl = A.xl + S.base;
   const int4* rows4 = reinterpret_cast<const int4*>(A.rows + S.row_base);
   double* f = A.f + 3 * size_t(S.base);
@@ -317,7 +317,7 @@ __device__ __forceinline__ void force_atom(const BArgs& A, const BSys& S, const 
   C.xi = xl[i];
   C.i = i;
   C.ti = 0;
-  C.shift = shift + (threadIdx.x & 7);
+  C.set_bin_width(float(S.w[0]), float(S.w[1]), float(S.w[2]));
   C.x4 = A.x + S.base;
   const int cnt = min(A.num[S.base + i], A.K);
   const int4* q = rows4 + i;
@@ -338,8 +338,8 @@ __device__ __forceinline__ void force_atom(const BArgs& A, const BSys& S, const 
   f[3 * i + 2] = double(acc.sz) - double(acc.cz);
 }
 
-__device__ void force(const BArgs& A, const BSys& S, const float4* shift) {
-  for (int i = threadIdx.x; i < S.n; i += blockDim.x) force_atom(A, S, shift, i);
+__device__ void force(const BArgs& A, const BSys& S) {
+  for (int i = threadIdx.x; i < S.n; i += blockDim.x) force_atom(A, S, i);
 }
 
 // IntegratorNVE::initial_integrate, with the FP32 bin-relative copy
@@ -370,29 +370,16 @@ __device__ __forceinline__ void nve_final_atom(const BArgs& A, const BSys& S, in
   v[3 * i + 2] = fma(A.dtf, f[3 * i + 2], v[3 * i + 2]);
 }
 
-// the 64 bin shifts in the eight interleaved copies lj_pair reads
-__device__ __forceinline__ void fill_shift(const BSys& S, float4* shift) {
-  for (int u = threadIdx.x; u < 64 * 8; u += blockDim.x) {
-    const int t = u >> 3, kx = (t >> 4) & 3, ky = (t >> 2) & 3, kz = t & 3;
-    shift[u] = make_float4(kx == 3 ? 1.0e4f : float(1 - kx) * float(S.w[0]),
-                           ky == 3 ? 1.0e4f : float(1 - ky) * float(S.w[1]),
-                           kz == 3 ? 1.0e4f : float(1 - kz) * float(S.w[2]), 0.f);
-  }
-}
-
 // Persistent form: one CTA advances one system.  mode 1: initial build +
 // force; mode 2: wrap, halo and binning only (the phased form's rebuild);
 // mode 0: nsteps timesteps.
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch(BArgs A) {
   extern __shared__ int hist[];
   __shared__ int sh[33];
-  __shared__ float4 shift[64 * 8];
   const BSys S = A.sys[blockIdx.x];
-  fill_shift(S, shift);
-  __syncthreads();
   if (A.mode != 0) {
     rebuild(A, S, sh, hist);
-    if (A.mode == 1) force(A, S, shift);
+    if (A.mode == 1) force(A, S);
     return;
   }
   int ng = A.nghost[blockIdx.x];
@@ -407,7 +394,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch(BArgs A) {
       halo_refresh(A, S, ng);
       __syncthreads();
     }
-    force(A, S, shift);
+    force(A, S);
     // each thread integrates the atoms it computed the force of
     for (int i = threadIdx.x; i < S.n; i += blockDim.x) nve_final_atom(A, S, i);
     __syncthreads();
@@ -424,13 +411,8 @@ struct BChunk {
 enum { BP_NVE_INITIAL = 0, BP_NEIGH = 1, BP_FORCE = 2, BP_NVE_FINAL = 3, BP_HALO = 4 };
 
 __global__ void __launch_bounds__(BP_THREADS) k_batch_phase(BArgs A, const BChunk* __restrict__ chunks, int phase) {
-  __shared__ float4 shift[64 * 8];
   const BChunk ch = chunks[blockIdx.x];
   const BSys& S = A.sys[ch.sys];
-  if (phase == BP_FORCE) {
-    fill_shift(S, shift);
-    __syncthreads();
-  }
   const int k = ch.first + threadIdx.x;
   if (phase == BP_HALO) {
     const int ng = min(A.nghost[ch.sys], S.cap - S.n);
@@ -440,7 +422,7 @@ __global__ void __launch_bounds__(BP_THREADS) k_batch_phase(BArgs A, const BChun
   if (k >= S.n) return;
   if (phase == BP_NVE_INITIAL) nve_initial_atom(A, S, k);
   else if (phase == BP_NEIGH) build_row(A, S, k);
-  else if (phase == BP_FORCE) force_atom(A, S, shift, k);
+  else if (phase == BP_FORCE) force_atom(A, S, k);
   else nve_final_atom(A, S, k);
 }
 

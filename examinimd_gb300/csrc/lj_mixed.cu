@@ -117,23 +117,13 @@ __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict_
                                                        const int4* __restrict__ rows4, int stride,
                                                        const int* __restrict__ num, LJParamsF P, float wx, float wy,
                                                        float wz, int n) {
-  // the 64 shifts (1 - k) w, eight copies interleaved by 16-byte granule:
-  // lane l reads copy l % 8, so the eight lanes of a 128-bit shared load
-  // phase always fall in eight different bank groups
-  __shared__ float4 shift[64 * 8];
-  for (int u = threadIdx.x; u < 64 * 8; u += blockDim.x) {
-    const int t = u >> 3, kx = (t >> 4) & 3, ky = (t >> 2) & 3, kz = t & 3;
-    shift[u] = make_float4(kx == 3 ? 1.0e4f : float(1 - kx) * wx, ky == 3 ? 1.0e4f : float(1 - ky) * wy,
-                           kz == 3 ? 1.0e4f : float(1 - kz) * wz, 0.f);
-  }
-  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PairCtx C;
   C.xi = xl[i];
   C.i = i;
   C.ti = __float_as_int(C.xi.w);
-  C.shift = shift + (threadIdx.x & 7);
+  C.set_bin_width(wx, wy, wz);
   C.x4 = x4;
   const int cnt = num[i];
   const int4* q = rows4 + i;

@@ -52,11 +52,26 @@ struct Acc {
   }
 };
 
+// The bin shift (1 - k) w of a pair, per dimension, is formed from the
+// entry's 2-bit code k where it sits (bits 4-5 x, 2-3 y, 0-1 z): those bits
+// placed under the exponent of 2^23 read as 2^23 + m k (m = 16, 4, 1), so
+// t = m k exactly and the shift is fma(t, -w / m, w): w, 0 or -w for k = 0, 1,
+// 2, exactly.  The padding code k = 3 gives -2 w, outside every cutoff (a bin
+// is at least the neighbour cutoff wide).  No table: a shared-memory table
+// read moved 16 bytes per pair through the L1 data path that the x_j gathers
+// also need.
 struct PairCtx {
   float4 xi;
   int i, ti;
-  const float4* shift;  // shared: (1 - k) w per stencil code, copy (lane % 8) of 8 interleaved copies
+  float2 nw_xy, w_xy;  // (-w_x / 16, -w_y / 4), (w_x, w_y)
+  float nw_z, w_z;     // -w_z, w_z
   const double4_32a* x4;
+  __device__ __forceinline__ void set_bin_width(float wx, float wy, float wz) {
+    nw_xy = make_float2(-wx * 0.0625f, -wy * 0.25f);
+    w_xy = make_float2(wx, wy);
+    nw_z = -wz;
+    w_z = wz;
+  }
 };
 
 // One pair's geometry and coefficients: x_i - x_j = (xl_i - xl_j) + (1 - k) w
@@ -70,10 +85,15 @@ struct PairGeo {
 template <bool SINGLE>
 __device__ __forceinline__ PairGeo lj_geo(const PairCtx& C, int e, const float4& xj, const LJParamsF& P) {
   PairGeo g;
-  const float4 sh = C.shift[(e & 63) << 3];
+  constexpr int kExp = 0x4B000000;  // bits of 2^23
+  const float2 txy = __fadd2_rn(make_float2(__int_as_float((e & 0x30) | kExp), __int_as_float((e & 0x0C) | kExp)),
+                                make_float2(-8388608.0f, -8388608.0f));
+  const float tz = __fadd_rn(__int_as_float((e & 0x03) | kExp), -8388608.0f);
+  const float2 sxy = __ffma2_rn(txy, C.nw_xy, C.w_xy);
+  const float sz = __fmaf_rn(tz, C.nw_z, C.w_z);
   g.dxy = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
-  g.dxy = __fadd2_rn(g.dxy, make_float2(sh.x, sh.y));
-  g.dz = __fadd_rn(__fsub_rn(C.xi.z, xj.z), sh.z);
+  g.dxy = __fadd2_rn(g.dxy, sxy);
+  g.dz = __fadd_rn(__fsub_rn(C.xi.z, xj.z), sz);
   const float2 sq = __fmul2_rn(g.dxy, g.dxy);
   g.rsq = __fmaf_rn(g.dz, g.dz, __fadd_rn(sq.x, sq.y));
   if (SINGLE) {
