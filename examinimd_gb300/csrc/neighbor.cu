@@ -172,7 +172,8 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
           c = make_float4(p.x + sx, p.y + sy, p.z + sz, __int_as_float(w));
           const float bx = fmaxf(fmaxf(lox - c.x, c.x - hix), 0.f), by = fmaxf(fmaxf(loy - c.y, c.y - hiy), 0.f),
                       bz = fmaxf(fmaxf(loz - c.z, c.z - hiz), 0.f);
-          keep = bx * bx + by * by + bz * bz <= prune_sq;
+          // the lanes' r^2 expression, so monotone rounding bounds it below
+          keep = __fmaf_rn(bz, bz, __fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by))) <= prune_sq;
         }
         const unsigned bal = __ballot_sync(FULL_MASK, keep);
         if (keep) cand[m + __popc(bal & lt)] = c;
@@ -190,8 +191,13 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
           for (int u = 0; u < 4; ++u) {
             const float4 c = cand[k + u];
             const int w = __float_as_int(c.w);
-            const float dx = xi.x - c.x, dy = xi.y - c.y, dz = xi.z - c.z;
-            const float rsq = dx * dx + dy * dy + dz * dz;
+            // FP32 r^2 with packed (x, y) and a fused z term (this file is
+            // compiled without contraction for the FP64 re-test; the FP32
+            // value only has to be within the guard band)
+            const float2 dxy = __ffma2_rn(make_float2(c.x, c.y), make_float2(-1.f, -1.f), make_float2(xi.x, xi.y));
+            const float dz = __fsub_rn(xi.z, c.z);
+            const float2 sq = __fmul2_rn(dxy, dxy);
+            const float rsq = __fmaf_rn(dz, dz, __fadd_rn(sq.x, sq.y));
             bool in = rsq < a.cut_lo;
             const bool decided = in || rsq > a.cut_hi;
             bool take;
