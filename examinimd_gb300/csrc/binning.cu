@@ -15,11 +15,24 @@
 namespace emd {
 namespace {
 
+// Bin centre coordinates, min_d + (i + 0.5) w_d for every bin index i of
+// each dimension (nbx | nby | nbz entries): the per-particle FP32 offsets and
+// the mixed form's FP64 centres both read them, so neither repeats the
+// conversion, multiply and adds per particle on the FP64 pipe.
+__global__ void k_bin_ctab(int nbx, int nby, int nbz, double minx, double miny, double minz, double wx, double wy,
+                           double wz, double* __restrict__ tab) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nbx) tab[t] = minx + (t + 0.5) * wx;
+  else if (t < nbx + nby) tab[t] = miny + (t - nbx + 0.5) * wy;
+  else if (t < nbx + nby + nbz) tab[t] = minz + (t - nbx - nby + 0.5) * wz;
+}
+
 __global__ void __launch_bounds__(256) k_bin_index(const double4_32a* __restrict__ x4, int first, int n, int nbx,
                                                    int nby, int nbz, double minx, double miny, double minz,
-                                                   double mulx, double muly, double mulz, double wx, double wy,
-                                                   double wz, int* __restrict__ binof, int* __restrict__ bincount,
-                                                   float4* __restrict__ xl, unsigned* status) {
+                                                   double mulx, double muly, double mulz,
+                                                   const double* __restrict__ ctab, int* __restrict__ binof,
+                                                   int* __restrict__ bincount, float4* __restrict__ xl,
+                                                   unsigned* status) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const double4_32a p = x4[first + r];
@@ -38,8 +51,8 @@ __global__ void __launch_bounds__(256) k_bin_index(const double4_32a* __restrict
   binof[r] = b;
   atomicAdd(&bincount[b], 1);
   // FP32 position relative to the bin centre, for the neighbour candidate tests
-  xl[first + r] = make_float4(float(p.x - (minx + (ix + 0.5) * wx)), float(p.y - (miny + (iy + 0.5) * wy)),
-                              float(p.z - (minz + (iz + 0.5) * wz)), __int_as_float(int(p.w)));
+  xl[first + r] = make_float4(float(p.x - ctab[ix]), float(p.y - ctab[nbx + iy]), float(p.z - ctab[nbx + nby + iz]),
+                              __int_as_float(int(p.w)));
 }
 
 __global__ void __launch_bounds__(256) k_bin_scatter(const int* __restrict__ binof, int n,
@@ -135,12 +148,21 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
   EMD_CUDA(cudaMemsetAsync(c.bincount.p, 0, sizeof(int) * nbins, c.stream));
   EMD_CUDA(cudaMemsetAsync(c.bin_cursor.p, 0, sizeof(int) * nbins, c.stream));
   c.xl_bin.reserve(size_t(first + n) + 1, c.stream, true);
+  const int ntab = nb[0] + nb[1] + nb[2];
+  c.bin_ctab.reserve(size_t(ntab), c.stream);
+  {
+    TimedLaunch t(c, "bin_ctab");
+    k_bin_ctab<<<blocks_for(ntab, 256), 256, 0, c.stream>>>(
+        nb[0], nb[1], nb[2], c.bmin[0], c.bmin[1], c.bmin[2], (c.bmax[0] - c.bmin[0]) / nb[0],
+        (c.bmax[1] - c.bmin[1]) / nb[1], (c.bmax[2] - c.bmin[2]) / nb[2], c.bin_ctab.p);
+    EMD_CHECK_LAUNCH();
+  }
   if (n > 0) {
     TimedLaunch t(c, "bin_index");
-    k_bin_index<<<blocks_for(n, 256), 256, 0, c.stream>>>(
-        c.x4.p, first, n, nb[0], nb[1], nb[2], c.bmin[0], c.bmin[1], c.bmin[2], c.bmul[0], c.bmul[1], c.bmul[2],
-        (c.bmax[0] - c.bmin[0]) / nb[0], (c.bmax[1] - c.bmin[1]) / nb[1], (c.bmax[2] - c.bmin[2]) / nb[2], c.binof.p,
-        c.bincount.p, c.xl_bin.p, c.d_status);
+    k_bin_index<<<blocks_for(n, 256), 256, 0, c.stream>>>(c.x4.p, first, n, nb[0], nb[1], nb[2], c.bmin[0],
+                                                          c.bmin[1], c.bmin[2], c.bmul[0], c.bmul[1], c.bmul[2],
+                                                          c.bin_ctab.p, c.binof.p, c.bincount.p, c.xl_bin.p,
+                                                          c.d_status);
     EMD_CHECK_LAUNCH();
   }
   exclusive_scan_int(c, c.bincount.p, c.binoffsets.p, nbins, nullptr);

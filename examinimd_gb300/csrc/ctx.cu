@@ -328,6 +328,7 @@ void emd_destroy(emd_ctx* ctx) {
   c.xl.release();
   c.xl_bin.release();
   c.bin_ctr.release();
+  c.bin_ctab.release();
   c.neigh_rows2d.release();
   c.lj_params_f.release();
   for (auto& b : c.scan_levels) b.release();

@@ -167,6 +167,7 @@ struct Ctx {
   float lj_single[3] = {0, 0, 0};
   double lj_single_cutsq_d = 0;
   DevBuf<double4_32a> bin_ctr;  // FP64 bin centre per particle (mixed form)
+  DevBuf<double> bin_ctab;      // bin centre coordinate per bin and dimension (nbx | nby | nbz)
   long long neigh_builds = 0;
   int xl_ok = 0;  // xl == FP32(x - bin centre) holds for owned (1) / ghost (2) rows
   // deep_copy(f, 0) not yet applied to owned (1) / ghost (2) rows; the full-list

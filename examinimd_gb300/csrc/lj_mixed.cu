@@ -30,16 +30,17 @@ struct BinFrame {
   double wx, wy, wz;  // bin widths
 };
 
-// FP64 centre of every particle's bin at the last list build
-__global__ void __launch_bounds__(256) k_bin_centres(const int* __restrict__ abin, int n, BinFrame F,
-                                                     double4_32a* __restrict__ ctr) {
+// FP64 centre of every particle's bin at the last list build, from the
+// binning's table of bin centre coordinates (nbx | nby | nbz)
+__global__ void __launch_bounds__(256) k_bin_centres(const int* __restrict__ abin, int n, int nbx, int nby, int nbz,
+                                                     const double* __restrict__ ctab, double4_32a* __restrict__ ctr) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
   const int b = abin[a];
-  const int bx = b / (F.nby * F.nbz);
-  const int by = (b / F.nbz) % F.nby;
-  const int bz = b % F.nbz;
-  ctr[a] = make_double4_32a(F.minx + (bx + 0.5) * F.wx, F.miny + (by + 0.5) * F.wy, F.minz + (bz + 0.5) * F.wz, 0.0);
+  const int bx = b / (nby * nbz);
+  const int by = (b / nbz) % nby;
+  const int bz = b % nbz;
+  ctr[a] = make_double4_32a(ctab[bx], ctab[nbx + by], ctab[nbx + nby + bz], 0.0);
 }
 
 __device__ __forceinline__ float4 rel(const double4_32a& p, const double4_32a& o) {
@@ -184,7 +185,8 @@ void lj_mixed_after_build(Ctx& c) {
   std::swap(c.xl, c.xl_bin);
   c.bin_ctr.reserve(size_t(n_all) + 1, c.stream);
   TimedLaunch t(c, "lj_bin_centres");
-  k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, frame(c), c.bin_ctr.p);
+  k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, c.nbin[0], c.nbin[1], c.nbin[2],
+                                                               c.bin_ctab.p, c.bin_ctr.p);
   EMD_CHECK_LAUNCH();
   c.xl_ok = 3;
 }
