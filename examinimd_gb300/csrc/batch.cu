@@ -150,10 +150,20 @@ __device__ void build_row(const BArgs& A, const BSys& S, int i) {
   const float4 xi = xl[i];
   int bx, by, bz;
   bin_coords(S, binof[i], bx, by, bz);
+  // A stencil bin whose box (centre d w in i's frame, half-width w / 2 plus
+  // a margin far above rounding) lies farther than the band's upper edge
+  // (x 1.001) from i holds no candidate i would accept or re-test: skipped,
+  // which leaves the row unchanged.
+  const float hx = 0.5001f * wx, hy = 0.5001f * wy, hz = 0.5001f * wz;
+  const float prune_sq = A.nb_hi * 1.001f;
   int cnt = 0;
   for (int dx = -1; dx <= 1; ++dx)
     for (int dy = -1; dy <= 1; ++dy)
       for (int dz = -1; dz <= 1; ++dz) {
+        const float ex = fmaxf(fabsf(xi.x - float(dx) * wx) - hx, 0.f);
+        const float ey = fmaxf(fabsf(xi.y - float(dy) * wy) - hy, 0.f);
+        const float ez = fmaxf(fabsf(xi.z - float(dz) * wz) - hz, 0.f);
+        if (ex * ex + ey * ey + ez * ez > prune_sq) continue;
         const int bj = ((bx + dx) * (S.nb[1] + 2) + (by + dy)) * (S.nb[2] + 2) + (bz + dz);
         const float sx = -dx * wx, sy = -dy * wy, sz = -dz * wz;
         const int code = ((dx + 1) << 4) | ((dy + 1) << 2) | (dz + 1);
