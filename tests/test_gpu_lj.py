@@ -201,3 +201,28 @@ def test_lj_mixed_on_2d_lists():
     np.testing.assert_array_equal(forces[0]["id"], forces[1]["id"])
     for k in ("x", "v", "f"):
         np.testing.assert_array_equal(forces[0][k], forces[1][k])
+
+
+@pytest.mark.parametrize("half,precision,rho", [(False, 0, 0.8442), (True, 0, 0.8442), (False, 1, 0.8442),
+                                                (False, 1, 2.0), (True, 0, 2.0)])
+def test_neighbour_rows_on_a_random_gas(half, precision, rho):
+    """Uniform random positions (no lattice order; at rho 2 a bin holds about
+    40 atoms, more than one warp's lanes): bins, ghosts and every neighbour row
+    entry for entry against the oracle.  The build drops staged candidates
+    beyond the cutoff from its centre atoms' bounding box and decides pairs in
+    FP32 outside a guard band; rows must still equal the FP64 reference's."""
+    from oracle.orc import Oracle
+    setup = mdloop.LJSetup(8, half=half, rho=rho)
+    state = dict(mdloop.make_lattice(setup))
+    rng = np.random.default_rng(20261205)
+    state["x"] = rng.uniform(0.0, 1.0, state["x"].shape) * np.array(setup.domain)
+    gpu, orc = _ctx(), Oracle()
+    tg = mdloop.init(gpu, setup, state, precision=precision)
+    to = mdloop.init(orc, setup, state)
+    assert tg == to
+    cg, pg = gpu.comm_ghosts()
+    co, po = orc.comm_ghosts()
+    np.testing.assert_array_equal(cg, co)
+    np.testing.assert_array_equal(pg, po)
+    for x, y in zip(gpu.neigh_get(tg), orc.neigh_get(to)):
+        np.testing.assert_array_equal(x, y)
