@@ -47,7 +47,7 @@ run {steps}
 """
 
 CASES = {
-    # LJ, full CSR list, newton off (the configuration BASELINE names)
+    # LJ, full CSR list, newton off (the configuration of the LJ-4M workload)
     "lj_fcc6_full_csr": dict(kind="lj", n=6, mass=1.0, temp=1.44, newton="off", every=20, thermo=10, steps=100,
                              args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL", "--comm-type", "SERIAL"],
                              dump_every=1, keep_steps=[0, 20, 21, 100]),
