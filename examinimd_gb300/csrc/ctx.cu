@@ -448,12 +448,14 @@ emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x
     c.xl_ok &= ~1;
     c.stage_d.reserve(3 * size_t(count), c.stream);
     EMD_CUDA(cudaMemcpyAsync(c.stage_d.p, x, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
+  }
+  if (v) EMD_CUDA(cudaMemcpyAsync(c.v.p + 3 * size_t(first), v, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
+  if (f) EMD_CUDA(cudaMemcpyAsync(c.f.p + 3 * size_t(first), f, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
+  if (x) {  // packed after the copies, so the host link is not left idle meanwhile
     TimedLaunch t(c, "system_pack_x");
     k_pack_x4_keep_type<<<blocks_for(count, 256), 256, 0, c.stream>>>(c.stage_d.p, c.x4.p + first, count);
     EMD_CHECK_LAUNCH();
   }
-  if (v) EMD_CUDA(cudaMemcpyAsync(c.v.p + 3 * size_t(first), v, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
-  if (f) EMD_CUDA(cudaMemcpyAsync(c.f.p + 3 * size_t(first), f, sizeof(double) * 3 * count, cudaMemcpyHostToDevice, c.stream));
   EMD_API_END
 }
 
