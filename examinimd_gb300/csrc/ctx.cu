@@ -327,7 +327,8 @@ void emd_destroy(emd_ctx* ctx) {
   c.stage_x4.release();
   c.xl.release();
   c.xl_bin.release();
-  c.bin_ctr.release();
+  c.bin_c3.release();
+  c.ctr_tab.release();
   c.bin_ctab.release();
   c.neigh_rows2d.release();
   c.lj_params_f.release();

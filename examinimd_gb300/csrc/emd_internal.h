@@ -166,7 +166,11 @@ struct Ctx {
   bool lj_uniform = false;   // every type pair has the same parameters
   float lj_single[3] = {0, 0, 0};
   double lj_single_cutsq_d = 0;
-  DevBuf<double4_32a> bin_ctr;  // FP64 bin centre per particle (mixed form)
+  // mixed form: bin coordinates of every particle at the last list build,
+  // packed bx | by << 10 | bz << 20, and that build's bin centre table
+  DevBuf<int> bin_c3;
+  DevBuf<double> ctr_tab;
+  int ctr_nb[3] = {0, 0, 0};
   DevBuf<double> bin_ctab;      // bin centre coordinate per bin and dimension (nbx | nby | nbz)
   long long neigh_builds = 0;
   int xl_ok = 0;  // xl == FP32(x - bin centre) holds for owned (1) / ghost (2) rows
@@ -229,6 +233,20 @@ void materialize_zero(Ctx& c, bool locals, bool ghosts);
 void materialize_kick(Ctx& c);
 // mixed-form hooks (lj_mixed.cu)
 bool mixed_xl_active(const Ctx& c);
+
+// FP64 centre of particle a's bin at the last list build (mixed form): 4
+// bytes per particle and a table that stays in L1, where a centre per
+// particle took 32 bytes of HBM traffic in the integrator and halo passes
+struct BinCentres {
+  const int* c3;
+  const double* tab;
+  int nbx, nby;
+  __device__ __forceinline__ double4_32a at(int a) const {
+    const int c = c3[a];
+    return make_double4_32a(tab[c & 1023], tab[nbx + ((c >> 10) & 1023)], tab[nbx + nby + (c >> 20)], 0.0);
+  }
+};
+BinCentres bin_centres(const Ctx& c);
 void lj_mixed_after_build(Ctx& c);
 void nve_initial_mixed(Ctx& c, bool kick_first);
 void nve_final_mixed(Ctx& c);

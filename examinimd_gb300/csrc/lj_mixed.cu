@@ -30,29 +30,28 @@ struct BinFrame {
   double wx, wy, wz;  // bin widths
 };
 
-// FP64 centre of every particle's bin at the last list build, from the
-// binning's table of bin centre coordinates (nbx | nby | nbz)
-__global__ void __launch_bounds__(256) k_bin_centres(const int* __restrict__ abin, int n, int nbx, int nby, int nbz,
-                                                     const double* __restrict__ ctab, double4_32a* __restrict__ ctr) {
+// Bin coordinates of every particle at the last list build, packed
+// bx | by << 10 | bz << 20 (BinCentres)
+__global__ void __launch_bounds__(256) k_bin_centres(const int* __restrict__ abin, int n, int nby, int nbz,
+                                                     int* __restrict__ c3) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
   const int b = abin[a];
   const int bx = b / (nby * nbz);
   const int by = (b / nbz) % nby;
   const int bz = b % nbz;
-  ctr[a] = make_double4_32a(ctab[bx], ctab[nbx + by], ctab[nbx + nby + bz], 0.0);
+  c3[a] = bx | (by << 10) | (bz << 20);
 }
 
 __device__ __forceinline__ float4 rel(const double4_32a& p, const double4_32a& o) {
   return make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(int(p.w)));
 }
 
-__global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restrict__ x4,
-                                                    const double4_32a* __restrict__ ctr, int n,
+__global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restrict__ x4, BinCentres ctr, int n,
                                                     float4* __restrict__ xl) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
-  xl[a] = rel(x4[a], ctr[a]);
+  xl[a] = rel(x4[a], ctr.at(a));
 }
 
 // IntegratorNVE::initial_integrate (integrator_nve.cpp:64-73) with FMA, plus
@@ -61,8 +60,7 @@ template <bool KICK>
 __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restrict__ x4, double* __restrict__ v,
                                                            const double* __restrict__ f, const int* __restrict__ type,
                                                            const double* __restrict__ dtfm_t, double dtv,
-                                                           const double4_32a* __restrict__ ctr,
-                                                           float4* __restrict__ xl, int n) {
+                                                           BinCentres ctr, float4* __restrict__ xl, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int ti = type[i];
@@ -85,7 +83,7 @@ __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restri
   p.z = fma(dtv, vz, p.z);
   x4[i] = p;
   if (xl) {  // the type from the int array: converting x4.w would cost an FP64-pipe instruction
-    const double4_32a o = ctr[i];
+    const double4_32a o = ctr.at(i);
     xl[i] = make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(ti));
   }
 }
@@ -183,13 +181,20 @@ void materialize_zero(Ctx& c, bool locals, bool ghosts);
 void lj_mixed_after_build(Ctx& c) {
   const int n_all = c.N_local + c.N_ghost;
   std::swap(c.xl, c.xl_bin);
-  c.bin_ctr.reserve(size_t(n_all) + 1, c.stream);
+  require(c.nbin[0] < 1024 && c.nbin[1] < 1024 && c.nbin[2] < 1024, EMD_ERR_ARG,
+          "mixed form: at most 1023 bins per dimension");
+  c.bin_c3.reserve(size_t(n_all) + 1, c.stream);
+  const int ntab = c.nbin[0] + c.nbin[1] + c.nbin[2];
+  c.ctr_tab.reserve(size_t(ntab), c.stream);
+  EMD_CUDA(cudaMemcpyAsync(c.ctr_tab.p, c.bin_ctab.p, sizeof(double) * ntab, cudaMemcpyDeviceToDevice, c.stream));
+  for (int d = 0; d < 3; ++d) c.ctr_nb[d] = c.nbin[d];
   TimedLaunch t(c, "lj_bin_centres");
-  k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, c.nbin[0], c.nbin[1], c.nbin[2],
-                                                               c.bin_ctab.p, c.bin_ctr.p);
+  k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, c.nbin[1], c.nbin[2], c.bin_c3.p);
   EMD_CHECK_LAUNCH();
   c.xl_ok = 3;
 }
+
+BinCentres bin_centres(const Ctx& c) { return BinCentres{c.bin_c3.p, c.ctr_tab.p, c.ctr_nb[0], c.ctr_nb[1]}; }
 
 bool mixed_xl_active(const Ctx& c) {
   return c.lj_ready && c.lj_prec == EMD_PREC_MIXED && c.neigh_ready && c.neigh_packed;
@@ -200,7 +205,7 @@ void nve_initial_mixed(Ctx& c, bool kick_first) {
   TimedLaunch t(c, kick_first ? "nve_final_initial" : "nve_initial");
   auto k = kick_first ? k_nve_initial_mixed<true> : k_nve_initial_mixed<false>;
   k<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.dt,
-                                                       live ? c.bin_ctr.p : nullptr, live ? c.xl.p : nullptr,
+                                                       bin_centres(c), live ? c.xl.p : nullptr,
                                                        c.N_local);
   EMD_CHECK_LAUNCH();
   if (!live) c.xl_ok &= ~1;
@@ -218,7 +223,7 @@ void lj_mixed_compute(Ctx& c) {
   const BinFrame F = frame(c);
   if (c.xl_ok != 3) {
     TimedLaunch t(c, "lj_refresh_xl");
-    k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, c.bin_ctr.p, n_all, c.xl.p);
+    k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, c.xl.p);
     EMD_CHECK_LAUNCH();
     c.xl_ok = 3;
   }
