@@ -82,9 +82,7 @@ __global__ void k_halo_update(double4_32a* __restrict__ x4, const int* __restric
   if (m & 8) p.y += ly;
   if (m & 16) p.z -= lz;
   if (m & 32) p.z += lz;
-  double4_32a o = x4[n_local + g];
-  p.w = o.w;
-  x4[n_local + g] = p;
+  x4[n_local + g] = p;  // w (the type) is the owner's, as the halo build copied it
   if (xl) {  // mixed form: FP32 position relative to the ghost's bin centre
     const double4_32a q = ctr.at(n_local + g);
     xl[n_local + g] = make_float4(float(p.x - q.x), float(p.y - q.y), float(p.z - q.z), __int_as_float(int(p.w)));

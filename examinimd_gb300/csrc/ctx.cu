@@ -387,11 +387,15 @@ emd_status emd_system_init(emd_ctx* ctx, int ntypes, const double* mass, double 
   EMD_CUDA(cudaMemcpyAsync(c.mass_d.p, c.mass.data(), sizeof(double) * ntypes, cudaMemcpyHostToDevice, c.stream));
   // dtfm = dtf / mass(type) (integrator_nve.cpp:43, 66): the same IEEE
   // operations as the per-atom division, done once per type
-  std::vector<double> dtfm(static_cast<size_t>(ntypes));
+  // ntypes more entries hold 2 dtfm (exact), the mixed form's fused double kick
+  std::vector<double> dtfm(2 * static_cast<size_t>(ntypes));
   const double dtf = 0.5 * dt / mvv2e;
-  for (int t = 0; t < ntypes; ++t) dtfm[size_t(t)] = dtf / mass[t];
-  c.dtfm_d.reserve(size_t(ntypes), c.stream);
-  EMD_CUDA(cudaMemcpyAsync(c.dtfm_d.p, dtfm.data(), sizeof(double) * ntypes, cudaMemcpyHostToDevice, c.stream));
+  for (int t = 0; t < ntypes; ++t) {
+    dtfm[size_t(t)] = dtf / mass[t];
+    dtfm[size_t(ntypes + t)] = 2.0 * dtfm[size_t(t)];
+  }
+  c.dtfm_d.reserve(2 * size_t(ntypes), c.stream);
+  EMD_CUDA(cudaMemcpyAsync(c.dtfm_d.p, dtfm.data(), sizeof(double) * 2 * ntypes, cudaMemcpyHostToDevice, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));
   EMD_API_END
 }

@@ -64,13 +64,13 @@ __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restri
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int ti = type[i];
-  const double dtfm = dtfm_t[ti];
   const double fx = f[3 * i], fy = f[3 * i + 1], fz = f[3 * i + 2];
   double vx = v[3 * i], vy = v[3 * i + 1], vz = v[3 * i + 2];
   // KICK: the previous step's final half kick and this step's first, with
   // the same forces, as one kick of 2 dtfm (one rounding; the FP64 drop-in
-  // keeps the reference's two)
-  const double k = KICK ? 2.0 * dtfm : dtfm;
+  // keeps the reference's two); dtfm_t then points at the table of 2 dtfm,
+  // so no FP64 multiply is spent on the doubling
+  const double k = dtfm_t[ti];
   vx = fma(k, fx, vx);
   vy = fma(k, fy, vy);
   vz = fma(k, fz, vz);
@@ -204,7 +204,8 @@ void nve_initial_mixed(Ctx& c, bool kick_first) {
   const bool live = mixed_xl_active(c);
   TimedLaunch t(c, kick_first ? "nve_final_initial" : "nve_initial");
   auto k = kick_first ? k_nve_initial_mixed<true> : k_nve_initial_mixed<false>;
-  k<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p, c.dtfm_d.p, c.dt,
+  k<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p,
+                                                       c.dtfm_d.p + (kick_first ? c.ntypes : 0), c.dt,
                                                        bin_centres(c), live ? c.xl.p : nullptr,
                                                        c.N_local);
   EMD_CHECK_LAUNCH();
