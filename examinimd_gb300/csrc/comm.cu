@@ -29,13 +29,19 @@ __global__ void k_exchange(double4_32a* __restrict__ x4, int n, double lx, doubl
 
 __device__ __forceinline__ double comp(const double4_32a& p, int d) { return d == 0 ? p.x : (d == 1 ? p.y : p.z); }
 
-// TagHaloSelf selection predicate for one phase (comm_serial.h:112-181).
-__global__ void k_halo_flag(const double4_32a* __restrict__ x4, int n, int dim, int upper, double bound,
-                            int* __restrict__ flag) {
+// TagHaloSelf selection predicate (comm_serial.h:112-181) for both phases
+// of one dimension: flag[i] for the upper face (x >= hi - depth), flag[n + i]
+// for the lower face (x <= lo + depth).  The odd phase's candidates are the
+// even phase's (comm_serial.cpp:68 leaves out only the ghosts the even phase
+// made), so one exclusive scan over the 2n flags ranks the upper face's
+// ghosts first and the lower face's after them, the reference's append order.
+__global__ void k_halo_flag2(const double4_32a* __restrict__ x4, int n, int dim, double bound_hi, double bound_lo,
+                             int* __restrict__ flag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double c = comp(x4[i], dim);
-  flag[i] = upper ? (c >= bound ? 1 : 0) : (c <= bound ? 1 : 0);
+  flag[i] = c >= bound_hi ? 1 : 0;
+  flag[n + i] = c <= bound_lo ? 1 : 0;
 }
 
 // Appends the flagged particles as shifted copies at dest_base + rank.
@@ -151,25 +157,27 @@ emd_status emd_comm_exchange_halo(emd_ctx* ctx, int* n_ghost_out) {
   int pack_total = 0;
   c.neigh_ready = false;
   c.xl_ok &= ~2;
-  for (int phase = 0; phase < 6; ++phase) {
-    const int dim = phase / 2;
-    const int upper = phase % 2 == 0;
-    // even phases: x >= hi - depth -> image at x - L; odd: x <= lo + depth -> x + L
-    const double bound = upper ? c.sub_hi[dim] - c.comm_depth : c.sub_lo[dim] + c.comm_depth;
-    const double shift = upper ? -c.domain[dim] : c.domain[dim];
-    const int nparticles = N_local + N_ghost - ((phase % 2 == 1) ? c.num_ghost[phase - 1] : 0);
-    c.flags.reserve(size_t(nparticles) + 1, c.stream);
-    c.flags_scan.reserve(size_t(nparticles) + 2, c.stream);
+  for (int dim = 0; dim < 3; ++dim) {
+    // phases 2 dim (upper face, image at x - L) and 2 dim + 1 (lower face,
+    // image at x + L) over the same candidates, with one count read-back
+    const double bound_hi = c.sub_hi[dim] - c.comm_depth, bound_lo = c.sub_lo[dim] + c.comm_depth;
+    const int nparticles = N_local + N_ghost;
+    const size_t n2 = 2 * size_t(nparticles);
+    c.flags.reserve(n2 + 1, c.stream);
+    c.flags_scan.reserve(n2 + 2, c.stream);
     if (nparticles > 0) {
       TimedLaunch t(c, "comm_halo_flag");
-      k_halo_flag<<<blocks_for(nparticles, 256), 256, 0, c.stream>>>(c.x4.p, nparticles, dim, upper, bound,
-                                                                     c.flags.p);
+      k_halo_flag2<<<blocks_for(nparticles, 256), 256, 0, c.stream>>>(c.x4.p, nparticles, dim, bound_hi, bound_lo,
+                                                                      c.flags.p);
       EMD_CHECK_LAUNCH();
     }
-    exclusive_scan_int(c, c.flags.p, c.flags_scan.p, nparticles, c.flags_scan.p + nparticles);
+    require(n2 < 0x7fffffffULL, EMD_ERR_OVERFLOW_GHOST, "emd_comm_exchange_halo: more than 2^30 particles");
+    exclusive_scan_int(c, c.flags.p, c.flags_scan.p, int(n2), c.flags_scan.p + n2);
     EMD_CUDA(cudaMemcpyAsync(c.h_int, c.flags_scan.p + nparticles, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    EMD_CUDA(cudaMemcpyAsync(c.h_int + 1, c.flags_scan.p + n2, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     EMD_CUDA(cudaStreamSynchronize(c.stream));
-    const int count = nparticles > 0 ? c.h_int[0] : 0;
+    const int count_hi = nparticles > 0 ? c.h_int[0] : 0;
+    const int count = nparticles > 0 ? c.h_int[1] : 0;
     // capacity (the reference grows System and the pack list, then redoes the phase)
     const long long need = (long long)N_local + N_ghost + count;
     require(need < 0x7fffffffLL, EMD_ERR_OVERFLOW_GHOST, "emd_comm_exchange_halo: more than 2^31 particles");
@@ -177,16 +185,20 @@ emd_status emd_comm_exchange_halo(emd_ctx* ctx, int* n_ghost_out) {
     c.pack.reserve(size_t(pack_total) + count + 1, c.stream, true);
     c.ghost_owner.reserve(size_t(N_ghost) + count + 1, c.stream, true);
     c.ghost_img.reserve(size_t(N_ghost) + count + 1, c.stream, true);
-    if (count > 0) {
+    for (int side = 0; side < 2 && count > 0; ++side) {
+      if ((side == 0 ? count_hi : count - count_hi) == 0) continue;
       TimedLaunch t(c, "comm_halo_scatter");
+      const size_t off = side == 0 ? 0 : size_t(nparticles);
       k_halo_scatter<<<blocks_for(nparticles, 256), 256, 0, c.stream>>>(
-          c.x4.p, c.v.p, c.q.p, c.id.p, c.type.p, c.flags.p, c.flags_scan.p, nparticles, dim, shift,
-          N_local + N_ghost, N_local, c.pack.p + pack_total, c.ghost_owner.p, c.ghost_img.p,
-          1 << (2 * dim + (upper ? 0 : 1)));
+          c.x4.p, c.v.p, c.q.p, c.id.p, c.type.p, c.flags.p + off, c.flags_scan.p + off, nparticles, dim,
+          side == 0 ? -c.domain[dim] : c.domain[dim], N_local + N_ghost, N_local, c.pack.p + pack_total,
+          c.ghost_owner.p, c.ghost_img.p, 1 << (2 * dim + side));
       EMD_CHECK_LAUNCH();
     }
-    c.num_ghost[phase] = count;
-    c.ghost_offsets[phase] = N_local + N_ghost;
+    c.num_ghost[2 * dim] = count_hi;
+    c.num_ghost[2 * dim + 1] = count - count_hi;
+    c.ghost_offsets[2 * dim] = N_local + N_ghost;
+    c.ghost_offsets[2 * dim + 1] = N_local + N_ghost + count_hi;
     pack_total += count;
     N_ghost += count;
   }
