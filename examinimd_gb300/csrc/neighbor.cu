@@ -352,9 +352,14 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
     K = int(c.h_int[1] * 1.2);
   }
   exclusive_scan_int(c, c.num_neighs.p, c.neigh_offsets.p, n, c.neigh_offsets.p + n);
-  EMD_CUDA(cudaMemcpyAsync(c.h_int, c.neigh_offsets.p + n, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  EMD_CUDA(cudaStreamSynchronize(c.stream));
-  const long long total = n > 0 ? c.h_int[0] : 0;
+  // the total sizes the compacted CSR list; column-major rows (2D, packed)
+  // need it only when the caller asks, so it is read later on demand there
+  long long total = -1;
+  if ((!two_d && !packed) || total_out) {
+    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.neigh_offsets.p + n, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    EMD_CUDA(cudaStreamSynchronize(c.stream));
+    total = n > 0 ? c.h_int[0] : 0;
+  }
   if (!two_d && !packed) {
     // NeighListCSR (neighbor_csr.h:81-124): rows contiguous at row_map(i)
     c.neighs.reserve(size_t(total) + 1, c.stream);
@@ -387,6 +392,11 @@ emd_status emd_neigh_get(emd_ctx* ctx, int* num_neighs, int* entries) {
   EMD_API_BEGIN
   require(c.neigh_ready, EMD_ERR_STATE, "emd_neigh_get: no neighbour list");
   const int n = c.neigh_rows;
+  if (c.neigh_total < 0) {  // not read at build time
+    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.neigh_offsets.p + n, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    EMD_CUDA(cudaStreamSynchronize(c.stream));
+    c.neigh_total = n > 0 ? c.h_int[0] : 0;
+  }
   if (num_neighs && n > 0)
     EMD_CUDA(cudaMemcpyAsync(num_neighs, c.num_neighs.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
   if (entries && c.neigh_total > 0) {

@@ -125,7 +125,6 @@ class NeighborGB300 : public Neighbor {
   void init(double neighcut) override;
   void create_neigh_list(System* system, Binning* binning, bool half_neigh, bool ghost_neighs) override;
   const char* name() override { return kind_ == NEIGH_CSR ? "NeighborCSR_GB300" : "Neighbor2D_GB300"; }
-  long long total = 0;
 };
 
 class Force {

@@ -77,7 +77,8 @@ void NeighborGB300::create_neigh_list(System* system, Binning*, bool half_neigh,
           system->ctx, "emd_neigh_init");
     inited_ = true;
   }
-  check(emd_neigh_create(system->ctx, half_neigh ? 1 : 0, &total), system->ctx, "emd_neigh_create");
+  // the entry count is not needed here: no read-back for column-major rows
+  check(emd_neigh_create(system->ctx, half_neigh ? 1 : 0, nullptr), system->ctx, "emd_neigh_create");
 }
 
 // ---------------------------------------------------------------- LJ
