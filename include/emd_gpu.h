@@ -131,7 +131,8 @@ emd_status emd_binning_get(emd_ctx* ctx, int* bincount, int* binoffsets, int* pe
 emd_status emd_neigh_init(emd_ctx* ctx, int kind, double neigh_cut, int comm_newton);
 /* create_neigh_list(system, binning, half_neigh, ghost_neighs=false).
  * total_out (host, may be NULL): number of entries (CSR) or sum of row
- * lengths (2D). */
+ * lengths (2D).  With NULL and column-major rows (2D, or the mixed form's
+ * packed rows) the call does not wait for the count. */
 emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out);
 /* Row lengths (N_local) and entries row by row (total) in list order. */
 emd_status emd_neigh_get(emd_ctx* ctx, int* num_neighs, int* entries);
