@@ -165,6 +165,7 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
                                                           c.d_status);
     EMD_CHECK_LAUNCH();
   }
+  c.xl_bin_valid = true;
   exclusive_scan_int(c, c.bincount.p, c.binoffsets.p, nbins, nullptr);
   if (n > 0) {
     {

@@ -153,6 +153,7 @@ struct Ctx {
   bool neigh_layout_2d = false;  // force kernels read column-major rows
   DevBuf<int> neigh_rows2d;      // column-major rows behind a CSR list
   DevBuf<float4> xl_bin;         // FP32 position relative to the bin centre (last binning)
+  bool xl_bin_valid = false;     // xl_bin holds the last binning's offsets (not handed to the mixed force)
   DevBuf<int> abin;         // bin of every particle at the last list build (packed rows)
   DevBuf<float4> xl;        // FP32 bin-relative positions (mixed force)
 

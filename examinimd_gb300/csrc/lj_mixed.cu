@@ -180,9 +180,12 @@ void materialize_zero(Ctx& c, bool locals, bool ghosts);
 // exactly the copy the force reads; keep them and record the bin centres.
 void lj_mixed_after_build(Ctx& c) {
   const int n_all = c.N_local + c.N_ghost;
-  std::swap(c.xl, c.xl_bin);
   require(c.nbin[0] < 1024 && c.nbin[1] < 1024 && c.nbin[2] < 1024, EMD_ERR_ARG,
           "mixed form: at most 1023 bins per dimension");
+  // the force takes the binning's buffer over; xl_bin is the force's old
+  // buffer now (unallocated after the first build) until the next binning
+  std::swap(c.xl, c.xl_bin);
+  c.xl_bin_valid = false;
   c.bin_c3.reserve(size_t(n_all) + 1, c.stream);
   const int ntab = c.nbin[0] + c.nbin[1] + c.nbin[2];
   c.ctr_tab.reserve(size_t(ntab), c.stream);

@@ -65,6 +65,21 @@ __device__ __noinline__ bool retest_fp64(const double4_32a* __restrict__ x4, int
   return (ddx * ddx + ddy * ddy + ddz * ddz) <= cutsq;
 }
 
+// FP32 offsets of the binned particles from their bin centres, exactly as
+// the binning writes them (k_bin_index), for a list built again from the
+// same binning after the mixed force took the binning's copy over
+__global__ void __launch_bounds__(256) k_xl_from_bins(const double4_32a* __restrict__ x4,
+                                                      const int* __restrict__ binof, int n, int nbx, int nby, int nbz,
+                                                      const double* __restrict__ ctab, float4* __restrict__ xl) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  const int b = binof[a];
+  const int bx = b / (nby * nbz), by = (b / nbz) % nby, bz = b % nbz;
+  const double4_32a p = x4[a];
+  xl[a] = make_float4(float(p.x - ctab[bx]), float(p.y - ctab[nbx + by]), float(p.z - ctab[nbx + nby + bz]),
+                      __int_as_float(int(p.w)));
+}
+
 // monotone integer key of a double (exact ordering, integer pipe)
 __device__ __forceinline__ long long okey(double v) {
   const long long b = __double_as_longlong(v);
@@ -294,6 +309,17 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   c.num_neighs.reserve(size_t(n) + 1, c.stream);
   c.neigh_offsets.reserve(size_t(n) + 2, c.stream);
   c.resize_flag.reserve(1 + NB_SLOTS, c.stream);
+  if (!c.xl_bin_valid) {  // a second build from one binning in the mixed form
+    const int n_all = c.N_local + c.N_ghost;
+    c.xl_bin.reserve(size_t(n_all) + 1, c.stream);
+    if (n_all > 0) {
+      TimedLaunch t(c, "neigh_xl_from_bins");
+      k_xl_from_bins<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, c.binof.p, n_all, c.nbin[0], c.nbin[1],
+                                                                   c.nbin[2], c.bin_ctab.p, c.xl_bin.p);
+      EMD_CHECK_LAUNCH();
+    }
+    c.xl_bin_valid = true;
+  }
   NeighArgs a;
   a.x4 = c.x4.p;
   a.xl = c.xl_bin.p;

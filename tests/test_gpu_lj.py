@@ -226,3 +226,23 @@ def test_neighbour_rows_on_a_random_gas(half, precision, rho):
     np.testing.assert_array_equal(pg, po)
     for x, y in zip(gpu.neigh_get(tg), orc.neigh_get(to)):
         np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("kind,precision", [(1, 0), (0, 1)])
+def test_neighbour_get_after_a_build_without_the_total(kind, precision):
+    """Column-major rows (2D, or the mixed form's packed rows) built again
+    from the same binning with no total requested, as the driver builds them:
+    the count is read when the rows are fetched, and the rows equal the first
+    build's.  In the mixed form the first build handed the binning's FP32
+    offsets to the force, so the second rebuilds them from the positions."""
+    setup = mdloop.LJSetup(6, kind=kind)
+    state = mdloop.make_lattice(setup)
+    ref, lazy = _ctx(), _ctx()
+    total = mdloop.init(ref, setup, state, precision=precision)
+    mdloop.init(lazy, setup, state, precision=precision)
+    assert lazy.lib.emd_neigh_create(lazy.h, 0, None) == 0
+    num, ent = lazy.neigh_get(2 * total)  # room for any count; the rows are compared below
+    rnum, rent = ref.neigh_get(total)
+    np.testing.assert_array_equal(num, rnum)
+    assert int(num.sum()) == total
+    np.testing.assert_array_equal(ent[:total], rent)
