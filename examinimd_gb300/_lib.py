@@ -8,6 +8,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 EMD_PREC_FP64, EMD_PREC_MIXED = 0, 1
+# emd_status codes (include/emd_gpu.h); a latched device status word holds bit (1 << code)
+(EMD_OK, EMD_ERR_OVERFLOW_GHOST, EMD_ERR_OVERFLOW_NEIGH, EMD_ERR_TIMEOUT, EMD_ERR_BOUNDS, EMD_ERR_CUDA, EMD_ERR_ARG,
+ EMD_ERR_STATE, EMD_ERR_NOMEM) = range(9)
 EMD_NEIGH_CSR, EMD_NEIGH_2D = 0, 1
 EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL = 4194304  # include/emd_gpu.h
 
@@ -38,6 +41,7 @@ _SIGS = {
     "emd_stream": ([_P], _P),
     "emd_synchronize": ([_P], _I),
     "emd_get_status": ([_P, C.POINTER(C.c_uint)], _I),
+    "emd_device_allocations": ([C.POINTER(C.c_ulonglong)], _I),
     "emd_system_init": ([_P, _I, _DP, _D, _D, _D, _DP, _DP, _DP], _I),
     "emd_system_grow": ([_P, _I], _I),
     "emd_system_set_local": ([_P, _I, _DP, _DP, _DP, _IP, _IP, _DP], _I),
@@ -135,6 +139,14 @@ def _f64(a, shape=None):
 
 def _i32(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+def device_allocations() -> int:
+    """Device allocations the library has made in this process (emd_device_allocations)."""
+    n = C.c_ulonglong()
+    if load_library().emd_device_allocations(C.byref(n)) != 0:
+        raise EmdError("emd_device_allocations failed")
+    return n.value
 
 
 class Context:
@@ -278,9 +290,14 @@ class Context:
         self._ok(self.lib.emd_neigh_create(self.h, int(half), C.byref(t)), "emd_neigh_create")
         return t.value
 
-    def neigh_get(self, total: int):
+    def neigh_get(self, total: int | None = None):
+        """Row lengths and entries.  The library writes every entry, so
+        without `total` the lengths are fetched first to size the buffer."""
         nl, _, _ = self.info()
         num = np.empty(max(nl, 1), np.int32)
+        if total is None:
+            self._ok(self.lib.emd_neigh_get(self.h, _ip(num), None), "emd_neigh_get")
+            total = int(num[:nl].sum())
         ent = np.empty(max(total, 1), np.int32)
         self._ok(self.lib.emd_neigh_get(self.h, _ip(num), _ip(ent)), "emd_neigh_get")
         return num[:nl], ent[:total]

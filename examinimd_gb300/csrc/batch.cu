@@ -611,7 +611,7 @@ emd_status emd_batch_create(emd_batch** out, int device, int nsys, const int* na
   EMD_CUDA(cudaSetDevice(device));
   b->device = device;
   EMD_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-  EMD_CUDA(cudaMalloc(&b->d_status, sizeof(unsigned)));
+  EMD_CUDA(device_malloc(reinterpret_cast<void**>(&b->d_status), sizeof(unsigned)));
   EMD_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), b->stream));
   b->nsys = nsys;
   b->mass = mass;
@@ -674,7 +674,7 @@ emd_status emd_batch_create(emd_batch** out, int device, int nsys, const int* na
   b->rows.reserve(size_t(rows), b->stream);
   b->nghost.reserve(size_t(nsys), b->stream);
   b->thermo.reserve(2 * size_t(nsys), b->stream);
-  EMD_CUDA(cudaMalloc(&b->d_sys, sizeof(BSys) * size_t(nsys)));
+  EMD_CUDA(device_malloc(reinterpret_cast<void**>(&b->d_sys), sizeof(BSys) * size_t(nsys)));
   EMD_CUDA(cudaMemcpyAsync(b->d_sys, b->sys.data(), sizeof(BSys) * size_t(nsys), cudaMemcpyHostToDevice, b->stream));
   {
     std::vector<BChunk> ch, gch;
@@ -685,8 +685,8 @@ emd_status emd_batch_create(emd_batch** out, int device, int nsys, const int* na
     }
     b->n_chunks = int(ch.size());
     b->n_gchunks = int(gch.size());
-    EMD_CUDA(cudaMalloc(&b->d_chunks, sizeof(BChunk) * ch.size()));
-    EMD_CUDA(cudaMalloc(&b->d_gchunks, sizeof(BChunk) * gch.size()));
+    EMD_CUDA(device_malloc(reinterpret_cast<void**>(&b->d_chunks), sizeof(BChunk) * ch.size()));
+    EMD_CUDA(device_malloc(reinterpret_cast<void**>(&b->d_gchunks), sizeof(BChunk) * gch.size()));
     EMD_CUDA(cudaMemcpyAsync(b->d_chunks, ch.data(), sizeof(BChunk) * ch.size(), cudaMemcpyHostToDevice, b->stream));
     EMD_CUDA(cudaMemcpyAsync(b->d_gchunks, gch.data(), sizeof(BChunk) * gch.size(), cudaMemcpyHostToDevice,
                              b->stream));

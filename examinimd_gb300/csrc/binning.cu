@@ -166,6 +166,7 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
     EMD_CHECK_LAUNCH();
   }
   c.xl_bin_valid = true;
+  c.bin_sorted = false;
   exclusive_scan_int(c, c.bincount.p, c.binoffsets.p, nbins, nullptr);
   if (n > 0) {
     {
@@ -208,6 +209,10 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
     EMD_CUDA(cudaMemcpyAsync(c.type.p + first, c.stage_i.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, c.stream));
     EMD_CUDA(cudaMemcpyAsync(c.id.p + first, c.stage_i.p + n, sizeof(int) * n, cudaMemcpyDeviceToDevice, c.stream));
     c.neigh_ready = false;
+    // the bin indices, FP32 offsets and permutation of this binning refer to
+    // the order before the sort: no neighbour list is built from it
+    c.bin_sorted = true;
+    c.xl_bin_valid = false;
   }
   c.binning_ready = true;
   if (nbin_out)

@@ -202,6 +202,11 @@ void materialize_zero(Ctx& c, bool locals, bool ghosts) {
   c.f_zero_pending &= ~todo;
 }
 
+std::atomic<unsigned long long>& device_alloc_counter() {
+  static std::atomic<unsigned long long> n{0};
+  return n;
+}
+
 unsigned read_status(Ctx& c, bool clear) {
   EMD_CUDA(cudaMemcpyAsync(c.h_status, c.d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, c.stream));
   if (clear) EMD_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(unsigned), c.stream));
@@ -265,6 +270,12 @@ extern "C" {
 
 int emd_abi_version(void) { return 1; }
 
+emd_status emd_device_allocations(unsigned long long* count) {
+  if (!count) return EMD_ERR_ARG;
+  *count = emd::device_alloc_counter().load(std::memory_order_relaxed);
+  return EMD_OK;
+}
+
 const char* emd_status_string(emd_status s) {
   switch (s) {
     case EMD_OK: return "ok";
@@ -294,7 +305,7 @@ emd_status emd_create(emd_ctx** out, int device) {
     c.device = device;
     EMD_CUDA(cudaSetDevice(device));
     EMD_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-    EMD_CUDA(cudaMalloc(&c.d_status, sizeof(unsigned)));
+    EMD_CUDA(device_malloc(reinterpret_cast<void**>(&c.d_status), sizeof(unsigned)));
     EMD_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(unsigned), c.stream));
     EMD_CUDA(cudaMallocHost(&c.h_status, sizeof(unsigned)));
     EMD_CUDA(cudaMallocHost(&c.h_scalar, 8 * sizeof(double)));

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -39,6 +40,16 @@ inline void require(bool ok, emd_status code, const char* msg) {
   if (!ok) throw Error(code, msg);
 }
 
+// Every device allocation of the library goes through device_malloc, which
+// counts it (emd_device_allocations), so callers and tests can check that a
+// call allocated nothing.
+std::atomic<unsigned long long>& device_alloc_counter();
+inline cudaError_t device_malloc(void** p, size_t bytes) {
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) device_alloc_counter().fetch_add(1, std::memory_order_relaxed);
+  return e;
+}
+
 // Growable device buffer (contents preserved on grow when keep = true).
 template <class T>
 struct DevBuf {
@@ -48,7 +59,7 @@ struct DevBuf {
     if (n <= cap) return;
     size_t ncap = n + n / 5 + 64;
     T* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, ncap * sizeof(T));
+    cudaError_t e = device_malloc(reinterpret_cast<void**>(&q), ncap * sizeof(T));
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
       throw Error(EMD_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
@@ -154,6 +165,7 @@ struct Ctx {
   DevBuf<int> neigh_rows2d;      // column-major rows behind a CSR list
   DevBuf<float4> xl_bin;         // FP32 position relative to the bin centre (last binning)
   bool xl_bin_valid = false;     // xl_bin holds the last binning's offsets (not handed to the mixed force)
+  bool bin_sorted = false;       // the last binning re-sorted the particles after binning them
   DevBuf<int> abin;         // bin of every particle at the last list build (packed rows)
   DevBuf<float4> xl;        // FP32 bin-relative positions (mixed force)
 

@@ -11,6 +11,8 @@
 #include <mutex>
 #include <vector>
 
+#include <cuda.h>
+
 #include "emd_device.cuh"
 #include "emd_internal.h"
 #include "neigh_rows.cuh"
@@ -251,22 +253,60 @@ static_assert(kNoAllocBlocks * 256 == EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL, "whole bl
 constexpr int kNoAllocDoubles = kNoAllocBlocks + kSumScratchDoubles;  // 133,512 bytes
 static __device__ __align__(256) double g_lj_energy_scratch[kNoAllocDoubles];
 
-// device address of the array per device, looked up on the first call made
-// with that device current
+// The array's device address belongs to a CUDA context, not to a device
+// number: after cudaDeviceReset, or with a caller's own driver-API context
+// current, the same device has a new copy at another address.  So the address
+// is kept per device together with the unique id of the context it was looked
+// up in (cuCtxGetCurrent / cuCtxGetId, reached through the runtime's driver
+// entry points so that the library does not link libcuda), and looked up
+// again when the current context is a different one.
 constexpr int kNoAllocMaxDevices = 64;
-static double* g_lj_energy_scratch_ptr[kNoAllocMaxDevices];
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;
+  double* p = nullptr;
+};
+static ScratchAddr g_lj_energy_scratch_ptr[kNoAllocMaxDevices];
 static std::mutex g_lj_energy_scratch_mu;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// unique id of the CUDA context current on this thread (0 if none)
+static unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    EMD_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q));
+    require(q == cudaDriverEntryPointSuccess && f, EMD_ERR_CUDA, "driver entry point cuCtxGetCurrent not found");
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    EMD_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q));
+    require(q == cudaDriverEntryPointSuccess && f, EMD_ERR_CUDA, "driver entry point cuCtxGetId not found");
+    get_id = reinterpret_cast<CtxGetIdFn>(f);
+  }
+  CUcontext cur = nullptr;
+  require(get_current(&cur) == CUDA_SUCCESS, EMD_ERR_CUDA, "cuCtxGetCurrent failed");
+  if (!cur) return 0;
+  unsigned long long id = 0;
+  require(get_id(cur, &id) == CUDA_SUCCESS, EMD_ERR_CUDA, "cuCtxGetId failed");
+  return id;
+}
 
 static double* lj_energy_scratch(int device) {
   require(device >= 0 && device < kNoAllocMaxDevices, EMD_ERR_ARG,
           "emd_lj_energy_noalloc: device ordinal beyond the 64 this library tracks");
   std::lock_guard<std::mutex> lock(g_lj_energy_scratch_mu);
-  if (!g_lj_energy_scratch_ptr[device]) {
+  ScratchAddr& a = g_lj_energy_scratch_ptr[device];
+  const unsigned long long id = current_context_id();
+  if (!a.p || a.ctx_id != id || id == 0) {
     void* p = nullptr;
     EMD_CUDA(cudaGetSymbolAddress(&p, g_lj_energy_scratch));
-    g_lj_energy_scratch_ptr[device] = static_cast<double*>(p);
+    // the runtime made its primary context current if none was: key by that one
+    a.ctx_id = id ? id : current_context_id();
+    a.p = static_cast<double*>(p);
   }
-  return g_lj_energy_scratch_ptr[device];
+  return a.p;
 }
 
 }  // namespace emd

@@ -301,6 +301,9 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   require(c.neigh_cut > 0, EMD_ERR_STATE, "emd_neigh_init not called");
   require(c.binning_ready && c.bin_first == 0 && c.bin_count_n == c.N_local + c.N_ghost, EMD_ERR_STATE,
           "emd_neigh_create: needs a binning of owned and ghost particles");
+  require(!c.bin_sorted, EMD_ERR_STATE,
+          "emd_neigh_create: the last binning re-sorted the particles, so its permutation no longer refers to "
+          "them; bin owned and ghost particles again without sorting first (as ExaMiniMD does)");
   const int n = c.N_local;
   c.half_neigh = half_neigh ? 1 : 0;
   const int packed = (c.lj_ready && c.lj_prec == EMD_PREC_MIXED) ? 1 : 0;

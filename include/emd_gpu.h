@@ -58,6 +58,10 @@ void* emd_stream(emd_ctx* ctx);
 emd_status emd_synchronize(emd_ctx* ctx);
 /* Device status word: bitmask of (1u << emd_status) latched by kernels. */
 emd_status emd_get_status(emd_ctx* ctx, unsigned* flags);
+/* Number of device allocations (cudaMalloc) this library has made in this
+ * process, over all contexts and devices.  No counterpart in ExaMiniMD: it
+ * lets a caller check that a sequence of calls allocated nothing. */
+emd_status emd_device_allocations(unsigned long long* count);
 
 /* --------------------------------------------------------------- System
  * System::init / grow / units / domain (system.h:57-143, system.cpp:71-109,
@@ -175,7 +179,11 @@ emd_status emd_lj_adjoint(emd_ctx* ctx, const double* dL_dF, double dL_dE, doubl
  * scratch in a fixed 133,512-byte array inside the library.
  * - The context's device must be current.  The first call on a device looks
  *   up the array's address (cudaGetSymbolAddress) and keeps it; make that
- *   first call before a stream capture if the call is to be captured.
+ *   first call before a stream capture if the call is to be captured.  The
+ *   address belongs to the CUDA context current at that call (normally the
+ *   device's primary context): a later call under another context (after
+ *   cudaDeviceReset, or with the caller's own context current) looks it up
+ *   again.
  * - More than EMD_LJ_ENERGY_NOALLOC_MAX_LOCAL owned atoms: EMD_ERR_ARG.
  * - Nothing has to be zeroed beforehand.
  * - One array per device and process: calls that can overlap on a device

@@ -5,6 +5,10 @@
 * oracle/_ref/ref_examinimd and ref_probe: ExaMiniMD's own sources compiled
   against the serial Kokkos shim (oracle/Makefile.ref), only where the
   ExaMiniMD source tree is present (it is not on the GPU machines).
+
+The ExaMiniMD tree is taken from the EXAMINIMD_SRC environment variable;
+without it this recipe looks in the one place the tree is mounted read-only
+on the machine that generates the golden fixtures.
 """
 from __future__ import annotations
 
@@ -15,7 +19,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-DEFAULT_REF_SRC = "/root/reference"
+REF_SRC_ENV = "EXAMINIMD_SRC"
+_MOUNTED_REF_SRC = "/root/reference"
+
+
+def reference_source() -> str:
+    """The ExaMiniMD source tree this recipe compiles."""
+    return os.environ.get(REF_SRC_ENV) or _MOUNTED_REF_SRC
 
 
 def build_oracle() -> str:
@@ -32,8 +42,9 @@ def build_oracle() -> str:
     return LIB
 
 
-def build_reference(ref_src: str = DEFAULT_REF_SRC) -> str | None:
+def build_reference(ref_src: str | None = None) -> str | None:
     """Compiles ExaMiniMD's sources against the shim when they are present."""
+    ref_src = ref_src or reference_source()
     if not os.path.isdir(os.path.join(ref_src, "src")):
         return None
     cmd = ["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), f"REF={ref_src}", f"-j{os.cpu_count() or 4}"]

@@ -180,9 +180,15 @@ class Oracle:
         self._ok(self.lib.orc_neigh_create(self.h, int(half), C.byref(t)), "orc_neigh_create")
         return t.value
 
-    def neigh_get(self, total):
+    def neigh_get(self, total=None):
+        """Row lengths and entries (every entry is written: without `total`
+        the lengths are read first to size the buffer)."""
         nl, _, _ = self.info()
-        num, ent = np.empty(max(nl, 1), np.int32), np.empty(max(total, 1), np.int32)
+        num = np.empty(max(nl, 1), np.int32)
+        if total is None:
+            self._ok(self.lib.orc_neigh_get(self.h, _ip(num), None), "orc_neigh_get")
+            total = int(num[:nl].sum())
+        ent = np.empty(max(total, 1), np.int32)
         self._ok(self.lib.orc_neigh_get(self.h, _ip(num), _ip(ent)), "orc_neigh_get")
         return num[:nl], ent[:total]
 

@@ -171,3 +171,35 @@ def write_case(case: dict, work: str, snap: dict | None = None) -> tuple[str, li
     if case["kind"] == "snap":
         write_snap_files(work, case, snap)
     return deck, list(case["args"])
+
+
+# Cases too large for array fixtures: make_golden.py stores SHA-256 digests of
+# the reference's dump arrays (in the reference's atom order) and of its
+# probe arrays after init, plus its thermo lines, in CASE.digest.json.
+DIGEST_CASES = {
+    # LJ-32k, the CPU-runnable LJ configuration: fcc 20^3 = 32,000 atoms, CSR
+    # full list, newton off, rebuild every 20, thermo every 10, 100 steps
+    "lj_fcc20_full_csr": dict(kind="lj", n=20, mass=1.0, temp=1.44, newton="off", every=20, thermo=10, steps=100,
+                              args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL", "--comm-type",
+                                    "SERIAL"],
+                              dump_every=1, keep_steps=[0, 20, 21, 100]),
+}
+
+
+def digest(a) -> str:
+    """SHA-256 of an array's bytes (C order, its own dtype)."""
+    import hashlib
+
+    import numpy as np
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def snap_w_synthetic(seed: int = 20261203) -> dict:
+    """The SNAP-W workload's coefficient set: element W (radius 0.5, weight
+    1), beta_0 = -8 and beta_1..55 ~ N(0, 0.1) from `seed`, with the shipped
+    W.snapparam values (twojmax 8, rcutfac 4.73442, rfac0 0.99363, rmin0 0)."""
+    import numpy as np
+    beta = [-8.0] + [float(b) for b in np.random.default_rng(seed).normal(0.0, 0.1, 55)]
+    return dict(elem="W", radius=0.5, weight=1.0, beta=beta,
+                params={"rcutfac": "4.73442", "twojmax": "8", "rfac0": "0.99363", "rmin0": "0",
+                        "diagonalstyle": "3", "bzeroflag": "0", "quadraticflag": "0"})

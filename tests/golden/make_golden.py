@@ -1,16 +1,20 @@
 """Regenerates the golden fixtures in tests/golden/ from ExaMiniMD itself.
 
-Requires the ExaMiniMD source tree (default /root/reference) and builds it
-against the serial Kokkos shim (oracle/Makefile.ref).  For every case it runs
+Requires the ExaMiniMD source tree (--ref, or $EXAMINIMD_SRC as
+oracle/build.py resolves it) and builds it against the serial Kokkos shim
+(oracle/Makefile.ref).  For every case it runs
 
   * ref_examinimd -il DECK ... --dumpbinary EVERY DIR  (the reference's own
     binary dumps: id, type, q, x, v, f of the owned atoms), and
   * ref_probe OUT DECK ...  (the reference's binning, ghosts, neighbour rows
     and initial forces right after ExaMiniMD::init),
 
-and stores the selected steps plus the thermo lines in CASE.npz.
+and stores the selected steps plus the thermo lines in CASE.npz.  For the
+DIGEST_CASES (too large for array fixtures) it stores SHA-256 digests of the
+same arrays, the dump arrays in the reference's atom order, in
+CASE.digest.json.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref SRC] [--only CASE]
 """
 from __future__ import annotations
 
@@ -29,7 +33,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from tests.golden.decks import CASES, read_snap_files, snap_elements, write_case  # noqa: E402
+from tests.golden.decks import CASES, DIGEST_CASES, digest, read_snap_files, snap_elements, write_case  # noqa: E402
 
 
 def read_probe(path: str) -> dict:
@@ -76,18 +80,50 @@ def parse_thermo(stdout: str) -> np.ndarray:
     return np.array(rows)
 
 
+def make_digest(exe: str, probe: str, name: str, case: dict) -> None:
+    """Digests of an LJ case's dumps (kept steps), probe arrays and thermo."""
+    import json
+    work = tempfile.mkdtemp(prefix="golden_")
+    try:
+        deck, args = write_case(case, work)
+        dump_dir = os.path.join(work, "dump")
+        os.makedirs(dump_dir)
+        r = subprocess.run([exe, "-il", deck] + args + ["--dumpbinary", str(case["dump_every"]), dump_dir],
+                           cwd=work, capture_output=True, text=True, check=True)
+        pr = os.path.join(work, "probe.bin")
+        subprocess.run([probe, pr, "-il", deck] + args, cwd=work, capture_output=True, text=True, check=True)
+        P = read_probe(pr)
+        out = dict(case=name, probe={k: digest(v) for k, v in P.items()},
+                   probe_counts=[int(v) for v in P["counts"]], probe_nbin=[int(v) for v in P["nbin"]],
+                   neigh_total=int(P["num_neighs"].sum()), thermo=parse_thermo(r.stdout).tolist(), steps={})
+        for step in case["keep_steps"]:
+            d = read_dump(os.path.join(dump_dir, f"output.{step:010d}.000"))
+            out["steps"][str(step)] = {k: digest(v) for k, v in d.items()}
+        path = os.path.join(HERE, f"{name}.digest.json")
+        with open(path, "w") as fp:
+            json.dump(out, fp, indent=1)
+        print(f"{name}: digests of {len(case['keep_steps'])} dumps, N={P['counts'][0]}, ghosts={P['counts'][1]}")
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="ExaMiniMD source tree (default: $EXAMINIMD_SRC)")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
     sys.path.insert(0, ROOT)
-    from oracle.build import build_reference  # noqa: E402
+    from oracle.build import build_reference, reference_source  # noqa: E402
 
+    a.ref = a.ref or reference_source()
     exe = build_reference(a.ref)
     if exe is None:
         sys.exit(f"ExaMiniMD sources not found under {a.ref}")
     probe = os.path.join(os.path.dirname(exe), "ref_probe")
+    for name, case in DIGEST_CASES.items():
+        if a.only and name != a.only:
+            continue
+        make_digest(exe, probe, name, case)
     for name, case in CASES.items():
         if a.only and name != a.only:
             continue

@@ -2,8 +2,9 @@
 
 The GPU evaluates SNAP in the adjoint form (Y = sum_t cY_t Z_t contracted
 with dU/dr); the oracle evaluates the reference formulation (U, Z, dU, dB
-per neighbour, sna_impl.hpp).  They agree to rounding: 1e-12 relative to
-the force scale for FP64.  The SNAP energy (absent from ExaMiniMD) is
+per neighbour, sna_impl.hpp).  They agree to rounding: 1e-12 of the RMS
+force for FP64 (on a perfect lattice, where every force cancels, both must
+vanish).  The SNAP energy (absent from ExaMiniMD) is
 checked against the oracle's explicit bispectrum sum and against central
 finite differences of the forces.
 """
@@ -21,10 +22,24 @@ def _ctx():
     return Context(0)
 
 
-def _max_rel(a, b, floor=1.0):
-    """max |a-b| over max(|b|, floor): forces on a perfect lattice cancel to
-    ~1e-15, so errors are measured against a 1 eV/A force scale floor."""
-    return np.abs(a - b).max() / max(np.abs(b).max(), floor)
+def _max_rel(a, b):
+    """max |a-b| over max |b| (positions, velocities)."""
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+# On a perfect lattice every SNAP force cancels by symmetry: below this RMS
+# force (eV/A) a state counts as one, and both force sets must vanish to it.
+LATTICE_RMS = 1e-10
+
+
+def _force_ok(a, b, tol=1e-12):
+    """max |a-b| within `tol` of the RMS force of b; on a perfect lattice
+    (RMS below LATTICE_RMS) both force sets must cancel instead."""
+    rms = float(np.sqrt(np.mean(np.sum(b * b, axis=1))))
+    err = float(np.abs(a - b).max())
+    if rms < LATTICE_RMS:
+        return float(np.abs(a).max()) < LATTICE_RMS, (err, rms)
+    return err <= tol * rms, (err, rms)
 
 
 def _snap_setup(golden, nx=None, ny=None, nz=None, lattice_style=0, a=3.1803):
@@ -50,14 +65,17 @@ def test_snap_modules_vs_oracle(name, golden):
     nl = orc.info()[0]
     a, b = gpu.get(0, nl), orc.get(0, nl)
     np.testing.assert_array_equal(a["id"], b["id"])
-    assert _max_rel(a["f"], b["f"]) <= 1e-12
+    ok, info = _force_ok(a["f"], b["f"])
+    assert ok, info
     for s in range(1, 6):
         mdloop.step(gpu, setup, s)
         mdloop.step(orc, setup, s)
         a, b = gpu.get(0, nl), orc.get(0, nl)
         np.testing.assert_array_equal(a["id"], b["id"])
-        for k in ("x", "v", "f"):
+        for k in ("x", "v"):
             assert _max_rel(a[k], b[k]) <= 1e-12, (s, k)
+        ok, info = _force_ok(a["f"], b["f"])
+        assert ok, (s, info)
     # energy: adjoint identity vs the oracle's explicit bispectrum sum
     eg, eo = gpu.snap_energy(), orc.snap_energy()
     assert abs(eg - eo) <= 1e-11 * abs(eo)
@@ -79,8 +97,10 @@ def test_snap_driver_vs_reference_dumps(name, golden, tmp_path, monkeypatch):
         nl = md.info()["N_local"]
         cur = md.ctx.get(0, nl)
         np.testing.assert_array_equal(cur["id"], g[f"s{s}_id"])
-        for k in ("x", "v", "f"):
+        for k in ("x", "v"):
             assert _max_rel(cur[k], g[f"s{s}_{k}"]) <= 1e-12, (s, k)
+        ok, info = _force_ok(cur["f"], g[f"s{s}_f"])
+        assert ok, (s, info)
     md.close()
 
 

@@ -79,3 +79,43 @@ def test_oracle_matches_reference_run(name, golden):
                 T, pe, et = mdloop.thermo(o, setup, nl)
                 np.testing.assert_allclose([T, pe, et], thermo_ref[s], rtol=0, atol=1.5e-6,
                                            err_msg=f"{name} thermo step {s}")
+
+
+def test_oracle_matches_reference_lj32k_digests():
+    """LJ-32k (fcc 20^3, CSR full, newton off, every 20, 100 steps): the
+    oracle's bins, permutation, particles, neighbour rows and forces after
+    init, and its owned state at steps 0, 20, 21 and 100, carry exactly the
+    bytes of ExaMiniMD's probe and --dumpbinary output (SHA-256 digests);
+    thermo to the printed precision."""
+    import json
+    import os
+
+    from tests.golden.decks import DIGEST_CASES, digest
+    name = "lj_fcc20_full_csr"
+    case = DIGEST_CASES[name]
+    with open(os.path.join(os.path.dirname(__file__), "golden", f"{name}.digest.json")) as fp:
+        D = json.load(fp)
+    setup = mdloop.setup_for_case(name, case)
+    o = Oracle(os.cpu_count() or 1)
+    mdloop.init(o, setup, mdloop.make_lattice(setup))
+    nl, ng, nt = o.info()
+    assert [nl, ng] == D["probe_counts"]
+    nb = int(np.prod(D["probe_nbin"][:3]))
+    bc, bo, perm, bounds = o.binning_get(nb, nt)
+    for k, v in (("bincount", bc), ("binoffsets", bo), ("permute", perm), ("bounds", bounds)):
+        assert digest(v) == D["probe"][k], k
+    allp = o.get(0, nt)
+    for k in ("x", "v", "id", "type"):
+        assert digest(allp[k].ravel()) == D["probe"][k], k
+    num, ent = o.neigh_get()
+    assert digest(num) == D["probe"]["num_neighs"] and digest(ent) == D["probe"]["neighs"]
+    thermo_ref = {int(r[0]): r[1:] for r in D["thermo"]}
+    for s in range(0, case["steps"] + 1):
+        if s > 0:
+            mdloop.step(o, setup, s)
+        if str(s) in D["steps"]:
+            cur = o.get(0, nl)
+            for k in ("id", "type", "q", "x", "v", "f"):
+                assert digest(cur[k]) == D["steps"][str(s)][k], f"step {s} field {k}"
+        if s in thermo_ref:
+            np.testing.assert_allclose(mdloop.thermo(o, setup, nl), thermo_ref[s], rtol=0, atol=1.5e-6)

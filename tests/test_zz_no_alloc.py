@@ -37,10 +37,13 @@ def test_noalloc_energy_matches_lj_energy(precision, half, kind):
         got = ctx.lj_energy_noalloc()
         assert np.isfinite(ref) and ref < 0.0
         assert abs(got - ref) <= RTOL * abs(ref), (got, ref)
-    # and twice in a row on its own
+    # and twice in a row on its own, with no device allocation in the library
+    from examinimd_gb300._lib import device_allocations
+    n0 = device_allocations()
     a = ctx.lj_energy_noalloc()
     b = ctx.lj_energy_noalloc()
     assert a == b
+    assert device_allocations() == n0
     ctx.close()
 
 
