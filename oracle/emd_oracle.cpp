@@ -1051,9 +1051,14 @@ int orc_lj_compute(orc_ctx* c) {
   ORC_END
 }
 
-int orc_lj_energy(orc_ctx* c, double* pe) {
-  ORC_TRY
-  double PE = 0.0;
+}  // extern "C"
+
+// Shifted LJ energy over the list, every pair term in the reference's order
+// (TagFullNeighPE / TagHalfNeighPE, force_lj_neigh_impl.h:259-343).  Acc is
+// the reduction: a plain running double, the reference's serial
+// parallel_reduce, or a compensated one.
+template <class Acc>
+static void lj_energy_terms(const orc_ctx* c, Acc& PE) {
   const int n = c->N_local;
   for (int i = 0; i < n; i++) {
     const double* xi = &c->x[3 * size_t(i)];
@@ -1081,7 +1086,48 @@ int orc_lj_energy(orc_ctx* c, double* pe) {
       }
     }
   }
+}
+
+// Neumaier's compensated sum (an improved Kahan sum): the running error of
+// every addition is carried exactly (two-sum) in a second double, so the
+// total is within about one rounding of the exact sum of the terms.
+struct CompensatedSum {
+  double s = 0.0, comp = 0.0;
+  void add(double v) {
+    const double t = s + v;
+    if (std::fabs(s) >= std::fabs(v)) comp += (s - t) + v;
+    else comp += (v - t) + s;
+    s = t;
+  }
+  CompensatedSum& operator+=(double v) {
+    add(v);
+    return *this;
+  }
+  CompensatedSum& operator-=(double v) {
+    add(-v);
+    return *this;
+  }
+  double value() const { return s + comp; }
+};
+
+extern "C" {
+
+int orc_lj_energy(orc_ctx* c, double* pe) {
+  ORC_TRY
+  double PE = 0.0;
+  lj_energy_terms(c, PE);
   *pe = PE;
+  ORC_END
+}
+
+// The same terms summed with compensation: a test-side value of the energy
+// free of the serial sum's rounding (about 1e-11 relative at 32,000 atoms,
+// 2.5 million pair terms), against which a differently ordered sum is judged.
+int orc_lj_energy_compensated(orc_ctx* c, double* pe) {
+  ORC_TRY
+  CompensatedSum PE;
+  lj_energy_terms(c, PE);
+  *pe = PE.value();
   ORC_END
 }
 

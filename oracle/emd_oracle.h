@@ -62,6 +62,7 @@ int orc_neigh_maxneighs(orc_ctx*, int* maxneighs);
 int orc_lj_init(orc_ctx*, int ntypes, const double* lj1, const double* lj2, const double* cutsq, int half);
 int orc_lj_compute(orc_ctx*);
 int orc_lj_energy(orc_ctx*, double* pe);
+int orc_lj_energy_compensated(orc_ctx*, double* pe);
 
 int orc_snap_init(orc_ctx*, int twojmax, double rfac0, double rmin0, int switchflag, double rcutfac, int nelem,
                   const double* radelem, const double* wjelem, const double* beta, int ncoeffall, int ntypes,

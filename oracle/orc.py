@@ -32,7 +32,7 @@ _SIGS = {
     "orc_neigh_init": ([_P, _I, _D, _I], _I), "orc_neigh_create": ([_P, _I, _LLP], _I),
     "orc_neigh_get": ([_P, _IP, _IP], _I), "orc_neigh_maxneighs": ([_P, _IP], _I),
     "orc_lj_init": ([_P, _I, _DP, _DP, _DP, _I], _I), "orc_lj_compute": ([_P], _I),
-    "orc_lj_energy": ([_P, _DP], _I),
+    "orc_lj_energy": ([_P, _DP], _I), "orc_lj_energy_compensated": ([_P, _DP], _I),
     "orc_snap_init": ([_P, _I, _D, _D, _I, _D, _I, _DP, _DP, _DP, _I, _I, _IP], _I),
     "orc_snap_compute": ([_P], _I), "orc_snap_energy": ([_P, _DP], _I),
     "orc_snap_bispectrum": ([_P, _DP], _I), "orc_snap_ncoeff": ([_P, _IP], _I),
@@ -208,6 +208,12 @@ class Oracle:
     def lj_energy(self):
         e = _D()
         self._ok(self.lib.orc_lj_energy(self.h, C.byref(e)), "orc_lj_energy")
+        return e.value
+
+    def lj_energy_compensated(self):
+        """The reference's pair terms summed with compensation (no serial-sum rounding)."""
+        e = _D()
+        self._ok(self.lib.orc_lj_energy_compensated(self.h, C.byref(e)), "orc_lj_energy_compensated")
         return e.value
 
     def snap_init(self, twojmax, rfac0, rmin0, switchflag, rcutfac, radelem, wjelem, beta, type_map, precision=0):

@@ -7,11 +7,11 @@ access and latches a status bit instead.
 * Capacities that start tiny grow and the call is redone, as CommSerial
   (comm_serial.cpp:73-89) and Neighbor2D (neighbor_2d.h:304-330) do:
   particle arrays, ghost lists and the 2D row stride sized for 108 lattice
-  atoms then serve a 1,741-atom random gas at twice the lattice density, with
-  the oracle's rows, ghosts and forces.
+  atoms then serve 2,048 atoms at twice the lattice density, with the
+  oracle's rows, ghosts and forces.
 * The batched ensemble has fixed capacities: a row capacity below the real
-  row length returns EMD_ERR_OVERFLOW_NEIGH from the run (rows are clamped
-  to the capacity on the device), and the process can go on using the GPU.
+  row length returns EMD_ERR_OVERFLOW_NEIGH (rows are clamped to the
+  capacity on the device), and the process can go on using the GPU.
 * A particle outside the binned box (not wrapped by an exchange) latches
   EMD_ERR_BOUNDS in the status word; the binning keeps it in the nearest bin.
 * A truncated deck, a truncated .snapcoeff and a malformed .snapparam give an
@@ -49,15 +49,15 @@ def test_tiny_capacities_grow_to_the_oracle_result(kind):
         mdloop.step(gpu, small, s)
     assert gpu.info()[0] == 108
     m0 = gpu.neigh_maxneighs()
-    # the same context, a box of 6^3 fcc cells holding a gas at rho 1.7
-    big = mdloop.LJSetup(6, kind=kind, every=2)
-    state = _gas(big, 1.7, 11)
-    assert len(state["x"]) > 10 * 108
+    # the same context, 8^3 fcc cells compressed to rho 1.7: 19x the atoms,
+    # twice the neighbours per row
+    big = mdloop.LJSetup(8, kind=kind, every=2, rho=1.7)
+    state = mdloop.make_lattice(big)
     orc = Oracle()
     tg, to = mdloop.init(gpu, big, state), mdloop.init(orc, big, state)
     assert tg == to
     nl, ng, nt = orc.info()
-    assert gpu.info()[:2] == (nl, ng) and ng > 20 * 108
+    assert gpu.info()[:2] == (nl, ng) and nl == 2048 and ng > 20 * 108
     for x, y in zip(gpu.comm_ghosts(), orc.comm_ghosts()):
         np.testing.assert_array_equal(x, y)
     for x, y in zip(gpu.neigh_get(tg), orc.neigh_get(to)):
@@ -91,10 +91,10 @@ def _fcc_batch_inputs(cells, seed=5):
 def test_batch_row_capacity_overflow_is_a_status():
     from examinimd_gb300 import Batch, EmdError
     ns, boxes, x, v = _fcc_batch_inputs([5, 6])
-    b = Batch(ns, boxes, x, v, max_neigh=8)  # rows hold about 77 entries
-    with pytest.raises(EmdError, match="OVERFLOW_NEIGH|neighbour row capacity"):
-        b.run(5)
-    b.close()
+    # rows hold about 77 entries: the first build, inside emd_batch_create,
+    # overflows a capacity of 8 and the call returns the status
+    with pytest.raises(EmdError, match="neighbour capacity overflow"):
+        Batch(ns, boxes, x, v, max_neigh=8)
     # the GPU and the library stay usable: the same ensemble with room runs
     ok = Batch(ns, boxes, x, v, max_neigh=128)
     ok.run(5)
@@ -191,11 +191,17 @@ def test_no_list_from_a_binning_that_sorted():
     EMD_ERR_STATE, and the next unsorted binning allows it again."""
     from examinimd_gb300 import EmdError
     setup = mdloop.LJSetup(4)
+    st = mdloop.make_lattice(setup)
     gpu = _ctx()
-    mdloop.init(gpu, setup, mdloop.make_lattice(setup))
+    gpu.system_init(setup.masses, setup.boltz, setup.mvv2e, setup.dt, setup.domain)
+    gpu.set_local(st["x"], st["type"], st["id"], v=st["v"])
+    setup.force_init(gpu)
+    gpu.comm_init(setup.neigh_cut)
+    gpu.neigh_init(setup.kind, setup.neigh_cut, setup.newton)
     c = setup.neigh_cut
-    gpu.binning_create(c, c, c, 1, True, True, True)
-    with pytest.raises(EmdError, match="call out of order"):
+    gpu.comm_exchange()
+    gpu.binning_create(c, c, c, 1, True, False, True)  # no ghosts yet: this binning covers every particle
+    with pytest.raises(EmdError, match="re-sorted"):
         gpu.neigh_create(False)
     gpu.comm_exchange_halo()
     gpu.binning_create(c, c, c, 1, True, True, False)

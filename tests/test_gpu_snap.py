@@ -55,10 +55,16 @@ SNAP_CASES = [k for k, v in CASES.items() if v["kind"] == "snap"]
 
 @pytest.mark.parametrize("name", SNAP_CASES)
 def test_snap_modules_vs_oracle(name, golden):
+    """Every golden deck from positions displaced by a seeded 0.05 A
+    Gaussian, so forces are of order 1 eV/A and 1e-12 of the RMS force is a
+    relative test from the first step (on the undisplaced decks the forces of
+    the first steps nearly cancel; the dump test below covers those)."""
     from oracle.orc import Oracle
     g = golden(name)
     setup = mdloop.setup_for_case(name, CASES[name], g)
-    state = mdloop.make_lattice(setup)
+    state = dict(mdloop.make_lattice(setup))
+    rng = np.random.default_rng(20261206)
+    state["x"] = state["x"] + rng.normal(0.0, 0.05, state["x"].shape)
     gpu, orc = _ctx(), Oracle()
     mdloop.init(gpu, setup, state)
     mdloop.init(orc, setup, state)
