@@ -69,6 +69,8 @@ _SIGS = {
     "emd_lj_compute": ([_P], _I),
     "emd_lj_energy": ([_P, _DP], _I),
     "emd_lj_energy_noalloc": ([_P, _DP], _I),
+    "emd_lj_request_energy": ([_P], _I),
+    "emd_lj_force_energy": ([_P, _DP, _IP], _I),
     "emd_lj_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_batch_create": ([C.POINTER(_P), _I, _I, _IP, _DP, _DP, _DP, _D, _D, _D, _D, _D, _D, _I, _I, _D], _I),
     "emd_batch_destroy": ([_P], None),
@@ -334,6 +336,16 @@ class Context:
         out = np.zeros((nelem, ncoeffall))
         self._ok(self.lib.emd_snap_adjoint(self.h, _dp(g), float(dL_dE), _dp(out)), "emd_snap_adjoint")
         return out
+
+    def lj_request_energy(self):
+        """The next lj_compute also sums the energy it can fuse (emd_lj_request_energy)."""
+        self._ok(self.lib.emd_lj_request_energy(self.h), "emd_lj_request_energy")
+
+    def lj_force_energy(self):
+        """The energy summed by the last lj_compute, or None (emd_lj_force_energy)."""
+        e, ok = _D(), _I()
+        self._ok(self.lib.emd_lj_force_energy(self.h, C.byref(e), C.byref(ok)), "emd_lj_force_energy")
+        return e.value if ok.value else None
 
     def lj_energy_noalloc(self) -> float:
         """emd_lj_energy_noalloc: the same energy, no device allocation."""

@@ -183,6 +183,7 @@ emd_status emd_binning_create(emd_ctx* ctx, double dx_in, double dy_in, double d
     }
   }
   if (sort && n > 0) {
+    c.x_version++;
     // BinSort::sort of x, v, f, type, id, q over the binned range: one
     // fused gather kernel into staging buffers, then copies back
     materialize_zero(c, true, false);

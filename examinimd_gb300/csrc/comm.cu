@@ -137,6 +137,7 @@ emd_status emd_comm_init(emd_ctx* ctx, double comm_depth) {
 
 emd_status emd_comm_exchange(emd_ctx* ctx) {
   EMD_API_BEGIN
+  c.x_version++;
   if (c.N_local == 0) return EMD_OK;
   TimedLaunch t(c, "comm_exchange");
   c.xl_ok &= ~1;

@@ -421,6 +421,7 @@ emd_status emd_system_grow(emd_ctx* ctx, int n_max) {
 emd_status emd_system_set_local(emd_ctx* ctx, int n, const double* x, const double* v, const double* f,
                                 const int* type, const int* id, const double* q) {
   EMD_API_BEGIN
+  c.x_version++;
   c.v_kick_pending = false;  // v and f are replaced
   require(n >= 0 && (n == 0 || (x && type && id)), EMD_ERR_ARG, "emd_system_set_local: x, type, id required");
   for (int i = 0; i < n; ++i)
@@ -456,6 +457,7 @@ emd_status emd_system_set_local(emd_ctx* ctx, int n, const double* x, const doub
 
 emd_status emd_system_update(emd_ctx* ctx, int first, int count, const double* x, const double* v, const double* f) {
   EMD_API_BEGIN
+  if (x) c.x_version++;
   require(first >= 0 && count >= 0 && first + count <= c.N_local, EMD_ERR_ARG, "emd_system_update: range");
   if (count == 0) return EMD_OK;
   materialize_kick(c);

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/emd_gpu.h"
+#include "lj_tile.cuh"
 
 namespace emd {
 
@@ -167,6 +168,13 @@ struct Ctx {
   bool xl_bin_valid = false;     // xl_bin holds the last binning's offsets (not handed to the mixed force)
   bool bin_sorted = false;       // the last binning re-sorted the particles after binning them
   DevBuf<int> abin;         // bin of every particle at the last list build (packed rows)
+  // tiled rows of the mixed form (lj_tile.cuh)
+  bool neigh_tiled = false;
+  int neigh_covered = 0;    // owned atoms with a row (binned into interior bins) at the last build
+  int n_tiles = 0, tile_stage_max = 0;
+  DevBuf<TileDesc> tiles;
+  DevBuf<int> tile_of_bin, tile_colc, tile_flags;
+  DevBuf<int> tile_perm;    // the permutation of the build the tiles index
   DevBuf<float4> xl;        // FP32 bin-relative positions (mixed force)
 
   // ---- LJ
@@ -179,6 +187,17 @@ struct Ctx {
   bool lj_uniform = false;   // every type pair has the same parameters
   float lj_single[3] = {0, 0, 0};
   double lj_single_cutsq_d = 0;
+  double lj_single_d[2] = {0, 0};  // lj1, lj2 of the uniform type pair in FP64
+  // energy of the mixed form fused into the force of the positions it used:
+  // asked for before a compute (emd_lj_request_energy), valid while the
+  // positions have not changed since (x_version)
+  bool lj_energy_request = false;
+  bool lj_pe_fused_valid = false;
+  double lj_pe_fused = 0;
+  unsigned long long lj_pe_fused_version = 0;
+  DevBuf<double> lj_pe_part;
+  // bumped by every call that moves owned positions
+  unsigned long long x_version = 0;
   // mixed form: bin coordinates of every particle at the last list build,
   // packed bx | by << 10 | bz << 20, and that build's bin centre table
   DevBuf<int> bin_c3;
@@ -260,6 +279,7 @@ struct BinCentres {
   }
 };
 BinCentres bin_centres(const Ctx& c);
+TileView tile_view(const Ctx& c);
 void lj_mixed_after_build(Ctx& c);
 void nve_initial_mixed(Ctx& c, bool kick_first);
 void nve_final_mixed(Ctx& c);

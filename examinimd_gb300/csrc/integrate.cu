@@ -74,6 +74,7 @@ extern "C" {
 
 emd_status emd_nve_initial(emd_ctx* ctx) {
   EMD_API_BEGIN
+  c.x_version++;
   if (c.N_local == 0) {
     c.v_kick_pending = false;
     return EMD_OK;

@@ -16,6 +16,7 @@
 #include "emd_device.cuh"
 #include "emd_internal.h"
 #include "lj_pair.cuh"
+#include "lj_tile.cuh"
 #include "neigh_rows.cuh"
 
 namespace emd {
@@ -159,6 +160,236 @@ __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict_
   }
 }
 
+// ---- tiled form (lj_tile.cuh)
+
+// Shifted LJ energy of the single type pair in FP32 terms: a = lj1 / 12 and
+// b = lj2 / 6 as FP32 values plus their FP32 remainders, the shift energy at
+// the cutoff in FP64 (subtracted per atom, once per interacting pair).
+struct LJEnergyF {
+  float a, a_lo, b, b_lo;
+  double ecut;
+};
+
+struct TileForceArgs {
+  const TileDesc* tiles;
+  const int* perm;  // the build's permutation
+  const float4* xl;  // FP32 positions relative to the build's bin centres (w = type bits)
+  const int* c3;     // the build's bin coordinates, bx | by << 10 | bz << 20
+  const double4_32a* x4;
+  double* f;
+  const uint4* rows;  // tiled rows, eight 16-bit entries per granule
+  int stride;
+  const int* num;
+  int n_local;
+  float wx, wy, wz;           // bin widths in FP32 ...
+  float wx_lo, wy_lo, wz_lo;  // ... and what FP32 leaves of them
+  int stage_cap;              // staged slots: the largest stage plus a far-away sentinel
+  LJParamsF P;
+  float cut_lo, cut_hi;  // single type: FP32 decision band around cutsq
+  LJEnergyF E;
+  double* e_part;  // ENERGY: one partial per tile
+};
+
+// Stage of one tile: its particles' FP32 positions relative to their bin
+// centres, x and y moved by the shift between their column and the tile's
+// (exactly the bin width times -1, 0 or 1, carried as an FP32 value and its
+// FP32 remainder), w = bz - bz0 + 1 as a small exact float; the particle index
+// beside it; then one sentinel far outside every cutoff for the unused slots
+// of a row's last granule.
+__device__ __forceinline__ void stage_tile(const TileForceArgs& A, const TileDesc& T, float4* st, int* sidx,
+                                           int* stype) {
+  const int total = T.base[9];
+  for (int s = threadIdx.x; s < total; s += blockDim.x) {
+    int r = 0;
+#pragma unroll
+    for (int q = 1; q < 9; ++q) r += (s >= T.base[q]) ? 1 : 0;
+    const int j = A.perm[T.seg[r] + (s - T.base[r])];
+    float4 p = A.xl[j];
+    const int bz = A.c3[j] >> 20;
+    const float sx = float(r / 3 - 1), sy = float(r % 3 - 1);
+    if (stype) stype[s] = __float_as_int(p.w);
+    p.x = __fmaf_rn(sx, A.wx, __fmaf_rn(sx, A.wx_lo, p.x));
+    p.y = __fmaf_rn(sy, A.wy, __fmaf_rn(sy, A.wy_lo, p.y));
+    p.w = float(bz - T.bz0 + 1);
+    st[s] = p;
+    sidx[s] = j;
+  }
+  if (threadIdx.x == 0) {
+    st[total] = make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0.0f);
+    sidx[total] = -1;
+    if (stype) stype[total] = 0;
+  }
+}
+
+// One pair of a tile row: x_i - x_j from the staged values (the z shift
+// from the two bin indices, exactly -1, 0 or 1 bin width), and r^2.
+struct TileGeo {
+  float2 dxy;
+  float dz, rsq;
+};
+__device__ __forceinline__ TileGeo tile_geo(const float4& xi, const float4& q, float wz, float wz_lo) {
+  TileGeo g;
+  g.dxy = __ffma2_rn(make_float2(q.x, q.y), make_float2(-1.f, -1.f), make_float2(xi.x, xi.y));
+  const float k = __fsub_rn(xi.w, q.w);
+  g.dz = __fmaf_rn(k, wz, __fmaf_rn(k, wz_lo, __fsub_rn(xi.z, q.z)));
+  const float2 sq = __fmul2_rn(g.dxy, g.dxy);
+  g.rsq = __fmaf_rn(g.dz, g.dz, __fadd_rn(sq.x, sq.y));
+  return g;
+}
+
+__device__ __forceinline__ const float4& staged(const float4* st, unsigned off) {
+  return *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(st) + off);
+}
+
+__device__ __forceinline__ uint4 ld_granule(const uint4* p) {
+  uint4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+  return r;
+}
+
+// Per-thread sums of one atom: compensated FP32 force, and for ENERGY the
+// compensated FP32 pair energy and the number of interacting pairs.
+struct TileAcc {
+  Acc f;
+  float es = 0.f, ec = 0.f;
+  int npair = 0;
+  __device__ __forceinline__ void add_e(float v) {
+    const float y = __fsub_rn(v, ec);
+    const float t = __fadd_rn(es, y);
+    ec = __fsub_rn(__fsub_rn(t, es), y);
+    es = t;
+  }
+};
+
+// Four entries of a granule (offsets o[0..3]) for atom i
+template <bool SINGLE, bool ENERGY>
+__device__ __forceinline__ void tile_quad(const TileForceArgs& A, const float4* st, const int* sidx,
+                                          const int* stype, const float4& xi, int i, int ti, const unsigned o[4],
+                                          TileAcc& acc) {
+  TileGeo g[4];
+  float lj1[4], lj2[4];
+  bool in[4], band[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    g[u] = tile_geo(xi, staged(st, o[u]), A.wz, A.wz_lo);
+    if (SINGLE) {
+      lj1[u] = A.P.lj1_0;
+      lj2[u] = A.P.lj2_0;
+      in[u] = g[u].rsq < A.cut_lo;
+      band[u] = g[u].rsq >= A.cut_lo && g[u].rsq <= A.cut_hi;
+    } else {
+      const int tp = ti * A.P.ntypes + stype[o[u] >> 4];
+      lj1[u] = __ldg(A.P.lj1 + tp);
+      lj2[u] = __ldg(A.P.lj2 + tp);
+      const float c = __ldg(A.P.cutsq + tp);
+      in[u] = g[u].rsq < c * (1.0f - LJ_BAND);
+      band[u] = g[u].rsq >= c * (1.0f - LJ_BAND) && g[u].rsq <= c * (1.0f + LJ_BAND);
+    }
+  }
+  if (band[0] || band[1] || band[2] || band[3]) {  // borderline: decide as FP64 does
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (band[u]) {
+        const int tp = SINGLE ? 0 : ti * A.P.ntypes + stype[o[u] >> 4];
+        in[u] = cut_fp64(A.x4, i, sidx[o[u] >> 4], SINGLE ? A.P.cutsq_d0 : __ldg(A.P.cutsq_d + tp));
+      }
+  }
+  float2 sxy = make_float2(0.f, 0.f);
+  float sz = 0.f, se = 0.f;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const float r2inv = in[u] ? rcp_approx(g[u].rsq) : 0.0f;
+    const float r6inv = r2inv * r2inv * r2inv;
+    const float fpair = (r6inv * __fmaf_rn(lj1[u], r6inv, -lj2[u])) * r2inv;
+    sxy = __ffma2_rn(g[u].dxy, make_float2(fpair, fpair), sxy);
+    sz = __fmaf_rn(g[u].dz, fpair, sz);
+    if (ENERGY) {
+      // the reciprocal refined by one Newton step (within about a rounding
+      // of 1/r^2), so the energy terms carry no one-sided bias of the
+      // approximate reciprocal; the force keeps the unrefined value
+      const float r1 = __fmaf_rn(r2inv, __fmaf_rn(-g[u].rsq, r2inv, 1.0f), r2inv);
+      const float r6e = r1 * r1 * r1;
+      se += __fmaf_rn(r6e, __fmaf_rn(A.E.a, r6e, -A.E.b), r6e * __fmaf_rn(A.E.a_lo, r6e, -A.E.b_lo));
+      acc.npair += in[u] ? 1 : 0;
+    }
+  }
+  acc.f.add(sxy, sz);
+  if (ENERGY) acc.add_e(se);
+}
+
+// One CTA per tile: the stage goes to shared memory, then each thread takes
+// one particle of the tile's own bins and walks its row, eight entries per
+// coalesced granule load.
+template <bool SINGLE, bool ZERO, bool ENERGY>
+__global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
+  extern __shared__ float4 smem_stage[];
+  __shared__ TileDesc T;
+  __shared__ double esum[kTileAtoms / 32];
+  if (threadIdx.x < 32) reinterpret_cast<int*>(&T)[threadIdx.x] = reinterpret_cast<const int*>(A.tiles + blockIdx.x)[threadIdx.x];
+  __syncthreads();
+  float4* st = smem_stage;
+  int* sidx = reinterpret_cast<int*>(st + A.stage_cap);
+  int* stype = SINGLE ? nullptr : sidx + A.stage_cap;
+  stage_tile(A, T, st, sidx, stype);
+  __syncthreads();
+  const unsigned sentinel = unsigned(T.base[9]) << 4;
+  double e_thread = 0.0;
+  for (int t = threadIdx.x; t < T.nown; t += blockDim.x) {
+    const int p = T.own0 + t;
+    const int i = sidx[p];
+    if (i >= A.n_local) continue;  // a ghost binned into an interior bin owns no row
+    const float4 xi = st[p];
+    const int ti = SINGLE ? 0 : stype[p];
+    const int cnt = A.num[i];
+    const uint4* q = A.rows + i;
+    const int nfull = cnt >> 3;
+    TileAcc acc;
+    uint4 e = nfull > 0 ? ld_granule(q) : make_uint4(0, 0, 0, 0);
+    for (int kq = 0; kq < nfull; ++kq) {
+      const uint4 en = (kq + 1 < nfull) ? ld_granule(q + (size_t)(kq + 1) * A.stride) : e;
+      const unsigned o0[4] = {e.x & 0xffffu, e.x >> 16, e.y & 0xffffu, e.y >> 16};
+      const unsigned o1[4] = {e.z & 0xffffu, e.z >> 16, e.w & 0xffffu, e.w >> 16};
+      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o0, acc);
+      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o1, acc);
+      e = en;
+    }
+    const int rem = cnt & 7;
+    if (rem) {
+      // the last granule's unused entries read the far-away sentinel
+      const uint4 w = ld_granule(q + (size_t)nfull * A.stride);
+      const unsigned v[8] = {w.x & 0xffffu, w.x >> 16, w.y & 0xffffu, w.y >> 16,
+                             w.z & 0xffffu, w.z >> 16, w.w & 0xffffu, w.w >> 16};
+      unsigned o0[4], o1[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        o0[u] = u < rem ? v[u] : sentinel;
+        o1[u] = u + 4 < rem ? v[u + 4] : sentinel;
+      }
+      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o0, acc);
+      if (rem > 4) tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o1, acc);
+    }
+    const double fx = double(acc.f.sxy.x) - double(acc.f.cxy.x);
+    const double fy = double(acc.f.sxy.y) - double(acc.f.cxy.y);
+    const double fz = double(acc.f.sz) - double(acc.f.cz);
+    if (ZERO) {  // the pending deep_copy(f, 0) folded into the store
+      A.f[3 * i] = 0.0 + fx;
+      A.f[3 * i + 1] = 0.0 + fy;
+      A.f[3 * i + 2] = 0.0 + fz;
+    } else {
+      A.f[3 * i] += fx;
+      A.f[3 * i + 1] += fy;
+      A.f[3 * i + 2] += fz;
+    }
+    if (ENERGY)  // full list: half of every ordered pair's shifted energy
+      e_thread += 0.5 * ((double(acc.es) - double(acc.ec)) - double(acc.npair) * A.E.ecut);
+  }
+  if (ENERGY) {
+    const double t = block_sum(e_thread, esum);
+    if (threadIdx.x == 0) A.e_part[blockIdx.x] = t;
+  }
+}
+
 BinFrame frame(const Ctx& c) {
   BinFrame F;
   F.nby = c.nbin[1];
@@ -221,6 +452,80 @@ void nve_final_mixed(Ctx& c) {
   EMD_CHECK_LAUNCH();
 }
 
+// Launches the tiled force (and, when the caller asked for it before this
+// compute, the fused energy of the same positions).
+static void lj_tile_compute(Ctx& c, bool zero, const LJParamsF& P) {
+  const bool single = c.lj_uniform;
+  const bool energy = c.lj_energy_request && single;
+  if (zero && c.neigh_covered < c.N_local) {
+    // owned atoms outside every tile (outside the interior bins) get no row
+    // and no store from the tiled kernel: clear them the ordinary way
+    materialize_zero(c, true, false);
+    zero = false;
+  }
+  TileForceArgs A;
+  A.tiles = c.tiles.p;
+  A.perm = c.tile_perm.p;
+  A.xl = c.xl.p;
+  A.c3 = c.bin_c3.p;
+  A.x4 = c.x4.p;
+  A.f = c.f.p;
+  A.rows = reinterpret_cast<const uint4*>(c.neigh_kind == EMD_NEIGH_2D ? c.neighs.p : c.neigh_rows2d.p);
+  A.stride = c.neigh_stride;
+  A.num = c.num_neighs.p;
+  A.n_local = c.N_local;
+  const BinFrame F = frame(c);
+  const double w64[3] = {F.wx, F.wy, F.wz};
+  float w32[3], wlo[3];
+  for (int d = 0; d < 3; ++d) {
+    w32[d] = float(w64[d]);
+    wlo[d] = float(w64[d] - double(w32[d]));
+  }
+  A.wx = w32[0];
+  A.wy = w32[1];
+  A.wz = w32[2];
+  A.wx_lo = wlo[0];
+  A.wy_lo = wlo[1];
+  A.wz_lo = wlo[2];
+  A.stage_cap = c.tile_stage_max + 1;
+  A.P = P;
+  A.cut_lo = P.cutsq_0 * (1.0f - LJ_BAND);
+  A.cut_hi = P.cutsq_0 * (1.0f + LJ_BAND);
+  A.E = LJEnergyF{0.f, 0.f, 0.f, 0.f, 0.0};
+  A.e_part = nullptr;
+  if (energy) {
+    const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
+    (void)nt2;
+    const double a64 = c.lj_single_d[0] / 12.0, b64 = c.lj_single_d[1] / 6.0;
+    const double r2c = 1.0 / c.lj_single_cutsq_d, r6c = r2c * r2c * r2c;
+    A.E.a = float(a64);
+    A.E.a_lo = float(a64 - double(A.E.a));
+    A.E.b = float(b64);
+    A.E.b_lo = float(b64 - double(A.E.b));
+    A.E.ecut = r6c * (a64 * r6c - b64);
+    c.lj_pe_part.reserve(size_t(c.n_tiles) + 1, c.stream);
+    A.e_part = c.lj_pe_part.p;
+  }
+  const size_t smem = size_t(A.stage_cap) * (sizeof(float4) + sizeof(int) + (single ? 0 : sizeof(int)));
+  require(smem <= 200 * 1024, EMD_ERR_ARG, "mixed form: a tile's stage exceeds shared memory");
+  using KernelT = void (*)(TileForceArgs);
+  KernelT k;
+  if (single) k = zero ? (energy ? k_lj_tile<true, true, true> : k_lj_tile<true, true, false>)
+                       : (energy ? k_lj_tile<true, false, true> : k_lj_tile<true, false, false>);
+  else k = zero ? k_lj_tile<false, true, false> : k_lj_tile<false, false, false>;
+  if (smem > 48 * 1024) EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  if (c.n_tiles > 0) {
+    TimedLaunch t(c, energy ? "lj_tile_mixed_energy" : "lj_full_mixed");
+    k<<<c.n_tiles, kTileAtoms, smem, c.stream>>>(A);
+    EMD_CHECK_LAUNCH();
+  }
+  if (energy) {
+    c.lj_pe_fused = c.n_tiles > 0 ? device_sum(c, c.lj_pe_part.p, c.n_tiles) : 0.0;
+    c.lj_pe_fused_version = c.x_version;
+    c.lj_pe_fused_valid = true;
+  }
+}
+
 void lj_mixed_compute(Ctx& c) {
   materialize_kick(c);
   const int n_all = c.N_local + c.N_ghost;
@@ -234,6 +539,11 @@ void lj_mixed_compute(Ctx& c) {
   const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
   LJParamsF P{c.lj_params_f.p, c.lj_params_f.p + nt2, c.lj_params_f.p + 2 * nt2, c.lj_params.p + 2 * nt2,
               c.lj_ntypes, c.lj_single[0], c.lj_single[1], c.lj_single[2], c.lj_single_cutsq_d};
+  if (c.neigh_tiled) {
+    lj_tile_compute(c, c.f_zero_pending & 1, P);
+    c.f_zero_pending &= ~1;
+    return;
+  }
   const ListView L = list_view(c);
   const int4* rows4 = reinterpret_cast<const int4*>(L.entries);
   const int n = c.N_local;
@@ -271,6 +581,8 @@ void lj_mixed_prepare(Ctx& c) {
   c.lj_single[1] = hf[nt2];
   c.lj_single[2] = hf[2 * nt2];
   c.lj_single_cutsq_d = h[2 * nt2];
+  c.lj_single_d[0] = h[0];
+  c.lj_single_d[1] = h[nt2];
   c.lj_params_f.reserve(3 * nt2, c.stream);
   EMD_CUDA(cudaMemcpyAsync(c.lj_params_f.p, hf.data(), sizeof(float) * 3 * nt2, cudaMemcpyHostToDevice, c.stream));
   EMD_CUDA(cudaStreamSynchronize(c.stream));

@@ -135,6 +135,9 @@ class Force {
   virtual void init_coeff(int nargs, char** args) = 0;
   virtual void compute(System* system, Binning* binning, Neighbor* neighbor) = 0;
   virtual double compute_energy(System*, Binning*, Neighbor*) { return 0.0; }
+  // the next compute is a thermo step's: a force that can sum the energy
+  // in the same pass is asked to (no reference counterpart)
+  virtual void request_energy() {}
   virtual const char* name() = 0;
 };
 
@@ -151,6 +154,7 @@ class ForceLJNeigh_GB300 : public Force {
   void init_coeff(int nargs, char** args) override;
   void compute(System* system, Binning*, Neighbor*) override;
   double compute_energy(System* system, Binning*, Neighbor*) override;
+  void request_energy() override;
   const char* name() override {
     if (idial_) return half_neigh ? "ForceLJIDialNeighHalf_GB300" : "ForceLJIDialNeighFull_GB300";
     return half_neigh ? "ForceLJNeighHalf_GB300" : "ForceLJNeighFull_GB300";

@@ -141,6 +141,7 @@ void ExaMiniMD::init(int argc, const char* const* argv) {
   neighbor->create_neigh_list(system, binning, force->half_neigh, false);
 
   check(emd_zero_forces(system->ctx), system->ctx, "emd_zero_forces");
+  if (input->thermo_rate > 0) force->request_energy();
   force->compute(system, binning, neighbor);
   if (input->comm_newton) comm->update_force();
 
@@ -214,6 +215,7 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
 
     e = clk.begin();
     check(emd_zero_forces(system->ctx), system->ctx, "emd_zero_forces");
+    if (input->thermo_rate > 0 && step % input->thermo_rate == 0) force->request_energy();
     force->compute(system, binning, neighbor);
     clk.end(B_FORCE, e);
 

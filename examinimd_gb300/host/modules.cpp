@@ -142,8 +142,17 @@ void ForceLJNeigh_GB300::compute(System* system, Binning*, Neighbor*) {
 double ForceLJNeigh_GB300::compute_energy(System* system, Binning*, Neighbor*) {
   if (idial_) return 0.0;  // ForceLJIDialNeigh keeps Force's default (force.h:54)
   double pe = 0.0;
-  check(emd_lj_energy(system->ctx, &pe), system->ctx, "emd_lj_energy");
+  int fused = 0;
+  // the mixed form's thermo steps sum the energy inside the force pass
+  if (precision_ == EMD_PREC_MIXED) check(emd_lj_force_energy(system->ctx, &pe, &fused), system->ctx,
+                                           "emd_lj_force_energy");
+  if (!fused) check(emd_lj_energy(system->ctx, &pe), system->ctx, "emd_lj_energy");
   return pe;
+}
+
+void ForceLJNeigh_GB300::request_energy() {
+  if (precision_ == EMD_PREC_MIXED && !idial_)
+    check(emd_lj_request_energy(system_->ctx), system_->ctx, "emd_lj_request_energy");
 }
 
 // ---------------------------------------------------------------- SNAP

@@ -1,0 +1,118 @@
+"""The tiled mixed-precision LJ force and its fused thermo-step energy (GPU).
+
+Rows of the mixed form address neighbours inside a per-tile stage in shared
+memory (examinimd_gb300/csrc/lj_tile.cuh); the row sets must be the FP64
+reference's (checked through emd_neigh_get elsewhere), forces within the
+mixed tolerance of FP64.  Where a stage would not fit (a very large cutoff)
+the list falls back to packed 32-bit rows with the same guarantees.
+
+The energy summed inside the force pass on request (emd_lj_request_energy)
+is compared with the FP64 energy of the same positions.  Its error is
+rounding of FP32 pair terms with random signs, about 3e-7 / sqrt(N)
+relative for N atoms (the systematic parts -- the FP32 bin width, the
+approximate reciprocal, FP32 coefficients and the cutoff shift -- are
+carried exactly), so the test bounds are 3e-8 at 864 and 4,000 atoms and
+1e-9 at LJ-4M.
+"""
+import numpy as np
+import pytest
+
+from tests import mdloop
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx():
+    from examinimd_gb300 import Context
+    return Context(0)
+
+
+def _rms_rel(a, b):
+    return np.sqrt(np.mean(np.sum((a - b) ** 2, axis=1))) / np.sqrt(np.mean(np.sum(b ** 2, axis=1)))
+
+
+@pytest.mark.parametrize("n,tol", [(6, 3e-8), (10, 3e-8), (100, 1e-9)])
+def test_fused_energy_matches_fp64_energy(n, tol):
+    setup = mdloop.LJSetup(n)
+    state = dict(mdloop.make_lattice(setup, 8))
+    rng = np.random.default_rng(n)
+    state["x"] = np.mod(state["x"] + rng.normal(0.0, 0.03, state["x"].shape), setup.domain[0])
+    mix = _ctx()
+    mdloop.init(mix, setup, state, precision=1)
+    for s in range(1, 4):
+        mdloop.step(mix, setup, s)
+    assert mix.lj_force_energy() is None  # not asked for
+    mix.zero_forces()
+    mix.lj_request_energy()
+    mix.lj_compute()
+    fused = mix.lj_force_energy()
+    exact = mix.lj_energy()  # FP64 over the same list and positions
+    assert fused is not None
+    assert abs(fused - exact) <= tol * abs(exact), (fused, exact, (fused - exact) / exact)
+    # the request served one compute only; a moved position retires the value
+    mix.lj_compute()
+    assert mix.lj_force_energy() is None
+    mix.lj_request_energy()
+    mix.lj_compute()
+    assert mix.lj_force_energy() is not None
+    mix.nve_initial()
+    assert mix.lj_force_energy() is None
+    mix.close()
+
+
+def test_fused_energy_does_not_change_the_forces():
+    """A compute with the energy gives the same force bits as one without."""
+    setup = mdloop.LJSetup(8)
+    state = mdloop.make_lattice(setup)
+    a, b = _ctx(), _ctx()
+    for c in (a, b):
+        mdloop.init(c, setup, state, precision=1)
+        for s in range(1, 25):
+            if c is b and s % 5 == 0:
+                c.lj_request_energy()
+            mdloop.step(c, setup, s)
+    nl = a.info()[0]
+    ga, gb = a.get(0, nl), b.get(0, nl)
+    for k in ("x", "v", "f"):
+        np.testing.assert_array_equal(ga[k], gb[k])
+
+
+def test_driver_thermo_uses_the_fused_energy(tmp_path):
+    """The driver asks for the energy on thermo steps: its thermo PE in the
+    mixed form stays within the fused-energy bound of the FP64 value."""
+    from examinimd_gb300 import MD
+    from tests.golden.decks import CASES, write_case
+    case = dict(CASES["lj_fcc6_full_csr"])
+    deck, args = write_case(case, str(tmp_path))
+    md = MD(["-il", deck, "--quiet", "--precision", "mixed"] + args)
+    md.run(20)  # thermo every 10: step 20 asked for the energy
+    assert md.ctx.lj_force_energy() is not None
+    T, pe, ke = md.thermo(recompute=True)
+    exact = md.ctx.lj_energy() / md.info()["N_local"]
+    assert abs(pe - exact) <= 3e-8 * abs(exact)
+    md.close()
+
+
+def test_large_cutoff_falls_back_to_packed_rows():
+    """rc = 6: a single bin's stencil holds more particles than a tile stage,
+    so the list uses packed rows; rows equal the oracle's, forces within the
+    mixed tolerance of FP64."""
+    from oracle.orc import Oracle
+    setup = mdloop.LJSetup(12, cut=6.0, skin=0.3, coeffs=[(1, 1, 1.0, 1.0, 6.0)])
+    state = dict(mdloop.make_lattice(setup))
+    rng = np.random.default_rng(4)
+    state["x"] = np.mod(state["x"] + rng.normal(0.0, 0.03, state["x"].shape), setup.domain[0])
+    mix, ref, orc = _ctx(), _ctx(), Oracle(8)
+    tm = mdloop.init(mix, setup, state, precision=1)
+    mdloop.init(ref, setup, state)
+    to = mdloop.init(orc, setup, state)
+    assert tm == to
+    for x, y in zip(mix.neigh_get(tm), orc.neigh_get(to)):
+        np.testing.assert_array_equal(x, y)
+    nl = ref.info()[0]
+    assert _rms_rel(mix.get(0, nl)["f"], ref.get(0, nl)["f"]) <= 1e-5
+    # the fused energy needs tiles: not offered here
+    mix.zero_forces()
+    mix.lj_request_energy()
+    mix.lj_compute()
+    assert mix.lj_force_energy() is None
