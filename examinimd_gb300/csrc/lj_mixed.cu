@@ -192,12 +192,20 @@ struct TileForceArgs {
 
 // Stage of one tile: its particles' FP32 positions relative to their bin
 // centres, x and y moved by the shift between their column and the tile's
-// (exactly the bin width times -1, 0 or 1, carried as an FP32 value and its
-// FP32 remainder), w = bz - bz0 + 1 as a small exact float; the particle index
-// beside it; then one sentinel far outside every cutoff for the unused slots
-// of a row's last granule.
+// (the FP32 bin width times -1, 0 or 1, one rounding), w = bz - bz0 + 1 as a
+// small exact float; the particle index beside it; then one sentinel far
+// outside every cutoff for the unused slots of a row's last granule.  For
+// the fused energy (sig != null) also the exact remainder of each shifted
+// x and y against x + k w in FP64 bin widths, as an FP32 pair.
+__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
+  // Knuth's two-sum: a + b - s exactly, for s = fl(a + b)
+  const float bv = __fsub_rn(s, a);
+  const float av = __fsub_rn(s, bv);
+  return __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+
 __device__ __forceinline__ void stage_tile(const TileForceArgs& A, const TileDesc& T, float4* st, int* sidx,
-                                           int* stype) {
+                                           int* stype, float2* sig) {
   const int total = T.base[9];
   for (int s = threadIdx.x; s < total; s += blockDim.x) {
     int r = 0;
@@ -208,8 +216,12 @@ __device__ __forceinline__ void stage_tile(const TileForceArgs& A, const TileDes
     const int bz = A.c3[j] >> 20;
     const float sx = float(r / 3 - 1), sy = float(r % 3 - 1);
     if (stype) stype[s] = __float_as_int(p.w);
-    p.x = __fmaf_rn(sx, A.wx, __fmaf_rn(sx, A.wx_lo, p.x));
-    p.y = __fmaf_rn(sy, A.wy, __fmaf_rn(sy, A.wy_lo, p.y));
+    const float xs = __fmaf_rn(sx, A.wx, p.x), ys = __fmaf_rn(sy, A.wy, p.y);
+    if (sig)
+      sig[s] = make_float2(__fmaf_rn(sx, A.wx_lo, two_sum_err(p.x, sx * A.wx, xs)),
+                           __fmaf_rn(sy, A.wy_lo, two_sum_err(p.y, sy * A.wy, ys)));
+    p.x = xs;
+    p.y = ys;
     p.w = float(bz - T.bz0 + 1);
     st[s] = p;
     sidx[s] = j;
@@ -218,20 +230,23 @@ __device__ __forceinline__ void stage_tile(const TileForceArgs& A, const TileDes
     st[total] = make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0.0f);
     sidx[total] = -1;
     if (stype) stype[total] = 0;
+    if (sig) sig[total] = make_float2(0.f, 0.f);
   }
 }
 
 // One pair of a tile row: x_i - x_j from the staged values (the z shift
-// from the two bin indices, exactly -1, 0 or 1 bin width), and r^2.
+// from the two bin indices, exactly -1, 0 or 1 FP32 bin width), and r^2.
 struct TileGeo {
   float2 dxy;
   float dz, rsq;
+  float tz, kz;  // the z difference before its shift, and the shift in bins
 };
-__device__ __forceinline__ TileGeo tile_geo(const float4& xi, const float4& q, float wz, float wz_lo) {
+__device__ __forceinline__ TileGeo tile_geo(const float4& xi, const float4& q, float wz) {
   TileGeo g;
   g.dxy = __ffma2_rn(make_float2(q.x, q.y), make_float2(-1.f, -1.f), make_float2(xi.x, xi.y));
-  const float k = __fsub_rn(xi.w, q.w);
-  g.dz = __fmaf_rn(k, wz, __fmaf_rn(k, wz_lo, __fsub_rn(xi.z, q.z)));
+  g.kz = __fsub_rn(xi.w, q.w);
+  g.tz = __fsub_rn(xi.z, q.z);
+  g.dz = __fmaf_rn(g.kz, wz, g.tz);
   const float2 sq = __fmul2_rn(g.dxy, g.dxy);
   g.rsq = __fmaf_rn(g.dz, g.dz, __fadd_rn(sq.x, sq.y));
   return g;
@@ -262,17 +277,28 @@ struct TileAcc {
   }
 };
 
-// Four entries of a granule (offsets o[0..3]) for atom i
+// Four entries of a granule (offsets o[0..3]) for atom i.
+//
+// ENERGY: the FP32 r^2 of a pair is biased, not just noisy: the bin shifts
+// added to grid-aligned FP32 coordinates round the same way pair after pair
+// (about 1e-8 relative in the energy of an fcc liquid).  So the energy takes
+// the exact difference dx + lo, lo from two-sum remainders of the pair's
+// subtraction and z shift and from the stage's remainders, and evaluates
+// e(r^2) + e'(r^2) * 2 (dx . lo): the correction lies below the rounding of
+// r^2 and would vanish if added to r^2 in FP32.  The reciprocal is refined by
+// one Newton step, the coefficients carry their FP32 remainders, and the
+// cutoff shift is subtracted per atom in FP64, so what is left is rounding
+// with random signs.  The forces are the ones of the force-only kernel.
 template <bool SINGLE, bool ENERGY>
 __device__ __forceinline__ void tile_quad(const TileForceArgs& A, const float4* st, const int* sidx,
-                                          const int* stype, const float4& xi, int i, int ti, const unsigned o[4],
-                                          TileAcc& acc) {
+                                          const int* stype, const float2* sig, const float4& xi, int i, int ti,
+                                          const unsigned o[4], TileAcc& acc) {
   TileGeo g[4];
   float lj1[4], lj2[4];
   bool in[4], band[4];
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
-    g[u] = tile_geo(xi, staged(st, o[u]), A.wz, A.wz_lo);
+    g[u] = tile_geo(xi, staged(st, o[u]), A.wz);
     if (SINGLE) {
       lj1[u] = A.P.lj1_0;
       lj2[u] = A.P.lj2_0;
@@ -305,12 +331,21 @@ __device__ __forceinline__ void tile_quad(const TileForceArgs& A, const float4* 
     sxy = __ffma2_rn(g[u].dxy, make_float2(fpair, fpair), sxy);
     sz = __fmaf_rn(g[u].dz, fpair, sz);
     if (ENERGY) {
-      // the reciprocal refined by one Newton step (within about a rounding
-      // of 1/r^2), so the energy terms carry no one-sided bias of the
-      // approximate reciprocal; the force keeps the unrefined value
+      const float4& q = staged(st, o[u]);
+      const float2 sg = sig[o[u] >> 4];
+      const float lox = __fsub_rn(two_sum_err(xi.x, -q.x, g[u].dxy.x), sg.x);
+      const float loy = __fsub_rn(two_sum_err(xi.y, -q.y, g[u].dxy.y), sg.y);
+      const float kw = g[u].kz * A.wz;
+      const float loz = __fmaf_rn(g[u].kz, A.wz_lo,
+                                  __fadd_rn(two_sum_err(xi.z, -q.z, g[u].tz), two_sum_err(g[u].tz, kw, g[u].dz)));
+      const float corr =
+          2.0f * __fmaf_rn(g[u].dz, loz, __fmaf_rn(g[u].dxy.y, loy, g[u].dxy.x * lox));  // r^2 - fl(r^2), first order
       const float r1 = __fmaf_rn(r2inv, __fmaf_rn(-g[u].rsq, r2inv, 1.0f), r2inv);
       const float r6e = r1 * r1 * r1;
-      se += __fmaf_rn(r6e, __fmaf_rn(A.E.a, r6e, -A.E.b), r6e * __fmaf_rn(A.E.a_lo, r6e, -A.E.b_lo));
+      const float e = __fmaf_rn(r6e, __fmaf_rn(A.E.a, r6e, -A.E.b), r6e * __fmaf_rn(A.E.a_lo, r6e, -A.E.b_lo));
+      // de/d(r^2) = -r^-2 r^-6 (6 a r^-6 - 3 b)
+      const float de = -(r1 * r6e) * __fmaf_rn(6.0f * A.E.a, r6e, -3.0f * A.E.b);
+      se += __fmaf_rn(de, corr, e);
       acc.npair += in[u] ? 1 : 0;
     }
   }
@@ -331,7 +366,8 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
   float4* st = smem_stage;
   int* sidx = reinterpret_cast<int*>(st + A.stage_cap);
   int* stype = SINGLE ? nullptr : sidx + A.stage_cap;
-  stage_tile(A, T, st, sidx, stype);
+  float2* sig = ENERGY ? reinterpret_cast<float2*>(sidx + A.stage_cap) : nullptr;
+  stage_tile(A, T, st, sidx, stype, sig);
   __syncthreads();
   const unsigned sentinel = unsigned(T.base[9]) << 4;
   double e_thread = 0.0;
@@ -350,8 +386,8 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
       const uint4 en = (kq + 1 < nfull) ? ld_granule(q + (size_t)(kq + 1) * A.stride) : e;
       const unsigned o0[4] = {e.x & 0xffffu, e.x >> 16, e.y & 0xffffu, e.y >> 16};
       const unsigned o1[4] = {e.z & 0xffffu, e.z >> 16, e.w & 0xffffu, e.w >> 16};
-      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o0, acc);
-      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o1, acc);
+      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o0, acc);
+      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o1, acc);
       e = en;
     }
     const int rem = cnt & 7;
@@ -366,8 +402,8 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
         o0[u] = u < rem ? v[u] : sentinel;
         o1[u] = u + 4 < rem ? v[u + 4] : sentinel;
       }
-      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o0, acc);
-      if (rem > 4) tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, xi, i, ti, o1, acc);
+      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o0, acc);
+      if (rem > 4) tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o1, acc);
     }
     const double fx = double(acc.f.sxy.x) - double(acc.f.cxy.x);
     const double fy = double(acc.f.sxy.y) - double(acc.f.cxy.y);
@@ -506,7 +542,8 @@ static void lj_tile_compute(Ctx& c, bool zero, const LJParamsF& P) {
     c.lj_pe_part.reserve(size_t(c.n_tiles) + 1, c.stream);
     A.e_part = c.lj_pe_part.p;
   }
-  const size_t smem = size_t(A.stage_cap) * (sizeof(float4) + sizeof(int) + (single ? 0 : sizeof(int)));
+  const size_t smem =
+      size_t(A.stage_cap) * (sizeof(float4) + sizeof(int) + (single ? 0 : sizeof(int)) + (energy ? sizeof(float2) : 0));
   require(smem <= 200 * 1024, EMD_ERR_ARG, "mixed form: a tile's stage exceeds shared memory");
   using KernelT = void (*)(TileForceArgs);
   KernelT k;
