@@ -44,15 +44,23 @@ __global__ void __launch_bounds__(256) k_bin_centres(const int* __restrict__ abi
   c3[a] = bx | (by << 10) | (bz << 20);
 }
 
-__device__ __forceinline__ float4 rel(const double4_32a& p, const double4_32a& o) {
-  return make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(int(p.w)));
-}
-
 __global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restrict__ x4, BinCentres ctr, int n,
-                                                    float4* __restrict__ xl) {
+                                                    XlOut out) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
-  xl[a] = rel(x4[a], ctr.at(a));
+  const double4_32a p = x4[a], o = ctr.at(a);
+  out.put(a, float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), int(p.w), ctr.c3[a]);
+}
+
+// At a tiled build: the binning's FP32 offsets (particle order, w = type)
+// into permutation order, w = type << 10 | bz
+__global__ void __launch_bounds__(256) k_xlb_from_bins(const float4* __restrict__ xl, const int* __restrict__ perm,
+                                                       const int* __restrict__ c3, int n, float4* __restrict__ xlb) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int i = perm[p];
+  const float4 v = xl[i];
+  xlb[p] = make_float4(v.x, v.y, v.z, __int_as_float((__float_as_int(v.w) << 10) | (c3[i] >> 20)));
 }
 
 // IntegratorNVE::initial_integrate (integrator_nve.cpp:64-73) with FMA, plus
@@ -61,7 +69,7 @@ template <bool KICK>
 __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restrict__ x4, double* __restrict__ v,
                                                            const double* __restrict__ f, const int* __restrict__ type,
                                                            const double* __restrict__ dtfm_t, double dtv,
-                                                           BinCentres ctr, float4* __restrict__ xl, int n) {
+                                                           BinCentres ctr, XlOut out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int ti = type[i];
@@ -83,9 +91,9 @@ __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restri
   p.y = fma(dtv, vy, p.y);
   p.z = fma(dtv, vz, p.z);
   x4[i] = p;
-  if (xl) {  // the type from the int array: converting x4.w would cost an FP64-pipe instruction
+  if (out.xl || out.xlb) {  // the type from the int array: converting x4.w would cost an FP64-pipe instruction
     const double4_32a o = ctr.at(i);
-    xl[i] = make_float4(float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), __int_as_float(ti));
+    out.put(i, float(p.x - o.x), float(p.y - o.y), float(p.z - o.z), ti, ctr.c3[i]);
   }
 }
 
@@ -172,9 +180,8 @@ struct LJEnergyF {
 
 struct TileForceArgs {
   const TileDesc* tiles;
-  const int* perm;  // the build's permutation
-  const float4* xl;  // FP32 positions relative to the build's bin centres (w = type bits)
-  const int* c3;     // the build's bin coordinates, bx | by << 10 | bz << 20
+  const int* perm;    // the build's permutation
+  const float4* xlb;  // FP32 positions relative to the build's bin centres in permutation order, w = type << 10 | bz
   const double4_32a* x4;
   double* f;
   const uint4* rows;  // tiled rows, eight 16-bit entries per granule
@@ -191,12 +198,13 @@ struct TileForceArgs {
 };
 
 // Stage of one tile: its particles' FP32 positions relative to their bin
-// centres, x and y moved by the shift between their column and the tile's
-// (the FP32 bin width times -1, 0 or 1, one rounding), w = bz - bz0 + 1 as a
-// small exact float; the particle index beside it; then one sentinel far
-// outside every cutoff for the unused slots of a row's last granule.  For
-// the fused energy (sig != null) also the exact remainder of each shifted
-// x and y against x + k w in FP64 bin widths, as an FP32 pair.
+// centres -- nine contiguous ranges of the permutation-ordered copy, read
+// four float4 per thread at a time -- with x and y moved by the shift between
+// their column and the tile's (the FP32 bin width times -1, 0 or 1, one
+// rounding) and w = bz - bz0 + 1 as a small exact float; then a sentinel far
+// outside every cutoff for the unused slots of a row's last granule.  For the
+// fused energy (sig != null) also the exact remainder of each shifted x and
+// y against x + k w in FP64 bin widths, as an FP32 pair.
 __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
   // Knuth's two-sum: a + b - s exactly, for s = fl(a + b)
   const float bv = __fsub_rn(s, a);
@@ -204,31 +212,57 @@ __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
   return __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
 }
 
-__device__ __forceinline__ void stage_tile(const TileForceArgs& A, const TileDesc& T, float4* st, int* sidx,
-                                           int* stype, float2* sig) {
-  const int total = T.base[9];
-  for (int s = threadIdx.x; s < total; s += blockDim.x) {
-    int r = 0;
+// segment of stage slot s (the segments are contiguous and in order)
+__device__ __forceinline__ int stage_segment(const TileDesc& T, int s) {
+  int r = 0;
 #pragma unroll
-    for (int q = 1; q < 9; ++q) r += (s >= T.base[q]) ? 1 : 0;
-    const int j = A.perm[T.seg[r] + (s - T.base[r])];
-    float4 p = A.xl[j];
-    const int bz = A.c3[j] >> 20;
-    const float sx = float(r / 3 - 1), sy = float(r % 3 - 1);
-    if (stype) stype[s] = __float_as_int(p.w);
-    const float xs = __fmaf_rn(sx, A.wx, p.x), ys = __fmaf_rn(sy, A.wy, p.y);
-    if (sig)
-      sig[s] = make_float2(__fmaf_rn(sx, A.wx_lo, two_sum_err(p.x, sx * A.wx, xs)),
-                           __fmaf_rn(sy, A.wy_lo, two_sum_err(p.y, sy * A.wy, ys)));
-    p.x = xs;
-    p.y = ys;
-    p.w = float(bz - T.bz0 + 1);
-    st[s] = p;
-    sidx[s] = j;
+  for (int q = 1; q < 9; ++q) r += (s >= T.base[q]) ? 1 : 0;
+  return r;
+}
+
+// the particle in stage slot s (rare paths: band re-tests)
+__device__ __forceinline__ int stage_particle(const TileForceArgs& A, const TileDesc& T, int s) {
+  const int r = stage_segment(T, s);
+  return A.perm[T.seg[r] + (s - T.base[r])];
+}
+
+__device__ __forceinline__ void stage_tile(const TileForceArgs& A, const TileDesc& T, float4* st, int* stype,
+                                           float2* sig) {
+  constexpr int U = 4;
+  const int total = T.base[9];
+  for (int s0 = threadIdx.x; s0 < total; s0 += U * blockDim.x) {
+    float4 v[U];
+    int rr[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int s = s0 + u * blockDim.x;
+      rr[u] = 0;
+      if (s < total) {
+        rr[u] = stage_segment(T, s);
+        v[u] = __ldg(A.xlb + T.seg[rr[u]] + (s - T.base[rr[u]]));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int s = s0 + u * blockDim.x;
+      if (s >= total) break;
+      const int r = rr[u];
+      float4 p = v[u];
+      const int bits = __float_as_int(p.w);
+      const float sx = float(r / 3 - 1), sy = float(r % 3 - 1);
+      if (stype) stype[s] = bits >> 10;
+      const float xs = __fmaf_rn(sx, A.wx, p.x), ys = __fmaf_rn(sy, A.wy, p.y);
+      if (sig)
+        sig[s] = make_float2(__fmaf_rn(sx, A.wx_lo, two_sum_err(p.x, sx * A.wx, xs)),
+                             __fmaf_rn(sy, A.wy_lo, two_sum_err(p.y, sy * A.wy, ys)));
+      p.x = xs;
+      p.y = ys;
+      p.w = float((bits & 1023) - T.bz0 + 1);
+      st[s] = p;
+    }
   }
   if (threadIdx.x == 0) {
     st[total] = make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0.0f);
-    sidx[total] = -1;
     if (stype) stype[total] = 0;
     if (sig) sig[total] = make_float2(0.f, 0.f);
   }
@@ -290,7 +324,7 @@ struct TileAcc {
 // cutoff shift is subtracted per atom in FP64, so what is left is rounding
 // with random signs.  The forces are the ones of the force-only kernel.
 template <bool SINGLE, bool ENERGY>
-__device__ __forceinline__ void tile_quad(const TileForceArgs& A, const float4* st, const int* sidx,
+__device__ __forceinline__ void tile_quad(const TileForceArgs& A, const TileDesc& T, const float4* st,
                                           const int* stype, const float2* sig, const float4& xi, int i, int ti,
                                           const unsigned o[4], TileAcc& acc) {
   TileGeo g[4];
@@ -318,7 +352,7 @@ __device__ __forceinline__ void tile_quad(const TileForceArgs& A, const float4* 
     for (int u = 0; u < 4; ++u)
       if (band[u]) {
         const int tp = SINGLE ? 0 : ti * A.P.ntypes + stype[o[u] >> 4];
-        in[u] = cut_fp64(A.x4, i, sidx[o[u] >> 4], SINGLE ? A.P.cutsq_d0 : __ldg(A.P.cutsq_d + tp));
+        in[u] = cut_fp64(A.x4, i, stage_particle(A, T, int(o[u] >> 4)), SINGLE ? A.P.cutsq_d0 : __ldg(A.P.cutsq_d + tp));
       }
   }
   float2 sxy = make_float2(0.f, 0.f);
@@ -363,17 +397,19 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
   __shared__ double esum[kTileAtoms / 32];
   if (threadIdx.x < 32) reinterpret_cast<int*>(&T)[threadIdx.x] = reinterpret_cast<const int*>(A.tiles + blockIdx.x)[threadIdx.x];
   __syncthreads();
+  // shared arrays in order of alignment: float4 stage, float2 remainders
+  // (ENERGY), int types (several types)
   float4* st = smem_stage;
-  int* sidx = reinterpret_cast<int*>(st + A.stage_cap);
-  int* stype = SINGLE ? nullptr : sidx + A.stage_cap;
-  float2* sig = ENERGY ? reinterpret_cast<float2*>(sidx + A.stage_cap) : nullptr;
-  stage_tile(A, T, st, sidx, stype, sig);
+  float2* sig = ENERGY ? reinterpret_cast<float2*>(st + A.stage_cap) : nullptr;
+  int* stype = SINGLE ? nullptr
+                      : (ENERGY ? reinterpret_cast<int*>(sig + A.stage_cap) : reinterpret_cast<int*>(st + A.stage_cap));
+  stage_tile(A, T, st, stype, sig);
   __syncthreads();
   const unsigned sentinel = unsigned(T.base[9]) << 4;
   double e_thread = 0.0;
   for (int t = threadIdx.x; t < T.nown; t += blockDim.x) {
     const int p = T.own0 + t;
-    const int i = sidx[p];
+    const int i = A.perm[T.seg[4] + (p - T.base[4])];
     if (i >= A.n_local) continue;  // a ghost binned into an interior bin owns no row
     const float4 xi = st[p];
     const int ti = SINGLE ? 0 : stype[p];
@@ -386,8 +422,8 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
       const uint4 en = (kq + 1 < nfull) ? ld_granule(q + (size_t)(kq + 1) * A.stride) : e;
       const unsigned o0[4] = {e.x & 0xffffu, e.x >> 16, e.y & 0xffffu, e.y >> 16};
       const unsigned o1[4] = {e.z & 0xffffu, e.z >> 16, e.w & 0xffffu, e.w >> 16};
-      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o0, acc);
-      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o1, acc);
+      tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o0, acc);
+      tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o1, acc);
       e = en;
     }
     const int rem = cnt & 7;
@@ -402,8 +438,8 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
         o0[u] = u < rem ? v[u] : sentinel;
         o1[u] = u + 4 < rem ? v[u + 4] : sentinel;
       }
-      tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o0, acc);
-      if (rem > 4) tile_quad<SINGLE, ENERGY>(A, st, sidx, stype, sig, xi, i, ti, o1, acc);
+      tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o0, acc);
+      if (rem > 4) tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o1, acc);
     }
     const double fx = double(acc.f.sxy.x) - double(acc.f.cxy.x);
     const double fy = double(acc.f.sxy.y) - double(acc.f.cxy.y);
@@ -458,13 +494,28 @@ void lj_mixed_after_build(Ctx& c) {
   c.ctr_tab.reserve(size_t(ntab), c.stream);
   EMD_CUDA(cudaMemcpyAsync(c.ctr_tab.p, c.bin_ctab.p, sizeof(double) * ntab, cudaMemcpyDeviceToDevice, c.stream));
   for (int d = 0; d < 3; ++d) c.ctr_nb[d] = c.nbin[d];
-  TimedLaunch t(c, "lj_bin_centres");
-  k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, c.nbin[1], c.nbin[2], c.bin_c3.p);
-  EMD_CHECK_LAUNCH();
+  {
+    TimedLaunch t(c, "lj_bin_centres");
+    k_bin_centres<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.abin.p, n_all, c.nbin[1], c.nbin[2], c.bin_c3.p);
+    EMD_CHECK_LAUNCH();
+  }
+  if (c.neigh_tiled && n_all > 0) {
+    c.xlb.reserve(size_t(n_all) + 1, c.stream);
+    TimedLaunch t(c, "lj_xlb_from_bins");
+    k_xlb_from_bins<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.xl.p, c.tile_perm.p, c.bin_c3.p, n_all,
+                                                                  c.xlb.p);
+    EMD_CHECK_LAUNCH();
+  }
   c.xl_ok = 3;
 }
 
 BinCentres bin_centres(const Ctx& c) { return BinCentres{c.bin_c3.p, c.ctr_tab.p, c.ctr_nb[0], c.ctr_nb[1]}; }
+
+XlOut xl_out(const Ctx& c, bool live) {
+  if (!live) return XlOut{nullptr, nullptr, nullptr};
+  if (c.neigh_tiled) return XlOut{nullptr, c.xlb.p, c.tile_pos.p};
+  return XlOut{c.xl.p, nullptr, nullptr};
+}
 
 bool mixed_xl_active(const Ctx& c) {
   return c.lj_ready && c.lj_prec == EMD_PREC_MIXED && c.neigh_ready && c.neigh_packed;
@@ -476,7 +527,7 @@ void nve_initial_mixed(Ctx& c, bool kick_first) {
   auto k = kick_first ? k_nve_initial_mixed<true> : k_nve_initial_mixed<false>;
   k<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p,
                                                        c.dtfm_d.p + (kick_first ? c.ntypes : 0), c.dt,
-                                                       bin_centres(c), live ? c.xl.p : nullptr,
+                                                       bin_centres(c), xl_out(c, live),
                                                        c.N_local);
   EMD_CHECK_LAUNCH();
   if (!live) c.xl_ok &= ~1;
@@ -502,8 +553,7 @@ static void lj_tile_compute(Ctx& c, bool zero, const LJParamsF& P) {
   TileForceArgs A;
   A.tiles = c.tiles.p;
   A.perm = c.tile_perm.p;
-  A.xl = c.xl.p;
-  A.c3 = c.bin_c3.p;
+  A.xlb = c.xlb.p;
   A.x4 = c.x4.p;
   A.f = c.f.p;
   A.rows = reinterpret_cast<const uint4*>(c.neigh_kind == EMD_NEIGH_2D ? c.neighs.p : c.neigh_rows2d.p);
@@ -543,7 +593,7 @@ static void lj_tile_compute(Ctx& c, bool zero, const LJParamsF& P) {
     A.e_part = c.lj_pe_part.p;
   }
   const size_t smem =
-      size_t(A.stage_cap) * (sizeof(float4) + sizeof(int) + (single ? 0 : sizeof(int)) + (energy ? sizeof(float2) : 0));
+      size_t(A.stage_cap) * (sizeof(float4) + (single ? 0 : sizeof(int)) + (energy ? sizeof(float2) : 0));
   require(smem <= 200 * 1024, EMD_ERR_ARG, "mixed form: a tile's stage exceeds shared memory");
   using KernelT = void (*)(TileForceArgs);
   KernelT k;
@@ -569,7 +619,7 @@ void lj_mixed_compute(Ctx& c) {
   const BinFrame F = frame(c);
   if (c.xl_ok != 3) {
     TimedLaunch t(c, "lj_refresh_xl");
-    k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, c.xl.p);
+    k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, xl_out(c, true));
     EMD_CHECK_LAUNCH();
     c.xl_ok = 3;
   }

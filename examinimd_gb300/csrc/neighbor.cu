@@ -312,6 +312,12 @@ __global__ void k_unpack(int* __restrict__ e, long long n) {
   if (t < n) e[t] = e[t] >> 6;
 }
 
+// slot of every particle in the permutation
+__global__ void __launch_bounds__(256) k_inverse_perm(const int* __restrict__ perm, int n, int* __restrict__ pos) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) pos[perm[p]] = p;
+}
+
 // tiled rows -> CSR rows of plain j at offs[i] (for emd_neigh_get)
 __global__ void __launch_bounds__(256) k_tiled_rows_to_csr(TileView V, const int* __restrict__ num,
                                                            const int* __restrict__ offs, int n, int* __restrict__ out) {
@@ -451,8 +457,13 @@ static bool build_tiles(Ctx& c) {
   c.n_tiles = ntiles;
   const int n_all = c.N_local + c.N_ghost;
   c.tile_perm.reserve(size_t(n_all) + 1, c.stream);
-  if (n_all > 0)
+  c.tile_pos.reserve(size_t(n_all) + 1, c.stream);
+  if (n_all > 0) {
     EMD_CUDA(cudaMemcpyAsync(c.tile_perm.p, c.permute.p, sizeof(int) * n_all, cudaMemcpyDeviceToDevice, c.stream));
+    TimedLaunch t(c, "neigh_tiles");
+    k_inverse_perm<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.tile_perm.p, n_all, c.tile_pos.p);
+    EMD_CHECK_LAUNCH();
+  }
   return true;
 }
 
