@@ -192,7 +192,7 @@ struct TileForceArgs {
   float wx_lo, wy_lo, wz_lo;  // ... and what FP32 leaves of them
   int stage_cap;              // staged slots: the largest stage plus a far-away sentinel
   LJParamsF P;
-  float cut_lo, cut_hi;  // single type: FP32 decision band around cutsq
+  float band_w;  // single type: half width of the FP32 guard band around cutsq
   LJEnergyF E;
   double* e_part;  // ENERGY: one partial per tile
 };
@@ -286,8 +286,10 @@ __device__ __forceinline__ TileGeo tile_geo(const float4& xi, const float4& q, f
   return g;
 }
 
-__device__ __forceinline__ const float4& staged(const float4* st, unsigned off) {
-  return *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(st) + off);
+// a staged float4 at a byte offset (always a multiple of 16: one 16-byte
+// shared load)
+__device__ __forceinline__ float4 staged(const float4* st, unsigned off) {
+  return *static_cast<const float4*>(__builtin_assume_aligned(reinterpret_cast<const char*>(st) + off, 16));
 }
 
 __device__ __forceinline__ uint4 ld_granule(const uint4* p) {
@@ -311,8 +313,73 @@ struct TileAcc {
   }
 };
 
-// Four entries of a granule (offsets o[0..3]) for atom i.
-//
+// Four entries of a granule: geometry, coefficients and the FP32 decision.
+// A pair whose FP32 r^2 lies within the guard band of its cutoff is marked
+// near: only FP64 decides it the way the reference does.
+template <bool SINGLE>
+struct Quad {
+  TileGeo g[4];
+  float lj1[4], lj2[4];
+  bool in[4], near[4];
+};
+
+template <bool SINGLE>
+__device__ __forceinline__ bool quad_geo(const TileForceArgs& A, const float4* st, const int* stype,
+                                         const float4& xi, int ti, const unsigned o[4], Quad<SINGLE>& Q) {
+  bool any = false;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    Q.g[u] = tile_geo(xi, staged(st, o[u]), A.wz);
+    float c, bw;
+    if (SINGLE) {
+      Q.lj1[u] = A.P.lj1_0;
+      Q.lj2[u] = A.P.lj2_0;
+      c = A.P.cutsq_0;
+      bw = A.band_w;
+    } else {
+      const int tp = ti * A.P.ntypes + stype[o[u] >> 4];
+      Q.lj1[u] = __ldg(A.P.lj1 + tp);
+      Q.lj2[u] = __ldg(A.P.lj2 + tp);
+      c = __ldg(A.P.cutsq + tp);
+      bw = c * LJ_BAND;
+    }
+    const float d = __fsub_rn(Q.g[u].rsq, c);
+    Q.in[u] = d < 0.0f;
+    Q.near[u] = fabsf(d) <= bw;
+    any = any | Q.near[u];
+  }
+  return any;
+}
+
+// the near pairs of a quad decided in FP64, as the reference decides them
+template <bool SINGLE>
+__device__ __forceinline__ void quad_exact(const TileForceArgs& A, const TileDesc& T, const int* stype, int i, int ti,
+                                           const unsigned o[4], Quad<SINGLE>& Q) {
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    if (Q.near[u]) {
+      const int tp = SINGLE ? 0 : ti * A.P.ntypes + stype[o[u] >> 4];
+      Q.in[u] = cut_fp64(A.x4, i, stage_particle(A, T, int(o[u] >> 4)), SINGLE ? A.P.cutsq_d0 : __ldg(A.P.cutsq_d + tp));
+    }
+}
+
+// The force of a quad, identical arithmetic in every path: the reciprocal
+// of r^2 (zero outside the cutoff), the LJ factor and the packed sums.
+template <bool SINGLE>
+__device__ __forceinline__ void quad_force(const Quad<SINGLE>& Q, float r2[4], float2& sxy, float& sz) {
+  sxy = make_float2(0.f, 0.f);
+  sz = 0.f;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const float r2inv = Q.in[u] ? rcp_approx(Q.g[u].rsq) : 0.0f;
+    const float r6inv = r2inv * r2inv * r2inv;
+    const float fpair = (r6inv * __fmaf_rn(Q.lj1[u], r6inv, -Q.lj2[u])) * r2inv;
+    sxy = __ffma2_rn(Q.g[u].dxy, make_float2(fpair, fpair), sxy);
+    sz = __fmaf_rn(Q.g[u].dz, fpair, sz);
+    r2[u] = r2inv;
+  }
+}
+
 // ENERGY: the FP32 r^2 of a pair is biased, not just noisy: the bin shifts
 // added to grid-aligned FP32 coordinates round the same way pair after pair
 // (about 1e-8 relative in the energy of an fcc liquid).  So the energy takes
@@ -322,69 +389,99 @@ struct TileAcc {
 // r^2 and would vanish if added to r^2 in FP32.  The reciprocal is refined by
 // one Newton step, the coefficients carry their FP32 remainders, and the
 // cutoff shift is subtracted per atom in FP64, so what is left is rounding
-// with random signs.  The forces are the ones of the force-only kernel.
-template <bool SINGLE, bool ENERGY>
+// with random signs.
+template <bool SINGLE>
+__device__ __forceinline__ float quad_energy(const TileForceArgs& A, const float4* st, const float2* sig,
+                                             const float4& xi, const unsigned o[4], const Quad<SINGLE>& Q,
+                                             const float r2[4], int& npair) {
+  float se = 0.f;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const TileGeo& g = Q.g[u];
+    const float4 q = staged(st, o[u]);
+    const float2 sg = sig[o[u] >> 4];
+    const float lox = __fsub_rn(two_sum_err(xi.x, -q.x, g.dxy.x), sg.x);
+    const float loy = __fsub_rn(two_sum_err(xi.y, -q.y, g.dxy.y), sg.y);
+    const float kw = g.kz * A.wz;
+    const float loz = __fmaf_rn(g.kz, A.wz_lo, __fadd_rn(two_sum_err(xi.z, -q.z, g.tz), two_sum_err(g.tz, kw, g.dz)));
+    const float corr = 2.0f * __fmaf_rn(g.dz, loz, __fmaf_rn(g.dxy.y, loy, g.dxy.x * lox));  // r^2 - fl(r^2)
+    const float r1 = __fmaf_rn(r2[u], __fmaf_rn(-g.rsq, r2[u], 1.0f), r2[u]);
+    const float r6e = r1 * r1 * r1;
+    const float e = __fmaf_rn(r6e, __fmaf_rn(A.E.a, r6e, -A.E.b), r6e * __fmaf_rn(A.E.a_lo, r6e, -A.E.b_lo));
+    // de/d(r^2) = -r^-2 r^-6 (6 a r^-6 - 3 b)
+    const float de = -(r1 * r6e) * __fmaf_rn(6.0f * A.E.a, r6e, -3.0f * A.E.b);
+    se += __fmaf_rn(de, corr, e);
+    npair += Q.in[u] ? 1 : 0;
+  }
+  return se;
+}
+
+template <bool SINGLE, bool ENERGY, bool EXACT>
 __device__ __forceinline__ void tile_quad(const TileForceArgs& A, const TileDesc& T, const float4* st,
                                           const int* stype, const float2* sig, const float4& xi, int i, int ti,
-                                          const unsigned o[4], TileAcc& acc) {
-  TileGeo g[4];
-  float lj1[4], lj2[4];
-  bool in[4], band[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    g[u] = tile_geo(xi, staged(st, o[u]), A.wz);
-    if (SINGLE) {
-      lj1[u] = A.P.lj1_0;
-      lj2[u] = A.P.lj2_0;
-      in[u] = g[u].rsq < A.cut_lo;
-      band[u] = g[u].rsq >= A.cut_lo && g[u].rsq <= A.cut_hi;
-    } else {
-      const int tp = ti * A.P.ntypes + stype[o[u] >> 4];
-      lj1[u] = __ldg(A.P.lj1 + tp);
-      lj2[u] = __ldg(A.P.lj2 + tp);
-      const float c = __ldg(A.P.cutsq + tp);
-      in[u] = g[u].rsq < c * (1.0f - LJ_BAND);
-      band[u] = g[u].rsq >= c * (1.0f - LJ_BAND) && g[u].rsq <= c * (1.0f + LJ_BAND);
-    }
+                                          const unsigned o[4], TileAcc& acc, bool& near) {
+  Quad<SINGLE> Q;
+  const bool nq = quad_geo<SINGLE>(A, st, stype, xi, ti, o, Q);
+  if (EXACT) {
+    if (nq) quad_exact<SINGLE>(A, T, stype, i, ti, o, Q);
+  } else {
+    near = near | nq;
   }
-  if (band[0] || band[1] || band[2] || band[3]) {  // borderline: decide as FP64 does
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (band[u]) {
-        const int tp = SINGLE ? 0 : ti * A.P.ntypes + stype[o[u] >> 4];
-        in[u] = cut_fp64(A.x4, i, stage_particle(A, T, int(o[u] >> 4)), SINGLE ? A.P.cutsq_d0 : __ldg(A.P.cutsq_d + tp));
-      }
-  }
-  float2 sxy = make_float2(0.f, 0.f);
-  float sz = 0.f, se = 0.f;
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const float r2inv = in[u] ? rcp_approx(g[u].rsq) : 0.0f;
-    const float r6inv = r2inv * r2inv * r2inv;
-    const float fpair = (r6inv * __fmaf_rn(lj1[u], r6inv, -lj2[u])) * r2inv;
-    sxy = __ffma2_rn(g[u].dxy, make_float2(fpair, fpair), sxy);
-    sz = __fmaf_rn(g[u].dz, fpair, sz);
-    if (ENERGY) {
-      const float4& q = staged(st, o[u]);
-      const float2 sg = sig[o[u] >> 4];
-      const float lox = __fsub_rn(two_sum_err(xi.x, -q.x, g[u].dxy.x), sg.x);
-      const float loy = __fsub_rn(two_sum_err(xi.y, -q.y, g[u].dxy.y), sg.y);
-      const float kw = g[u].kz * A.wz;
-      const float loz = __fmaf_rn(g[u].kz, A.wz_lo,
-                                  __fadd_rn(two_sum_err(xi.z, -q.z, g[u].tz), two_sum_err(g[u].tz, kw, g[u].dz)));
-      const float corr =
-          2.0f * __fmaf_rn(g[u].dz, loz, __fmaf_rn(g[u].dxy.y, loy, g[u].dxy.x * lox));  // r^2 - fl(r^2), first order
-      const float r1 = __fmaf_rn(r2inv, __fmaf_rn(-g[u].rsq, r2inv, 1.0f), r2inv);
-      const float r6e = r1 * r1 * r1;
-      const float e = __fmaf_rn(r6e, __fmaf_rn(A.E.a, r6e, -A.E.b), r6e * __fmaf_rn(A.E.a_lo, r6e, -A.E.b_lo));
-      // de/d(r^2) = -r^-2 r^-6 (6 a r^-6 - 3 b)
-      const float de = -(r1 * r6e) * __fmaf_rn(6.0f * A.E.a, r6e, -3.0f * A.E.b);
-      se += __fmaf_rn(de, corr, e);
-      acc.npair += in[u] ? 1 : 0;
-    }
-  }
+  float r2[4];
+  float2 sxy;
+  float sz;
+  quad_force<SINGLE>(Q, r2, sxy, sz);
   acc.f.add(sxy, sz);
-  if (ENERGY) acc.add_e(se);
+  if (ENERGY) acc.add_e(quad_energy<SINGLE>(A, st, sig, xi, o, Q, r2, acc.npair));
+}
+
+// One row: eight entries per coalesced granule load, the next granule
+// prefetched; the last granule's unused entries read the far-away sentinel.
+// EXACT decides near pairs in FP64 per quad; otherwise the FP32 decisions
+// stand and the return value says whether any pair was near.
+template <bool SINGLE, bool ENERGY, bool EXACT>
+__device__ __forceinline__ bool tile_row(const TileForceArgs& A, const TileDesc& T, const float4* st,
+                                         const int* stype, const float2* sig, const float4& xi, int i, int ti,
+                                         unsigned sentinel, TileAcc& acc) {
+  bool near = false;
+  const int cnt = A.num[i];
+  const uint4* q = A.rows + i;
+  const int nfull = cnt >> 3;
+  uint4 e = nfull > 0 ? ld_granule(q) : make_uint4(0, 0, 0, 0);
+  for (int kq = 0; kq < nfull; ++kq) {
+    const uint4 en = (kq + 1 < nfull) ? ld_granule(q + (size_t)(kq + 1) * A.stride) : e;
+    const unsigned o0[4] = {e.x & 0xffffu, e.x >> 16, e.y & 0xffffu, e.y >> 16};
+    const unsigned o1[4] = {e.z & 0xffffu, e.z >> 16, e.w & 0xffffu, e.w >> 16};
+    tile_quad<SINGLE, ENERGY, EXACT>(A, T, st, stype, sig, xi, i, ti, o0, acc, near);
+    tile_quad<SINGLE, ENERGY, EXACT>(A, T, st, stype, sig, xi, i, ti, o1, acc, near);
+    e = en;
+  }
+  const int rem = cnt & 7;
+  if (rem) {
+    const uint4 w = ld_granule(q + (size_t)nfull * A.stride);
+    const unsigned v[8] = {w.x & 0xffffu, w.x >> 16, w.y & 0xffffu, w.y >> 16,
+                           w.z & 0xffffu, w.z >> 16, w.w & 0xffffu, w.w >> 16};
+    unsigned o0[4], o1[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      o0[u] = u < rem ? v[u] : sentinel;
+      o1[u] = u + 4 < rem ? v[u + 4] : sentinel;
+    }
+    tile_quad<SINGLE, ENERGY, EXACT>(A, T, st, stype, sig, xi, i, ti, o0, acc, near);
+    if (rem > 4) tile_quad<SINGLE, ENERGY, EXACT>(A, T, st, stype, sig, xi, i, ti, o1, acc, near);
+  }
+  return near;
+}
+
+// the rare row with a pair near the cutoff, again with FP64 decisions; out
+// of line so the common path carries none of it
+template <bool SINGLE>
+__device__ __forceinline__ void tile_row_exact(const TileForceArgs& A, const TileDesc& T, const float4* st,
+                                            const int* stype, const float4 xi, int i, int ti, unsigned sentinel,
+                                            TileAcc* acc) {
+  TileAcc a;
+  tile_row<SINGLE, false, true>(A, T, st, stype, nullptr, xi, i, ti, sentinel, a);
+  *acc = a;
 }
 
 // One CTA per tile: the stage goes to shared memory, then each thread takes
@@ -413,41 +510,19 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
     if (i >= A.n_local) continue;  // a ghost binned into an interior bin owns no row
     const float4 xi = st[p];
     const int ti = SINGLE ? 0 : stype[p];
-    const int cnt = A.num[i];
-    const uint4* q = A.rows + i;
-    const int nfull = cnt >> 3;
     TileAcc acc;
-    uint4 e = nfull > 0 ? ld_granule(q) : make_uint4(0, 0, 0, 0);
-    for (int kq = 0; kq < nfull; ++kq) {
-      const uint4 en = (kq + 1 < nfull) ? ld_granule(q + (size_t)(kq + 1) * A.stride) : e;
-      const unsigned o0[4] = {e.x & 0xffffu, e.x >> 16, e.y & 0xffffu, e.y >> 16};
-      const unsigned o1[4] = {e.z & 0xffffu, e.z >> 16, e.w & 0xffffu, e.w >> 16};
-      tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o0, acc);
-      tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o1, acc);
-      e = en;
-    }
-    const int rem = cnt & 7;
-    if (rem) {
-      // the last granule's unused entries read the far-away sentinel
-      const uint4 w = ld_granule(q + (size_t)nfull * A.stride);
-      const unsigned v[8] = {w.x & 0xffffu, w.x >> 16, w.y & 0xffffu, w.y >> 16,
-                             w.z & 0xffffu, w.z >> 16, w.w & 0xffffu, w.w >> 16};
-      unsigned o0[4], o1[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        o0[u] = u < rem ? v[u] : sentinel;
-        o1[u] = u + 4 < rem ? v[u + 4] : sentinel;
-      }
-      tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o0, acc);
-      if (rem > 4) tile_quad<SINGLE, ENERGY>(A, T, st, stype, sig, xi, i, ti, o1, acc);
+    if (ENERGY) {
+      tile_row<SINGLE, true, true>(A, T, st, stype, sig, xi, i, ti, sentinel, acc);
+    } else if (tile_row<SINGLE, false, false>(A, T, st, stype, sig, xi, i, ti, sentinel, acc)) {
+      tile_row_exact<SINGLE>(A, T, st, stype, xi, i, ti, sentinel, &acc);
     }
     const double fx = double(acc.f.sxy.x) - double(acc.f.cxy.x);
     const double fy = double(acc.f.sxy.y) - double(acc.f.cxy.y);
     const double fz = double(acc.f.sz) - double(acc.f.cz);
-    if (ZERO) {  // the pending deep_copy(f, 0) folded into the store
-      A.f[3 * i] = 0.0 + fx;
-      A.f[3 * i + 1] = 0.0 + fy;
-      A.f[3 * i + 2] = 0.0 + fz;
+    if (ZERO) {  // the pending deep_copy(f, 0): the sum is the whole force
+      A.f[3 * i] = fx;
+      A.f[3 * i + 1] = fy;
+      A.f[3 * i + 2] = fz;
     } else {
       A.f[3 * i] += fx;
       A.f[3 * i + 1] += fy;
@@ -575,8 +650,7 @@ static void lj_tile_compute(Ctx& c, bool zero, const LJParamsF& P) {
   A.wz_lo = wlo[2];
   A.stage_cap = c.tile_stage_max + 1;
   A.P = P;
-  A.cut_lo = P.cutsq_0 * (1.0f - LJ_BAND);
-  A.cut_hi = P.cutsq_0 * (1.0f + LJ_BAND);
+  A.band_w = P.cutsq_0 * LJ_BAND;
   A.E = LJEnergyF{0.f, 0.f, 0.f, 0.f, 0.0};
   A.e_part = nullptr;
   if (energy) {
