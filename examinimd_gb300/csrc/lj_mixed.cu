@@ -229,38 +229,40 @@ __device__ __forceinline__ int stage_particle(const TileForceArgs& A, const Tile
 __device__ __forceinline__ void stage_tile(const TileForceArgs& A, const TileDesc& T, float4* st, int* stype,
                                            float2* sig) {
   constexpr int U = 4;
-  const int total = T.base[9];
-  for (int s0 = threadIdx.x; s0 < total; s0 += U * blockDim.x) {
-    float4 v[U];
-    int rr[U];
+  // segment by segment (each a contiguous range of the permutation-ordered
+  // copy), four float4 loads in flight per thread
+#pragma unroll 1
+  for (int r = 0; r < 9; ++r) {
+    const int b0 = T.base[r], b1 = T.base[r + 1];
+    const int shift = T.seg[r] - b0;  // permutation slot = stage slot + shift
+    const float sx = float(r / 3 - 1), sy = float(r % 3 - 1);
+    const float kx = sx * A.wx, ky = sy * A.wy;
+    for (int s0 = b0 + threadIdx.x; s0 < b1; s0 += U * blockDim.x) {
+      float4 v[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int s = s0 + u * blockDim.x;
-      rr[u] = 0;
-      if (s < total) {
-        rr[u] = stage_segment(T, s);
-        v[u] = __ldg(A.xlb + T.seg[rr[u]] + (s - T.base[rr[u]]));
+      for (int u = 0; u < U; ++u) {
+        const int s = s0 + u * blockDim.x;
+        if (s < b1) v[u] = __ldg(A.xlb + (s + shift));
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int s = s0 + u * blockDim.x;
+        if (s >= b1) break;
+        float4 p = v[u];
+        const int bits = __float_as_int(p.w);
+        if (stype) stype[s] = bits >> 10;
+        const float xs = __fadd_rn(p.x, kx), ys = __fadd_rn(p.y, ky);
+        if (sig)
+          sig[s] = make_float2(__fmaf_rn(sx, A.wx_lo, two_sum_err(p.x, kx, xs)),
+                               __fmaf_rn(sy, A.wy_lo, two_sum_err(p.y, ky, ys)));
+        p.x = xs;
+        p.y = ys;
+        p.w = float((bits & 1023) - T.bz0 + 1);
+        st[s] = p;
       }
     }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int s = s0 + u * blockDim.x;
-      if (s >= total) break;
-      const int r = rr[u];
-      float4 p = v[u];
-      const int bits = __float_as_int(p.w);
-      const float sx = float(r / 3 - 1), sy = float(r % 3 - 1);
-      if (stype) stype[s] = bits >> 10;
-      const float xs = __fmaf_rn(sx, A.wx, p.x), ys = __fmaf_rn(sy, A.wy, p.y);
-      if (sig)
-        sig[s] = make_float2(__fmaf_rn(sx, A.wx_lo, two_sum_err(p.x, sx * A.wx, xs)),
-                             __fmaf_rn(sy, A.wy_lo, two_sum_err(p.y, sy * A.wy, ys)));
-      p.x = xs;
-      p.y = ys;
-      p.w = float((bits & 1023) - T.bz0 + 1);
-      st[s] = p;
-    }
   }
+  const int total = T.base[9];
   if (threadIdx.x == 0) {
     st[total] = make_float4(1.0e4f, 1.0e4f, 1.0e4f, 0.0f);
     if (stype) stype[total] = 0;
@@ -286,10 +288,13 @@ __device__ __forceinline__ TileGeo tile_geo(const float4& xi, const float4& q, f
   return g;
 }
 
-// a staged float4 at a byte offset (always a multiple of 16: one 16-byte
-// shared load)
+// a staged float4 at a byte offset (always a multiple of 16): one 16-byte
+// shared load at the stage's shared-window address plus the offset
 __device__ __forceinline__ float4 staged(const float4* st, unsigned off) {
-  return *static_cast<const float4*>(__builtin_assume_aligned(reinterpret_cast<const char*>(st) + off, 16));
+  const unsigned a = unsigned(__cvta_generic_to_shared(st)) + off;
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+  return v;
 }
 
 __device__ __forceinline__ uint4 ld_granule(const uint4* p) {
