@@ -447,13 +447,12 @@ __device__ __forceinline__ void tile_quad(const TileForceArgs& A, const TileDesc
 template <bool SINGLE, bool ENERGY, bool EXACT>
 __device__ __forceinline__ bool tile_row(const TileForceArgs& A, const TileDesc& T, const float4* st,
                                          const int* stype, const float2* sig, const float4& xi, int i, int ti,
-                                         unsigned sentinel, TileAcc& acc) {
+                                         unsigned sentinel, TileAcc& acc, int cnt, int g0 = 0) {
   bool near = false;
-  const int cnt = A.num[i];
   const uint4* q = A.rows + i;
   const int nfull = cnt >> 3;
-  uint4 e = nfull > 0 ? ld_granule(q) : make_uint4(0, 0, 0, 0);
-  for (int kq = 0; kq < nfull; ++kq) {
+  uint4 e = g0 < nfull ? ld_granule(q + (size_t)g0 * A.stride) : make_uint4(0, 0, 0, 0);
+  for (int kq = g0; kq < nfull; ++kq) {
     const uint4 en = (kq + 1 < nfull) ? ld_granule(q + (size_t)(kq + 1) * A.stride) : e;
     const unsigned o0[4] = {e.x & 0xffffu, e.x >> 16, e.y & 0xffffu, e.y >> 16};
     const unsigned o1[4] = {e.z & 0xffffu, e.z >> 16, e.w & 0xffffu, e.w >> 16};
@@ -485,18 +484,69 @@ __device__ __forceinline__ void tile_row_exact(const TileForceArgs& A, const Til
                                             const int* stype, const float4 xi, int i, int ti, unsigned sentinel,
                                             TileAcc* acc) {
   TileAcc a;
-  tile_row<SINGLE, false, true>(A, T, st, stype, nullptr, xi, i, ti, sentinel, a);
+  tile_row<SINGLE, false, true>(A, T, st, stype, nullptr, xi, i, ti, sentinel, a, A.num[i]);
   *acc = a;
+}
+
+// Two rows of one thread, their full granules interleaved (two independent
+// chains of loads and arithmetic per thread), then what is left of the
+// longer row and both last granules.  FP32 decisions; near reports rows with
+// a pair in the guard band.
+template <bool SINGLE>
+__device__ __forceinline__ void tile_rows2(const TileForceArgs& A, const TileDesc& T, const float4* st,
+                                           const int* stype, unsigned sentinel, const float4& xa, int ia, int ta,
+                                           int ca, TileAcc& aa, bool& na, const float4& xb, int ib, int tb, int cb,
+                                           TileAcc& ab, bool& nb) {
+  const uint4* qa = A.rows + ia;
+  const uint4* qb = A.rows + ib;
+  const int fa = ca >> 3, fb = cb >> 3, f2 = min(fa, fb);
+  na = false;
+  nb = false;
+  if (f2 > 0) {
+    uint4 ea = ld_granule(qa), eb = ld_granule(qb);
+    for (int g = 0; g < f2; ++g) {
+      const uint4 ena = (g + 1 < fa) ? ld_granule(qa + (size_t)(g + 1) * A.stride) : ea;
+      const uint4 enb = (g + 1 < fb) ? ld_granule(qb + (size_t)(g + 1) * A.stride) : eb;
+      const unsigned a0[4] = {ea.x & 0xffffu, ea.x >> 16, ea.y & 0xffffu, ea.y >> 16};
+      const unsigned b0[4] = {eb.x & 0xffffu, eb.x >> 16, eb.y & 0xffffu, eb.y >> 16};
+      const unsigned a1[4] = {ea.z & 0xffffu, ea.z >> 16, ea.w & 0xffffu, ea.w >> 16};
+      const unsigned b1[4] = {eb.z & 0xffffu, eb.z >> 16, eb.w & 0xffffu, eb.w >> 16};
+      tile_quad<SINGLE, false, false>(A, T, st, stype, nullptr, xa, ia, ta, a0, aa, na);
+      tile_quad<SINGLE, false, false>(A, T, st, stype, nullptr, xb, ib, tb, b0, ab, nb);
+      tile_quad<SINGLE, false, false>(A, T, st, stype, nullptr, xa, ia, ta, a1, aa, na);
+      tile_quad<SINGLE, false, false>(A, T, st, stype, nullptr, xb, ib, tb, b1, ab, nb);
+      ea = ena;
+      eb = enb;
+    }
+  }
+  na = na | tile_row<SINGLE, false, false>(A, T, st, stype, nullptr, xa, ia, ta, sentinel, aa, ca, f2);
+  nb = nb | tile_row<SINGLE, false, false>(A, T, st, stype, nullptr, xb, ib, tb, sentinel, ab, cb, f2);
+}
+
+template <bool ZERO>
+__device__ __forceinline__ void store_force(double* f, int i, const TileAcc& acc) {
+  const double fx = double(acc.f.sxy.x) - double(acc.f.cxy.x);
+  const double fy = double(acc.f.sxy.y) - double(acc.f.cxy.y);
+  const double fz = double(acc.f.sz) - double(acc.f.cz);
+  if (ZERO) {  // the pending deep_copy(f, 0): the sum is the whole force
+    f[3 * i] = fx;
+    f[3 * i + 1] = fy;
+    f[3 * i + 2] = fz;
+  } else {
+    f[3 * i] += fx;
+    f[3 * i + 1] += fy;
+    f[3 * i + 2] += fz;
+  }
 }
 
 // One CTA per tile: the stage goes to shared memory, then each thread takes
 // one particle of the tile's own bins and walks its row, eight entries per
 // coalesced granule load.
 template <bool SINGLE, bool ZERO, bool ENERGY>
-__global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
+__global__ void __launch_bounds__(kTileThreads) k_lj_tile(TileForceArgs A) {
   extern __shared__ float4 smem_stage[];
   __shared__ TileDesc T;
-  __shared__ double esum[kTileAtoms / 32];
+  __shared__ double esum[kTileThreads / 32];
   if (threadIdx.x < 32) reinterpret_cast<int*>(&T)[threadIdx.x] = reinterpret_cast<const int*>(A.tiles + blockIdx.x)[threadIdx.x];
   __syncthreads();
   // shared arrays in order of alignment: float4 stage, float2 remainders
@@ -509,32 +559,39 @@ __global__ void __launch_bounds__(kTileAtoms) k_lj_tile(TileForceArgs A) {
   __syncthreads();
   const unsigned sentinel = unsigned(T.base[9]) << 4;
   double e_thread = 0.0;
-  for (int t = threadIdx.x; t < T.nown; t += blockDim.x) {
-    const int p = T.own0 + t;
-    const int i = A.perm[T.seg[4] + (p - T.base[4])];
-    if (i >= A.n_local) continue;  // a ghost binned into an interior bin owns no row
-    const float4 xi = st[p];
-    const int ti = SINGLE ? 0 : stype[p];
-    TileAcc acc;
-    if (ENERGY) {
-      tile_row<SINGLE, true, true>(A, T, st, stype, sig, xi, i, ti, sentinel, acc);
-    } else if (tile_row<SINGLE, false, false>(A, T, st, stype, sig, xi, i, ti, sentinel, acc)) {
-      tile_row_exact<SINGLE>(A, T, st, stype, xi, i, ti, sentinel, &acc);
-    }
-    const double fx = double(acc.f.sxy.x) - double(acc.f.cxy.x);
-    const double fy = double(acc.f.sxy.y) - double(acc.f.cxy.y);
-    const double fz = double(acc.f.sz) - double(acc.f.cz);
-    if (ZERO) {  // the pending deep_copy(f, 0): the sum is the whole force
-      A.f[3 * i] = fx;
-      A.f[3 * i + 1] = fy;
-      A.f[3 * i + 2] = fz;
-    } else {
-      A.f[3 * i] += fx;
-      A.f[3 * i + 1] += fy;
-      A.f[3 * i + 2] += fz;
-    }
-    if (ENERGY)  // full list: half of every ordered pair's shifted energy
+  if (ENERGY) {
+    for (int t = threadIdx.x; t < T.nown; t += blockDim.x) {
+      const int p = T.own0 + t;
+      const int i = A.perm[T.seg[4] + (p - T.base[4])];
+      if (i >= A.n_local) continue;  // a ghost binned into an interior bin owns no row
+      const float4 xi = st[p];
+      const int ti = SINGLE ? 0 : stype[p];
+      TileAcc acc;
+      tile_row<SINGLE, true, true>(A, T, st, stype, sig, xi, i, ti, sentinel, acc, A.num[i]);
+      store_force<ZERO>(A.f, i, acc);
+      // full list: half of every ordered pair's shifted energy
       e_thread += 0.5 * ((double(acc.es) - double(acc.ec)) - double(acc.npair) * A.E.ecut);
+    }
+  } else {
+    // two particles per thread: slots t and t + blockDim of the tile's own bins
+    for (int t = threadIdx.x; t < T.nown; t += 2 * blockDim.x) {
+      const int pa = T.own0 + t, pb = pa + blockDim.x;
+      const bool hb = t + int(blockDim.x) < T.nown;
+      const int ia = A.perm[T.seg[4] + (pa - T.base[4])];
+      const int ib = hb ? A.perm[T.seg[4] + (pb - T.base[4])] : ia;
+      // a ghost binned into an interior bin owns no row
+      const bool va = ia < A.n_local, vb = hb && ib < A.n_local;
+      const int ca = va ? A.num[ia] : 0, cb = vb ? A.num[ib] : 0;
+      const float4 xa = st[pa], xb = hb ? st[pb] : xa;
+      const int ta = SINGLE ? 0 : stype[pa], tb = (SINGLE || !hb) ? 0 : stype[pb];
+      TileAcc aa, ab;
+      bool na, nb;
+      tile_rows2<SINGLE>(A, T, st, stype, sentinel, xa, ia, ta, ca, aa, na, xb, ib, tb, cb, ab, nb);
+      if (na) tile_row_exact<SINGLE>(A, T, st, stype, xa, ia, ta, sentinel, &aa);
+      if (nb) tile_row_exact<SINGLE>(A, T, st, stype, xb, ib, tb, sentinel, &ab);
+      if (va) store_force<ZERO>(A.f, ia, aa);
+      if (vb) store_force<ZERO>(A.f, ib, ab);
+    }
   }
   if (ENERGY) {
     const double t = block_sum(e_thread, esum);
@@ -682,7 +739,7 @@ static void lj_tile_compute(Ctx& c, bool zero, const LJParamsF& P) {
   if (smem > 48 * 1024) EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   if (c.n_tiles > 0) {
     TimedLaunch t(c, energy ? "lj_tile_mixed_energy" : "lj_full_mixed");
-    k<<<c.n_tiles, kTileAtoms, smem, c.stream>>>(A);
+    k<<<c.n_tiles, kTileThreads, smem, c.stream>>>(A);
     EMD_CHECK_LAUNCH();
   }
   if (energy) {

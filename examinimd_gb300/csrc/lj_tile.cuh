@@ -20,7 +20,8 @@
 
 namespace emd {
 
-constexpr int kTileAtoms = 128;      // particles binned into a tile's own bins (one per force thread)
+constexpr int kTileAtoms = 256;      // particles binned into a tile's own bins (two per force thread)
+constexpr int kTileThreads = 128;    // threads of a force CTA
 constexpr int kTileStageMax = 4096;  // staged particles per tile (entries are 16-bit byte offsets)
 
 struct __align__(16) TileDesc {
