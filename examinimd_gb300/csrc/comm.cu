@@ -77,7 +77,7 @@ __global__ void k_halo_scatter(double4_32a* __restrict__ x4, double* __restrict_
 // for bit.
 __global__ void k_halo_update(double4_32a* __restrict__ x4, const int* __restrict__ owner,
                               const int* __restrict__ img, int n_local, int n_ghost, double lx, double ly,
-                              double lz, BinCentres ctr, XlOut out) {
+                              double lz, BinCentres ctr, float4* __restrict__ xl) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_ghost) return;
   const int m = img[g];
@@ -89,9 +89,9 @@ __global__ void k_halo_update(double4_32a* __restrict__ x4, const int* __restric
   if (m & 16) p.z -= lz;
   if (m & 32) p.z += lz;
   x4[n_local + g] = p;  // w (the type) is the owner's, as the halo build copied it
-  if (out.xl || out.xlb) {  // mixed form: FP32 position relative to the ghost's bin centre
+  if (xl) {  // mixed form: FP32 position relative to the ghost's bin centre
     const double4_32a q = ctr.at(n_local + g);
-    out.put(n_local + g, float(p.x - q.x), float(p.y - q.y), float(p.z - q.z), int(p.w), ctr.c3[n_local + g]);
+    xl[n_local + g] = make_float4(float(p.x - q.x), float(p.y - q.y), float(p.z - q.z), __int_as_float(int(p.w)));
   }
 }
 
@@ -215,7 +215,7 @@ emd_status emd_comm_update_halo(emd_ctx* ctx) {
   const bool live = mixed_xl_active(c);
   k_halo_update<<<blocks_for(c.N_ghost, 256), 256, 0, c.stream>>>(
       c.x4.p, c.ghost_owner.p, c.ghost_img.p, c.N_local, c.N_ghost, c.domain[0], c.domain[1], c.domain[2],
-      bin_centres(c), xl_out(c, live));
+      bin_centres(c), live ? c.xl.p : nullptr);
   if (!live) c.xl_ok &= ~2;
   EMD_CHECK_LAUNCH();
   EMD_API_END

@@ -12,7 +12,6 @@
 #include <vector>
 
 #include "../../include/emd_gpu.h"
-#include "lj_tile.cuh"
 
 namespace emd {
 
@@ -168,15 +167,6 @@ struct Ctx {
   bool xl_bin_valid = false;     // xl_bin holds the last binning's offsets (not handed to the mixed force)
   bool bin_sorted = false;       // the last binning re-sorted the particles after binning them
   DevBuf<int> abin;         // bin of every particle at the last list build (packed rows)
-  // tiled rows of the mixed form (lj_tile.cuh)
-  bool neigh_tiled = false;
-  int neigh_covered = 0;    // owned atoms with a row (binned into interior bins) at the last build
-  int n_tiles = 0, tile_stage_max = 0;
-  DevBuf<TileDesc> tiles;
-  DevBuf<int> tile_of_bin, tile_colc, tile_flags;
-  DevBuf<int> tile_perm;    // the permutation of the build the tiles index
-  DevBuf<int> tile_pos;     // its inverse: slot of every particle
-  DevBuf<float4> xlb;       // FP32 bin-relative positions in permutation order (tiled rows)
   DevBuf<float4> xl;        // FP32 bin-relative positions (mixed force)
 
   // ---- LJ
@@ -281,22 +271,6 @@ struct BinCentres {
   }
 };
 BinCentres bin_centres(const Ctx& c);
-TileView tile_view(const Ctx& c);
-
-// Where the mixed form's FP32 bin-relative positions go: xl in particle order
-// (packed rows, w = type), or, with tiled rows, xlb in the order of the
-// build's permutation (slot pos[i]), w = type << 10 | bz, so a tile's stage
-// is nine contiguous ranges of it.  All null: the copy is not kept up.
-struct XlOut {
-  float4* xl;
-  float4* xlb;
-  const int* pos;
-  __device__ __forceinline__ void put(int i, float x, float y, float z, int type, int c3) const {
-    if (xlb) xlb[pos[i]] = make_float4(x, y, z, __int_as_float((type << 10) | (c3 >> 20)));
-    else if (xl) xl[i] = make_float4(x, y, z, __int_as_float(type));
-  }
-};
-XlOut xl_out(const Ctx& c, bool live);
 void lj_mixed_after_build(Ctx& c);
 void nve_initial_mixed(Ctx& c, bool kick_first);
 void nve_final_mixed(Ctx& c);

@@ -49,37 +49,6 @@ __device__ __forceinline__ double lj_fpair(double rsq, double lj1, double lj2, d
 
 __device__ __forceinline__ int entry_j(int e, bool packed) { return packed ? (e >> 6) : e; }
 
-// Neighbour j of entry k of row i in any row format: CSR (LAYOUT 0),
-// column-major 32-bit rows (1, plain or packed), tiled 16-bit rows (2).
-template <int LAYOUT>
-struct AnyRow {
-  int n;
-  const int* p;
-  int stride;
-  bool packed;
-  const TileView* V;
-  int i;
-  const TileDesc* t;
-  __device__ __forceinline__ AnyRow(const ListView& L, const TileView& v, int i_, bool packed_)
-      : packed(packed_), V(&v), i(i_), t(nullptr) {
-    n = L.num_neighs[i];
-    if (LAYOUT == 2) {
-      if (n > 0) t = v.tiles + v.tile_of_bin[v.abin[i]];
-    } else if (LAYOUT == 1) {
-      p = L.entries + 4 * (size_t)i;
-      stride = L.stride;
-    } else {
-      p = L.entries + L.offsets[i];
-      stride = 1;
-    }
-  }
-  __device__ __forceinline__ int operator[](int k) const {
-    if (LAYOUT == 2) return tile_stage_particle(*t, V->perm, int(V->rows[tile_entry_index(i, k, V->stride)]) >> 4);
-    const int e = LAYOUT == 1 ? __ldg(p + (((size_t)(k >> 2) * stride) << 2) + (k & 3)) : __ldg(p + k);
-    return entry_j(e, packed);
-  }
-};
-
 // TagFullNeigh (force_lj_neigh_impl.h:164-206).  ZERO folds the pending
 // deep_copy(f, 0) into the store as 0.0 + sum, the reference's exact result.
 template <bool TWO_D, bool ZERO, bool IDIAL = false>
@@ -161,19 +130,18 @@ __global__ void __launch_bounds__(128) k_lj_half_fp64(const double4_32a* __restr
 
 // TagFullNeighPE / TagHalfNeighPE (force_lj_neigh_impl.h:259-343), one
 // partial per block.
-template <int LAYOUT>
-__global__ void __launch_bounds__(256) k_lj_energy(const double4_32a* __restrict__ x4, ListView L, TileView V,
-                                                   LJParams P, int n, int half, int packed,
-                                                   double* __restrict__ part) {
+template <bool TWO_D>
+__global__ void __launch_bounds__(256) k_lj_energy(const double4_32a* __restrict__ x4, ListView L, LJParams P, int n,
+                                                   int half, int packed, double* __restrict__ part) {
   __shared__ double sh[8];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double pe = 0.0;
   if (i < n) {
     const double4_32a xi = x4[i];
     const int ti = int(xi.w);
-    const AnyRow<LAYOUT> row(L, V, i, packed);
+    const Row<TWO_D> row(L, i);
     for (int jj = 0; jj < row.n; ++jj) {
-      const int j = row[jj];
+      const int j = entry_j(row[jj], packed);
       const double4_32a xj = x4[j];
       const double dx = xi.x - xj.x;
       const double dy = xi.y - xj.y;
@@ -218,9 +186,9 @@ void lj_mixed_prepare(Ctx& c);
 //   eps d/deps   of e and fpair: e and fpair themselves
 //   sigma d/dsigma: lj1 -> 12 lj1, lj2 -> 6 lj2.
 // Block partial sums of the four values, in a fixed order.
-template <int LAYOUT>
-__global__ void __launch_bounds__(256) k_lj_adjoint(const double4_32a* __restrict__ x4, ListView L, TileView V,
-                                                    double lj1, double lj2, double cutsq, int n, int packed,
+template <bool TWO_D>
+__global__ void __launch_bounds__(256) k_lj_adjoint(const double4_32a* __restrict__ x4, ListView L, double lj1,
+                                                    double lj2, double cutsq, int n, int packed,
                                                     const double* __restrict__ g, int nblk,
                                                     double* __restrict__ part) {
   __shared__ double sh[8];
@@ -230,9 +198,9 @@ __global__ void __launch_bounds__(256) k_lj_adjoint(const double4_32a* __restric
     const double4_32a xi = x4[i];
     const double gx = g[3 * i], gy = g[3 * i + 1], gz = g[3 * i + 2];
     const double r2c = 1.0 / cutsq, r6c = r2c * r2c * r2c;
-    const AnyRow<LAYOUT> row(L, V, i, packed);
+    const Row<TWO_D> row(L, i);
     for (int jj = 0; jj < row.n; ++jj) {
-      const int j = row[jj];
+      const int j = entry_j(row[jj], packed);
       const double4_32a xj = x4[j];
       const double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
       const double rsq = dx * dx + dy * dy + dz * dz;
@@ -267,17 +235,6 @@ static LJParams lj_params(Ctx& c) {
   const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
   return LJParams{c.lj_params.p, c.lj_params.p + nt2, c.lj_params.p + 2 * nt2, c.lj_ntypes,
                   c.lj_idial ? c.lj_intensity.p : nullptr};
-}
-
-// k_lj_energy over the current list, in whichever row format it has
-static void launch_lj_energy(Ctx& c, int grid, const ListView& L, const LJParams& P, int n, double* part) {
-  const TileView V = tile_view(c);
-  if (c.neigh_tiled)
-    k_lj_energy<2><<<grid, 256, 0, c.stream>>>(c.x4.p, L, V, P, n, c.lj_half, c.neigh_packed, part);
-  else if (c.neigh_layout_2d)
-    k_lj_energy<1><<<grid, 256, 0, c.stream>>>(c.x4.p, L, V, P, n, c.lj_half, c.neigh_packed, part);
-  else
-    k_lj_energy<0><<<grid, 256, 0, c.stream>>>(c.x4.p, L, V, P, n, c.lj_half, c.neigh_packed, part);
 }
 
 // ---- scratch of emd_lj_energy_noalloc
@@ -478,7 +435,10 @@ emd_status emd_lj_energy(emd_ctx* ctx, double* pe) {
   const LJParams P = lj_params(c);
   {
     TimedLaunch t(c, "lj_energy");
-    launch_lj_energy(c, grid, L, P, n, c.red2.p);
+    if (c.neigh_layout_2d)
+      k_lj_energy<true><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, c.red2.p);
+    else
+      k_lj_energy<false><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, c.red2.p);
     EMD_CHECK_LAUNCH();
   }
   *pe = device_sum(c, c.red2.p, grid);
@@ -511,15 +471,12 @@ emd_status emd_lj_adjoint(emd_ctx* ctx, const double* dL_dF, double dL_dE, doubl
     {
       TimedLaunch t(c, "lj_adjoint");
       const ListView L = list_view(c);
-      if (c.neigh_tiled)
-        k_lj_adjoint<2><<<grid, 256, 0, c.stream>>>(c.x4.p, L, tile_view(c), lj1, lj2, cutsq, n, c.neigh_packed,
-                                                    g.p, grid, c.red2.p);
-      else if (c.neigh_layout_2d)
-        k_lj_adjoint<1><<<grid, 256, 0, c.stream>>>(c.x4.p, L, tile_view(c), lj1, lj2, cutsq, n, c.neigh_packed,
-                                                    g.p, grid, c.red2.p);
+      if (c.neigh_layout_2d)
+        k_lj_adjoint<true><<<grid, 256, 0, c.stream>>>(c.x4.p, L, lj1, lj2, cutsq, n, c.neigh_packed, g.p, grid,
+                                                       c.red2.p);
       else
-        k_lj_adjoint<0><<<grid, 256, 0, c.stream>>>(c.x4.p, L, tile_view(c), lj1, lj2, cutsq, n, c.neigh_packed,
-                                                    g.p, grid, c.red2.p);
+        k_lj_adjoint<false><<<grid, 256, 0, c.stream>>>(c.x4.p, L, lj1, lj2, cutsq, n, c.neigh_packed, g.p, grid,
+                                                        c.red2.p);
       EMD_CHECK_LAUNCH();
     }
     for (int k = 0; k < 4; ++k) s[k] = device_sum(c, c.red2.p + size_t(k) * grid, grid);
@@ -551,7 +508,10 @@ emd_status emd_lj_energy_noalloc(emd_ctx* ctx, double* pe) {
   const int grid = blocks_for(n, 256);
   const ListView L = list_view(c);
   const LJParams P = lj_params(c);
-  launch_lj_energy(c, grid, L, P, n, scratch);
+  if (c.neigh_layout_2d)
+    k_lj_energy<true><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, scratch);
+  else
+    k_lj_energy<false><<<grid, 256, 0, c.stream>>>(c.x4.p, L, P, n, c.lj_half, c.neigh_packed, scratch);
   EMD_CHECK_LAUNCH();
   double* sum = scratch + kNoAllocBlocks;
   device_sum_launch(c, scratch, grid, sum);

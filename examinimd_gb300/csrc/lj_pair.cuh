@@ -133,13 +133,78 @@ __device__ __forceinline__ void lj_force(const PairGeo& g, bool in, float2& fxy,
   fz = g.dz * fpair;
 }
 
+// ---- the energy fused into the force pass (single type pair, thermo steps)
+//
+// The FP32 r^2 of a pair is biased, not just noisy: the bin shift added to
+// grid-aligned FP32 coordinates rounds the same way pair after pair, about
+// 1e-8 relative in the energy of an fcc liquid.  So the energy takes the
+// exact difference dx + lo, lo from the two-sum remainders of the pair's
+// subtraction and shift and from the FP32 bin width's own remainder, and
+// evaluates e(r^2) + e'(r^2) * 2 (dx . lo); the correction lies below the
+// rounding of r^2 and would vanish if added to r^2 in FP32.  The reciprocal
+// is refined by one Newton step, the coefficients a = lj1 / 12, b = lj2 / 6
+// carry their FP32 remainders, and the cutoff shift is subtracted per atom in
+// FP64, so what is left is rounding with random signs.  The forces are the
+// force-only kernel's, bit for bit.
+struct LJEnergyF {
+  float a, a_lo, b, b_lo;
+  double ecut;                 // shifted energy at the cutoff, FP64
+  float2 nwlo_xy, wlo_xy;      // the FP32 bin width's remainders, as PairCtx holds the widths
+  float nwlo_z, wlo_z;
+};
+
+struct EAcc {
+  float es = 0.f, ec = 0.f;  // compensated FP32 energy sum
+  int npair = 0;             // interacting pairs
+  __device__ __forceinline__ void add(float v) {
+    const float y = __fsub_rn(v, ec);
+    const float t = __fadd_rn(es, y);
+    ec = __fsub_rn(__fsub_rn(t, es), y);
+    es = t;
+  }
+};
+
+// Knuth's two-sum: a + b - s exactly, for s = fl(a + b)
+__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
+  const float bv = __fsub_rn(s, a);
+  const float av = __fsub_rn(s, bv);
+  return __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+
+__device__ __forceinline__ float pair_energy(const PairCtx& C, const LJEnergyF& E, int e, const float4& xj,
+                                             const PairGeo& g, bool in) {
+  constexpr int kExp = 0x4B000000;  // bits of 2^23, as lj_geo forms the shift
+  const float2 txy = __fadd2_rn(make_float2(__int_as_float((e & 0x30) | kExp), __int_as_float((e & 0x0C) | kExp)),
+                                make_float2(-8388608.0f, -8388608.0f));
+  const float tz = __fadd_rn(__int_as_float((e & 0x03) | kExp), -8388608.0f);
+  const float2 sxy = __ffma2_rn(txy, C.nw_xy, C.w_xy);      // (1 - k) w, FP32 widths
+  const float sz = __fmaf_rn(tz, C.nw_z, C.w_z);
+  const float2 sl = __ffma2_rn(txy, E.nwlo_xy, E.wlo_xy);  // (1 - k) times their remainders
+  const float slz = __fmaf_rn(tz, E.nwlo_z, E.wlo_z);
+  const float2 t1 = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
+  const float t1z = __fsub_rn(C.xi.z, xj.z);
+  const float lox = __fadd_rn(__fadd_rn(two_sum_err(C.xi.x, -xj.x, t1.x), two_sum_err(t1.x, sxy.x, g.dxy.x)), sl.x);
+  const float loy = __fadd_rn(__fadd_rn(two_sum_err(C.xi.y, -xj.y, t1.y), two_sum_err(t1.y, sxy.y, g.dxy.y)), sl.y);
+  const float loz = __fadd_rn(__fadd_rn(two_sum_err(C.xi.z, -xj.z, t1z), two_sum_err(t1z, sz, g.dz)), slz);
+  const float corr = 2.0f * __fmaf_rn(g.dz, loz, __fmaf_rn(g.dxy.y, loy, g.dxy.x * lox));  // r^2 - fl(r^2)
+  const float r0 = in ? rcp_approx(g.rsq) : 0.0f;
+  const float r1 = __fmaf_rn(r0, __fmaf_rn(-g.rsq, r0, 1.0f), r0);
+  const float r6 = r1 * r1 * r1;
+  const float ev = __fmaf_rn(r6, __fmaf_rn(E.a, r6, -E.b), r6 * __fmaf_rn(E.a_lo, r6, -E.b_lo));
+  // de/d(r^2) = -r^-2 r^-6 (6 a r^-6 - 3 b)
+  const float de = -(r1 * r6) * __fmaf_rn(6.0f * E.a, r6, -3.0f * E.b);
+  return __fmaf_rn(de, corr, ev);
+}
+
 // Four entries of one int4 granule, summed in FP32 and then added to the
 // compensated accumulator.  The FP32 cutoff test decides a pair unless its
 // r^2 lies in the guard band; one branch per granule re-tests such pairs in
-// FP64, as the reference decides them.
-template <bool SINGLE>
+// FP64, as the reference decides them.  ENERGY (single type) also adds the
+// four pairs' energies to `ea`.
+template <bool SINGLE, bool ENERGY = false>
 __device__ __forceinline__ void lj_quad(const PairCtx& C, const int4& e, const float4* __restrict__ xl,
-                                        const LJParamsF& P, Acc& acc) {
+                                        const LJParamsF& P, Acc& acc, const LJEnergyF* E = nullptr,
+                                        EAcc* ea = nullptr) {
   const float4 x0 = xl[e.x >> 6], x1 = xl[e.y >> 6], x2 = xl[e.z >> 6], x3 = xl[e.w >> 6];
   const PairGeo g0 = lj_geo<SINGLE>(C, e.x, x0, P), g1 = lj_geo<SINGLE>(C, e.y, x1, P);
   const PairGeo g2 = lj_geo<SINGLE>(C, e.z, x2, P), g3 = lj_geo<SINGLE>(C, e.w, x3, P);
@@ -158,6 +223,12 @@ __device__ __forceinline__ void lj_quad(const PairCtx& C, const int4& e, const f
   lj_force(g2, in2, a2, z2);
   lj_force(g3, in3, a3, z3);
   acc.add(__fadd2_rn(__fadd2_rn(a0, a1), __fadd2_rn(a2, a3)), __fadd_rn(__fadd_rn(z0, z1), __fadd_rn(z2, z3)));
+  if (ENERGY) {
+    const float s01 = __fadd_rn(pair_energy(C, *E, e.x, x0, g0, in0), pair_energy(C, *E, e.y, x1, g1, in1));
+    const float s23 = __fadd_rn(pair_energy(C, *E, e.z, x2, g2, in2), pair_energy(C, *E, e.w, x3, g3, in3));
+    ea->add(__fadd_rn(s01, s23));
+    ea->npair += int(in0) + int(in1) + int(in2) + int(in3);
+  }
 }
 
 }  // namespace

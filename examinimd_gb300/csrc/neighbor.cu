@@ -19,17 +19,14 @@
 // per granule) with capacity K; the host grows K like
 // Neighbor2D's regrow loop (x1.2) when a row overflows.
 // NeighborCSR rows are then compacted behind an exclusive scan of the
-// counts.  The FP64 drop-in stores plain j.  Rows built for the
-// mixed-precision force are tiled (lj_tile.cuh): 16-bit byte offsets of the
-// neighbours in the shared-memory stage of the centre atom's tile, eight per
-// granule.  Where a tile's stage would exceed its 4,096 slots they carry
-// packed 32-bit entries (j << 6) | (kx << 4) | (ky << 2) | kz with
-// k = (bin_j - bin_i) + 1 per dimension instead.
+// counts.  Rows built for the mixed-precision force carry packed entries
+// (j << 6) | (kx << 4) | (ky << 2) | kz with k = (bin_j - bin_i) + 1 per
+// dimension, which the force kernel uses to difference FP32 bin-relative
+// coordinates; the FP64 drop-in stores plain j.
 #include <algorithm>
 
 #include "emd_device.cuh"
 #include "emd_internal.h"
-#include "lj_tile.cuh"
 #include "neigh_rows.cuh"
 
 namespace emd {
@@ -38,10 +35,7 @@ namespace {
 constexpr int NB_THREADS = 32;  // one warp per interior bin
 constexpr int NB_CAP = 384;     // staged candidates per chunk
 constexpr int NB_SLOTS = 64;  // spread slots for the longest-row reduction
-static_assert(2 + NB_SLOTS <= kHostInts, "read-back of the row-length slots exceeds the pinned scratch");
-
-// row entry formats
-enum { FMT_PLAIN = 0, FMT_PACKED = 1, FMT_TILED = 2 };
+static_assert(1 + NB_SLOTS <= kHostInts, "read-back of the row-length slots exceeds the pinned scratch");
 
 struct NeighArgs {
   const double4_32a* x4;
@@ -54,14 +48,11 @@ struct NeighArgs {
   int n_local;
   double cutsq;
   float cut_lo, cut_hi;  // FP32 decision band
-  int half, newton;
+  int half, newton, packed;
   int* num_neighs;
   int* rows;  // column-major, leading dimension `stride`, capacity K
-  unsigned short* rows16;  // the same storage for tiled rows
   int stride, K;
-  int* flags;  // [0] overflow, [1 .. NB_SLOTS] longest row, [1 + NB_SLOTS] owned atoms with a row
-  const TileDesc* tiles;  // tiled rows: the tile of every interior bin
-  const int* tile_of_bin;
+  int* flags;  // [0] overflow, [1] longest row
 };
 
 // Exact FP64 re-test of a pair whose FP32 r^2 fell inside the guard band.
@@ -95,15 +86,11 @@ __device__ __forceinline__ long long okey(double v) {
   return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
-template <bool HALF, int FMT>
+template <bool HALF, bool PACKED>
 __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
-  constexpr bool PACKED = FMT == FMT_PACKED;
-  constexpr bool TILED = FMT == FMT_TILED;
   __shared__ float4 cand[NB_CAP];
-  __shared__ unsigned short cande[TILED ? NB_CAP : 1];  // tiled entry of each staged candidate
   __shared__ int pre[28];
   __shared__ int boff[27];
-  __shared__ int loff[27];  // tiled: stage index of each stencil bin's first particle
   const int lane = threadIdx.x;
   // interior bin of this warp
   const int ix = a.nbx - 2 * a.nhalo, iy = a.nby - 2 * a.nhalo, iz = a.nbz - 2 * a.nhalo;
@@ -118,13 +105,6 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
     const int b = ((bx + dbx) * a.nby + (by + dby)) * a.nbz + (bz + dbz);
     cntb = a.bincount[b];
     offb = a.binoffsets[b];
-    if (TILED) {
-      // the stencil bin lies in segment r of the tile's stage, which starts at
-      // permutation index seg[r] and stage index base[r]
-      const TileDesc& t = a.tiles[a.tile_of_bin[bc]];
-      const int r = (dbx + 1) * 3 + (dby + 1);
-      loff[lane] = t.base[r] + (offb - t.seg[r]);
-    }
   }
   // inclusive scan of the 27 stencil counts over the lanes
   int inc = cntb;
@@ -150,17 +130,14 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
   // accept the pair or re-test it in FP64.  Rows keep their order.
   const float prune_sq = a.cut_hi * 1.00001f;
   const unsigned lt = (1u << lane) - 1u;
-  int owners = 0;
   for (int a0 = 0; a0 < nc; a0 += 32) {
     // this lane's centre atom
     const int bi = a0 + lane;
     const int i = bi < nc ? a.permute[oc + bi] : -1;
     const bool own = i >= 0 && i < a.n_local;  // ghosts own no row
-    owners += __popc(__ballot_sync(FULL_MASK, own));
     float4 xi = make_float4(0.f, 0.f, 0.f, 0.f);
     long long kx = 0, ky = 0, kz = 0;
-    // i's own entry: the centre bin's code (1, 1, 1) when packed; tiled
-    // candidates carry plain j
+    // i's own entry: the centre bin's code (1, 1, 1) when packed
     const int self = PACKED ? int((unsigned(i) << 6) | 0x15u) : i;
     if (own) {
       xi = a.xl[i];
@@ -188,8 +165,6 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
     // row's next granule (4 stride - 3 ints further)
     int* rp = a.rows + quad_index(own ? i : 0, 0, a.stride);
     const int jump = 4 * a.stride - 3;
-    unsigned short* rp16 = a.rows16 + tile_entry_index(own ? i : 0, 0, a.stride);
-    const int jump16 = 8 * a.stride - 7;
     for (int base = 0; base < M; base += NB_CAP) {
       const int mc = min(NB_CAP, M - base);
       int m = 0;  // candidates kept
@@ -198,7 +173,6 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
         const int t = t0 + lane;
         bool keep = false;
         float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-        unsigned short te = 0;
         if (t < mc) {
           const int g = base + t;
           int s = 0;  // stencil bin of candidate g: binary search of the prefix
@@ -210,7 +184,6 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
           const float sx = float(s / 9 - 1) * a.wx, sy = float((s / 3) % 3 - 1) * a.wy, sz = float(s % 3 - 1) * a.wz;
           const int code = ((s / 9) << 4) | (((s / 3) % 3) << 2) | (s % 3);
           const int w = PACKED ? ((j << 6) | code) : j;
-          if (TILED) te = (unsigned short)((loff[s] + (g - pre[s])) << 4);
           c = make_float4(p.x + sx, p.y + sy, p.z + sz, __int_as_float(w));
           const float bx = fmaxf(fmaxf(lox - c.x, c.x - hix), 0.f), by = fmaxf(fmaxf(loy - c.y, c.y - hiy), 0.f),
                       bz = fmaxf(fmaxf(loz - c.z, c.z - hiz), 0.f);
@@ -218,10 +191,7 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
           keep = __fmaf_rn(bz, bz, __fadd_rn(__fmul_rn(bx, bx), __fmul_rn(by, by))) <= prune_sq;
         }
         const unsigned bal = __ballot_sync(FULL_MASK, keep);
-        if (keep) {
-          cand[m + __popc(bal & lt)] = c;
-          if (TILED) cande[m + __popc(bal & lt)] = te;
-        }
+        if (keep) cand[m + __popc(bal & lt)] = c;
         m += __popc(bal);
       }
       const int m4 = (m + 3) & ~3;
@@ -261,13 +231,8 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
               take = in && (w != self);
             }
             if (take) {
-              if (TILED) {
-                if (cnt < a.K) *rp16 = cande[k + u];
-                rp16 += (cnt & 7) == 7 ? jump16 : 1;
-              } else {
-                if (cnt < a.K) *rp = w;
-                rp += (cnt & 3) == 3 ? jump : 1;
-              }
+              if (cnt < a.K) *rp = w;
+              rp += (cnt & 3) == 3 ? jump : 1;
               ++cnt;
             }
           }
@@ -285,7 +250,6 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
   if (lane == 0) {
     if (mx > 0) atomicMax(&a.flags[1 + (blockIdx.x & (NB_SLOTS - 1))], mx);
     if (mx > a.K) a.flags[0] = 1;
-    if (owners > 0) atomicAdd(&a.flags[1 + NB_SLOTS], owners);
   }
 }
 
@@ -312,172 +276,7 @@ __global__ void k_unpack(int* __restrict__ e, long long n) {
   if (t < n) e[t] = e[t] >> 6;
 }
 
-// slot of every particle in the permutation
-__global__ void __launch_bounds__(256) k_inverse_perm(const int* __restrict__ perm, int n, int* __restrict__ pos) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < n) pos[perm[p]] = p;
-}
-
-// tiled rows -> CSR rows of plain j at offs[i] (for emd_neigh_get)
-__global__ void __launch_bounds__(256) k_tiled_rows_to_csr(TileView V, const int* __restrict__ num,
-                                                           const int* __restrict__ offs, int n, int* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int m = num[i], o = offs[i];
-  if (m == 0) return;
-  const TileRow row(V, i);
-  for (int k = 0; k < m; ++k) out[o + k] = row[k];
-}
-
-struct TileArgs {
-  const int* bincount;
-  const int* binoffsets;
-  int nbx, nby, nbz, nhalo;
-  int* col_count;       // tiles per interior column (counting pass)
-  const int* col_base;  // first tile of each interior column (writing pass)
-  TileDesc* tiles;
-  int* tile_of_bin;
-  int* flags;  // [0] a stage above kTileStageMax, [1] the largest stage
-};
-
-__device__ __forceinline__ int tile_bin(const TileArgs& A, int x, int y, int z) { return (x * A.nby + y) * A.nbz + z; }
-// permutation range of bins z0..z1 of column (x, y)
-__device__ __forceinline__ int col_start(const TileArgs& A, int x, int y, int z0) {
-  return A.binoffsets[tile_bin(A, x, y, z0)];
-}
-__device__ __forceinline__ int col_end(const TileArgs& A, int x, int y, int z1) {
-  const int b = tile_bin(A, x, y, z1);
-  return A.binoffsets[b] + A.bincount[b];
-}
-// particles in the stage of a tile over bins z0..z1 of column (x, y)
-__device__ __forceinline__ int stage_size(const TileArgs& A, int x, int y, int z0, int z1) {
-  int n = 0;
-  for (int dx = -1; dx <= 1; ++dx)
-    for (int dy = -1; dy <= 1; ++dy) n += col_end(A, x + dx, y + dy, z1 + 1) - col_start(A, x + dx, y + dy, z0 - 1);
-  return n;
-}
-
-// One thread per interior column cuts the column's interior bins into tiles
-// from the bottom up: a tile takes the next bin while its own bins hold at
-// most kTileAtoms particles and its stage at most kTileStageMax (a single
-// bin always forms a tile).  The counting pass stores the number of tiles
-// per column; after a scan of those counts the writing pass stores the
-// tiles in column order and the tile of every interior bin.
-template <bool WRITE>
-__global__ void __launch_bounds__(128) k_tiles(TileArgs A) {
-  const int iy = A.nby - 2 * A.nhalo, ix = A.nbx - 2 * A.nhalo;
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ix * iy) return;
-  const int bx = col / iy + A.nhalo, by = col % iy + A.nhalo;
-  const int zlo = A.nhalo, zhi = A.nbz - A.nhalo - 1;
-  int nt = 0, biggest = 0;
-  bool over = false;
-  for (int z0 = zlo; z0 <= zhi;) {
-    int z1 = z0;
-    const int s0 = col_start(A, bx, by, z0);
-    while (z1 < zhi && col_end(A, bx, by, z1 + 1) - s0 <= kTileAtoms &&
-           stage_size(A, bx, by, z0, z1 + 1) <= kTileStageMax)
-      ++z1;
-    const int st = stage_size(A, bx, by, z0, z1);
-    over = over || st > kTileStageMax;
-    biggest = max(biggest, st);
-    if (WRITE) {
-      const int slot = A.col_base[col] + nt;
-      TileDesc t;
-      t.bx = bx;
-      t.by = by;
-      t.bz0 = z0;
-      t.bz1 = z1;
-      t.base[0] = 0;
-      for (int r = 0; r < 9; ++r) {
-        const int x = bx + r / 3 - 1, y = by + r % 3 - 1;
-        t.seg[r] = col_start(A, x, y, z0 - 1);
-        t.base[r + 1] = t.base[r] + (col_end(A, x, y, z1 + 1) - t.seg[r]);
-      }
-      t.own0 = t.base[4] + (s0 - t.seg[4]);
-      t.nown = col_end(A, bx, by, z1) - s0;
-      for (int q = 0; q < 5; ++q) t.pad[q] = 0;
-      A.tiles[slot] = t;
-      for (int z = z0; z <= z1; ++z) A.tile_of_bin[tile_bin(A, bx, by, z)] = slot;
-    }
-    ++nt;
-    z0 = z1 + 1;
-  }
-  if (!WRITE) A.col_count[col] = nt;
-  if (over) A.flags[0] = 1;
-  atomicMax(&A.flags[1], biggest);
-}
-
 }  // namespace
-
-// Cuts the interior bins into tiles for the mixed force (k_tiles) and keeps
-// the build's permutation for them.  Returns false, with no tiles, when a
-// stage would exceed kTileStageMax particles (one very dense bin stencil):
-// the list is then built in the packed format.  One host read-back.
-static bool build_tiles(Ctx& c) {
-  const int ix = c.nbin[0] - 2 * c.nhalo, iy = c.nbin[1] - 2 * c.nhalo, iz = c.nbin[2] - 2 * c.nhalo;
-  if (c.nhalo < 1 || ix < 1 || iy < 1 || iz < 1) return false;
-  const int ncol = ix * iy;
-  const size_t nbins = size_t(c.nbin[0]) * c.nbin[1] * c.nbin[2];
-  c.tile_colc.reserve(size_t(ncol) + 1, c.stream);
-  c.tile_of_bin.reserve(nbins, c.stream);
-  c.tile_flags.reserve(4, c.stream);
-  EMD_CUDA(cudaMemsetAsync(c.tile_flags.p, 0, 4 * sizeof(int), c.stream));
-  EMD_CUDA(cudaMemsetAsync(c.tile_of_bin.p, 0xff, nbins * sizeof(int), c.stream));
-  TileArgs A;
-  A.bincount = c.bincount.p;
-  A.binoffsets = c.binoffsets.p;
-  A.nbx = c.nbin[0];
-  A.nby = c.nbin[1];
-  A.nbz = c.nbin[2];
-  A.nhalo = c.nhalo;
-  A.col_count = c.tile_colc.p;
-  A.col_base = c.tile_colc.p;
-  A.tiles = nullptr;
-  A.tile_of_bin = c.tile_of_bin.p;
-  A.flags = c.tile_flags.p;
-  {
-    TimedLaunch t(c, "neigh_tiles");
-    k_tiles<false><<<blocks_for(ncol, 128), 128, 0, c.stream>>>(A);
-    EMD_CHECK_LAUNCH();
-  }
-  exclusive_scan_int(c, c.tile_colc.p, c.tile_colc.p, ncol, c.tile_flags.p + 2);
-  EMD_CUDA(cudaMemcpyAsync(c.h_int, c.tile_flags.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  EMD_CUDA(cudaStreamSynchronize(c.stream));
-  if (c.h_int[0]) return false;
-  const int ntiles = c.h_int[2];
-  c.tile_stage_max = c.h_int[1];
-  c.tiles.reserve(size_t(ntiles) + 1, c.stream);
-  A.tiles = c.tiles.p;
-  {
-    TimedLaunch t(c, "neigh_tiles");
-    k_tiles<true><<<blocks_for(ncol, 128), 128, 0, c.stream>>>(A);
-    EMD_CHECK_LAUNCH();
-  }
-  c.n_tiles = ntiles;
-  const int n_all = c.N_local + c.N_ghost;
-  c.tile_perm.reserve(size_t(n_all) + 1, c.stream);
-  c.tile_pos.reserve(size_t(n_all) + 1, c.stream);
-  if (n_all > 0) {
-    EMD_CUDA(cudaMemcpyAsync(c.tile_perm.p, c.permute.p, sizeof(int) * n_all, cudaMemcpyDeviceToDevice, c.stream));
-    TimedLaunch t(c, "neigh_tiles");
-    k_inverse_perm<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.tile_perm.p, n_all, c.tile_pos.p);
-    EMD_CHECK_LAUNCH();
-  }
-  return true;
-}
-
-TileView tile_view(const Ctx& c) {
-  TileView V;
-  V.tiles = c.tiles.p;
-  V.tile_of_bin = c.tile_of_bin.p;
-  V.abin = c.abin.p;
-  V.perm = c.tile_perm.p;
-  V.rows = reinterpret_cast<const unsigned short*>(c.neigh_kind == EMD_NEIGH_2D ? c.neighs.p : c.neigh_rows2d.p);
-  V.stride = c.neigh_stride;
-  return V;
-}
-
 }  // namespace emd
 
 using namespace emd;
@@ -508,14 +307,11 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   const int n = c.N_local;
   c.half_neigh = half_neigh ? 1 : 0;
   const int packed = (c.lj_ready && c.lj_prec == EMD_PREC_MIXED) ? 1 : 0;
-  // rows of the mixed form are tiled where every tile's stage fits
-  const bool tiled = packed && !half_neigh && n > 0 && build_tiles(c);
-  const int fmt = tiled ? FMT_TILED : (packed ? FMT_PACKED : FMT_PLAIN);
   require(!packed || (long long)(c.N_local + c.N_ghost) < (1LL << 25), EMD_ERR_ARG,
           "emd_neigh_create: packed rows need fewer than 2^25 particles");
   c.num_neighs.reserve(size_t(n) + 1, c.stream);
   c.neigh_offsets.reserve(size_t(n) + 2, c.stream);
-  c.resize_flag.reserve(2 + NB_SLOTS, c.stream);
+  c.resize_flag.reserve(1 + NB_SLOTS, c.stream);
   if (!c.xl_bin_valid) {  // a second build from one binning in the mixed form
     const int n_all = c.N_local + c.N_ghost;
     c.xl_bin.reserve(size_t(n_all) + 1, c.stream);
@@ -546,9 +342,8 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   a.cut_hi = float(a.cutsq * (1.0 + 4e-5));
   a.half = c.half_neigh;
   a.newton = c.comm_newton;
+  a.packed = packed;
   a.num_neighs = c.num_neighs.p;
-  a.tiles = c.tiles.p;
-  a.tile_of_bin = c.tile_of_bin.p;
   a.stride = n + 1;
   a.flags = c.resize_flag.p;
   const int ibins = (c.nbin[0] - 2 * c.nhalo) * (c.nbin[1] - 2 * c.nhalo) * (c.nbin[2] - 2 * c.nhalo);
@@ -556,13 +351,10 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   int& K = two_d ? c.maxneighs : c.neigh_scratch_k;
   DevBuf<int>& rows = two_d ? c.neighs : c.neigh_rows2d;
   while (true) {
-    // ints: K entries per row, four per granule (32-bit) or eight (tiled)
-    const size_t per_row = tiled ? size_t((K + 7) & ~7) / 2 : size_t((K + 3) & ~3);
-    rows.reserve(size_t(n + 1) * per_row + 4, c.stream);
+    rows.reserve(size_t(n + 1) * size_t((K + 3) & ~3) + 4, c.stream);
     a.rows = rows.p;
-    a.rows16 = reinterpret_cast<unsigned short*>(rows.p);
     a.K = K;
-    EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, (2 + NB_SLOTS) * sizeof(int), c.stream));
+    EMD_CUDA(cudaMemsetAsync(c.resize_flag.p, 0, (1 + NB_SLOTS) * sizeof(int), c.stream));
     if (n > 0) {
       {
         TimedLaunch t(c, "neigh_zero_rows");
@@ -571,17 +363,15 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
       }
       if (ibins > 0) {
         TimedLaunch t(c, "neigh_build");
-        auto k = a.half ? (packed ? k_neigh_bin<true, FMT_PACKED> : k_neigh_bin<true, FMT_PLAIN>)
-                        : (fmt == FMT_TILED ? k_neigh_bin<false, FMT_TILED>
-                                            : (packed ? k_neigh_bin<false, FMT_PACKED> : k_neigh_bin<false, FMT_PLAIN>));
+        auto k = a.half ? (packed ? k_neigh_bin<true, true> : k_neigh_bin<true, false>)
+                        : (packed ? k_neigh_bin<false, true> : k_neigh_bin<false, false>);
         k<<<ibins, NB_THREADS, 0, c.stream>>>(a);
         EMD_CHECK_LAUNCH();
       }
     }
-    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, (2 + NB_SLOTS) * sizeof(int), cudaMemcpyDeviceToHost,
+    EMD_CUDA(cudaMemcpyAsync(c.h_int, c.resize_flag.p, (1 + NB_SLOTS) * sizeof(int), cudaMemcpyDeviceToHost,
                              c.stream));
     EMD_CUDA(cudaStreamSynchronize(c.stream));
-    c.neigh_covered = n > 0 ? c.h_int[1 + NB_SLOTS] : 0;
     int longest = 0;
     for (int k = 1; k <= NB_SLOTS; ++k) longest = std::max(longest, c.h_int[k]);
     c.h_int[1] = longest;
@@ -619,7 +409,6 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   c.neigh_total = total;
   c.neigh_ready = true;
   c.neigh_packed = packed;
-  c.neigh_tiled = tiled;
   c.neigh_builds++;
   if (packed) lj_mixed_after_build(c);
   // the force kernels read CSR (plain rows) or column-major rows
@@ -642,11 +431,7 @@ emd_status emd_neigh_get(emd_ctx* ctx, int* num_neighs, int* entries) {
   if (entries && c.neigh_total > 0) {
     DevBuf<int> tmp;
     tmp.reserve(size_t(c.neigh_total), c.stream);
-    if (c.neigh_tiled) {
-      k_tiled_rows_to_csr<<<blocks_for(n, 256), 256, 0, c.stream>>>(tile_view(c), c.num_neighs.p, c.neigh_offsets.p,
-                                                                    n, tmp.p);
-      EMD_CHECK_LAUNCH();
-    } else if (!c.neigh_layout_2d) {
+    if (!c.neigh_layout_2d) {
       EMD_CUDA(cudaMemcpyAsync(tmp.p, c.neighs.p, sizeof(int) * c.neigh_total, cudaMemcpyDeviceToDevice, c.stream));
     } else {
       const int* src = c.neigh_kind == EMD_NEIGH_2D ? c.neighs.p : c.neigh_rows2d.p;
@@ -654,7 +439,7 @@ emd_status emd_neigh_get(emd_ctx* ctx, int* num_neighs, int* entries) {
                                                               c.neigh_offsets.p, n, tmp.p);
       EMD_CHECK_LAUNCH();
     }
-    if (c.neigh_packed && !c.neigh_tiled) {
+    if (c.neigh_packed) {
       k_unpack<<<blocks_for(c.neigh_total, 256), 256, 0, c.stream>>>(tmp.p, c.neigh_total);
       EMD_CHECK_LAUNCH();
     }

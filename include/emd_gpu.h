@@ -166,13 +166,15 @@ emd_status emd_lj_energy(emd_ctx* ctx, double* pe);
 /* The energy of a thermo step without a second pass over the list (no
  * counterpart in ExaMiniMD, whose PotE::compute runs compute_energy after the
  * step).  After emd_lj_request_energy, the next emd_lj_compute of the mixed
- * form (one type pair, the tiled list of a full-list build) also sums the
- * shifted energy of the positions it uses, inside the force kernel: FP32
- * pair terms with a refined reciprocal, compensated FP32 sums per atom and
- * FP64 sums per tile, within ~1e-10 relative of emd_lj_energy at LJ-4M.
- * emd_lj_force_energy returns it (*available = 1) while no call has moved
- * the owned positions since that compute; otherwise *available = 0 and the
- * caller uses emd_lj_energy.  The request is consumed by that one compute. */
+ * form (one type pair) also sums the shifted energy of the pairs it
+ * evaluates, inside the force kernel: FP32 pair terms corrected to first
+ * order for the exact pair distance, compensated FP32 sums per atom and FP64
+ * sums per block, within ~1e-9 relative of emd_lj_energy at LJ-4M (rounding
+ * with random signs, ~3e-7 / sqrt(atoms)).  The forces are the same bits as
+ * without the energy.  emd_lj_force_energy returns it (*available = 1) while
+ * no call has moved the owned positions since that compute; otherwise
+ * *available = 0 and the caller uses emd_lj_energy.  The request is consumed
+ * by that one compute. */
 emd_status emd_lj_request_energy(emd_ctx* ctx);
 emd_status emd_lj_force_energy(emd_ctx* ctx, double* pe, int* available);
 /* Gradient of a loss L(E, F) with respect to the LJ eps and sigma, for

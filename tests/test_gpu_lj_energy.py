@@ -1,18 +1,15 @@
-"""The tiled mixed-precision LJ force and its fused thermo-step energy (GPU).
+"""The mixed-precision LJ energy fused into the force pass (GPU).
 
-Rows of the mixed form address neighbours inside a per-tile stage in shared
-memory (examinimd_gb300/csrc/lj_tile.cuh); the row sets must be the FP64
-reference's (checked through emd_neigh_get elsewhere), forces within the
-mixed tolerance of FP64.  Where a stage would not fit (a very large cutoff)
-the list falls back to packed 32-bit rows with the same guarantees.
-
-The energy summed inside the force pass on request (emd_lj_request_energy)
-is compared with the FP64 energy of the same positions.  Its error is
-rounding of FP32 pair terms with random signs, about 3e-7 / sqrt(N)
-relative for N atoms (the systematic parts -- the FP32 bin width, the
+On thermo steps the driver asks for the energy with the force
+(emd_lj_request_energy): the mixed kernel then sums the shifted LJ energy of
+the pairs it evaluates, and emd_lj_force_energy returns it while the
+positions stay unchanged.  It is compared with the FP64 energy of the same
+positions (emd_lj_energy).  Its error is rounding of FP32 pair terms with
+random signs, about 3e-7 / sqrt(N) relative for N atoms: the systematic
+parts -- the FP32 bin widths, the shifts added to FP32 coordinates, the
 approximate reciprocal, FP32 coefficients and the cutoff shift -- are
-carried exactly), so the test bounds are 3e-8 at 864 and 4,000 atoms and
-1e-9 at LJ-4M.
+carried exactly.  The test bounds are 3e-8 at 864 and 4,000 atoms and 1e-9
+at LJ-4M.
 """
 import numpy as np
 import pytest
@@ -93,10 +90,25 @@ def test_driver_thermo_uses_the_fused_energy(tmp_path):
     md.close()
 
 
-def test_large_cutoff_falls_back_to_packed_rows():
-    """rc = 6: a single bin's stencil holds more particles than a tile stage,
-    so the list uses packed rows; rows equal the oracle's, forces within the
-    mixed tolerance of FP64."""
+def test_several_types_have_no_fused_energy():
+    """The fused energy covers one type pair; with per-pair parameters the
+    caller falls back to emd_lj_energy."""
+    rng = np.random.default_rng(13)
+    coeffs = [(a, b, float(rng.uniform(0.8, 1.2)), float(rng.uniform(0.9, 1.05)), 2.5)
+              for a in range(1, 14) for b in range(a, 14)]
+    setup = mdloop.LJSetup(5, masses=list(rng.uniform(0.8, 2.0, 13)), coeffs=coeffs)
+    mix = _ctx()
+    mdloop.init(mix, setup, mdloop.make_lattice(setup), precision=1)
+    mix.zero_forces()
+    mix.lj_request_energy()
+    mix.lj_compute()
+    assert mix.lj_force_energy() is None
+
+
+def test_large_cutoff_rows_and_forces():
+    """rc = 6: bins of about 250 particles; rows equal the oracle's, mixed
+    forces within the mixed tolerance of FP64, and the fused energy within
+    its bound."""
     from oracle.orc import Oracle
     setup = mdloop.LJSetup(12, cut=6.0, skin=0.3, coeffs=[(1, 1, 1.0, 1.0, 6.0)])
     state = dict(mdloop.make_lattice(setup))
@@ -111,8 +123,8 @@ def test_large_cutoff_falls_back_to_packed_rows():
         np.testing.assert_array_equal(x, y)
     nl = ref.info()[0]
     assert _rms_rel(mix.get(0, nl)["f"], ref.get(0, nl)["f"]) <= 1e-5
-    # the fused energy needs tiles: not offered here
     mix.zero_forces()
     mix.lj_request_energy()
     mix.lj_compute()
-    assert mix.lj_force_energy() is None
+    fused, exact = mix.lj_force_energy(), ref.lj_energy()
+    assert fused is not None and abs(fused - exact) <= 3e-8 * abs(exact)
