@@ -102,7 +102,7 @@ run {steps}
 """
 
 
-def deck_text(cells: int, steps: int, mass=1.0, temp=1.44) -> str:
+def deck_text(cells: int, steps: int, mass=1.0, temp=1.44, thermo: int = 0) -> str:
     return f"""units lj
 atom_style atomic
 newton off
@@ -117,7 +117,7 @@ pair_coeff 1 1 1.0 1.0 2.5
 neighbor 0.3 bin
 neigh_modify delay 0 every 20 check no
 fix 1 all nve
-thermo 0
+thermo {thermo}
 run {steps}
 """
 
@@ -423,6 +423,12 @@ def run_gpu_arm(a, ws, rank, local):
     T, pe, ke = md.thermo(recompute=True)
 
     extra = {}
+    if not a.no_fp64 and a.workload.startswith("lj") and a.precision == "mixed":
+        extra["fp64"] = fp64_block(local, wl["cells"], a.fp64_steps, 3)
+        extra["fp64"]["mixed_over_fp64"] = value / ws / extra["fp64"]["value"]
+    if not a.no_thermo and a.workload.startswith("lj") and a.precision == "mixed":
+        extra["thermo10"] = thermo_block(local, wl["cells"], a.thermo_steps, 5)
+        extra["thermo10"]["relative_to_thermo0"] = extra["thermo10"]["value"] / (value / ws)
     if not a.no_accuracy and a.workload.startswith("lj") and a.precision == "mixed":
         extra["accuracy"] = lj_accuracy(md, wl["cells"], a.drift_steps, local)
     if not a.no_snap and a.workload == "lj4m":
@@ -536,25 +542,28 @@ def snap_accuracy(md, device: int, cells: int, coeff: str, param: str, steps_don
     return out
 
 
-def snap_cpu_sample(coeff: str, param: str, cells: int = 10, steps: int = 2) -> dict:
-    """The CPU oracle's SNAP (the reference formulation, serial) on a bcc
-    cells^3 sample of the SNAP-W workload, timed per atom-step."""
+def snap_cpu_sample(coeff: str, param: str, cells: int = 16, steps: int = 3, threads: int | None = None) -> dict:
+    """The CPU oracle's SNAP (the reference formulation, OpenMP over atoms on
+    every host core) on a bcc cells^3 sample of the SNAP-W workload, timed per
+    atom-step."""
     from oracle.orc import Oracle
     from tests import mdloop
     from tests.golden.decks import read_snap_files
     setup = mdloop.SnapSetup(cells, cells, cells, read_snap_files(coeff, param), a=3.1803, mass=183.84,
                              lattice_style=2, dt=0.0005)
     state = mdloop.make_lattice(setup)
-    o = Oracle(1)
+    threads = threads or os.cpu_count() or 1
+    o = Oracle(threads)
     mdloop.init(o, setup, state)
     n = o.info()[0]
     t0 = time.perf_counter()
     for s_ in range(1, steps + 1):
         mdloop.step(o, setup, s_)
     dt = time.perf_counter() - t0
-    return {"value": n * steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
-            "sample": f"CPU oracle (ExaMiniMD's SNAP formulation, serial), bcc {cells}^3 = {n} atoms of the SNAP-W "
-                      f"workload, {steps} steps (neighbour rebuild every step)"}
+    return {"value": n * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"CPU oracle (ExaMiniMD's SNAP formulation, OpenMP over atoms with a force buffer per thread), "
+                      f"bcc {cells}^3 = {n} atoms of the SNAP-W workload, {steps} steps (neighbour rebuild every "
+                      f"step), {dt:.1f} s"}
 
 
 def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells: int = 40,
@@ -619,10 +628,117 @@ def snap_measure(local: int, steps_mixed: int, steps_fp64: int, warm: int, cells
         md.close()
     res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
     res["accuracy"] = acc
+    res["energy_drift"] = snap_drift(local, coeff, param)
     if with_cpu:
         res["cpu_baseline"] = snap_cpu_sample(coeff, param)
     res["config"] = SNAP_DESC
     return res
+
+
+def timed_lj(local: int, cells: int, precision: str, steps: int, warm: int, thermo: int = 0) -> dict:
+    """One LJ run of the benchmark deck through the driver, device-timed with
+    CUDA events on the library's stream; returns the run's figures and the
+    per-kernel report (the MD object is closed)."""
+    import torch
+
+    from examinimd_gb300 import MD
+    tmp = tempfile.mkdtemp(prefix="emdlj_")
+    deck = os.path.join(tmp, "in.deck")
+    with open(deck, "w") as fp:
+        fp.write(deck_text(cells, warm + steps, thermo=thermo))
+    md = MD(["-il", deck, "--quiet", "--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL", "--comm-type",
+             "SERIAL", "--precision", precision, "--device", str(local)])
+    ctx = md.ctx
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+    md.run(warm)
+    ctx.synchronize()
+    ctx.timing(True)
+    ctx.timing_reset()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    md.run(steps)
+    e1.record(stream)
+    ctx.synchronize()
+    ms = e0.elapsed_time(e1)
+    rep = ctx.timing_report()
+    ctx.timing(False)
+    N, nl = md.info()["N"], md.info()["N_local"]
+    mean_row = float(md_row_mean(ctx, nl))
+    md.close()
+    return {"value": N * steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps, "warmup": warm,
+            "atoms": N, "n_local": nl, "mean_row": mean_row, "report": rep,
+            "gpu_launches": sum(c for _, c in rep.values())}
+
+
+def fp64_block(local: int, cells: int, steps: int, warm: int) -> dict:
+    """The FP64 drop-in on the same LJ workload: throughput and the roofline
+    of its force kernel (bound by the FP64 pipe)."""
+    r = timed_lj(local, cells, "fp64", steps, warm)
+    kms, kn = r["report"].get("lj_full_fp64", (0.0, 0))
+    out = {k: r[k] for k in ("value", "ms_per_step", "steps", "warmup", "atoms", "gpu_launches")}
+    out["unit"] = METRIC
+    if kn:
+        pk = fp_pipe_peaks(local)
+        inside = (2.5 / 2.8) ** 3
+        flops = r["n_local"] * r["mean_row"] * (8.0 + 13.0 * inside)
+        t = kms / kn * 1e-3
+        bytes_launch = algorithmic_bytes_per_atom("fp64", r["mean_row"]) * r["n_local"]
+        out["roofline"] = {"kernel": "lj_full_fp64", "bound": "fp64", "launch_ms": kms / kn,
+                           "achieved": flops / t / 1e9, "peak": pk["fp64"], "unit": "GFLOP/s",
+                           "frac": flops / t / 1e9 / pk["fp64"], "flops_per_launch": flops,
+                           "hbm_gbs": bytes_launch / t / 1e9, "peak_how": pk["how"],
+                           "note": "8 FP64 operations per listed pair and 13 more inside the cutoff"}
+    return out
+
+
+def thermo_block(local: int, cells: int, steps: int, warm: int, every: int = 10) -> dict:
+    """The mixed form with a thermo evaluation every `every` steps (ExaMiniMD's
+    LJ-32k deck prints thermo every 10): the energy is fused into the force
+    pass of those steps (emd_lj_request_energy)."""
+    r = timed_lj(local, cells, "mixed", steps, warm, thermo=every)
+    rep = r["report"]
+    out = {k: r[k] for k in ("value", "ms_per_step", "steps", "warmup", "atoms", "gpu_launches")}
+    out.update(unit=METRIC, thermo_every=every,
+               kernels_ms_per_launch={k: v[0] / v[1] for k, v in rep.items() if v[1] and k.startswith("lj_full")})
+    return out
+
+
+def snap_drift(local: int, coeff: str, param: str, cells: int = 16, steps: int = 1000, every: int = 25) -> dict:
+    """NVE total-energy drift of SNAP-W in both forms: the SNAP energy (with
+    the 1.25e5 / r^12 term of the reference's repulsion) plus the kinetic
+    energy, both in FP64, sampled every `every` steps of a bcc cells^3 W
+    system from the 300 K lattice; drift = slope of a least-squares line
+    through the samples, relative to |E0|, per 1000 steps."""
+    import numpy as np
+
+    from examinimd_gb300 import MD
+    tmp = tempfile.mkdtemp(prefix="emdsnapdrift_")
+    out = {"atoms": None, "steps": steps, "sample_every": every,
+           "units": "relative change of total energy per 1000 steps (least-squares slope)"}
+    for prec in ("mixed", "fp64"):
+        deck = os.path.join(tmp, f"in.snap.{prec}")
+        with open(deck, "w") as fp:
+            fp.write(snap_deck_text(cells, steps, coeff, param))
+        md = MD(["-il", deck, "--quiet", "--neigh-type", "CSR", "--force-iteration", "NEIGH_FULL",
+                 "--comm-type", "SERIAL", "--precision", prec, "--device", str(local)])
+        t0 = time.perf_counter()
+        es, ts = [], []
+        for s_ in range(0, steps + 1, every):
+            if s_ > 0:
+                md.run(every)
+            T, pe, ke = md.thermo(recompute=True)
+            es.append(pe + ke)
+            ts.append(s_)
+        wall = time.perf_counter() - t0
+        out["atoms"] = md.info()["N"]
+        md.close()
+        e = np.array(es)
+        slope = np.polyfit(np.array(ts, float), e, 1)[0]
+        out[prec] = {"drift_per_1000": slope * 1000.0 / abs(e[0]), "E0_per_atom": float(e[0]),
+                     "end_to_end_per_1000": (e[-1] - e[0]) / abs(e[0]) * 1000.0 / steps,
+                     "max_dev_rel": float(np.abs(e - e[0]).max() / abs(e[0])), "wall_s": wall}
+    return out
 
 
 def fit_measure(local: int, evals: int) -> dict:
@@ -796,6 +912,10 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--no-fit", action="store_true", help="skip the fitting-gradient measurement")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 drop-in sub-block")
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--no-thermo", action="store_true", help="skip the thermo-every-10 sub-block")
+    ap.add_argument("--thermo-steps", type=int, default=100)
     ap.add_argument("--fit-evals", type=int, default=5)
     a = ap.parse_args()
     if a.warmup < 3:

@@ -1181,9 +1181,62 @@ void snap_inside(const orc_ctx* c, int i, std::vector<double>& rij, std::vector<
 }  // namespace
 
 // ForceSNAP::compute / operator() (force_snap_neigh_impl.h:160-208, 591-724)
+// One atom of ForceSNAP::operator() (force_snap_neigh_impl.h:591-724): its
+// pair forces f_ij added to i and subtracted from j in `f`.
+static void snap_atom(orc_ctx* c, Sna& sna, int i, std::vector<double>& rij, std::vector<int>& inside,
+                      std::vector<double>& wj, std::vector<double>& rcutij, std::vector<double>& dbvec, double* f) {
+  snap_inside(c, i, rij, inside, wj, rcutij);
+  const int ninside = int(inside.size());
+  sna.compute_ui(rij, wj, rcutij, ninside);
+  sna.compute_zi();
+  const double* coeffi = &c->beta[size_t(c->snap_map[size_t(c->type[size_t(i)])]) * c->ncoeffall];
+  for (int jj = 0; jj < ninside; jj++) {
+    const int j = inside[size_t(jj)];
+    sna.compute_duidrj(&rij[3 * size_t(jj)], wj[size_t(jj)], rcutij[size_t(jj)]);
+    sna.compute_dbidrj(dbvec);
+    double fij[3] = {0.0, 0.0, 0.0};
+    for (int k = 1; k <= sna.ncoeff; k++) {
+      const double bgb = coeffi[k];
+      fij[0] += bgb * dbvec[3 * size_t(k - 1)];
+      fij[1] += bgb * dbvec[3 * size_t(k - 1) + 1];
+      fij[2] += bgb * dbvec[3 * size_t(k - 1) + 2];
+    }
+    const double dx = rij[3 * size_t(jj)], dy = rij[3 * size_t(jj) + 1], dz = rij[3 * size_t(jj) + 2];
+    const double fdivr = -1.5e6 / std::pow(dx * dx + dy * dy + dz * dz, 7.0);
+    fij[0] += dx * fdivr;
+    fij[1] += dy * fdivr;
+    fij[2] += dz * fdivr;
+    for (int d = 0; d < 3; d++) {
+      f[3 * size_t(i) + d] += fij[d];
+      f[3 * size_t(j) + d] -= fij[d];
+    }
+  }
+}
+
 int orc_snap_compute(orc_ctx* c) {
   ORC_TRY
   if (!c->snap_ready) throw OrcErr("orc_snap_compute: not initialised");
+  if (c->threads > 1) {
+    // OpenMP over atoms (the CPU baseline): each thread its own SNA state and
+    // force buffer, added to f in thread order afterwards.  Serial (one
+    // thread) keeps the reference's order of the f_j subtractions.
+    const int T = c->threads;
+    const size_t nall = size_t(c->N_local + c->N_ghost);
+    std::vector<Sna> snas(size_t(T), c->sna);
+    std::vector<std::vector<double>> fb(size_t(T), std::vector<double>(3 * nall, 0.0));
+#pragma omp parallel num_threads(T)
+    {
+      const int t = omp_get_thread_num();
+      std::vector<double> rij, wj, rcutij, dbvec;
+      std::vector<int> inside;
+#pragma omp for schedule(dynamic, 8)
+      for (int i = 0; i < c->N_local; i++) snap_atom(c, snas[size_t(t)], i, rij, inside, wj, rcutij, dbvec,
+                                                     fb[size_t(t)].data());
+    }
+    for (int t = 0; t < T; t++)
+      for (size_t k = 0; k < 3 * nall; k++) c->f[k] += fb[size_t(t)][k];
+    return 0;
+  }
   std::vector<double> rij, wj, rcutij, dbvec;
   std::vector<int> inside;
   Sna& sna = c->sna;
