@@ -17,6 +17,7 @@
 #include <examinimd.h>
 #include <neighbor_2d.h>
 #include <neighbor_csr.h>
+#include <neighbor_csr_map_constr.h>
 
 static void rec(FILE* fp, const char* name, char t, long long n, const void* p) {
   char nm[32] = {0};
@@ -82,6 +83,14 @@ int main(int argc, char* argv[]) {
     std::vector<int> num(nl), ent;
     if (e.input->neighbor_type == NEIGH_CSR) {
       auto list = ((NeighborCSR<t_neigh_mem_space>*)e.neighbor)->get_neigh_list();
+      for (int i = 0; i < nl; i++) {
+        auto row = list.get_neighs(i);
+        num[i] = row.get_num_neighs();
+        for (int k = 0; k < num[i]; k++) ent.push_back(row(k));
+      }
+    } else if (e.input->neighbor_type == NEIGH_CSR_MAPCONSTR) {
+      // the same CSR container, rows in the hash map's order
+      auto list = ((NeighborCSRMapConstr<t_neigh_mem_space>*)e.neighbor)->get_neigh_list();
       for (int i = 0; i < nl; i++) {
         auto row = list.get_neighs(i);
         num[i] = row.get_num_neighs();

@@ -84,6 +84,13 @@ CASES = {
                                    args=["--neigh-type", "CSR", "--force-iteration", "NEIGH_HALF",
                                          "--comm-type", "SERIAL"],
                                    dump_every=10, keep_steps=[0, 10, 30]),
+    # LJ, CSR_MAPCONSTR (neighbor_csr_map_constr.h): the CSR list built through
+    # a hash set, so its rows hold the CSR pairs in the hash map's order
+    "lj_fcc4_full_csrmap": dict(kind="lj_mapconstr", n=4, mass=1.0, temp=1.44, newton="off", every=10, thermo=10,
+                                steps=30,
+                                args=["--neigh-type", "CSR_MAPCONSTR", "--force-iteration", "NEIGH_FULL",
+                                      "--comm-type", "SERIAL"],
+                                dump_every=10, keep_steps=[0, 10, 30]),
     # SNAP W, the shipped in.snap.W geometry (sc 4x8x8 = 256 atoms)
     "snap_W_sc": dict(kind="snap", a=3.1803, nx=4, ny=8, nz=8, mass=183.84, elem="W", every=1, thermo=5, steps=5,
                       coeff="W.snapcoeff", param="W.snapparam",
@@ -121,7 +128,7 @@ def deck_text(case: dict) -> str:
                            mass_lines="\n".join(f"mass {t + 1} {m}" for t, m in enumerate(masses)),
                            elem_names=" ".join(elems),
                            type_elems=" ".join(case.get("type_elems", [case["elem"]] * len(masses))), **fields)
-    if case["kind"] in ("lj", "lj_idial"):
+    if case["kind"] in ("lj", "lj_idial", "lj_mapconstr"):
         masses = case.get("masses", [case["mass"]])
         coeffs = case.get("coeffs", [(1, 1, 1.0, 1.0, 2.5)])
         style = "lj/cut/idial" if case["kind"] == "lj_idial" else "lj/cut"

@@ -198,7 +198,7 @@ def golden_snap(g) -> dict:
 
 
 def setup_for_case(name: str, case: dict, g=None) -> Setup:
-    if case["kind"] == "lj":
+    if case["kind"] in ("lj", "lj_mapconstr"):
         return LJSetup(case["n"], mass=case["mass"], temp=case["temp"], every=case["every"],
                        newton=case["newton"] == "on", half="NEIGH_HALF" in case["args"],
                        kind=1 if "2D" in case["args"] else 0, masses=case.get("masses"), coeffs=case.get("coeffs"))
