@@ -70,6 +70,8 @@ _SIGS = {
     "emd_lj_energy": ([_P, _DP], _I),
     "emd_lj_energy_noalloc": ([_P, _DP], _I),
     "emd_lj_request_energy": ([_P], _I),
+    "emd_snap_request_energy": ([_P], _I),
+    "emd_snap_force_energy": ([_P, _DP, _IP], _I),
     "emd_lj_force_energy": ([_P, _DP, _IP], _I),
     "emd_lj_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_batch_create": ([C.POINTER(_P), _I, _I, _IP, _DP, _DP, _DP, _D, _D, _D, _D, _D, _D, _I, _I, _D], _I),
@@ -345,6 +347,16 @@ class Context:
         """The energy summed by the last lj_compute, or None (emd_lj_force_energy)."""
         e, ok = _D(), _I()
         self._ok(self.lib.emd_lj_force_energy(self.h, C.byref(e), C.byref(ok)), "emd_lj_force_energy")
+        return e.value if ok.value else None
+
+    def snap_request_energy(self):
+        """The next snap_compute (FP64 form) also sums the energy (emd_snap_request_energy)."""
+        self._ok(self.lib.emd_snap_request_energy(self.h), "emd_snap_request_energy")
+
+    def snap_force_energy(self):
+        """The energy summed by the last snap_compute, or None (emd_snap_force_energy)."""
+        e, ok = _D(), _I()
+        self._ok(self.lib.emd_snap_force_energy(self.h, C.byref(e), C.byref(ok)), "emd_snap_force_energy")
         return e.value if ok.value else None
 
     def lj_energy_noalloc(self) -> float:

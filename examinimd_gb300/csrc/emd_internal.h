@@ -188,6 +188,11 @@ struct Ctx {
   double lj_pe_fused = 0;
   unsigned long long lj_pe_fused_version = 0;
   DevBuf<double> lj_pe_part;
+  // the same for SNAP (FP64 form): per-atom energies written by the force
+  // kernel, summed when asked for
+  bool snap_energy_request = false;
+  bool snap_pe_fused_valid = false;
+  unsigned long long snap_pe_fused_version = 0;
   // bumped by every call that moves owned positions
   unsigned long long x_version = 0;
   // mixed form: bin coordinates of every particle at the last list build,

@@ -276,10 +276,20 @@ static void snap_launch(Ctx& c, bool energy) {
     return;
   }
   if (fp64) {
+    // asked for (emd_snap_request_energy): the per-atom energies in the same pass
+    const bool fused = c.snap_energy_request;
+    if (fused) {
+      h->eatom.reserve(size_t(n), c.stream);
+      A.eatom = h->eatom.p;
+    }
     auto k = k_snap<double, 0>;
     EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    TimedLaunch t(c, "snap_fp64");
+    TimedLaunch t(c, fused ? "snap_fp64_energy" : "snap_fp64");
     k<<<n, SNAP_THREADS, smem, c.stream>>>(A);
+    if (fused) {
+      c.snap_pe_fused_valid = true;
+      c.snap_pe_fused_version = c.x_version;
+    }
   } else {
     TimedLaunch t(c, "snap_mixed");
     snap_mixed_launch(A, smem, c.stream);
@@ -538,7 +548,28 @@ emd_status emd_snap_set_beta(emd_ctx* ctx, const double* beta) {
 
 emd_status emd_snap_compute(emd_ctx* ctx) {
   EMD_API_BEGIN
+  struct EndRequest {  // a request serves this compute only
+    Ctx& c;
+    ~EndRequest() { c.snap_energy_request = false; }
+  } end_request{c};
+  c.snap_pe_fused_valid = false;
   snap_launch(c, false);
+  EMD_API_END
+}
+
+emd_status emd_snap_request_energy(emd_ctx* ctx) {
+  EMD_API_BEGIN
+  require(c.snap != nullptr, EMD_ERR_STATE, "emd_snap_request_energy: SNAP not initialised");
+  c.snap_energy_request = true;
+  EMD_API_END
+}
+
+emd_status emd_snap_force_energy(emd_ctx* ctx, double* pe, int* available) {
+  EMD_API_BEGIN
+  require(pe && available, EMD_ERR_ARG, "emd_snap_force_energy: null output");
+  *available = (c.snap_pe_fused_valid && c.snap_pe_fused_version == c.x_version) ? 1 : 0;
+  *pe = 0.0;
+  if (*available && c.N_local > 0) *pe = device_sum(c, static_cast<SnapHost*>(c.snap)->eatom.p, c.N_local);
   EMD_API_END
 }
 

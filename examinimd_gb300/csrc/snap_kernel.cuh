@@ -715,6 +715,10 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
   __syncthreads();
   const R* cY = (sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cY) : reinterpret_cast<const R*>(S.cY_f)) +
                 (size_t)ei * S.nfull;
+  // FP64 forces with A.eatom set: the atom's energy in the same pass, the
+  // terms and order of the energy variant (MODE 1) below
+  const bool fuse_e = MODE == 0 && kF64 && A.eatom != nullptr;
+  double eacc = 0.0;
   for (int e = tid; e < (MODE == 2 ? 0 : S.nyh); e += SNAP_THREADS) {
     R yr = 0, yi = 0;
     for (int k = S.yred_off[e]; k < S.yred_off[e + 1]; ++k) {
@@ -722,6 +726,13 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
       const R cy = cY[S.jobs[jb] >> 8];
       yr += cy * zs[jb].r;
       yi += cy * zs[jb].i;
+    }
+    if (fuse_e) {
+      int j = 0;
+      while (yoff(j + 1) <= e) ++j;
+      const int q = e - yoff(j), mb = q / (j + 1), ma = q % (j + 1);
+      const Cplx<double> u = utot[uoff(j) + ma * (j + 1) + mb];
+      eacc += hw(j, ma, mb) * (u.r * double(yr) + u.i * double(yi));
     }
     if constexpr (MODE == 0) {  // w Y / f: the force runs on V = f U (d_reverse)
       const R f = sizeof(R) == sizeof(double) ? R(S.yscale[e]) : R(S.yscale_f[e]);
@@ -731,6 +742,11 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
     ytot[e] = Cplx<R>{yr, yi};
   }
   __syncthreads();
+  if (fuse_e) {
+    for (int nb = tid; nb < ninside; nb += SNAP_THREADS) eacc += nd[ND_EP * A.cap + nb] * 1.5;  // x 2/3 below
+    const double t = block_sum(eacc, red);
+    if (tid == 0) A.eatom[i] = S.beta0[ei] + (2.0 / 3.0) * t;
+  }
 
   // ---- energy (optional): beta_0 + (2/3) sum_j sum_half w Re(conj(U) Y) + pair terms
   if constexpr (MODE == 1) {

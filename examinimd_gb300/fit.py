@@ -133,10 +133,13 @@ class SnapConfig(_Config):
         self.build()
 
     def _compute(self):
+        # the energy of this configuration from the same FP64 pass
+        self.ctx.snap_request_energy()
         self.ctx.snap_compute()
 
     def energy(self):
-        return self.ctx.snap_energy()
+        e = self.ctx.snap_force_energy()
+        return self.ctx.snap_energy() if e is None else e
 
     def adjoint(self, dL_dF, dL_dE, ncoeffall):
         return self.ctx.snap_adjoint(self.to_ctx_order(dL_dF), dL_dE, 1, ncoeffall)[0]

@@ -171,6 +171,7 @@ class ForceSNAP_GB300 : public Force {
   void init_coeff(int nargs, char** args) override;
   void compute(System* system, Binning*, Neighbor*) override;
   double compute_energy(System* system, Binning*, Neighbor*) override;
+  void request_energy() override;
   const char* name() override { return "ForceSNAP_GB300"; }
   double rcutmax = 0;
 };

@@ -205,8 +205,17 @@ void ForceSNAP_GB300::compute(System* system, Binning*, Neighbor*) {
 
 double ForceSNAP_GB300::compute_energy(System* system, Binning*, Neighbor*) {
   double pe = 0.0;
-  check(emd_snap_energy(system->ctx, &pe), system->ctx, "emd_snap_energy");
+  int fused = 0;
+  check(emd_snap_force_energy(system->ctx, &pe, &fused), system->ctx, "emd_snap_force_energy");
+  if (!fused) check(emd_snap_energy(system->ctx, &pe), system->ctx, "emd_snap_energy");
   return pe;
+}
+
+void ForceSNAP_GB300::request_energy() {
+  // the FP64 form sums the energy inside the force pass (the mixed form keeps
+  // the separate FP64 energy pass)
+  if (precision_ == EMD_PREC_FP64)
+    check(emd_snap_request_energy(system_->ctx), system_->ctx, "emd_snap_request_energy");
 }
 
 // ---------------------------------------------------------------- NVE

@@ -223,6 +223,16 @@ emd_status emd_snap_compute(emd_ctx* ctx);
  * per ordered pair that integrates the reference's extra repulsion.
  * ExaMiniMD has no SNAP energy (force.h:54); this is an extension. */
 emd_status emd_snap_energy(emd_ctx* ctx, double* pe);
+/* The energy of a thermo step (or of a fitting forward pass) from the force
+ * pass itself (no counterpart in ExaMiniMD, which has no SNAP energy).
+ * After emd_snap_request_energy, the next emd_snap_compute of the FP64 form
+ * also writes every owned atom's emd_snap_energy term, with the same
+ * arithmetic and order as emd_snap_energy, so the sum is the same bits.
+ * emd_snap_force_energy returns that sum (*available = 1) while no call has
+ * moved the owned positions since; the mixed form and every other case give
+ * *available = 0 (use emd_snap_energy).  The request serves one compute. */
+emd_status emd_snap_request_energy(emd_ctx* ctx);
+emd_status emd_snap_force_energy(emd_ctx* ctx, double* pe, int* available);
 /* Number of bispectrum components (55 at twojmax 8). */
 emd_status emd_snap_ncoeff(emd_ctx* ctx, int* ncoeff);
 /* Gradient of a loss L(E, F) with respect to the SNAP linear coefficients,

@@ -174,3 +174,33 @@ def test_snap_mixed_force_error_on_golden_decks(name, golden):
     assert err.max() / scale <= 1e-4
     ref.close()
     mix.close()
+
+
+def test_snap_energy_from_the_force_pass(golden):
+    """After emd_snap_request_energy the FP64 force kernel also writes every
+    atom's energy term with the energy pass's arithmetic and order: the sum
+    equals emd_snap_energy bit for bit, and the forces are those of a plain
+    compute.  A moved position retires the value; the mixed form offers none."""
+    from examinimd_gb300 import EMD_PREC_MIXED
+    setup, _ = _snap_setup(golden, 4, 4, 4, lattice_style=2)
+    state = dict(mdloop.make_lattice(setup))
+    state["x"] = state["x"] + np.random.default_rng(9).normal(0, 0.05, state["x"].shape)
+    a, b = _ctx(), _ctx()
+    mdloop.init(a, setup, state)
+    mdloop.init(b, setup, state)
+    nl = a.info()[0]
+    b.zero_forces()
+    b.snap_request_energy()
+    b.snap_compute()
+    b.comm_update_force()
+    fused = b.snap_force_energy()
+    assert fused is not None and fused == b.snap_energy() == a.snap_energy()
+    np.testing.assert_array_equal(a.get(0, nl)["f"], b.get(0, nl)["f"])
+    b.nve_initial()
+    assert b.snap_force_energy() is None
+    mix = _ctx()
+    mdloop.init(mix, setup, state, precision=EMD_PREC_MIXED)
+    mix.zero_forces()
+    mix.snap_request_energy()
+    mix.snap_compute()
+    assert mix.snap_force_energy() is None
