@@ -180,7 +180,7 @@ def test_snap_energy_from_the_force_pass(golden):
     """After emd_snap_request_energy the FP64 force kernel also writes every
     atom's energy term with the energy pass's arithmetic and order: the sum
     equals emd_snap_energy bit for bit, and the forces are those of a plain
-    compute.  A moved position retires the value; the mixed form offers none."""
+    compute (to the rounding of their atomic scatter).  A moved position retires the value; the mixed form offers none."""
     from examinimd_gb300 import EMD_PREC_MIXED
     setup, _ = _snap_setup(golden, 4, 4, 4, lattice_style=2)
     state = dict(mdloop.make_lattice(setup))
@@ -195,7 +195,9 @@ def test_snap_energy_from_the_force_pass(golden):
     b.comm_update_force()
     fused = b.snap_force_energy()
     assert fused is not None and fused == b.snap_energy() == a.snap_energy()
-    np.testing.assert_array_equal(a.get(0, nl)["f"], b.get(0, nl)["f"])
+    # f_j is scattered with FP64 atomics: two computes agree to rounding
+    ok, info = _force_ok(b.get(0, nl)["f"], a.get(0, nl)["f"])
+    assert ok, info
     b.nve_initial()
     assert b.snap_force_energy() is None
     mix = _ctx()
