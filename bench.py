@@ -694,13 +694,15 @@ def fp64_block(local: int, cells: int, steps: int, warm: int) -> dict:
 
 def thermo_block(local: int, cells: int, steps: int, warm: int, every: int = 10) -> dict:
     """The mixed form with a thermo evaluation every `every` steps (ExaMiniMD's
-    LJ-32k deck prints thermo every 10): the energy is fused into the force
-    pass of those steps (emd_lj_request_energy)."""
+    LJ-32k deck prints thermo every 10): on those steps the force call also
+    runs the mixed-precision energy kernel over the same rows
+    (emd_lj_request_energy)."""
     r = timed_lj(local, cells, "mixed", steps, warm, thermo=every)
     rep = r["report"]
     out = {k: r[k] for k in ("value", "ms_per_step", "steps", "warmup", "atoms", "gpu_launches")}
     out.update(unit=METRIC, thermo_every=every,
-               kernels_ms_per_launch={k: v[0] / v[1] for k, v in rep.items() if v[1] and k.startswith("lj_full")})
+               kernels_ms_per_launch={k: v[0] / v[1] for k, v in rep.items()
+                                      if v[1] and k.startswith(("lj_full", "lj_energy", "lj_pos"))})
     return out
 
 

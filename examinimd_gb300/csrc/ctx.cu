@@ -329,7 +329,9 @@ void emd_destroy(emd_ctx* ctx) {
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
   free_snap(c);
-  for (auto* b : {&c.v, &c.f, &c.q, &c.mass_d, &c.stage_d, &c.stage_dl, &c.lj_params, &c.red, &c.red2}) b->release();
+  for (auto* b : {&c.v, &c.f, &c.q, &c.mass_d, &c.stage_d, &c.stage_dl, &c.lj_params, &c.red, &c.red2, &c.dtfm_d,
+                  &c.lj_intensity, &c.lj_pe_part})
+    b->release();
   for (auto* b : {&c.type, &c.id, &c.stage_i, &c.pack, &c.ghost_owner, &c.ghost_img, &c.flags, &c.flags_scan,
                   &c.bincount, &c.binoffsets, &c.permute, &c.binof, &c.bin_cursor, &c.perm_tmp, &c.num_neighs,
                   &c.neigh_offsets, &c.neighs, &c.resize_flag, &c.abin})
@@ -338,6 +340,7 @@ void emd_destroy(emd_ctx* ctx) {
   c.stage_x4.release();
   c.xl.release();
   c.xl_bin.release();
+  c.lj_xlo.release();
   c.bin_c3.release();
   c.ctr_tab.release();
   c.bin_ctab.release();

@@ -188,6 +188,7 @@ struct Ctx {
   double lj_pe_fused = 0;
   unsigned long long lj_pe_fused_version = 0;
   DevBuf<double> lj_pe_part;
+  DevBuf<float4> lj_xlo;    // x - bin centre - xl per particle (fused energy)
   // the same for SNAP (FP64 form): per-atom energies written by the force
   // kernel, summed when asked for
   bool snap_energy_request = false;

@@ -10,7 +10,7 @@
 // positions.  List rows are column-major int4 granules (neigh_rows.cuh) and
 // each packed entry carries the per-dimension bin offset k = (bin_j - bin_i)
 // + 1, so x_i - x_j = (xl_i - xl_j) + (1 - k) w is formed in FP32 from small
-// numbers.  Pairs whose FP32 r^2 lies within 1e-6 relative of the cutoff are
+// numbers.  Pairs whose FP32 r^2 lies within 4e-6 relative of the cutoff are
 // re-tested with the FP64 positions, so the set of interacting pairs equals
 // the FP64 drop-in's.
 #include "emd_device.cuh"
@@ -52,6 +52,18 @@ __global__ void __launch_bounds__(256) k_refresh_xl(const double4_32a* __restric
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
   xl[a] = rel(x4[a], ctr.at(a));
+}
+
+// The rounding of each particle's FP32 copy: xl + xlo = x - bin centre to
+// FP64 precision (the thermo-step energy's pair differences)
+__global__ void __launch_bounds__(256) k_pos_remainder(const double4_32a* __restrict__ x4, BinCentres ctr, int n,
+                                                       const float4* __restrict__ xl, float4* __restrict__ xlo) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  const double4_32a p = x4[a], o = ctr.at(a);
+  const float4 q = xl[a];
+  xlo[a] = make_float4(float((p.x - o.x) - double(q.x)), float((p.y - o.y) - double(q.y)),
+                       float((p.z - o.z) - double(q.z)), 0.f);
 }
 
 // IntegratorNVE::initial_integrate (integrator_nve.cpp:64-73) with FMA, plus
@@ -110,66 +122,89 @@ __device__ __forceinline__ int4 ld_list(const int4* p) {
   return r;
 }
 
-// ENERGY (single type): also the shifted energy of the same pairs, one FP64
-// partial per block (lj_pair.cuh, pair_energy)
-template <bool SINGLE, bool ZERO, bool ENERGY>
+// One row: four entries per coalesced int4 load, the next granule
+// prefetched while the current four pairs are evaluated; `quad` evaluates a
+// granule.  Unused slots of the last granule become padding: i itself with
+// the code k = (3, 3, 3), far outside the cutoff, so they add nothing.
+template <typename Quad>
+__device__ __forceinline__ void lj_row(int i, const int4* __restrict__ q, int cnt, int stride, Quad&& quad) {
+  const int nfull = cnt >> 2;
+  int4 e = nfull > 0 ? ld_list(q) : make_int4(0, 0, 0, 0);
+  for (int kq = 0; kq < nfull; ++kq) {
+    const int4 en = (kq + 1 < nfull) ? ld_list(q + (size_t)(kq + 1) * stride) : e;
+    quad(e);
+    e = en;
+  }
+  const int rem = cnt & 3;
+  if (rem) {
+    int4 t = ld_list(q + (size_t)nfull * stride);
+    const int self = (i << 6) | 0x3f;
+    if (rem < 2) t.y = self;
+    if (rem < 3) t.z = self;
+    t.w = self;
+    quad(t);
+  }
+}
+
+template <bool SINGLE, bool ZERO>
 __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict__ xl,
                                                        const double4_32a* __restrict__ x4, double* __restrict__ f,
                                                        const int4* __restrict__ rows4, int stride,
                                                        const int* __restrict__ num, LJParamsF P, float wx, float wy,
-                                                       float wz, int n, LJEnergyF E, double* __restrict__ e_part) {
-  __shared__ double esum[ENERGY ? 4 : 1];
+                                                       float wz, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!ENERGY && i >= n) return;
+  if (i >= n) return;
+  PairCtx C;
+  C.xi = xl[i];
+  C.i = i;
+  C.ti = __float_as_int(C.xi.w);
+  C.set_bin_width(wx, wy, wz);
+  C.x4 = x4;
+  Acc acc;
+  lj_row(i, rows4 + i, num[i], stride, [&](const int4& e) { lj_quad<SINGLE>(C, e, xl, P, acc); });
+  const double fx = double(acc.sxy.x) - double(acc.cxy.x);
+  const double fy = double(acc.sxy.y) - double(acc.cxy.y);
+  const double fz = double(acc.sz) - double(acc.cz);
+  if (ZERO) {  // the pending deep_copy(f, 0) folded into the store
+    f[3 * i] = 0.0 + fx;
+    f[3 * i + 1] = 0.0 + fy;
+    f[3 * i + 2] = 0.0 + fz;
+  } else {
+    f[3 * i] += fx;
+    f[3 * i + 1] += fy;
+    f[3 * i + 2] += fz;
+  }
+}
+
+// The shifted LJ energy over the same rows and pair decisions as the force
+// (single type pair), one FP64 partial per block (lj_pair.cuh, pair_energy).
+// A kernel of its own: evaluated inside the force loop, the compiler's
+// treatment of the shared expressions moved force sums by an ulp (measured),
+// and the forces of a thermo step must be the force-only kernel's bits.
+__global__ void __launch_bounds__(128) k_lj_energy_mixed(const float4* __restrict__ xl,
+                                                         const double4_32a* __restrict__ x4,
+                                                         const int4* __restrict__ rows4, int stride,
+                                                         const int* __restrict__ num, LJParamsF P, float wx,
+                                                         float wy, float wz, int n, LJEnergyF E,
+                                                         double* __restrict__ e_part) {
+  __shared__ double esum[4];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double e_atom = 0.0;
   if (i < n) {
     PairCtx C;
     C.xi = xl[i];
     C.i = i;
-    C.ti = __float_as_int(C.xi.w);
+    C.ti = 0;
     C.set_bin_width(wx, wy, wz);
     C.x4 = x4;
-    const int cnt = num[i];
-    const int4* q = rows4 + i;
-    const int nfull = cnt >> 2;
-    Acc acc;
     EAcc ea;
-    int4 e = nfull > 0 ? ld_list(q) : make_int4(0, 0, 0, 0);
-    for (int kq = 0; kq < nfull; ++kq) {
-      const int4 en = (kq + 1 < nfull) ? ld_list(q + (size_t)(kq + 1) * stride) : e;
-      lj_quad<SINGLE, ENERGY>(C, e, xl, P, acc, &E, &ea);
-      e = en;
-    }
-    const int rem = cnt & 3;
-    if (rem) {
-      // unused slots of the last granule become padding: i itself with the
-      // code k = (3, 3, 3), far outside the cutoff, so they add nothing
-      int4 t = ld_list(q + (size_t)nfull * stride);
-      const int self = (i << 6) | 0x3f;
-      if (rem < 2) t.y = self;
-      if (rem < 3) t.z = self;
-      t.w = self;
-      lj_quad<SINGLE, ENERGY>(C, t, xl, P, acc, &E, &ea);
-    }
-    const double fx = double(acc.sxy.x) - double(acc.cxy.x);
-    const double fy = double(acc.sxy.y) - double(acc.cxy.y);
-    const double fz = double(acc.sz) - double(acc.cz);
-    if (ZERO) {  // the pending deep_copy(f, 0) folded into the store
-      f[3 * i] = 0.0 + fx;
-      f[3 * i + 1] = 0.0 + fy;
-      f[3 * i + 2] = 0.0 + fz;
-    } else {
-      f[3 * i] += fx;
-      f[3 * i + 1] += fy;
-      f[3 * i + 2] += fz;
-    }
+    ea.lo_i = E.xlo[i];
+    lj_row(i, rows4 + i, num[i], stride, [&](const int4& e) { lj_energy_quad(C, e, xl, P, E, ea); });
     // full list: half of every ordered pair's shifted energy
-    if (ENERGY) e_atom = 0.5 * ((double(ea.es) - double(ea.ec)) - double(ea.npair) * E.ecut);
+    e_atom = 0.5 * ea.energy(E);
   }
-  if (ENERGY) {
-    const double t = block_sum(e_atom, esum);
-    if (threadIdx.x == 0) e_part[blockIdx.x] = t;
-  }
+  const double t = block_sum(e_atom, esum);
+  if (threadIdx.x == 0) e_part[blockIdx.x] = t;
 }
 
 BinFrame frame(const Ctx& c) {
@@ -253,17 +288,15 @@ void lj_mixed_compute(Ctx& c) {
   const bool zero = c.f_zero_pending & 1;
   const dim3 g(blocks_for(n, 128)), b(128);
   const float wx = float(F.wx), wy = float(F.wy), wz = float(F.wz);
-  // the fused energy of a thermo step (emd_lj_request_energy), single type pair
+  // the energy of a thermo step (emd_lj_request_energy), single type pair
   const bool energy = c.lj_energy_request && c.lj_uniform;
   LJEnergyF E{};
   double* part = nullptr;
   if (energy) {
     const double a64 = c.lj_single_d[0] / 12.0, b64 = c.lj_single_d[1] / 6.0;
     const double r2c = 1.0 / c.lj_single_cutsq_d, r6c = r2c * r2c * r2c;
-    E.a = float(a64);
-    E.a_lo = float(a64 - double(E.a));
-    E.b = float(b64);
-    E.b_lo = float(b64 - double(E.b));
+    E.a = a64;
+    E.b = b64;
     E.ecut = r6c * (a64 * r6c - b64);
     const double w64[3] = {F.wx, F.wy, F.wz};
     const float wl[3] = {float(w64[0] - double(wx)), float(w64[1] - double(wy)), float(w64[2] - double(wz))};
@@ -273,22 +306,24 @@ void lj_mixed_compute(Ctx& c) {
     E.wlo_z = wl[2];
     c.lj_pe_part.reserve(size_t(g.x) + 1, c.stream);
     part = c.lj_pe_part.p;
+    c.lj_xlo.reserve(size_t(n_all) + 1, c.stream);
+    E.xlo = c.lj_xlo.p;
+    TimedLaunch t(c, "lj_pos_remainder");
+    k_pos_remainder<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, c.xl.p, c.lj_xlo.p);
+    EMD_CHECK_LAUNCH();
   }
   {
-    TimedLaunch t(c, energy ? "lj_full_mixed_energy" : "lj_full_mixed");
-    using KernelT = void (*)(const float4*, const double4_32a*, double*, const int4*, int, const int*, LJParamsF,
-                             float, float, float, int, LJEnergyF, double*);
-    KernelT k;
-    if (c.lj_uniform) {
-      if (energy) k = zero ? k_lj_full_mixed<true, true, true> : k_lj_full_mixed<true, false, true>;
-      else k = zero ? k_lj_full_mixed<true, true, false> : k_lj_full_mixed<true, false, false>;
-    } else {
-      k = zero ? k_lj_full_mixed<false, true, false> : k_lj_full_mixed<false, false, false>;
-    }
-    k<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n, E, part);
+    TimedLaunch t(c, "lj_full_mixed");
+    auto k = c.lj_uniform ? (zero ? k_lj_full_mixed<true, true> : k_lj_full_mixed<true, false>)
+                          : (zero ? k_lj_full_mixed<false, true> : k_lj_full_mixed<false, false>);
+    k<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n);
     EMD_CHECK_LAUNCH();
   }
   if (energy) {
+    TimedLaunch t(c, "lj_energy_mixed");
+    k_lj_energy_mixed<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n, E,
+                                              part);
+    EMD_CHECK_LAUNCH();
     c.lj_pe_fused = device_sum(c, part, int(g.x));
     c.lj_pe_fused_version = c.x_version;
     c.lj_pe_fused_valid = true;

@@ -135,32 +135,58 @@ __device__ __forceinline__ void lj_force(const PairGeo& g, bool in, float2& fxy,
 
 // ---- the energy fused into the force pass (single type pair, thermo steps)
 //
-// The FP32 r^2 of a pair is biased, not just noisy: the bin shift added to
-// grid-aligned FP32 coordinates rounds the same way pair after pair, about
-// 1e-8 relative in the energy of an fcc liquid.  So the energy takes the
-// exact difference dx + lo, lo from the two-sum remainders of the pair's
-// subtraction and shift and from the FP32 bin width's own remainder, and
-// evaluates e(r^2) + e'(r^2) * 2 (dx . lo); the correction lies below the
-// rounding of r^2 and would vanish if added to r^2 in FP32.  The reciprocal
-// is refined by one Newton step, the coefficients a = lj1 / 12, b = lj2 / 6
-// carry their FP32 remainders, and the cutoff shift is subtracted per atom in
-// FP64, so what is left is rounding with random signs.  The forces are the
+// The energy of pair evaluations in plain FP32 is biased, not just noisy.
+// The bin shift added to grid-aligned FP32 coordinates rounds the same way
+// pair after pair (about 1e-8 relative in an fcc liquid), and on a lattice,
+// where thousands of pairs share one distance, the rounding of e(r^2) at
+// that distance repeats in every one of them (5e-8 relative).  So each pair
+// is carried as a value and its first-order remainder, with error-free
+// transformations (Knuth's two-sum, Dekker's product through FMA):
+//  * the difference x_i - x_j = dx + lo: lo from the two-sum remainders of
+//    the pair's subtraction and shift, the FP32 bin width's own remainder
+//    and the rounding of both FP32 positions (xlo: an owned particle and its
+//    ghost copies round differently, and on a lattice that repeats too);
+//  * r^2 = t + delta: t the force's FP32 value, delta = 2 dx . lo plus the
+//    exact rounding of t's squares and sums;
+//  * 1 / r^2 = s (1 + eps), s the Newton-refined reciprocal of t, eps =
+//    1 - t s - delta s;
+//  * r^-6 = s3 + d3 and r^-12 = s6 + d6 from the products' remainders.
+// Per atom the values go to compensated sums and the remainders to plain
+// sums; the energy a S12 - b S6 - n ecut is formed in FP64 at the end.  What
+// is left is second order, about 1e-14 relative.  The forces are the
 // force-only kernel's, bit for bit.
 struct LJEnergyF {
-  float a, a_lo, b, b_lo;
+  double a, b;                 // lj1 / 12, lj2 / 6
   double ecut;                 // shifted energy at the cutoff, FP64
   float2 nwlo_xy, wlo_xy;      // the FP32 bin width's remainders, as PairCtx holds the widths
   float nwlo_z, wlo_z;
+  const float4* xlo;           // per particle: x - bin centre - xl, rounded to FP32
+};
+
+// Sum of a series of non-negative FP32 values with every addition's exact
+// rounding error kept (Fast2Sum on the larger and smaller operand), read
+// back in FP64 as s + c.  Kahan's form would lose the rounding of x - c at
+// every step: about 1e-9 of the energy on a lattice.
+struct NSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float hi = fmaxf(s, x), lo = fminf(s, x);
+    const float t = __fadd_rn(hi, lo);
+    c = __fadd_rn(c, __fsub_rn(lo, __fsub_rn(t, hi)));
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return double(s) + double(c); }
 };
 
 struct EAcc {
-  float es = 0.f, ec = 0.f;  // compensated FP32 energy sum
+  NSum s6, s12;              // sum of r^-6 and r^-12 over the interacting pairs
+  float d6 = 0.f, d12 = 0.f;  // their remainders
   int npair = 0;             // interacting pairs
-  __device__ __forceinline__ void add(float v) {
-    const float y = __fsub_rn(v, ec);
-    const float t = __fadd_rn(es, y);
-    ec = __fsub_rn(__fsub_rn(t, es), y);
-    es = t;
+  float4 lo_i;               // the row atom's xlo
+  // the row's shifted pair energies, in FP64
+  __device__ __forceinline__ double energy(const LJEnergyF& E) const {
+    const double r6 = s6.value() + double(d6), r12 = s12.value() + double(d12);
+    return (E.a * r12 - E.b * r6) - double(npair) * E.ecut;
   }
 };
 
@@ -171,8 +197,8 @@ __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
   return __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
 }
 
-__device__ __forceinline__ float pair_energy(const PairCtx& C, const LJEnergyF& E, int e, const float4& xj,
-                                             const PairGeo& g, bool in) {
+__device__ __forceinline__ void pair_energy(const PairCtx& C, const LJEnergyF& E, int e, const float4& xj,
+                                            const PairGeo& g, bool in, EAcc& ea) {
   constexpr int kExp = 0x4B000000;  // bits of 2^23, as lj_geo forms the shift
   const float2 txy = __fadd2_rn(make_float2(__int_as_float((e & 0x30) | kExp), __int_as_float((e & 0x0C) | kExp)),
                                 make_float2(-8388608.0f, -8388608.0f));
@@ -183,28 +209,48 @@ __device__ __forceinline__ float pair_energy(const PairCtx& C, const LJEnergyF& 
   const float slz = __fmaf_rn(tz, E.nwlo_z, E.wlo_z);
   const float2 t1 = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
   const float t1z = __fsub_rn(C.xi.z, xj.z);
-  const float lox = __fadd_rn(__fadd_rn(two_sum_err(C.xi.x, -xj.x, t1.x), two_sum_err(t1.x, sxy.x, g.dxy.x)), sl.x);
-  const float loy = __fadd_rn(__fadd_rn(two_sum_err(C.xi.y, -xj.y, t1.y), two_sum_err(t1.y, sxy.y, g.dxy.y)), sl.y);
-  const float loz = __fadd_rn(__fadd_rn(two_sum_err(C.xi.z, -xj.z, t1z), two_sum_err(t1z, sz, g.dz)), slz);
-  const float corr = 2.0f * __fmaf_rn(g.dz, loz, __fmaf_rn(g.dxy.y, loy, g.dxy.x * lox));  // r^2 - fl(r^2)
+  const float4 lj = E.xlo[e >> 6];
+  const float2 pl = __ffma2_rn(make_float2(lj.x, lj.y), make_float2(-1.f, -1.f), make_float2(ea.lo_i.x, ea.lo_i.y));
+  const float plz = __fsub_rn(ea.lo_i.z, lj.z);
+  const float lox = __fadd_rn(__fadd_rn(two_sum_err(C.xi.x, -xj.x, t1.x), two_sum_err(t1.x, sxy.x, g.dxy.x)),
+                              __fadd_rn(sl.x, pl.x));
+  const float loy = __fadd_rn(__fadd_rn(two_sum_err(C.xi.y, -xj.y, t1.y), two_sum_err(t1.y, sxy.y, g.dxy.y)),
+                              __fadd_rn(sl.y, pl.y));
+  const float loz = __fadd_rn(__fadd_rn(two_sum_err(C.xi.z, -xj.z, t1z), two_sum_err(t1z, sz, g.dz)),
+                              __fadd_rn(slz, plz));
+  // t = fma(dz, dz, fl(dx^2 + dy^2)) as lj_geo forms it; its exact rounding
+  // from the squares' Dekker remainders and the sums' two-sum remainders (the
+  // difference of two roundings of dz^2 + fl(dx^2 + dy^2) is exact)
+  const float2 sq = __fmul2_rn(g.dxy, g.dxy);
+  const float2 esq = __ffma2_rn(g.dxy, g.dxy, make_float2(-sq.x, -sq.y));
+  const float A = __fadd_rn(sq.x, sq.y);
+  const float pz = __fmul_rn(g.dz, g.dz);
+  const float B = __fadd_rn(pz, A);
+  const float rnd = __fadd_rn(__fadd_rn(__fsub_rn(B, g.rsq), two_sum_err(pz, A, B)),
+                              __fadd_rn(__fadd_rn(two_sum_err(sq.x, sq.y, A), __fmaf_rn(g.dz, g.dz, -pz)),
+                                        __fadd_rn(esq.x, esq.y)));
+  const float delta = __fmaf_rn(2.0f, __fmaf_rn(g.dz, loz, __fmaf_rn(g.dxy.y, loy, __fmul_rn(g.dxy.x, lox))), rnd);
   const float r0 = in ? rcp_approx(g.rsq) : 0.0f;
-  const float r1 = __fmaf_rn(r0, __fmaf_rn(-g.rsq, r0, 1.0f), r0);
-  const float r6 = r1 * r1 * r1;
-  const float ev = __fmaf_rn(r6, __fmaf_rn(E.a, r6, -E.b), r6 * __fmaf_rn(E.a_lo, r6, -E.b_lo));
-  // de/d(r^2) = -r^-2 r^-6 (6 a r^-6 - 3 b)
-  const float de = -(r1 * r6) * __fmaf_rn(6.0f * E.a, r6, -3.0f * E.b);
-  return __fmaf_rn(de, corr, ev);
+  const float s = __fmaf_rn(r0, __fmaf_rn(-g.rsq, r0, 1.0f), r0);
+  const float eps = __fmaf_rn(-s, delta, __fmaf_rn(-g.rsq, s, 1.0f));
+  const float s2 = __fmul_rn(s, s);
+  const float s3 = __fmul_rn(s2, s);
+  const float d3 = __fmaf_rn(__fmul_rn(3.0f, s3), eps, __fmaf_rn(__fmaf_rn(s, s, -s2), s, __fmaf_rn(s2, s, -s3)));
+  const float s6 = __fmul_rn(s3, s3);
+  const float d6 = __fmaf_rn(__fmul_rn(2.0f, s3), d3, __fmaf_rn(s3, s3, -s6));
+  ea.s6.add(s3);
+  ea.s12.add(s6);
+  ea.d6 = __fadd_rn(ea.d6, d3);
+  ea.d12 = __fadd_rn(ea.d12, d6);
 }
 
 // Four entries of one int4 granule, summed in FP32 and then added to the
 // compensated accumulator.  The FP32 cutoff test decides a pair unless its
 // r^2 lies in the guard band; one branch per granule re-tests such pairs in
-// FP64, as the reference decides them.  ENERGY (single type) also adds the
-// four pairs' energies to `ea`.
-template <bool SINGLE, bool ENERGY = false>
+// FP64, as the reference decides them.
+template <bool SINGLE>
 __device__ __forceinline__ void lj_quad(const PairCtx& C, const int4& e, const float4* __restrict__ xl,
-                                        const LJParamsF& P, Acc& acc, const LJEnergyF* E = nullptr,
-                                        EAcc* ea = nullptr) {
+                                        const LJParamsF& P, Acc& acc) {
   const float4 x0 = xl[e.x >> 6], x1 = xl[e.y >> 6], x2 = xl[e.z >> 6], x3 = xl[e.w >> 6];
   const PairGeo g0 = lj_geo<SINGLE>(C, e.x, x0, P), g1 = lj_geo<SINGLE>(C, e.y, x1, P);
   const PairGeo g2 = lj_geo<SINGLE>(C, e.z, x2, P), g3 = lj_geo<SINGLE>(C, e.w, x3, P);
@@ -223,12 +269,28 @@ __device__ __forceinline__ void lj_quad(const PairCtx& C, const int4& e, const f
   lj_force(g2, in2, a2, z2);
   lj_force(g3, in3, a3, z3);
   acc.add(__fadd2_rn(__fadd2_rn(a0, a1), __fadd2_rn(a2, a3)), __fadd_rn(__fadd_rn(z0, z1), __fadd_rn(z2, z3)));
-  if (ENERGY) {
-    const float s01 = __fadd_rn(pair_energy(C, *E, e.x, x0, g0, in0), pair_energy(C, *E, e.y, x1, g1, in1));
-    const float s23 = __fadd_rn(pair_energy(C, *E, e.z, x2, g2, in2), pair_energy(C, *E, e.w, x3, g3, in3));
-    ea->add(__fadd_rn(s01, s23));
-    ea->npair += int(in0) + int(in1) + int(in2) + int(in3);
+}
+
+// The same four pairs, energy only (single type pair): the decisions are the
+// force's, the pair energies go to `ea`.
+__device__ __forceinline__ void lj_energy_quad(const PairCtx& C, const int4& e, const float4* __restrict__ xl,
+                                               const LJParamsF& P, const LJEnergyF& E, EAcc& ea) {
+  const float4 x0 = xl[e.x >> 6], x1 = xl[e.y >> 6], x2 = xl[e.z >> 6], x3 = xl[e.w >> 6];
+  const PairGeo g0 = lj_geo<true>(C, e.x, x0, P), g1 = lj_geo<true>(C, e.y, x1, P);
+  const PairGeo g2 = lj_geo<true>(C, e.z, x2, P), g3 = lj_geo<true>(C, e.w, x3, P);
+  bool in0 = g0.rsq < g0.cutsq, in1 = g1.rsq < g1.cutsq, in2 = g2.rsq < g2.cutsq, in3 = g3.rsq < g3.cutsq;
+  const bool b0 = in_band(g0), b1 = in_band(g1), b2 = in_band(g2), b3 = in_band(g3);
+  if (b0 || b1 || b2 || b3) {
+    if (b0) in0 = cut_fp64(C.x4, C.i, e.x >> 6, g0.cutsq_d);
+    if (b1) in1 = cut_fp64(C.x4, C.i, e.y >> 6, g1.cutsq_d);
+    if (b2) in2 = cut_fp64(C.x4, C.i, e.z >> 6, g2.cutsq_d);
+    if (b3) in3 = cut_fp64(C.x4, C.i, e.w >> 6, g3.cutsq_d);
   }
+  pair_energy(C, E, e.x, x0, g0, in0, ea);
+  pair_energy(C, E, e.y, x1, g1, in1, ea);
+  pair_energy(C, E, e.z, x2, g2, in2, ea);
+  pair_energy(C, E, e.w, x3, g3, in3, ea);
+  ea.npair += int(in0) + int(in1) + int(in2) + int(in3);
 }
 
 }  // namespace

@@ -32,8 +32,9 @@
 namespace emd {
 namespace {
 
-constexpr int NB_THREADS = 32;  // one warp per interior bin
-constexpr int NB_CAP = 384;     // staged candidates per chunk
+constexpr int NB_WARPS = 4;     // warps per CTA, one interior bin each (independent)
+constexpr int NB_THREADS = 32 * NB_WARPS;
+constexpr int NB_CAP = 256;     // staged candidates per chunk and warp
 constexpr int NB_SLOTS = 64;  // spread slots for the longest-row reduction
 static_assert(1 + NB_SLOTS <= kHostInts, "read-back of the row-length slots exceeds the pinned scratch");
 
@@ -53,6 +54,7 @@ struct NeighArgs {
   int* rows;  // column-major, leading dimension `stride`, capacity K
   int stride, K;
   int* flags;  // [0] overflow, [1] longest row
+  int ibins;   // interior bins
 };
 
 // Exact FP64 re-test of a pair whose FP32 r^2 fell inside the guard band.
@@ -88,16 +90,24 @@ __device__ __forceinline__ long long okey(double v) {
 
 template <bool HALF, bool PACKED>
 __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
-  __shared__ float4 cand[NB_CAP];
-  __shared__ int pre[28];
-  __shared__ int boff[27];
-  const int lane = threadIdx.x;
+  // each warp of the CTA builds the rows of its own bin with its own staging
+  // arrays; the warps never wait for each other (more resident warps than one
+  // warp per CTA allows, at the same shared memory per warp)
+  __shared__ float4 cand_w[NB_WARPS][NB_CAP];
+  __shared__ int pre_w[NB_WARPS][28];
+  __shared__ int boff_w[NB_WARPS][27];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int bin = blockIdx.x * NB_WARPS + warp;
+  if (bin >= a.ibins) return;
+  float4* cand = cand_w[warp];
+  int* pre = pre_w[warp];
+  int* boff = boff_w[warp];
   // interior bin of this warp
   const int ix = a.nbx - 2 * a.nhalo, iy = a.nby - 2 * a.nhalo, iz = a.nbz - 2 * a.nhalo;
   (void)ix;
-  const int bx = blockIdx.x / (iy * iz) + a.nhalo;
-  const int by = (blockIdx.x / iz) % iy + a.nhalo;
-  const int bz = blockIdx.x % iz + a.nhalo;
+  const int bx = bin / (iy * iz) + a.nhalo;
+  const int by = (bin / iz) % iy + a.nhalo;
+  const int bz = bin % iz + a.nhalo;
   const int bc = (bx * a.nby + by) * a.nbz + bz;
   int cntb = 0, offb = 0;
   if (lane < 27) {
@@ -248,7 +258,7 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
   // (a single shared address would serialise millions of atomics in L2)
   mx = __reduce_max_sync(FULL_MASK, mx);
   if (lane == 0) {
-    if (mx > 0) atomicMax(&a.flags[1 + (blockIdx.x & (NB_SLOTS - 1))], mx);
+    if (mx > 0) atomicMax(&a.flags[1 + (bin & (NB_SLOTS - 1))], mx);
     if (mx > a.K) a.flags[0] = 1;
   }
 }
@@ -347,6 +357,7 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
   a.stride = n + 1;
   a.flags = c.resize_flag.p;
   const int ibins = (c.nbin[0] - 2 * c.nhalo) * (c.nbin[1] - 2 * c.nhalo) * (c.nbin[2] - 2 * c.nhalo);
+  a.ibins = ibins;
   const bool two_d = c.neigh_kind == EMD_NEIGH_2D;
   int& K = two_d ? c.maxneighs : c.neigh_scratch_k;
   DevBuf<int>& rows = two_d ? c.neighs : c.neigh_rows2d;
@@ -365,7 +376,7 @@ emd_status emd_neigh_create(emd_ctx* ctx, int half_neigh, long long* total_out) 
         TimedLaunch t(c, "neigh_build");
         auto k = a.half ? (packed ? k_neigh_bin<true, true> : k_neigh_bin<true, false>)
                         : (packed ? k_neigh_bin<false, true> : k_neigh_bin<false, false>);
-        k<<<ibins, NB_THREADS, 0, c.stream>>>(a);
+        k<<<(ibins + NB_WARPS - 1) / NB_WARPS, NB_THREADS, 0, c.stream>>>(a);
         EMD_CHECK_LAUNCH();
       }
     }

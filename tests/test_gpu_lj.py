@@ -6,6 +6,8 @@ whole trajectories.  Half lists scatter with atomics and are compared to
 1e-12 relative.  The mixed form is checked against the FP64 forces at the
 tolerances the hot path is specified with (RMS relative force error <= 1e-5).
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -152,6 +154,38 @@ def test_lj_mixed_force_error(n):
     assert abs(mix2.lj_energy() - ref2.lj_energy()) <= 1e-9 * abs(ref2.lj_energy())
     # 40 steps of mixed dynamics stay close to FP64 dynamics
     assert _rel_err(fm["x"], fr["x"]) <= 1e-6
+
+
+def test_lj_mixed_pairs_on_the_cutoff():
+    """fcc with the cutoff equal to the lattice constant: the second shell
+    lies on the cutoff (positions displaced by 1e-7 a), so every row holds
+    pairs whose FP32 r^2 falls in the guard band.  They must be decided as
+    the FP64 drop-in decides them: one pair decided otherwise moves an atom's
+    force by about 0.6, against an RMS force near 1.  The force pass with the
+    energy (an FP64 re-test per band pair) and the one without it (FP32
+    decisions, the row redone in full when it holds a band pair) give the
+    same bits."""
+    from examinimd_gb300 import EMD_PREC_MIXED
+    a = math.pow(4.0 / 0.8442, 1.0 / 3.0)
+    setup = mdloop.LJSetup(8, cut=a, coeffs=[(1, 1, 1.0, 1.0, a)])
+    state = dict(mdloop.make_lattice(setup))
+    rng = np.random.default_rng(31)
+    state["x"] = np.mod(state["x"] + rng.normal(0.0, 1e-7 * a, state["x"].shape), setup.domain[0])
+    ref, mix = _ctx(), _ctx()
+    mdloop.init(ref, setup, state)
+    mdloop.init(mix, setup, state, precision=EMD_PREC_MIXED)
+    nl = ref.info()[0]
+    fr, fm = ref.get(0, nl)["f"], mix.get(0, nl)["f"]
+    rms = np.sqrt(np.mean(np.sum(fr * fr, axis=1)))
+    assert rms > 0.1  # the shell is split: some pairs in, some out
+    err = np.linalg.norm(fm - fr, axis=1)
+    assert err.max() <= 1e-4 * rms, (err.max(), rms)
+    mix.zero_forces()
+    mix.lj_request_energy()
+    mix.lj_compute()
+    np.testing.assert_array_equal(mix.get(0, nl)["f"], fm)
+    pe = mix.lj_force_energy()
+    assert pe is not None and abs(pe - ref.lj_energy()) <= 1e-11 * abs(ref.lj_energy())
 
 
 def test_lj_many_types_per_pair_parameters():

@@ -4,12 +4,14 @@ On thermo steps the driver asks for the energy with the force
 (emd_lj_request_energy): the mixed kernel then sums the shifted LJ energy of
 the pairs it evaluates, and emd_lj_force_energy returns it while the
 positions stay unchanged.  It is compared with the FP64 energy of the same
-positions (emd_lj_energy).  Its error is rounding of FP32 pair terms with
-random signs, about 3e-7 / sqrt(N) relative for N atoms: the systematic
-parts -- the FP32 bin widths, the shifts added to FP32 coordinates, the
-approximate reciprocal, FP32 coefficients and the cutoff shift -- are
-carried exactly.  The test bounds are 3e-8 at 864 and 4,000 atoms and 1e-9
-at LJ-4M.
+positions (emd_lj_energy).  Every pair is carried as an FP32 value and its
+first-order remainder (the exact pair difference including the rounding of
+the FP32 positions, the rounding of r^2, the reciprocal's and the products'
+remainders) and the per-atom sums keep every addition's rounding error, so
+what is left is second order: the bound is 1e-11 relative everywhere, on
+perfect fcc lattices (where all pairs of a shell share one distance and any
+FP32 rounding would add up coherently, 5e-8 relative) as on thermalised
+ones, from 864 atoms to LJ-4M.
 """
 import numpy as np
 import pytest
@@ -28,7 +30,7 @@ def _rms_rel(a, b):
     return np.sqrt(np.mean(np.sum((a - b) ** 2, axis=1))) / np.sqrt(np.mean(np.sum(b ** 2, axis=1)))
 
 
-@pytest.mark.parametrize("n,tol", [(6, 3e-8), (10, 3e-8), (100, 1e-9)])
+@pytest.mark.parametrize("n,tol", [(6, 1e-11), (10, 1e-11), (100, 1e-11)])
 def test_fused_energy_matches_fp64_energy(n, tol):
     setup = mdloop.LJSetup(n)
     state = dict(mdloop.make_lattice(setup, 8))
@@ -54,6 +56,23 @@ def test_fused_energy_matches_fp64_energy(n, tol):
     assert mix.lj_force_energy() is not None
     mix.nve_initial()
     assert mix.lj_force_energy() is None
+    mix.close()
+
+
+@pytest.mark.parametrize("n", [20, 100])
+def test_fused_energy_on_the_perfect_lattice(n):
+    """The thermo step 0 of the LJ decks: every pair of a neighbour shell
+    has the same distance, so an FP32 rounding of the pair energy would add
+    up coherently (5e-8 relative); the carried remainders do not."""
+    setup = mdloop.LJSetup(n)
+    mix = _ctx()
+    mdloop.init(mix, setup, mdloop.make_lattice(setup, 8), precision=1)
+    mix.zero_forces()
+    mix.lj_request_energy()
+    mix.lj_compute()
+    fused, exact = mix.lj_force_energy(), mix.lj_energy()
+    assert fused is not None
+    assert abs(fused - exact) <= 1e-11 * abs(exact), (fused, exact, (fused - exact) / exact)
     mix.close()
 
 
@@ -86,7 +105,7 @@ def test_driver_thermo_uses_the_fused_energy(tmp_path):
     assert md.ctx.lj_force_energy() is not None
     T, pe, ke = md.thermo(recompute=True)
     exact = md.ctx.lj_energy() / md.info()["N_local"]
-    assert abs(pe - exact) <= 3e-8 * abs(exact)
+    assert abs(pe - exact) <= 1e-11 * abs(exact)
     md.close()
 
 
@@ -127,4 +146,4 @@ def test_large_cutoff_rows_and_forces():
     mix.lj_request_energy()
     mix.lj_compute()
     fused, exact = mix.lj_force_energy(), ref.lj_energy()
-    assert fused is not None and abs(fused - exact) <= 3e-8 * abs(exact)
+    assert fused is not None and abs(fused - exact) <= 1e-11 * abs(exact)
