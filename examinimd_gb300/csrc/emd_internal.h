@@ -185,7 +185,7 @@ struct Ctx {
   // positions have not changed since (x_version)
   bool lj_energy_request = false;
   bool lj_pe_fused_valid = false;
-  double lj_pe_fused = 0;
+  const double* lj_pe_dev = nullptr;  // device address of that energy
   unsigned long long lj_pe_fused_version = 0;
   DevBuf<double> lj_pe_part;
   DevBuf<float4> lj_xlo;    // x - bin centre - xl per particle (fused energy)

@@ -533,7 +533,12 @@ emd_status emd_lj_force_energy(emd_ctx* ctx, double* pe, int* available) {
   EMD_API_BEGIN
   require(pe && available, EMD_ERR_ARG, "emd_lj_force_energy: null output");
   *available = (c.lj_pe_fused_valid && c.lj_pe_fused_version == c.x_version) ? 1 : 0;
-  *pe = *available ? c.lj_pe_fused : 0.0;
+  *pe = 0.0;
+  if (*available) {  // the sum was left on the device by the force call; read it now
+    EMD_CUDA(cudaMemcpyAsync(c.h_scalar, c.lj_pe_dev, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    EMD_CUDA(cudaStreamSynchronize(c.stream));
+    *pe = *c.h_scalar;
+  }
   EMD_API_END
 }
 

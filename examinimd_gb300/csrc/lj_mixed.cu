@@ -177,19 +177,20 @@ __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict_
 }
 
 // The shifted LJ energy over the same rows and pair decisions as the force
-// (single type pair), one FP64 partial per block (lj_pair.cuh, pair_energy).
+// (single type pair), one FP64 partial per warp (lj_pair.cuh, energy_pair2):
+// the sums stay FP32 hi + lo pairs through the warp reduction and only lane
+// 0 forms the FP64 energy (the FP64 pipe runs at 1/64 of the FP32 rate).
 // A kernel of its own: evaluated inside the force loop, the compiler's
 // treatment of the shared expressions moved force sums by an ulp (measured),
 // and the forces of a thermo step must be the force-only kernel's bits.
-__global__ void __launch_bounds__(128) k_lj_energy_mixed(const float4* __restrict__ xl,
+__global__ void __launch_bounds__(128, 3) k_lj_energy_mixed(const float4* __restrict__ xl,
                                                          const double4_32a* __restrict__ x4,
                                                          const int4* __restrict__ rows4, int stride,
                                                          const int* __restrict__ num, LJParamsF P, float wx,
                                                          float wy, float wz, int n, LJEnergyF E,
                                                          double* __restrict__ e_part) {
-  __shared__ double esum[4];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double e_atom = 0.0;
+  EAcc ea;
   if (i < n) {
     PairCtx C;
     C.xi = xl[i];
@@ -197,14 +198,17 @@ __global__ void __launch_bounds__(128) k_lj_energy_mixed(const float4* __restric
     C.ti = 0;
     C.set_bin_width(wx, wy, wz);
     C.x4 = x4;
-    EAcc ea;
     ea.lo_i = E.xlo[i];
     lj_row(i, rows4 + i, num[i], stride, [&](const int4& e) { lj_energy_quad(C, e, xl, P, E, ea); });
-    // full list: half of every ordered pair's shifted energy
-    e_atom = 0.5 * ea.energy(E);
   }
-  const double t = block_sum(e_atom, esum);
-  if (threadIdx.x == 0) e_part[blockIdx.x] = t;
+  const float2 r6 = df_warp_sum(df_total(ea.r6, ea.d6));
+  const float2 r12 = df_warp_sum(df_total(ea.r12, ea.d12));
+  const int np = __reduce_add_sync(FULL_MASK, ea.npair);
+  if ((threadIdx.x & 31) == 0) {
+    // full list: half of every ordered pair's shifted energy
+    const double a6 = double(r6.x) + double(r6.y), a12 = double(r12.x) + double(r12.y);
+    e_part[i >> 5] = 0.5 * ((E.a * a12 - E.b * a6) - double(np) * E.ecut);
+  }
 }
 
 BinFrame frame(const Ctx& c) {
@@ -304,7 +308,7 @@ void lj_mixed_compute(Ctx& c) {
     E.wlo_xy = make_float2(wl[0], wl[1]);
     E.nwlo_z = -wl[2];
     E.wlo_z = wl[2];
-    c.lj_pe_part.reserve(size_t(g.x) + 1, c.stream);
+    c.lj_pe_part.reserve(size_t(g.x) * 4 + kSumScratchDoubles, c.stream);
     part = c.lj_pe_part.p;
     c.lj_xlo.reserve(size_t(n_all) + 1, c.stream);
     E.xlo = c.lj_xlo.p;
@@ -324,7 +328,9 @@ void lj_mixed_compute(Ctx& c) {
     k_lj_energy_mixed<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n, E,
                                               part);
     EMD_CHECK_LAUNCH();
-    c.lj_pe_fused = device_sum(c, part, int(g.x));
+    // summed on the device; no host wait inside the force call
+    device_sum_launch(c, part, int(g.x) * 4, part + size_t(g.x) * 4);
+    c.lj_pe_dev = part + size_t(g.x) * 4 + kSumScratchDoubles - 1;
     c.lj_pe_fused_version = c.x_version;
     c.lj_pe_fused_valid = true;
   }

@@ -163,85 +163,154 @@ struct LJEnergyF {
   const float4* xlo;           // per particle: x - bin centre - xl, rounded to FP32
 };
 
-// Sum of a series of non-negative FP32 values with every addition's exact
-// rounding error kept (Fast2Sum on the larger and smaller operand), read
-// back in FP64 as s + c.  Kahan's form would lose the rounding of x - c at
-// every step: about 1e-9 of the energy on a lattice.
-struct NSum {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float x) {
-    const float hi = fmaxf(s, x), lo = fminf(s, x);
-    const float t = __fadd_rn(hi, lo);
-    c = __fadd_rn(c, __fsub_rn(lo, __fsub_rn(t, hi)));
-    s = t;
-  }
-  __device__ __forceinline__ double value() const { return double(s) + double(c); }
-};
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {  // a - b, one rounding per lane
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
 
-struct EAcc {
-  NSum s6, s12;              // sum of r^-6 and r^-12 over the interacting pairs
-  float d6 = 0.f, d12 = 0.f;  // their remainders
-  int npair = 0;             // interacting pairs
-  float4 lo_i;               // the row atom's xlo
-  // the row's shifted pair energies, in FP64
-  __device__ __forceinline__ double energy(const LJEnergyF& E) const {
-    const double r6 = s6.value() + double(d6), r12 = s12.value() + double(d12);
-    return (E.a * r12 - E.b * r6) - double(npair) * E.ecut;
-  }
-};
-
-// Knuth's two-sum: a + b - s exactly, for s = fl(a + b)
+// a - b - s exactly for s = fl(a - b) (Knuth's two-sum, per lane)
+__device__ __forceinline__ float2 two_diff_err2(float2 a, float2 b, float2 s) {
+  const float2 bv = sub2(a, s);  // b as the subtraction saw it
+  const float2 av = __fadd2_rn(s, bv);
+  return sub2(sub2(a, av), sub2(b, bv));
+}
+__device__ __forceinline__ float two_diff_err(float a, float b, float s) {
+  const float bv = __fsub_rn(a, s);
+  const float av = __fadd_rn(s, bv);
+  return __fsub_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+// a + b - s exactly for s = fl(a + b), per lane
+__device__ __forceinline__ float2 two_sum_err2(float2 a, float2 b, float2 s) {
+  const float2 bv = sub2(s, a);
+  const float2 av = sub2(s, bv);
+  return __fadd2_rn(sub2(a, av), sub2(b, bv));
+}
 __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
   const float bv = __fsub_rn(s, a);
   const float av = __fsub_rn(s, bv);
   return __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
 }
+// a + b - s exactly for s = fl(a + b), a, b >= 0 (Dekker's Fast2Sum on the
+// larger and the smaller)
+__device__ __forceinline__ float fast_sum_err(float a, float b, float s) {
+  return __fsub_rn(fminf(a, b), __fsub_rn(s, fmaxf(a, b)));
+}
 
-__device__ __forceinline__ void pair_energy(const PairCtx& C, const LJEnergyF& E, int e, const float4& xj,
-                                            const PairGeo& g, bool in, EAcc& ea) {
-  constexpr int kExp = 0x4B000000;  // bits of 2^23, as lj_geo forms the shift
-  const float2 txy = __fadd2_rn(make_float2(__int_as_float((e & 0x30) | kExp), __int_as_float((e & 0x0C) | kExp)),
-                                make_float2(-8388608.0f, -8388608.0f));
-  const float tz = __fadd_rn(__int_as_float((e & 0x03) | kExp), -8388608.0f);
-  const float2 sxy = __ffma2_rn(txy, C.nw_xy, C.w_xy);      // (1 - k) w, FP32 widths
-  const float sz = __fmaf_rn(tz, C.nw_z, C.w_z);
-  const float2 sl = __ffma2_rn(txy, E.nwlo_xy, E.wlo_xy);  // (1 - k) times their remainders
-  const float slz = __fmaf_rn(tz, E.nwlo_z, E.wlo_z);
-  const float2 t1 = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), make_float2(C.xi.x, C.xi.y));
-  const float t1z = __fsub_rn(C.xi.z, xj.z);
-  const float4 lj = E.xlo[e >> 6];
-  const float2 pl = __ffma2_rn(make_float2(lj.x, lj.y), make_float2(-1.f, -1.f), make_float2(ea.lo_i.x, ea.lo_i.y));
-  const float plz = __fsub_rn(ea.lo_i.z, lj.z);
-  const float lox = __fadd_rn(__fadd_rn(two_sum_err(C.xi.x, -xj.x, t1.x), two_sum_err(t1.x, sxy.x, g.dxy.x)),
-                              __fadd_rn(sl.x, pl.x));
-  const float loy = __fadd_rn(__fadd_rn(two_sum_err(C.xi.y, -xj.y, t1.y), two_sum_err(t1.y, sxy.y, g.dxy.y)),
-                              __fadd_rn(sl.y, pl.y));
-  const float loz = __fadd_rn(__fadd_rn(two_sum_err(C.xi.z, -xj.z, t1z), two_sum_err(t1z, sz, g.dz)),
-                              __fadd_rn(slz, plz));
-  // t = fma(dz, dz, fl(dx^2 + dy^2)) as lj_geo forms it; its exact rounding
-  // from the squares' Dekker remainders and the sums' two-sum remainders (the
-  // difference of two roundings of dz^2 + fl(dx^2 + dy^2) is exact)
-  const float2 sq = __fmul2_rn(g.dxy, g.dxy);
-  const float2 esq = __ffma2_rn(g.dxy, g.dxy, make_float2(-sq.x, -sq.y));
-  const float A = __fadd_rn(sq.x, sq.y);
-  const float pz = __fmul_rn(g.dz, g.dz);
-  const float B = __fadd_rn(pz, A);
-  const float rnd = __fadd_rn(__fadd_rn(__fsub_rn(B, g.rsq), two_sum_err(pz, A, B)),
-                              __fadd_rn(__fadd_rn(two_sum_err(sq.x, sq.y, A), __fmaf_rn(g.dz, g.dz, -pz)),
-                                        __fadd_rn(esq.x, esq.y)));
-  const float delta = __fmaf_rn(2.0f, __fmaf_rn(g.dz, loz, __fmaf_rn(g.dxy.y, loy, __fmul_rn(g.dxy.x, lox))), rnd);
-  const float r0 = in ? rcp_approx(g.rsq) : 0.0f;
-  const float s = __fmaf_rn(r0, __fmaf_rn(-g.rsq, r0, 1.0f), r0);
-  const float eps = __fmaf_rn(-s, delta, __fmaf_rn(-g.rsq, s, 1.0f));
-  const float s2 = __fmul_rn(s, s);
-  const float s3 = __fmul_rn(s2, s);
-  const float d3 = __fmaf_rn(__fmul_rn(3.0f, s3), eps, __fmaf_rn(__fmaf_rn(s, s, -s2), s, __fmaf_rn(s2, s, -s3)));
-  const float s6 = __fmul_rn(s3, s3);
-  const float d6 = __fmaf_rn(__fmul_rn(2.0f, s3), d3, __fmaf_rn(s3, s3, -s6));
-  ea.s6.add(s3);
-  ea.s12.add(s6);
-  ea.d6 = __fadd_rn(ea.d6, d3);
-  ea.d12 = __fadd_rn(ea.d12, d6);
+// Sum of non-negative terms in each lane with every addition's exact
+// rounding error kept (Fast2Sum on the larger and the smaller operand), read
+// back in FP64 as s + c.  Kahan's form would lose the rounding of x - c at
+// every step: about 1e-9 of the energy on a lattice.
+struct NSum2 {
+  float2 s = {0.f, 0.f}, c = {0.f, 0.f};
+  __device__ __forceinline__ void add(float2 v) {
+    const float2 hi = make_float2(fmaxf(s.x, v.x), fmaxf(s.y, v.y));
+    const float2 lo = make_float2(fminf(s.x, v.x), fminf(s.y, v.y));
+    const float2 t = __fadd2_rn(hi, lo);
+    c = __fadd2_rn(c, sub2(lo, sub2(t, hi)));
+    s = t;
+  }
+};
+
+struct EAcc {
+  NSum2 r6, r12;                     // r^-6 and r^-12 of the interacting pairs (two lanes each)
+  float2 d6 = {0.f, 0.f}, d12 = {0.f, 0.f};  // their remainders
+  int npair = 0;                     // interacting pairs
+  float4 lo_i;                       // the row atom's xlo
+};
+
+// One summed quantity as an unevaluated FP32 pair hi + lo: both lanes'
+// Fast2Sum totals and remainders (terms >= 0)
+__device__ __forceinline__ float2 df_total(const NSum2& q, float2 d) {
+  const float h = __fadd_rn(q.s.x, q.s.y);
+  const float e = fast_sum_err(q.s.x, q.s.y, h);
+  return make_float2(h, __fadd_rn(__fadd_rn(__fadd_rn(q.c.x, q.c.y), __fadd_rn(d.x, d.y)), e));
+}
+
+// Sum of hi + lo pairs (hi >= 0) over the warp, every lane gets the total;
+// each addition of the his keeps its exact rounding error
+__device__ __forceinline__ float2 df_warp_sum(float2 v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(FULL_MASK, v.x, o), l2 = __shfl_xor_sync(FULL_MASK, v.y, o);
+    const float h = __fadd_rn(v.x, h2);
+    v = make_float2(h, __fadd_rn(__fadd_rn(v.y, l2), fast_sum_err(v.x, h2, h)));
+  }
+  return v;
+}
+
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+
+// Two pairs of one row at once, lane k of every f32x2 value holding pair k.
+// The geometry repeats lj_geo's operations lane by lane, so r^2 and the
+// cutoff decisions are the force's bits (single type pair).
+__device__ __forceinline__ void energy_pair2(const PairCtx& C, const LJParamsF& P, const LJEnergyF& E, int e0,
+                                             int e1, const float4& xj0, const float4& xj1, EAcc& ea) {
+  constexpr int kExp = 0x4B000000;  // bits of 2^23
+  const float2 m23 = splat(-8388608.0f);
+  const float2 tx = __fadd2_rn(make_float2(__int_as_float((e0 & 0x30) | kExp), __int_as_float((e1 & 0x30) | kExp)), m23);
+  const float2 ty = __fadd2_rn(make_float2(__int_as_float((e0 & 0x0C) | kExp), __int_as_float((e1 & 0x0C) | kExp)), m23);
+  const float2 tz = __fadd2_rn(make_float2(__int_as_float((e0 & 0x03) | kExp), __int_as_float((e1 & 0x03) | kExp)), m23);
+  const float2 sx = __ffma2_rn(tx, splat(C.nw_xy.x), splat(C.w_xy.x));  // (1 - k) w, FP32 widths
+  const float2 sy = __ffma2_rn(ty, splat(C.nw_xy.y), splat(C.w_xy.y));
+  const float2 sz = __ffma2_rn(tz, splat(C.nw_z), splat(C.w_z));
+  const float2 xix = splat(C.xi.x), xiy = splat(C.xi.y), xiz = splat(C.xi.z);
+  const float2 xjx = make_float2(xj0.x, xj1.x), xjy = make_float2(xj0.y, xj1.y), xjz = make_float2(xj0.z, xj1.z);
+  const float2 t1x = sub2(xix, xjx), t1y = sub2(xiy, xjy), t1z = sub2(xiz, xjz);
+  const float2 dx = __fadd2_rn(t1x, sx), dy = __fadd2_rn(t1y, sy), dz = __fadd2_rn(t1z, sz);
+  const float2 px = __fmul2_rn(dx, dx), py = __fmul2_rn(dy, dy);
+  const float2 A = __fadd2_rn(px, py);
+  const float2 t = __ffma2_rn(dz, dz, A);  // the force's r^2
+  const float c = P.cutsq_0, clo = c * (1.0f - LJ_BAND), chi = c * (1.0f + LJ_BAND);
+  bool in0 = t.x < c, in1 = t.y < c;
+  const bool b0 = t.x > clo && t.x < chi, b1 = t.y > clo && t.y < chi;
+  if (b0 || b1) {  // borderline: decide as FP64 does
+    if (b0) in0 = cut_fp64(C.x4, C.i, e0 >> 6, P.cutsq_d0);
+    if (b1) in1 = cut_fp64(C.x4, C.i, e1 >> 6, P.cutsq_d0);
+  }
+  // the exact difference dx + lo: the two roundings of each coordinate's
+  // difference (Knuth), the FP32 bin width's remainder and both positions'
+  // FP32 roundings
+  const float4 l0 = E.xlo[e0 >> 6], l1 = E.xlo[e1 >> 6];
+  const float2 lox = __fadd2_rn(__fadd2_rn(two_diff_err2(xix, xjx, t1x), two_sum_err2(t1x, sx, dx)),
+                                __fadd2_rn(__ffma2_rn(tx, splat(E.nwlo_xy.x), splat(E.wlo_xy.x)),
+                                           sub2(splat(ea.lo_i.x), make_float2(l0.x, l1.x))));
+  const float2 loy = __fadd2_rn(__fadd2_rn(two_diff_err2(xiy, xjy, t1y), two_sum_err2(t1y, sy, dy)),
+                                __fadd2_rn(__ffma2_rn(ty, splat(E.nwlo_xy.y), splat(E.wlo_xy.y)),
+                                           sub2(splat(ea.lo_i.y), make_float2(l0.y, l1.y))));
+  const float2 loz = __fadd2_rn(__fadd2_rn(two_diff_err2(xiz, xjz, t1z), two_sum_err2(t1z, sz, dz)),
+                                __fadd2_rn(__ffma2_rn(tz, splat(E.nwlo_z), splat(E.wlo_z)),
+                                           sub2(splat(ea.lo_i.z), make_float2(l0.z, l1.z))));
+  // r^2 - t exactly: the squares' Dekker remainders, the sums' Fast2Sum
+  // remainders (terms >= 0) and B - t (two roundings of one sum: exact)
+  const float2 m1 = splat(-1.0f);
+  const float2 pz = __fmul2_rn(dz, dz);
+  const float2 B = __fadd2_rn(pz, A);
+  const float2 ex = __ffma2_rn(dx, dx, __fmul2_rn(px, m1)), ey = __ffma2_rn(dy, dy, __fmul2_rn(py, m1));
+  const float2 ez = __ffma2_rn(dz, dz, __fmul2_rn(pz, m1));
+  const float2 eA = sub2(make_float2(fminf(px.x, py.x), fminf(px.y, py.y)),
+                         sub2(A, make_float2(fmaxf(px.x, py.x), fmaxf(px.y, py.y))));
+  const float2 eB = sub2(make_float2(fminf(pz.x, A.x), fminf(pz.y, A.y)),
+                         sub2(B, make_float2(fmaxf(pz.x, A.x), fmaxf(pz.y, A.y))));
+  const float2 rnd = __fadd2_rn(__fadd2_rn(sub2(B, t), eB), __fadd2_rn(__fadd2_rn(eA, ez), __fadd2_rn(ex, ey)));
+  const float2 two = splat(2.0f);
+  const float2 delta = __ffma2_rn(two, __ffma2_rn(dz, loz, __ffma2_rn(dy, loy, __fmul2_rn(dx, lox))), rnd);
+  const float2 r0 = make_float2(in0 ? rcp_approx(t.x) : 0.0f, in1 ? rcp_approx(t.y) : 0.0f);
+  const float2 one = splat(1.0f);
+  const float2 mt = __fmul2_rn(t, m1);
+  const float2 s = __ffma2_rn(r0, __ffma2_rn(mt, r0, one), r0);
+  // 1 / (t + delta) = s (1 + eps) to first order
+  const float2 eps = __ffma2_rn(__fmul2_rn(s, m1), delta, __ffma2_rn(mt, s, one));
+  const float2 s2 = __fmul2_rn(s, s);
+  const float2 s3 = __fmul2_rn(s2, s);
+  // r^-6 = s3 + d3: the products' remainders and the reciprocal's (1 + eps)^3
+  const float2 e2 = __ffma2_rn(s, s, __fmul2_rn(s2, m1));
+  const float2 e3 = __ffma2_rn(s2, s, __fmul2_rn(s3, m1));
+  const float2 d3 = __ffma2_rn(__fmul2_rn(splat(3.0f), s3), eps, __ffma2_rn(e2, s, e3));
+  const float2 s6 = __fmul2_rn(s3, s3);
+  const float2 d6 = __ffma2_rn(__fmul2_rn(two, s3), d3, __ffma2_rn(s3, s3, __fmul2_rn(s6, m1)));
+  ea.r6.add(s3);
+  ea.r12.add(s6);
+  ea.d6 = __fadd2_rn(ea.d6, d3);
+  ea.d12 = __fadd2_rn(ea.d12, d6);
+  ea.npair += int(in0) + int(in1);
 }
 
 // Four entries of one int4 granule, summed in FP32 and then added to the
@@ -276,21 +345,8 @@ __device__ __forceinline__ void lj_quad(const PairCtx& C, const int4& e, const f
 __device__ __forceinline__ void lj_energy_quad(const PairCtx& C, const int4& e, const float4* __restrict__ xl,
                                                const LJParamsF& P, const LJEnergyF& E, EAcc& ea) {
   const float4 x0 = xl[e.x >> 6], x1 = xl[e.y >> 6], x2 = xl[e.z >> 6], x3 = xl[e.w >> 6];
-  const PairGeo g0 = lj_geo<true>(C, e.x, x0, P), g1 = lj_geo<true>(C, e.y, x1, P);
-  const PairGeo g2 = lj_geo<true>(C, e.z, x2, P), g3 = lj_geo<true>(C, e.w, x3, P);
-  bool in0 = g0.rsq < g0.cutsq, in1 = g1.rsq < g1.cutsq, in2 = g2.rsq < g2.cutsq, in3 = g3.rsq < g3.cutsq;
-  const bool b0 = in_band(g0), b1 = in_band(g1), b2 = in_band(g2), b3 = in_band(g3);
-  if (b0 || b1 || b2 || b3) {
-    if (b0) in0 = cut_fp64(C.x4, C.i, e.x >> 6, g0.cutsq_d);
-    if (b1) in1 = cut_fp64(C.x4, C.i, e.y >> 6, g1.cutsq_d);
-    if (b2) in2 = cut_fp64(C.x4, C.i, e.z >> 6, g2.cutsq_d);
-    if (b3) in3 = cut_fp64(C.x4, C.i, e.w >> 6, g3.cutsq_d);
-  }
-  pair_energy(C, E, e.x, x0, g0, in0, ea);
-  pair_energy(C, E, e.y, x1, g1, in1, ea);
-  pair_energy(C, E, e.z, x2, g2, in2, ea);
-  pair_energy(C, E, e.w, x3, g3, in3, ea);
-  ea.npair += int(in0) + int(in1) + int(in2) + int(in3);
+  energy_pair2(C, P, E, e.x, e.y, x0, x1, ea);
+  energy_pair2(C, P, E, e.z, e.w, x2, x3, ea);
 }
 
 }  // namespace
