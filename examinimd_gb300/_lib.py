@@ -340,11 +340,11 @@ class Context:
         return out
 
     def lj_request_energy(self):
-        """The next lj_compute also sums the energy it can fuse (emd_lj_request_energy)."""
+        """The next lj_compute (mixed form, one type pair) also computes the energy (emd_lj_request_energy)."""
         self._ok(self.lib.emd_lj_request_energy(self.h), "emd_lj_request_energy")
 
     def lj_force_energy(self):
-        """The energy summed by the last lj_compute, or None (emd_lj_force_energy)."""
+        """The energy computed by the last lj_compute, or None (emd_lj_force_energy)."""
         e, ok = _D(), _I()
         self._ok(self.lib.emd_lj_force_energy(self.h, C.byref(e), C.byref(ok)), "emd_lj_force_energy")
         return e.value if ok.value else None

@@ -180,15 +180,15 @@ struct Ctx {
   float lj_single[3] = {0, 0, 0};
   double lj_single_cutsq_d = 0;
   double lj_single_d[2] = {0, 0};  // lj1, lj2 of the uniform type pair in FP64
-  // energy of the mixed form fused into the force of the positions it used:
-  // asked for before a compute (emd_lj_request_energy), valid while the
-  // positions have not changed since (x_version)
+  // the mixed form's thermo-step energy, computed by the force call of the
+  // positions it used: asked for before a compute (emd_lj_request_energy),
+  // valid while the positions have not changed since (x_version)
   bool lj_energy_request = false;
-  bool lj_pe_fused_valid = false;
+  bool lj_pe_valid = false;
   const double* lj_pe_dev = nullptr;  // device address of that energy
-  unsigned long long lj_pe_fused_version = 0;
+  unsigned long long lj_pe_version = 0;
   DevBuf<double> lj_pe_part;
-  DevBuf<float4> lj_xlo;    // x - bin centre - xl per particle (fused energy)
+  DevBuf<float4> lj_xlo;    // x - bin centre - xl per particle (that energy's pair differences)
   // the same for SNAP (FP64 form): per-atom energies written by the force
   // kernel, summed when asked for
   bool snap_energy_request = false;

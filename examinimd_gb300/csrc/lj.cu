@@ -352,7 +352,7 @@ emd_status emd_lj_compute(emd_ctx* ctx) {
     Ctx& c;
     ~EndRequest() { c.lj_energy_request = false; }
   } end_request{c};
-  c.lj_pe_fused_valid = false;
+  c.lj_pe_valid = false;
   materialize_kick(c);  // the forces are about to be overwritten
   require(c.lj_ready, EMD_ERR_STATE, "emd_lj_compute: emd_lj_init not called");
   require(c.neigh_ready && c.neigh_rows == c.N_local, EMD_ERR_STATE, "emd_lj_compute: no current neighbour list");
@@ -532,7 +532,7 @@ emd_status emd_lj_request_energy(emd_ctx* ctx) {
 emd_status emd_lj_force_energy(emd_ctx* ctx, double* pe, int* available) {
   EMD_API_BEGIN
   require(pe && available, EMD_ERR_ARG, "emd_lj_force_energy: null output");
-  *available = (c.lj_pe_fused_valid && c.lj_pe_fused_version == c.x_version) ? 1 : 0;
+  *available = (c.lj_pe_valid && c.lj_pe_version == c.x_version) ? 1 : 0;
   *pe = 0.0;
   if (*available) {  // the sum was left on the device by the force call; read it now
     EMD_CUDA(cudaMemcpyAsync(c.h_scalar, c.lj_pe_dev, sizeof(double), cudaMemcpyDeviceToHost, c.stream));

@@ -331,8 +331,8 @@ void lj_mixed_compute(Ctx& c) {
     // summed on the device; no host wait inside the force call
     device_sum_launch(c, part, int(g.x) * 4, part + size_t(g.x) * 4);
     c.lj_pe_dev = part + size_t(g.x) * 4 + kSumScratchDoubles - 1;
-    c.lj_pe_fused_version = c.x_version;
-    c.lj_pe_fused_valid = true;
+    c.lj_pe_version = c.x_version;
+    c.lj_pe_valid = true;
   }
   c.f_zero_pending &= ~1;
 }

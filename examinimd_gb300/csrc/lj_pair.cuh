@@ -133,7 +133,7 @@ __device__ __forceinline__ void lj_force(const PairGeo& g, bool in, float2& fxy,
   fz = g.dz * fpair;
 }
 
-// ---- the energy fused into the force pass (single type pair, thermo steps)
+// ---- the energy of a thermo step (single type pair), a kernel of its own
 //
 // The energy of pair evaluations in plain FP32 is biased, not just noisy.
 // The bin shift added to grid-aligned FP32 coordinates rounds the same way

@@ -142,11 +142,11 @@ void ForceLJNeigh_GB300::compute(System* system, Binning*, Neighbor*) {
 double ForceLJNeigh_GB300::compute_energy(System* system, Binning*, Neighbor*) {
   if (idial_) return 0.0;  // ForceLJIDialNeigh keeps Force's default (force.h:54)
   double pe = 0.0;
-  int fused = 0;
-  // the mixed form's thermo steps sum the energy inside the force pass
-  if (precision_ == EMD_PREC_MIXED) check(emd_lj_force_energy(system->ctx, &pe, &fused), system->ctx,
+  int delivered = 0;
+  // on the mixed form's thermo steps the force call also computed the energy
+  if (precision_ == EMD_PREC_MIXED) check(emd_lj_force_energy(system->ctx, &pe, &delivered), system->ctx,
                                            "emd_lj_force_energy");
-  if (!fused) check(emd_lj_energy(system->ctx, &pe), system->ctx, "emd_lj_energy");
+  if (!delivered) check(emd_lj_energy(system->ctx, &pe), system->ctx, "emd_lj_energy");
   return pe;
 }
 
@@ -205,9 +205,9 @@ void ForceSNAP_GB300::compute(System* system, Binning*, Neighbor*) {
 
 double ForceSNAP_GB300::compute_energy(System* system, Binning*, Neighbor*) {
   double pe = 0.0;
-  int fused = 0;
-  check(emd_snap_force_energy(system->ctx, &pe, &fused), system->ctx, "emd_snap_force_energy");
-  if (!fused) check(emd_snap_energy(system->ctx, &pe), system->ctx, "emd_snap_energy");
+  int delivered = 0;
+  check(emd_snap_force_energy(system->ctx, &pe, &delivered), system->ctx, "emd_snap_force_energy");
+  if (!delivered) check(emd_snap_energy(system->ctx, &pe), system->ctx, "emd_snap_energy");
   return pe;
 }
 

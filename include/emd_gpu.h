@@ -163,18 +163,19 @@ emd_status emd_lj_compute(emd_ctx* ctx);
 emd_status emd_lj_set_intensity(emd_ctx* ctx, const double* intensity);
 /* compute_energy(): shifted LJ potential energy (force_lj_neigh_impl.h:129-156, 259-343). */
 emd_status emd_lj_energy(emd_ctx* ctx, double* pe);
-/* The energy of a thermo step without a second pass over the list (no
- * counterpart in ExaMiniMD, whose PotE::compute runs compute_energy after the
- * step).  After emd_lj_request_energy, the next emd_lj_compute of the mixed
- * form (one type pair) also sums the shifted energy of the pairs it
- * evaluates, inside the force kernel: FP32 pair terms corrected to first
- * order for the exact pair distance, compensated FP32 sums per atom and FP64
- * sums per block, within ~1e-9 relative of emd_lj_energy at LJ-4M (rounding
- * with random signs, ~3e-7 / sqrt(atoms)).  The forces are the same bits as
- * without the energy.  emd_lj_force_energy returns it (*available = 1) while
- * no call has moved the owned positions since that compute; otherwise
- * *available = 0 and the caller uses emd_lj_energy.  The request is consumed
- * by that one compute. */
+/* The energy of a thermo step, delivered by the force call (no counterpart
+ * in ExaMiniMD, whose PotE::compute runs compute_energy, a second pass over
+ * the list, after the step: examinimd.cpp:250-262, force_lj_neigh_impl.h:
+ * 129-156).  After emd_lj_request_energy, the next emd_lj_compute of the
+ * mixed form (one type pair) runs the force kernel unchanged and then an
+ * energy kernel over the same rows and pair decisions, which carries every
+ * pair's FP32 rounding remainders (pair difference, position rounding, r^2,
+ * reciprocal, products) and keeps every addition's error: within 1e-11
+ * relative of emd_lj_energy, lattices included.  The forces are the same bits
+ * as without the request.  The sum stays on the device until
+ * emd_lj_force_energy reads it (*available = 1) while no call has moved the
+ * owned positions since that compute; otherwise *available = 0 and the
+ * caller uses emd_lj_energy.  The request is consumed by that one compute. */
 emd_status emd_lj_request_energy(emd_ctx* ctx);
 emd_status emd_lj_force_energy(emd_ctx* ctx, double* pe, int* available);
 /* Gradient of a loss L(E, F) with respect to the LJ eps and sigma, for

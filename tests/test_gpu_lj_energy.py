@@ -1,8 +1,8 @@
-"""The mixed-precision LJ energy fused into the force pass (GPU).
+"""The mixed-precision LJ energy of a thermo step, delivered by the force call (GPU).
 
 On thermo steps the driver asks for the energy with the force
-(emd_lj_request_energy): the mixed kernel then sums the shifted LJ energy of
-the pairs it evaluates, and emd_lj_force_energy returns it while the
+(emd_lj_request_energy): the force call then runs the energy kernel over the
+same rows and pair decisions, and emd_lj_force_energy returns it while the
 positions stay unchanged.  It is compared with the FP64 energy of the same
 positions (emd_lj_energy).  Every pair is carried as an FP32 value and its
 first-order remainder (the exact pair difference including the rounding of
@@ -31,7 +31,7 @@ def _rms_rel(a, b):
 
 
 @pytest.mark.parametrize("n,tol", [(6, 1e-11), (10, 1e-11), (100, 1e-11)])
-def test_fused_energy_matches_fp64_energy(n, tol):
+def test_thermo_energy_matches_fp64_energy(n, tol):
     setup = mdloop.LJSetup(n)
     state = dict(mdloop.make_lattice(setup, 8))
     rng = np.random.default_rng(n)
@@ -44,10 +44,10 @@ def test_fused_energy_matches_fp64_energy(n, tol):
     mix.zero_forces()
     mix.lj_request_energy()
     mix.lj_compute()
-    fused = mix.lj_force_energy()
+    delivered = mix.lj_force_energy()
     exact = mix.lj_energy()  # FP64 over the same list and positions
-    assert fused is not None
-    assert abs(fused - exact) <= tol * abs(exact), (fused, exact, (fused - exact) / exact)
+    assert delivered is not None
+    assert abs(delivered - exact) <= tol * abs(exact), (delivered, exact, (delivered - exact) / exact)
     # the request served one compute only; a moved position retires the value
     mix.lj_compute()
     assert mix.lj_force_energy() is None
@@ -60,7 +60,7 @@ def test_fused_energy_matches_fp64_energy(n, tol):
 
 
 @pytest.mark.parametrize("n", [20, 100])
-def test_fused_energy_on_the_perfect_lattice(n):
+def test_thermo_energy_on_the_perfect_lattice(n):
     """The thermo step 0 of the LJ decks: every pair of a neighbour shell
     has the same distance, so an FP32 rounding of the pair energy would add
     up coherently (5e-8 relative); the carried remainders do not."""
@@ -70,13 +70,13 @@ def test_fused_energy_on_the_perfect_lattice(n):
     mix.zero_forces()
     mix.lj_request_energy()
     mix.lj_compute()
-    fused, exact = mix.lj_force_energy(), mix.lj_energy()
-    assert fused is not None
-    assert abs(fused - exact) <= 1e-11 * abs(exact), (fused, exact, (fused - exact) / exact)
+    delivered, exact = mix.lj_force_energy(), mix.lj_energy()
+    assert delivered is not None
+    assert abs(delivered - exact) <= 1e-11 * abs(exact), (delivered, exact, (delivered - exact) / exact)
     mix.close()
 
 
-def test_fused_energy_does_not_change_the_forces():
+def test_thermo_energy_does_not_change_the_forces():
     """A compute with the energy gives the same force bits as one without."""
     setup = mdloop.LJSetup(8)
     state = mdloop.make_lattice(setup)
@@ -93,9 +93,9 @@ def test_fused_energy_does_not_change_the_forces():
         np.testing.assert_array_equal(ga[k], gb[k])
 
 
-def test_driver_thermo_uses_the_fused_energy(tmp_path):
+def test_driver_thermo_uses_the_delivered_energy(tmp_path):
     """The driver asks for the energy on thermo steps: its thermo PE in the
-    mixed form stays within the fused-energy bound of the FP64 value."""
+    mixed form stays within the delivered-energy bound of the FP64 value."""
     from examinimd_gb300 import MD
     from tests.golden.decks import CASES, write_case
     case = dict(CASES["lj_fcc6_full_csr"])
@@ -109,8 +109,8 @@ def test_driver_thermo_uses_the_fused_energy(tmp_path):
     md.close()
 
 
-def test_several_types_have_no_fused_energy():
-    """The fused energy covers one type pair; with per-pair parameters the
+def test_several_types_have_no_delivered_energy():
+    """The delivered energy covers one type pair; with per-pair parameters the
     caller falls back to emd_lj_energy."""
     rng = np.random.default_rng(13)
     coeffs = [(a, b, float(rng.uniform(0.8, 1.2)), float(rng.uniform(0.9, 1.05)), 2.5)
@@ -126,7 +126,7 @@ def test_several_types_have_no_fused_energy():
 
 def test_large_cutoff_rows_and_forces():
     """rc = 6: bins of about 250 particles; rows equal the oracle's, mixed
-    forces within the mixed tolerance of FP64, and the fused energy within
+    forces within the mixed tolerance of FP64, and the delivered energy within
     its bound."""
     from oracle.orc import Oracle
     setup = mdloop.LJSetup(12, cut=6.0, skin=0.3, coeffs=[(1, 1, 1.0, 1.0, 6.0)])
@@ -145,5 +145,5 @@ def test_large_cutoff_rows_and_forces():
     mix.zero_forces()
     mix.lj_request_energy()
     mix.lj_compute()
-    fused, exact = mix.lj_force_energy(), ref.lj_energy()
-    assert fused is not None and abs(fused - exact) <= 1e-11 * abs(exact)
+    delivered, exact = mix.lj_force_energy(), ref.lj_energy()
+    assert delivered is not None and abs(delivered - exact) <= 1e-11 * abs(exact)
