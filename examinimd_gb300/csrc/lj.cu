@@ -320,8 +320,6 @@ emd_status emd_lj_init(emd_ctx* ctx, int ntypes, const double* lj1, const double
   EMD_API_BEGIN
   require(ntypes >= 1 && lj1 && lj2 && cutsq, EMD_ERR_ARG, "emd_lj_init: bad parameter tables");
   require(precision == EMD_PREC_FP64 || precision == EMD_PREC_MIXED, EMD_ERR_ARG, "emd_lj_init: precision");
-  require(!(precision == EMD_PREC_MIXED && half_neigh), EMD_ERR_ARG,
-          "emd_lj_init: the mixed-precision form uses the full list");
   const size_t nt2 = size_t(ntypes) * ntypes;
   std::vector<double> h(3 * nt2);
   for (size_t k = 0; k < nt2; ++k) {

@@ -176,6 +176,65 @@ __global__ void __launch_bounds__(128) k_lj_full_mixed(const float4* __restrict_
   }
 }
 
+// TagHalfNeigh (force_lj_neigh_impl.h:211-254) in the mixed form: every
+// pair once, its FP32 force as the full form computes it (lj_quad's
+// arithmetic), f_i summed in the compensated accumulator and -F_ij scattered
+// to j (owned or ghost) with FP64 atomics, so the sums round in no fixed
+// order, as in the FP64 half form.
+template <bool SINGLE>
+__device__ __forceinline__ void lj_quad_half(const PairCtx& C, const int4& e, const float4* __restrict__ xl,
+                                             const LJParamsF& P, Acc& acc, double* __restrict__ f) {
+  const int js[4] = {e.x >> 6, e.y >> 6, e.z >> 6, e.w >> 6};
+  const float4 x0 = xl[js[0]], x1 = xl[js[1]], x2 = xl[js[2]], x3 = xl[js[3]];
+  const PairGeo g0 = lj_geo<SINGLE>(C, e.x, x0, P), g1 = lj_geo<SINGLE>(C, e.y, x1, P);
+  const PairGeo g2 = lj_geo<SINGLE>(C, e.z, x2, P), g3 = lj_geo<SINGLE>(C, e.w, x3, P);
+  bool in[4] = {g0.rsq < g0.cutsq, g1.rsq < g1.cutsq, g2.rsq < g2.cutsq, g3.rsq < g3.cutsq};
+  const bool b0 = in_band(g0), b1 = in_band(g1), b2 = in_band(g2), b3 = in_band(g3);
+  if (b0 || b1 || b2 || b3) {  // borderline: decide as FP64 does
+    if (b0) in[0] = cut_fp64(C.x4, C.i, js[0], g0.cutsq_d);
+    if (b1) in[1] = cut_fp64(C.x4, C.i, js[1], g1.cutsq_d);
+    if (b2) in[2] = cut_fp64(C.x4, C.i, js[2], g2.cutsq_d);
+    if (b3) in[3] = cut_fp64(C.x4, C.i, js[3], g3.cutsq_d);
+  }
+  float2 a[4];
+  float z[4];
+  lj_force(g0, in[0], a[0], z[0]);
+  lj_force(g1, in[1], a[1], z[1]);
+  lj_force(g2, in[2], a[2], z[2]);
+  lj_force(g3, in[3], a[3], z[3]);
+  acc.add(__fadd2_rn(__fadd2_rn(a[0], a[1]), __fadd2_rn(a[2], a[3])),
+          __fadd_rn(__fadd_rn(z[0], z[1]), __fadd_rn(z[2], z[3])));
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (in[k]) {
+      double* fj = f + 3 * size_t(js[k]);
+      atomicAdd(fj, -double(a[k].x));
+      atomicAdd(fj + 1, -double(a[k].y));
+      atomicAdd(fj + 2, -double(z[k]));
+    }
+}
+
+template <bool SINGLE>
+__global__ void __launch_bounds__(128) k_lj_half_mixed(const float4* __restrict__ xl,
+                                                       const double4_32a* __restrict__ x4, double* __restrict__ f,
+                                                       const int4* __restrict__ rows4, int stride,
+                                                       const int* __restrict__ num, LJParamsF P, float wx, float wy,
+                                                       float wz, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PairCtx C;
+  C.xi = xl[i];
+  C.i = i;
+  C.ti = __float_as_int(C.xi.w);
+  C.set_bin_width(wx, wy, wz);
+  C.x4 = x4;
+  Acc acc;
+  lj_row(i, rows4 + i, num[i], stride, [&](const int4& e) { lj_quad_half<SINGLE>(C, e, xl, P, acc, f); });
+  atomicAdd(f + 3 * i, double(acc.sxy.x) - double(acc.cxy.x));
+  atomicAdd(f + 3 * i + 1, double(acc.sxy.y) - double(acc.cxy.y));
+  atomicAdd(f + 3 * i + 2, double(acc.sz) - double(acc.cz));
+}
+
 // The shifted LJ energy over the same rows and pair decisions as the force
 // (single type pair), one FP64 partial per warp (lj_pair.cuh, energy_pair2):
 // the sums stay FP32 hi + lo pairs through the warp reduction and only lane
@@ -292,6 +351,15 @@ void lj_mixed_compute(Ctx& c) {
   const bool zero = c.f_zero_pending & 1;
   const dim3 g(blocks_for(n, 128)), b(128);
   const float wx = float(F.wx), wy = float(F.wy), wz = float(F.wz);
+  if (c.lj_half) {  // every pair once, scattered to both atoms (the energy: emd_lj_energy)
+    materialize_zero(c, true, true);
+    TimedLaunch t(c, "lj_half_mixed");
+    auto k = c.lj_uniform ? k_lj_half_mixed<true> : k_lj_half_mixed<false>;
+    k<<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy,
+                                                 wz, n);
+    EMD_CHECK_LAUNCH();
+    return;
+  }
   // the energy of a thermo step (emd_lj_request_energy), single type pair
   const bool energy = c.lj_energy_request && c.lj_uniform;
   LJEnergyF E{};

@@ -188,6 +188,39 @@ def test_lj_mixed_pairs_on_the_cutoff():
     assert pe is not None and abs(pe - ref.lj_energy()) <= 1e-11 * abs(ref.lj_energy())
 
 
+@pytest.mark.parametrize("kind,newton", [(0, False), (0, True), (1, True)])
+def test_lj_mixed_half_list(kind, newton):
+    """NEIGH_HALF in the mixed form (force_lj_neigh_impl.h:211-254): every
+    pair once, its FP32 force added to i and scattered to j with FP64 atomics
+    (folded back from the ghosts with newton on).  Forces within the mixed
+    tolerance of the FP64 half form on the same positions, the energy over
+    the packed half rows equal to the FP64 form's to 1e-12, and 20 steps
+    across a rebuild close to the FP64 trajectory."""
+    from examinimd_gb300 import EMD_PREC_MIXED
+    setup = mdloop.LJSetup(6, kind=kind, half=True, newton=newton)
+    state = dict(mdloop.make_lattice(setup))
+    rng = np.random.default_rng(7)
+    state["x"] = np.mod(state["x"] + rng.normal(0.0, 0.03, state["x"].shape), setup.domain[0])
+    ref, mix = _ctx(), _ctx()
+    mdloop.init(ref, setup, state)
+    mdloop.init(mix, setup, state, precision=EMD_PREC_MIXED)
+    nl = ref.info()[0]
+    a, b = ref.get(0, nl), mix.get(0, nl)
+    np.testing.assert_array_equal(a["id"], b["id"])
+    err = np.linalg.norm(b["f"] - a["f"], axis=1)
+    scale = np.sqrt(np.mean(np.sum(a["f"] ** 2, axis=1)))
+    assert np.sqrt(np.mean(err ** 2)) <= 1e-5 * scale, np.sqrt(np.mean(err ** 2)) / scale
+    assert err.max() <= 1e-4 * scale
+    assert abs(mix.lj_energy() - ref.lj_energy()) <= 1e-12 * abs(ref.lj_energy())
+    for s in range(1, 21):
+        mdloop.step(ref, setup, s)
+        mdloop.step(mix, setup, s)
+    a, b = ref.get(0, nl), mix.get(0, nl)
+    np.testing.assert_array_equal(a["id"], b["id"])
+    assert _rel_err(b["x"], a["x"]) <= 1e-6
+    assert mix.status() == 0
+
+
 def test_lj_many_types_per_pair_parameters():
     """13 types: above ExaMiniMD's 12-type stack-parameter limit, so every
     type pair keeps its own eps / sigma (force_lj_neigh_impl.h:75-98).  The
@@ -239,7 +272,7 @@ def test_lj_mixed_on_2d_lists():
 
 
 @pytest.mark.parametrize("half,precision,rho", [(False, 0, 0.8442), (True, 0, 0.8442), (False, 1, 0.8442),
-                                                (False, 1, 2.0), (True, 0, 2.0)])
+                                                (False, 1, 2.0), (True, 0, 2.0), (True, 1, 0.8442)])
 def test_neighbour_rows_on_a_random_gas(half, precision, rho):
     """Uniform random positions (no lattice order; at rho 2 a bin holds about
     40 atoms, more than one warp's lanes): bins, ghosts and every neighbour row
