@@ -88,6 +88,16 @@ __device__ __forceinline__ long long okey(double v) {
   return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
+// The half list's order rule (neighbor_csr.h:287-291): j "above" i when
+// (x_j, y_j, z_j) > (x_i, y_i, z_i) lexicographically, from the FP64
+// positions.  Out of line for the same reason as retest_fp64.
+__device__ __noinline__ bool above_fp64(const double4_32a* __restrict__ x4, long long kx, long long ky,
+                                        long long kz, int j) {
+  const double4_32a xj = x4[j];
+  const long long jx = okey(xj.x), jy = okey(xj.y), jz = okey(xj.z);
+  return (jx > kx) || ((jx == kx) && ((jy > ky) || ((jy == ky) && (jz > kz))));
+}
+
 template <bool HALF, bool PACKED>
 __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
   // each warp of the CTA builds the rows of its own bin with its own staging
@@ -139,6 +149,11 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
   // dropped candidate's exceeds cut_hi by a 1e-5 margin, so no lane would
   // accept the pair or re-test it in FP64.  Rows keep their order.
   const float prune_sq = a.cut_hi * 1.00001f;
+  // half lists: the FP32 x offset of a candidate from a centre atom has the
+  // sign of the FP64 x difference once it exceeds the FP32 rounding of the
+  // two offsets and the bin shift (below 2^-24 (3 w + 2 drift) in all); only
+  // x ties within that bound need the FP64 order keys
+  const float otol = 1e-6f * (1.0f + 4.0f * fmaxf(a.wx, fmaxf(a.wy, a.wz)));
   const unsigned lt = (1u << lane) - 1u;
   for (int a0 = 0; a0 < nc; a0 += 32) {
     // this lane's centre atom
@@ -230,10 +245,11 @@ __global__ void __launch_bounds__(NB_THREADS) k_neigh_bin(NeighArgs a) {
               // neighbor_csr.h:287-291: skip unless j is "above" i
               // lexicographically, or j is a ghost with newton off
               const int j = PACKED ? (w >> 6) : w;
-              const double4_32a xj = a.x4[j];
-              const long long jx = okey(xj.x), jy = okey(xj.y), jz = okey(xj.z);
-              const bool above = (jx > kx) || ((jx == kx) && ((jy > ky) || ((jy == ky) && (jz > kz))));
-              const bool skip = ((j == i) || (j < a.n_local || a.newton)) && !above;
+              bool skip = false;
+              if ((j == i) || (j < a.n_local || a.newton)) {
+                const float gx = __fsub_rn(c.x, xi.x);
+                skip = fabsf(gx) > otol ? !(gx > 0.f) : !above_fp64(a.x4, kx, ky, kz, j);
+              }
               if (!skip && !decided) in = retest_fp64(a.x4, i, j, a.cutsq);
               take = !skip && in;
             } else {
