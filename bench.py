@@ -542,7 +542,7 @@ def snap_accuracy(md, device: int, cells: int, coeff: str, param: str, steps_don
     return out
 
 
-def snap_cpu_sample(coeff: str, param: str, cells: int = 16, steps: int = 3, threads: int | None = None) -> dict:
+def snap_cpu_sample(coeff: str, param: str, cells: int = 20, steps: int = 20, threads: int | None = None) -> dict:
     """The CPU oracle's SNAP (the reference formulation, OpenMP over atoms on
     every host core) on a bcc cells^3 sample of the SNAP-W workload, timed per
     atom-step."""
@@ -928,7 +928,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cells", type=int, default=None, help="override the lattice size (profiling cases)")
     ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=60)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the full-size force-error / drift check")
     ap.add_argument("--drift-steps", type=int, default=1000)

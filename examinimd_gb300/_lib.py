@@ -73,6 +73,7 @@ _SIGS = {
     "emd_snap_request_energy": ([_P], _I),
     "emd_snap_force_energy": ([_P, _DP, _IP], _I),
     "emd_lj_force_energy": ([_P, _DP, _IP], _I),
+    "emd_lj_energy_mixed": ([_P, _DP, _IP], _I),
     "emd_lj_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_batch_create": ([C.POINTER(_P), _I, _I, _IP, _DP, _DP, _DP, _D, _D, _D, _D, _D, _D, _I, _I, _D], _I),
     "emd_batch_destroy": ([_P], None),
@@ -347,6 +348,12 @@ class Context:
         """The energy computed by the last lj_compute, or None (emd_lj_force_energy)."""
         e, ok = _D(), _I()
         self._ok(self.lib.emd_lj_force_energy(self.h, C.byref(e), C.byref(ok)), "emd_lj_force_energy")
+        return e.value if ok.value else None
+
+    def lj_energy_mixed(self):
+        """The mixed form's energy kernel alone, or None where it does not apply (emd_lj_energy_mixed)."""
+        e, ok = _D(), _I()
+        self._ok(self.lib.emd_lj_energy_mixed(self.h, C.byref(e), C.byref(ok)), "emd_lj_energy_mixed")
         return e.value if ok.value else None
 
     def snap_request_energy(self):

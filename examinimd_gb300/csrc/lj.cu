@@ -177,6 +177,8 @@ __global__ void __launch_bounds__(256) k_lj_energy(const double4_32a* __restrict
 // shared with lj_mixed.cu
 void lj_mixed_compute(Ctx& c);
 void lj_mixed_prepare(Ctx& c);
+bool lj_mixed_energy_available(const Ctx& c);
+double lj_mixed_energy(Ctx& c);
 
 // Fitting adjoint of the single-parameter-set LJ model (no counterpart in
 // ExaMiniMD): per owned atom over its full row, the eps- and sigma-
@@ -524,6 +526,17 @@ emd_status emd_lj_request_energy(emd_ctx* ctx) {
   EMD_API_BEGIN
   require(c.lj_ready, EMD_ERR_STATE, "emd_lj_request_energy: emd_lj_init not called");
   c.lj_energy_request = true;
+  EMD_API_END
+}
+
+emd_status emd_lj_energy_mixed(emd_ctx* ctx, double* pe, int* available) {
+  EMD_API_BEGIN
+  require(pe && available, EMD_ERR_ARG, "emd_lj_energy_mixed: null output");
+  *pe = 0.0;
+  *available = 0;
+  if (!lj_mixed_energy_available(c)) return EMD_OK;
+  *pe = lj_mixed_energy(c);
+  *available = 1;
   EMD_API_END
 }
 

@@ -332,19 +332,87 @@ void nve_final_mixed(Ctx& c) {
   EMD_CHECK_LAUNCH();
 }
 
+namespace {
+
+// The FP32 positions must equal FP32(x - bin centre) for every particle
+void ensure_xl(Ctx& c) {
+  if (c.xl_ok == 3) return;
+  const int n_all = c.N_local + c.N_ghost;
+  TimedLaunch t(c, "lj_refresh_xl");
+  k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, c.xl.p);
+  EMD_CHECK_LAUNCH();
+  c.xl_ok = 3;
+}
+
+LJParamsF params_f(const Ctx& c) {
+  const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
+  return LJParamsF{c.lj_params_f.p, c.lj_params_f.p + nt2, c.lj_params_f.p + 2 * nt2, c.lj_params.p + 2 * nt2,
+                   c.lj_ntypes, c.lj_single[0], c.lj_single[1], c.lj_single[2], c.lj_single_cutsq_d};
+}
+
+// The shifted LJ energy of the current positions over the current packed
+// full list (one type pair): position remainders, the energy kernel and the
+// device sum, all stream-ordered; the sum lands at c.lj_pe_dev.
+void launch_energy_mixed(Ctx& c) {
+  const int n_all = c.N_local + c.N_ghost, n = c.N_local;
+  const BinFrame F = frame(c);
+  const float wx = float(F.wx), wy = float(F.wy), wz = float(F.wz);
+  const ListView L = list_view(c);
+  const int4* rows4 = reinterpret_cast<const int4*>(L.entries);
+  const dim3 g(blocks_for(n, 128)), b(128);
+  LJEnergyF E{};
+  const double a64 = c.lj_single_d[0] / 12.0, b64 = c.lj_single_d[1] / 6.0;
+  const double r2c = 1.0 / c.lj_single_cutsq_d, r6c = r2c * r2c * r2c;
+  E.a = a64;
+  E.b = b64;
+  E.ecut = r6c * (a64 * r6c - b64);
+  const double w64[3] = {F.wx, F.wy, F.wz};
+  const float wl[3] = {float(w64[0] - double(wx)), float(w64[1] - double(wy)), float(w64[2] - double(wz))};
+  E.nwlo_xy = make_float2(-wl[0] * 0.0625f, -wl[1] * 0.25f);
+  E.wlo_xy = make_float2(wl[0], wl[1]);
+  E.nwlo_z = -wl[2];
+  E.wlo_z = wl[2];
+  c.lj_pe_part.reserve(size_t(g.x) * 4 + kSumScratchDoubles, c.stream);
+  double* part = c.lj_pe_part.p;
+  c.lj_xlo.reserve(size_t(n_all) + 1, c.stream);
+  E.xlo = c.lj_xlo.p;
+  {
+    TimedLaunch t(c, "lj_pos_remainder");
+    k_pos_remainder<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, c.xl.p, c.lj_xlo.p);
+    EMD_CHECK_LAUNCH();
+  }
+  {
+    TimedLaunch t(c, "lj_energy_mixed");
+    k_lj_energy_mixed<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, rows4, L.stride, L.num_neighs, params_f(c), wx, wy, wz,
+                                              n, E, part);
+    EMD_CHECK_LAUNCH();
+  }
+  // summed on the device: no host wait here
+  device_sum_launch(c, part, int(g.x) * 4, part + size_t(g.x) * 4);
+  c.lj_pe_dev = part + size_t(g.x) * 4 + kSumScratchDoubles - 1;
+}
+
+}  // namespace
+
+bool lj_mixed_energy_available(const Ctx& c) {
+  return c.lj_ready && c.lj_prec == EMD_PREC_MIXED && c.lj_uniform && !c.lj_half && c.neigh_ready &&
+         c.neigh_packed && !c.half_neigh && c.neigh_rows == c.N_local;
+}
+
+double lj_mixed_energy(Ctx& c) {
+  if (c.N_local == 0) return 0.0;
+  ensure_xl(c);
+  launch_energy_mixed(c);
+  EMD_CUDA(cudaMemcpyAsync(c.h_scalar, c.lj_pe_dev, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  return *c.h_scalar;
+}
+
 void lj_mixed_compute(Ctx& c) {
   materialize_kick(c);
-  const int n_all = c.N_local + c.N_ghost;
+  ensure_xl(c);
   const BinFrame F = frame(c);
-  if (c.xl_ok != 3) {
-    TimedLaunch t(c, "lj_refresh_xl");
-    k_refresh_xl<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, c.xl.p);
-    EMD_CHECK_LAUNCH();
-    c.xl_ok = 3;
-  }
-  const size_t nt2 = size_t(c.lj_ntypes) * c.lj_ntypes;
-  LJParamsF P{c.lj_params_f.p, c.lj_params_f.p + nt2, c.lj_params_f.p + 2 * nt2, c.lj_params.p + 2 * nt2,
-              c.lj_ntypes, c.lj_single[0], c.lj_single[1], c.lj_single[2], c.lj_single_cutsq_d};
+  const LJParamsF P = params_f(c);
   const ListView L = list_view(c);
   const int4* rows4 = reinterpret_cast<const int4*>(L.entries);
   const int n = c.N_local;
@@ -355,34 +423,9 @@ void lj_mixed_compute(Ctx& c) {
     materialize_zero(c, true, true);
     TimedLaunch t(c, "lj_half_mixed");
     auto k = c.lj_uniform ? k_lj_half_mixed<true> : k_lj_half_mixed<false>;
-    k<<<blocks_for(n, 128), 128, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy,
-                                                 wz, n);
+    k<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n);
     EMD_CHECK_LAUNCH();
     return;
-  }
-  // the energy of a thermo step (emd_lj_request_energy), single type pair
-  const bool energy = c.lj_energy_request && c.lj_uniform;
-  LJEnergyF E{};
-  double* part = nullptr;
-  if (energy) {
-    const double a64 = c.lj_single_d[0] / 12.0, b64 = c.lj_single_d[1] / 6.0;
-    const double r2c = 1.0 / c.lj_single_cutsq_d, r6c = r2c * r2c * r2c;
-    E.a = a64;
-    E.b = b64;
-    E.ecut = r6c * (a64 * r6c - b64);
-    const double w64[3] = {F.wx, F.wy, F.wz};
-    const float wl[3] = {float(w64[0] - double(wx)), float(w64[1] - double(wy)), float(w64[2] - double(wz))};
-    E.nwlo_xy = make_float2(-wl[0] * 0.0625f, -wl[1] * 0.25f);
-    E.wlo_xy = make_float2(wl[0], wl[1]);
-    E.nwlo_z = -wl[2];
-    E.wlo_z = wl[2];
-    c.lj_pe_part.reserve(size_t(g.x) * 4 + kSumScratchDoubles, c.stream);
-    part = c.lj_pe_part.p;
-    c.lj_xlo.reserve(size_t(n_all) + 1, c.stream);
-    E.xlo = c.lj_xlo.p;
-    TimedLaunch t(c, "lj_pos_remainder");
-    k_pos_remainder<<<blocks_for(n_all, 256), 256, 0, c.stream>>>(c.x4.p, bin_centres(c), n_all, c.xl.p, c.lj_xlo.p);
-    EMD_CHECK_LAUNCH();
   }
   {
     TimedLaunch t(c, "lj_full_mixed");
@@ -391,18 +434,14 @@ void lj_mixed_compute(Ctx& c) {
     k<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, c.f.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n);
     EMD_CHECK_LAUNCH();
   }
-  if (energy) {
-    TimedLaunch t(c, "lj_energy_mixed");
-    k_lj_energy_mixed<<<g, b, 0, c.stream>>>(c.xl.p, c.x4.p, rows4, L.stride, L.num_neighs, P, wx, wy, wz, n, E,
-                                              part);
-    EMD_CHECK_LAUNCH();
-    // summed on the device; no host wait inside the force call
-    device_sum_launch(c, part, int(g.x) * 4, part + size_t(g.x) * 4);
-    c.lj_pe_dev = part + size_t(g.x) * 4 + kSumScratchDoubles - 1;
+  c.f_zero_pending &= ~1;
+  // the energy of a thermo step (emd_lj_request_energy), single type pair:
+  // its own kernel after the force, over the same rows
+  if (c.lj_energy_request && c.lj_uniform) {
+    launch_energy_mixed(c);
     c.lj_pe_version = c.x_version;
     c.lj_pe_valid = true;
   }
-  c.f_zero_pending &= ~1;
 }
 
 void lj_mixed_prepare(Ctx& c) {

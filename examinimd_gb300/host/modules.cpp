@@ -143,9 +143,12 @@ double ForceLJNeigh_GB300::compute_energy(System* system, Binning*, Neighbor*) {
   if (idial_) return 0.0;  // ForceLJIDialNeigh keeps Force's default (force.h:54)
   double pe = 0.0;
   int delivered = 0;
-  // on the mixed form's thermo steps the force call also computed the energy
-  if (precision_ == EMD_PREC_MIXED) check(emd_lj_force_energy(system->ctx, &pe, &delivered), system->ctx,
-                                           "emd_lj_force_energy");
+  // the mixed form: the energy the force call computed on a thermo step, or
+  // the same kernel on its own (one type pair, full list)
+  if (precision_ == EMD_PREC_MIXED) {
+    check(emd_lj_force_energy(system->ctx, &pe, &delivered), system->ctx, "emd_lj_force_energy");
+    if (!delivered) check(emd_lj_energy_mixed(system->ctx, &pe, &delivered), system->ctx, "emd_lj_energy_mixed");
+  }
   if (!delivered) check(emd_lj_energy(system->ctx, &pe), system->ctx, "emd_lj_energy");
   return pe;
 }

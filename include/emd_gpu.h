@@ -178,6 +178,13 @@ emd_status emd_lj_energy(emd_ctx* ctx, double* pe);
  * caller uses emd_lj_energy.  The request is consumed by that one compute. */
 emd_status emd_lj_request_energy(emd_ctx* ctx);
 emd_status emd_lj_force_energy(emd_ctx* ctx, double* pe, int* available);
+/* The same mixed-precision energy kernel on its own, for the current
+ * positions and list, without a force call (compute_energy in the mixed
+ * form, force_lj_neigh_impl.h:129-156; about 20x cheaper than the FP64 pass
+ * of emd_lj_energy at LJ-4M, within 1e-11 relative of it).  *available = 0
+ * (and nothing launched) unless the context runs the mixed form with one type
+ * pair on a current full list. */
+emd_status emd_lj_energy_mixed(emd_ctx* ctx, double* pe, int* available);
 /* Gradient of a loss L(E, F) with respect to the LJ eps and sigma, for
  * fitting them (no counterpart in ExaMiniMD).  Every type pair must share one
  * eps / sigma / cutoff (the cutoff is held fixed); full list (NEIGH_FULL)

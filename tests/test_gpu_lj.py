@@ -212,6 +212,7 @@ def test_lj_mixed_half_list(kind, newton):
     assert np.sqrt(np.mean(err ** 2)) <= 1e-5 * scale, np.sqrt(np.mean(err ** 2)) / scale
     assert err.max() <= 1e-4 * scale
     assert abs(mix.lj_energy() - ref.lj_energy()) <= 1e-12 * abs(ref.lj_energy())
+    assert mix.lj_energy_mixed() is None  # the mixed energy kernel covers full lists
     for s in range(1, 21):
         mdloop.step(ref, setup, s)
         mdloop.step(mix, setup, s)

@@ -76,6 +76,26 @@ def test_thermo_energy_on_the_perfect_lattice(n):
     mix.close()
 
 
+@pytest.mark.parametrize("n,moved", [(20, False), (10, True)])
+def test_standalone_mixed_energy(n, moved):
+    """emd_lj_energy_mixed: the energy kernel alone on the current positions
+    and list, without a force call: within 1e-11 of emd_lj_energy, the
+    forces untouched."""
+    setup = mdloop.LJSetup(n)
+    mix = _ctx()
+    mdloop.init(mix, setup, mdloop.make_lattice(setup, 8), precision=1)
+    if moved:
+        for s in range(1, 8):
+            mdloop.step(mix, setup, s)
+    nl = mix.info()[0]
+    f0 = mix.get(0, nl)["f"]
+    e, exact = mix.lj_energy_mixed(), mix.lj_energy()
+    assert e is not None
+    assert abs(e - exact) <= 1e-11 * abs(exact), (e, exact, (e - exact) / exact)
+    np.testing.assert_array_equal(mix.get(0, nl)["f"], f0)
+    mix.close()
+
+
 def test_thermo_energy_does_not_change_the_forces():
     """A compute with the energy gives the same force bits as one without."""
     setup = mdloop.LJSetup(8)
@@ -122,6 +142,7 @@ def test_several_types_have_no_delivered_energy():
     mix.lj_request_energy()
     mix.lj_compute()
     assert mix.lj_force_energy() is None
+    assert mix.lj_energy_mixed() is None
 
 
 def test_large_cutoff_rows_and_forces():
