@@ -181,10 +181,14 @@ constexpr int BG = 4;
 // seeded with sfac * w_j, so each layer's sum over the neighbours is a plain
 // sum: one warp adds up layer j - 1 (in a fixed order) while the others run
 // layer j.  `work` holds SNAP_WARPS * BG slots of (bh_even + bh_odd) elements.
-template <typename R>
+// JF > 0: twojmax fixed at compile time (the layer loop unrolls and the
+// element index arithmetic divides by constants); 0: S.twojmax.
+template <typename R, int JF = 0>
 __device__ __forceinline__ void b_stage(const SnapDev& S, const double* nd, int cap, int ninside, Cplx<double>* work,
                                         Cplx<double>* utot, Cplx<R>* utot_r) {
   constexpr bool kCopy = sizeof(R) != sizeof(double);
+  constexpr int kUnroll = JF > 0 ? JF + 1 : 1;
+  const int J = JF > 0 ? JF : S.twojmax;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int sw = S.bh_even + S.bh_odd, per_round = SNAP_WARPS * BG;
   Cplx<double>* mine = work + size_t(warp) * BG * sw;
@@ -195,8 +199,9 @@ __device__ __forceinline__ void b_stage(const SnapDev& S, const double* nd, int 
     const int gw = nin > warp ? (nin - warp + SNAP_WARPS - 1) / SNAP_WARPS : 0;  // this warp's slots
     if (lane < gw) mine[lane * sw] = Cplx<double>{nd[ndx<!kCopy>(ND_SFAC) * cap + nb0 + lane * SNAP_WARPS + warp], 0.0};
     __syncthreads();
-    for (int j = 1; j <= S.twojmax + 1; ++j) {
-      if (j <= S.twojmax) {
+#pragma unroll kUnroll
+    for (int j = 1; j <= J + 1; ++j) {
+      if (j <= J) {
         const int nh = (j + 1) * (j / 2 + 1);
         const int po = ((j - 1) & 1) * S.bh_even, co = (j & 1) * S.bh_even;
         for (int it = lane; it < gw * nh; it += 32) {
@@ -304,9 +309,13 @@ __host__ __device__ __forceinline__ int drev_words(int J) {
   return (J * (J + 1) * (2 * J + 1) / 6 > 1 ? J * (J + 1) * (2 * J + 1) / 6 : 1) +
          2 * (J * (J / 2 + 1) > 1 ? J * (J / 2 + 1) : 1) + (J + 1) * (J / 2 + 1);
 }
-template <typename R, int NB>
-__device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, const Cplx<R>* __restrict__ ytot,
+// JF > 0: twojmax fixed at compile time (the layer loops unroll and the
+// element index arithmetic divides by constants); 0: twojmax = Jrt.
+template <typename R, int NB, int JF = 0>
+__device__ __forceinline__ void d_reverse(int Jrt, int lane, const DRevAB<R>* ab, const Cplx<R>* __restrict__ ytot,
                                           Cplx<R>* W, R* phi, Cplx<R>* ga, Cplx<R>* gb) {
+  constexpr int kUnroll = JF > 0 ? JF : 1;
+  const int J = JF > 0 ? JF : Jrt;
   const int nF = max(1, uoff(J)), nL = max(1, J * (J / 2 + 1)), stride = drev_words(J);
 #pragma unroll
   for (int n = 0; n < NB; ++n) {
@@ -315,6 +324,7 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, 
     if (lane == 0) W[n * stride] = Cplx<R>{R(1), R(0)};
   }
   __syncwarp();
+#pragma unroll kUnroll
   for (int j = 1; j <= J; ++j) {
     const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j), po = uoff(j - 1), co = uoff(j);
     for (int e = lane; e < nh; e += 32) {
@@ -353,6 +363,7 @@ __device__ __forceinline__ void d_reverse(int J, int lane, const DRevAB<R>* ab, 
   }
   int lam = nF, nxt = nF + nL;  // offsets of the current and next adjoint layers
   const int lp = nF + 2 * nL;
+#pragma unroll kUnroll
   for (int j = J; j >= 1; --j) {
     const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j), po = uoff(j - 1);
     for (int e = lane; e < nh; e += 32) {
@@ -675,8 +686,11 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
   }
   __syncthreads();
 
-  // ---- B: U_tot (FP64, both forms)
-  b_stage<R>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
+  // ---- B: U_tot (FP64, both forms); layer loops unrolled at the SNAP-W setting
+  if (S.twojmax == 8)
+    b_stage<R, 8>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
+  else
+    b_stage<R>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
 
   // ---- C: Z jobs and Y = sum_t cY_t Z_t
   // (the adjoint keeps Z for its final contraction, beyond `work`)
@@ -874,10 +888,16 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
       }
       R phi[2];
       Cplx<R> ga[2], gb[2];
-      if (nn == 2)
+      if (J == 8) {  // the SNAP-W setting: layer loops unrolled
+        if (nn == 2)
+          d_reverse<R, 2, 8>(J, lane, ab, ytot, W, phi, ga, gb);
+        else
+          d_reverse<R, 1, 8>(J, lane, ab, ytot, W, phi, ga, gb);
+      } else if (nn == 2) {
         d_reverse<R, 2>(J, lane, ab, ytot, W, phi, ga, gb);
-      else
+      } else {
         d_reverse<R, 1>(J, lane, ab, ytot, W, phi, ga, gb);
+      }
       for (int n = 0; n < nn; ++n) {
         const int nb = n ? nb1 : nb0;
         const R* qr = ndr + nb;
