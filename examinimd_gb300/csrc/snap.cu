@@ -91,7 +91,13 @@ std::vector<int4> zjob_order(const std::vector<int>& trip, const std::vector<int
   }
   std::vector<int> idx(static_cast<size_t>(nj));
   for (int k = 0; k < nj; ++k) idx[size_t(k)] = k;
-  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return cost[size_t(x)] > cost[size_t(y)]; });
+  // longest first; within one length, jobs of equal row counts together, so
+  // a warp's lanes run the same inner loops (no divergence between na x nb
+  // splits of one length)
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+    if (cost[size_t(x)] != cost[size_t(y)]) return cost[size_t(x)] > cost[size_t(y)];
+    return (desc[size_t(x)].w & 0xff) > (desc[size_t(y)].w & 0xff);
+  });
   const int nchunk = (nj + 31) / 32, nround = (nchunk + SNAP_WARPS - 1) / SNAP_WARPS;
   std::vector<int4> out(size_t(nround) * SNAP_THREADS, int4{-1, 0, 0, 0});
   for (int c = 0; c < nchunk; ++c) {
