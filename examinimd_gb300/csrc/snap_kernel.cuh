@@ -475,6 +475,66 @@ __device__ __forceinline__ void dt_layer(int j, int lane, R ar, R ai, R br, R bi
   __syncwarp();
 }
 
+// C: the Z jobs, one per thread (compute_zi, sna_impl.hpp:197-283).  A
+// job's descriptor holds the U_tot offsets of its first U1 and U2 terms, its
+// first inner and outer Clebsch-Gordan offsets, its counts (ma1, mb1) and the
+// row strides j1 + 1, j2 + 1.  Along mb1 the U1 index rises by 1, the U2
+// index falls by 1 and the CG index rises by j2; along ma1 the rows move by
+// +(j1 + 1) and -(j2 + 1).  NBMAX > 0 (twojmax = NBMAX - 1): the inner
+// Clebsch-Gordan row, the same for every ma1, is read once into registers
+// and the inner loop unrolls over NBMAX slots (constant offsets); the
+// arithmetic and its order are the same either way.
+template <typename R, int NBMAX>
+__device__ __forceinline__ void z_jobs(const SnapDev& S, const Cplx<R>* __restrict__ utot_r, const R* __restrict__ cg,
+                                       Cplx<R>* __restrict__ zs) {
+  for (int k = threadIdx.x; k < S.nzo; k += SNAP_THREADS) {
+    const int4 d = S.zord[k];
+    if (d.x < 0) continue;
+    const int u1 = d.y & 0xffff, u2 = int(unsigned(d.y) >> 16);
+    const int ci = d.z & 0xffff, co = int(unsigned(d.z) >> 16);
+    const int na = d.w & 0xff, nbb = (d.w >> 8) & 0xff, s1 = (d.w >> 16) & 0xff, s2 = int(unsigned(d.w) >> 24);
+    const int cs = s2 - 1;
+    R zr = 0, zi = 0;
+    if constexpr (NBMAX > 0) {
+      R cb[NBMAX];
+#pragma unroll
+      for (int b = 0; b < NBMAX; ++b) cb[b] = b < nbb ? cg[ci + b * cs] : R(0);
+      for (int a = 0; a < na; ++a) {
+        const Cplx<R>* A1 = utot_r + u1 + a * s1;
+        const Cplx<R>* B2 = utot_r + u2 - a * s2;
+        R sr = 0, si = 0;
+#pragma unroll
+        for (int b = 0; b < NBMAX; ++b) {
+          if (b < nbb) {
+            const Cplx<R> x = A1[b], y = B2[-b];
+            sr = fma(cb[b], fma(x.r, y.r, -x.i * y.i), sr);
+            si = fma(cb[b], fma(x.r, y.i, x.i * y.r), si);
+          }
+        }
+        const R c = cg[co + a * cs];
+        zr = fma(sr, c, zr);
+        zi = fma(si, c, zi);
+      }
+    } else {
+      for (int a = 0; a < na; ++a) {
+        const Cplx<R>* A1 = utot_r + u1 + a * s1;
+        const Cplx<R>* B2 = utot_r + u2 - a * s2;
+        R sr = 0, si = 0;
+        for (int b = 0; b < nbb; ++b) {
+          const R c = cg[ci + b * cs];
+          const Cplx<R> x = A1[b], y = B2[-b];
+          sr = fma(c, fma(x.r, y.r, -x.i * y.i), sr);
+          si = fma(c, fma(x.r, y.i, x.i * y.r), si);
+        }
+        const R c = cg[co + a * cs];
+        zr = fma(sr, c, zr);
+        zi = fma(si, c, zi);
+      }
+    }
+    zs[d.x] = Cplx<R>{zr, zi};
+  }
+}
+
 struct SnapArgs {
   SnapDev S;
   const double4_32a* x4;
@@ -696,36 +756,10 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
   // (the adjoint keeps Z for its final contraction, beyond `work`)
   Cplx<R>* zs = reinterpret_cast<Cplx<R>*>(MODE == 2 ? work + A.work_bytes : work);
   const R* cg = sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cg) : reinterpret_cast<const R*>(S.cg_f);
-  // descriptor: x the job, y the U_tot offsets of the first U1 and U2
-  // terms, z the first inner and outer Clebsch-Gordan offsets, w the counts
-  // (ma1, mb1) and the row strides j1 + 1, j2 + 1.  Along mb1 the U1 index
-  // rises by 1, the U2 index falls by 1 and the CG index rises by j2; along
-  // ma1 the rows move by +(j1 + 1) and -(j2 + 1) (compute_zi,
-  // sna_impl.hpp:197-283).
-  for (int k = tid; k < S.nzo; k += SNAP_THREADS) {
-    const int4 d = S.zord[k];
-    if (d.x < 0) continue;
-    const int u1 = d.y & 0xffff, u2 = int(unsigned(d.y) >> 16);
-    const int ci = d.z & 0xffff, co = int(unsigned(d.z) >> 16);
-    const int na = d.w & 0xff, nbb = (d.w >> 8) & 0xff, s1 = (d.w >> 16) & 0xff, s2 = int(unsigned(d.w) >> 24);
-    const int cs = s2 - 1;
-    R zr = 0, zi = 0;
-    for (int a = 0; a < na; ++a) {
-      const Cplx<R>* A1 = utot_r + u1 + a * s1;
-      const Cplx<R>* B2 = utot_r + u2 - a * s2;
-      R sr = 0, si = 0;
-      for (int b = 0; b < nbb; ++b) {
-        const R c = cg[ci + b * cs];
-        const Cplx<R> x = A1[b], y = B2[-b];
-        sr = fma(c, fma(x.r, y.r, -x.i * y.i), sr);
-        si = fma(c, fma(x.r, y.i, x.i * y.r), si);
-      }
-      const R c = cg[co + a * cs];
-      zr = fma(sr, c, zr);
-      zi = fma(si, c, zi);
-    }
-    zs[d.x] = Cplx<R>{zr, zi};
-  }
+  if (S.twojmax == 8)
+    z_jobs<R, 9>(S, utot_r, cg, zs);
+  else
+    z_jobs<R, 0>(S, utot_r, cg, zs);
   __syncthreads();
   const R* cY = (sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cY) : reinterpret_cast<const R*>(S.cY_f)) +
                 (size_t)ei * S.nfull;
