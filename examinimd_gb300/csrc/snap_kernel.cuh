@@ -329,8 +329,14 @@ __device__ __forceinline__ void d_reverse(int Jrt, int lane, const DRevAB<R>* ab
     const int nh = (j + 1) * (j / 2 + 1), yo = yoff(j), po = uoff(j - 1), co = uoff(j);
     for (int e = lane; e < nh; e += 32) {
       const int mb = e / (j + 1), ma = e - mb * (j + 1);
+      // the lower half of the middle column is the mirror of its upper half
+      // (written below by the lane that computes the source); its Y' is 0
+      if (2 * mb == j && 2 * ma > j) continue;
       const Cplx<R> y = ytot[yo + e];
       const bool centre = 2 * ma == j && 2 * mb == j;
+      const bool mirrored = 2 * mb < j || 2 * ma < j;
+      const bool even = ((ma + mb) & 1) == 0;
+      const int t = co + (j - mb) * (j + 1) + (j - ma);
 #pragma unroll
       for (int n = 0; n < NB; ++n) {
         const Cplx<R>* P = W + n * stride + po;
@@ -341,25 +347,13 @@ __device__ __forceinline__ void d_reverse(int Jrt, int lane, const DRevAB<R>* ab
         R vi = fma(ab[n].ar, u2.i, fma(-ab[n].ai, u2.r, fma(-ab[n].br, u1.i, ab[n].bi * u1.r)));
         if (centre) vi = -vi;
         phi[n] = fma(vr, y.r, fma(vi, y.i, phi[n]));
-        if (j < J) W[n * stride + co + e] = Cplx<R>{vr, vi};
+        if (j < J) {
+          W[n * stride + co + e] = Cplx<R>{vr, vi};
+          if (mirrored) W[n * stride + t] = even ? Cplx<R>{vr, -vi} : Cplx<R>{-vr, vi};
+        }
       }
     }
     __syncwarp();
-    if (j < J) {
-      for (int e = lane; e < nh; e += 32) {
-        const int mb = e / (j + 1), ma = e - mb * (j + 1);
-        if (2 * mb < j || 2 * ma < j) {
-          const bool even = ((ma + mb) & 1) == 0;
-          const int t = co + (j - mb) * (j + 1) + (j - ma);
-#pragma unroll
-          for (int n = 0; n < NB; ++n) {
-            const Cplx<R> u = W[n * stride + co + e];
-            W[n * stride + t] = even ? Cplx<R>{u.r, -u.i} : Cplx<R>{-u.r, u.i};
-          }
-        }
-      }
-      __syncwarp();
-    }
   }
   int lam = nF, nxt = nF + nL;  // offsets of the current and next adjoint layers
   const int lp = nF + 2 * nL;
