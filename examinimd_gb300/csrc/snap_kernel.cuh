@@ -851,7 +851,7 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
         dp[0].r += sv;
       }
       __syncwarp();
-      for (int jl = 1; jl <= S.twojmax; ++jl) {
+      auto layer = [&](int jl) {
         dt_layer<R>(jl, lane, Rar, Rai, Rbr, Rbi, tar, tai, tbr, tbi, P, TP, C, TC);
         const int nh = (jl + 1) * (jl / 2 + 1), yo = yoff(jl);
         for (int e = lane; e < nh; e += 32) {  // rescaled: D = sum (sv V + sfac T), times 1/f below
@@ -865,6 +865,12 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
         t = TP;
         TP = TC;
         TC = t;
+      };
+      if (S.twojmax == 8) {  // layer loop unrolled: constant index arithmetic
+#pragma unroll
+        for (int jl = 1; jl <= 8; ++jl) layer(jl);
+      } else {
+        for (int jl = 1; jl <= S.twojmax; ++jl) layer(jl);
       }
     }
     __syncthreads();
