@@ -93,6 +93,7 @@ _SIGS = {
     "emd_snap_ncoeff": ([_P, _IP], _I),
     "emd_thermo_mv2": ([_P, _DP], _I),
     "emd_timing_enable": ([_P, _I], _I),
+    "emd_timing_only": ([_P, C.c_char_p], _I),
     "emd_timing_reset": ([_P], _I),
     "emd_timing_report": ([_P, C.c_char_p, _I], _I),
     "emd_timing_get": ([_P, C.c_char_p, _DP, _LLP], _I),
@@ -401,6 +402,13 @@ class Context:
 
     def timing(self, on=True):
         self._ok(self.lib.emd_timing_enable(self.h, int(on)), "emd_timing_enable")
+
+    def timing_only(self, kernels=None):
+        """Events only for these kernel names (a list or comma-separated string; None: all)."""
+        if kernels is not None and not isinstance(kernels, str):
+            kernels = ",".join(kernels)
+        arg = kernels.encode() if kernels else None
+        self._ok(self.lib.emd_timing_only(self.h, arg), "emd_timing_only")
 
     def timing_reset(self):
         self._ok(self.lib.emd_timing_reset(self.h), "emd_timing_reset")

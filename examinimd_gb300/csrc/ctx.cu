@@ -13,6 +13,15 @@ namespace emd {
 TimedLaunch::TimedLaunch(Ctx& ctx, const char* name) : c(ctx) {
   if (!c.timer.on) return;
   slot = &c.timer.slots[name];
+  if (!c.timer.only.empty()) {
+    bool timed = false;
+    for (const std::string& k : c.timer.only) timed = timed || k == name;
+    if (!timed) {  // counted, no events
+      slot->n += 1;
+      slot = nullptr;
+      return;
+    }
+  }
   for (cudaEvent_t* e : {&a, &b}) {
     if (!c.timer.pool.empty()) {
       *e = c.timer.pool.back();
@@ -574,6 +583,21 @@ emd_status emd_thermo_mv2(emd_ctx* ctx, double* sum_mv2) {
 emd_status emd_timing_enable(emd_ctx* ctx, int on) {
   EMD_API_BEGIN
   c.timer.on = on != 0;
+  EMD_API_END
+}
+
+emd_status emd_timing_only(emd_ctx* ctx, const char* kernels) {
+  EMD_API_BEGIN
+  c.timer.only.clear();
+  if (kernels) {
+    std::string s(kernels);
+    size_t p = 0;
+    while (p <= s.size()) {
+      const size_t q = std::min(s.find(',', p), s.size());
+      if (q > p) c.timer.only.push_back(s.substr(p, q - p));
+      p = q + 1;
+    }
+  }
   EMD_API_END
 }
 

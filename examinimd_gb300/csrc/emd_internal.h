@@ -101,6 +101,8 @@ struct LaunchTimer {
   std::map<std::string, Slot> slots;
   std::vector<cudaEvent_t> pool;
   bool on = false;
+  // when non-empty, only these kernels get events; the others are counted
+  std::vector<std::string> only;
 };
 
 struct Ctx {

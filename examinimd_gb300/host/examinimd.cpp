@@ -16,20 +16,21 @@
 namespace emdhost {
 
 namespace {
+// ExaMiniMD's four phase timers (examinimd.cpp:192-276) from CUDA events on
+// the context stream.  Consecutive phases share their boundary event:
+// anchor() starts a run of phases, split(b) closes the phase that just ended
+// into bucket b and opens the next one (five events per plain step).
 struct PhaseClock {
   cudaStream_t s;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> marks[4];
-  std::vector<cudaEvent_t> pool;
+  std::vector<cudaEvent_t> used, pool;
+  cudaEvent_t last = nullptr;
   explicit PhaseClock(void* stream) : s((cudaStream_t)stream) {}
   ~PhaseClock() {
-    for (auto& v : marks)
-      for (auto& p : v) {
-        cudaEventDestroy(p.first);
-        cudaEventDestroy(p.second);
-      }
+    for (auto e : used) cudaEventDestroy(e);
     for (auto e : pool) cudaEventDestroy(e);
   }
-  cudaEvent_t ev() {
+  cudaEvent_t rec() {
     cudaEvent_t e;
     if (!pool.empty()) {
       e = pool.back();
@@ -37,30 +38,32 @@ struct PhaseClock {
     } else {
       cudaEventCreate(&e);
     }
-    return e;
-  }
-  cudaEvent_t begin() {
-    cudaEvent_t e = ev();
     cudaEventRecord(e, s);
+    used.push_back(e);
     return e;
   }
-  void end(int bucket, cudaEvent_t a) {
-    cudaEvent_t b = ev();
-    cudaEventRecord(b, s);
-    marks[bucket].push_back({a, b});
+  void anchor() { last = rec(); }
+  void split(int bucket) {
+    const cudaEvent_t e = rec();
+    marks[bucket].push_back({last, e});
+    last = e;
   }
-  double collect(int bucket) {
-    double t = 0;
-    for (auto& p : marks[bucket]) {
-      float ms = 0;
-      cudaEventSynchronize(p.second);
-      cudaEventElapsedTime(&ms, p.first, p.second);
-      t += ms * 1e-3;
-      pool.push_back(p.first);
-      pool.push_back(p.second);
+  // seconds per bucket; the events go back to the pool
+  void collect(double out[4]) {
+    for (int b = 0; b < 4; ++b) {
+      double t = 0;
+      for (auto& p : marks[b]) {
+        float ms = 0;
+        cudaEventSynchronize(p.second);
+        cudaEventElapsedTime(&ms, p.first, p.second);
+        t += ms * 1e-3;
+      }
+      marks[b].clear();
+      out[b] = t;
     }
-    marks[bucket].clear();
-    return t;
+    pool.insert(pool.end(), used.begin(), used.end());
+    used.clear();
+    last = nullptr;
   }
 };
 enum { B_FORCE = 0, B_NEIGH = 1, B_COMM = 2, B_OTHER = 3 };
@@ -187,48 +190,49 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
   for (int step = step_done + 1; step <= step_done + nsteps; step++) {
     const bool rebuild = step % input->comm_exchange_rate == 0 && step > 0;
     if (host) check(emd_system_update(ctx, 0, system->N_local, hx, hv, hf), ctx, "emd_system_update");
-    cudaEvent_t e = clk.begin();
+    clk.anchor();
     integrator->initial_integrate();
-    clk.end(B_OTHER, e);
-    if (host && !rebuild) check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
-
-    if (rebuild) {
-      e = clk.begin();
-      comm->exchange();
-      clk.end(B_COMM, e);
-      e = clk.begin();
-      binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, false, true);
-      clk.end(B_OTHER, e);
-      e = clk.begin();
-      comm->exchange_halo();
-      clk.end(B_COMM, e);
-      e = clk.begin();
-      binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, true, false);
-      neighbor->create_neigh_list(system, binning, force->half_neigh, false);
-      clk.end(B_NEIGH, e);
-      if (host) check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
-    } else {
-      e = clk.begin();
-      comm->update_halo();
-      clk.end(B_COMM, e);
+    clk.split(B_OTHER);
+    if (host && !rebuild) {
+      check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
+      clk.anchor();
     }
 
-    e = clk.begin();
+    if (rebuild) {
+      comm->exchange();
+      clk.split(B_COMM);
+      binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, false, true);
+      clk.split(B_OTHER);
+      comm->exchange_halo();
+      clk.split(B_COMM);
+      binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, true, false);
+      neighbor->create_neigh_list(system, binning, force->half_neigh, false);
+      clk.split(B_NEIGH);
+      if (host) {
+        check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
+        clk.anchor();
+      }
+    } else {
+      comm->update_halo();
+      clk.split(B_COMM);
+    }
+
     check(emd_zero_forces(system->ctx), system->ctx, "emd_zero_forces");
     if (input->thermo_rate > 0 && step % input->thermo_rate == 0) force->request_energy();
     force->compute(system, binning, neighbor);
-    clk.end(B_FORCE, e);
+    clk.split(B_FORCE);
 
     if (input->comm_newton) {
-      e = clk.begin();
       comm->update_force();
-      clk.end(B_COMM, e);
+      clk.split(B_COMM);
     }
 
-    if (host) check(emd_system_download(ctx, 2, hf), ctx, "emd_system_download");
-    e = clk.begin();
+    if (host) {
+      check(emd_system_download(ctx, 2, hf), ctx, "emd_system_download");
+      clk.anchor();
+    }
     integrator->final_integrate();
-    clk.end(B_OTHER, e);
+    clk.split(B_OTHER);
     if (host) {
       check(emd_system_download(ctx, 1, hv), ctx, "emd_system_download");
       check(emd_system_download_wait(ctx), ctx, "emd_system_download_wait");
@@ -247,8 +251,9 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
   const double time = wall() - t0;
   step_done += nsteps;
   time_total += time;
-  const double tf = clk.collect(B_FORCE), tn = clk.collect(B_NEIGH), tc = clk.collect(B_COMM),
-               to = clk.collect(B_OTHER);
+  double tb[4];
+  clk.collect(tb);
+  const double tf = tb[B_FORCE], tn = tb[B_NEIGH], tc = tb[B_COMM], to = tb[B_OTHER];
   time_force += tf;
   time_neigh += tn;
   time_comm += tc;

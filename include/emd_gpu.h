@@ -264,6 +264,10 @@ emd_status emd_thermo_mv2(emd_ctx* ctx, double* sum_mv2);
  * When enabled, every kernel launch of the context is bracketed by CUDA
  * events on the context stream; totals are per kernel name. */
 emd_status emd_timing_enable(emd_ctx* ctx, int on);
+/* Restricts the events to the kernels named in a comma-separated list (NULL
+ * or "" restores all); launches of the other kernels are still counted.  Each
+ * bracketed launch costs two events on the stream. */
+emd_status emd_timing_only(emd_ctx* ctx, const char* kernels);
 emd_status emd_timing_reset(emd_ctx* ctx);
 /* Writes "name ms launches\n" lines into buf (truncated to len). */
 emd_status emd_timing_report(emd_ctx* ctx, char* buf, int len);
