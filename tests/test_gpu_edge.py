@@ -81,3 +81,33 @@ def test_full_size_net_force_and_mixed_error():
     err = np.linalg.norm(forces[1] - forces[0], axis=1)
     scale = np.sqrt(np.mean(np.sum(forces[0] ** 2, axis=1)))
     assert np.sqrt(np.mean(err ** 2)) / scale <= 1e-5
+
+
+def test_kernel_timing_restricted_to_named_kernels():
+    """emd_timing_only: events on the named kernels only, every launch counted;
+    the results do not depend on the timing mode."""
+    setup = mdloop.LJSetup(5)
+    state = mdloop.make_lattice(setup)
+    runs = []
+    for only in (None, "lj_full_fp64"):
+        c = _ctx()
+        mdloop.init(c, setup, state)
+        c.timing(True)
+        c.timing_only(only)
+        c.timing_reset()
+        for s in range(1, 22):
+            mdloop.step(c, setup, s)
+        rep = c.timing_report()
+        c.timing(False)
+        runs.append((rep, c.get(0, c.info()[0])))
+        c.close()
+    full, part = runs[0][0], runs[1][0]
+    assert set(full) == set(part)
+    for k in full:
+        assert full[k][1] == part[k][1], k  # the same launches counted
+        if k == "lj_full_fp64":
+            assert part[k][0] > 0.0
+        else:
+            assert part[k][0] == 0.0 and full[k][0] > 0.0, k
+    for k in ("x", "v", "f"):
+        np.testing.assert_array_equal(runs[0][1][k], runs[1][1][k])
