@@ -422,7 +422,8 @@ def run_gpu_arm(a, ws, rank, local):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     # every step: x, v, f uploaded from the pinned host arrays, one ExaMiniMD
-    # step, x, v, f read back into them (x's read-back overlaps the force)
+    # step, x, v, f read back into them (x's read-back overlaps the force; each
+    # field's upload for the next step follows its read-back)
     md.run_host(e2e_steps, hx, hv, hf)
     ctx.synchronize()
     t_e2e = reduce_max(dist, time.perf_counter() - t0)
@@ -430,7 +431,8 @@ def run_gpu_arm(a, ws, rank, local):
     e2e = {"value": ws * N * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": int(nl * 72),
            "d2h_bytes_per_step": int(nl * 72), "steps": e2e_steps,
            "path": "emd_md_run_host: per step x,v,f pinned H2D, one ExaMiniMD step, x,v,f D2H (x's read-back "
-                   "overlapping the force, f's the final integration)"}
+                   "overlapping the force, f's the final integration; each H2D of the next step queued behind "
+                   "the same field's D2H, so the two directions overlap)"}
     T, pe, ke = md.thermo(recompute=True)
 
     extra = {}

@@ -50,6 +50,8 @@ _SIGS = {
     "emd_system_info": ([_P, _IP, _IP, _IP], _I),
     "emd_system_download": ([_P, _I, _DP], _I),
     "emd_system_download_wait": ([_P], _I),
+    "emd_system_stage": ([_P, _I, _DP], _I),
+    "emd_system_commit": ([_P], _I),
     "emd_zero_forces": ([_P], _I),
     "emd_nve_initial": ([_P], _I),
     "emd_nve_final": ([_P], _I),
@@ -238,6 +240,18 @@ class Context:
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x, v, f)]
         n = next((a.shape[0] for a in arrs if a is not None), 0)
         self._ok(self.lib.emd_system_update(self.h, first, n, *[_dp(a) for a in arrs]), "emd_system_update")
+
+    def stage(self, field, arr):
+        """emd_system_stage: queues the upload of x (0), v (1) or f (2) of the
+        owned particles from ``arr`` (N_local x 3 float64, C order, kept alive
+        and unwritten until a later synchronisation); applied by commit()."""
+        if not (isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.flags.c_contiguous):
+            raise TypeError("stage: a C-contiguous float64 array is required")
+        self._ok(self.lib.emd_system_stage(self.h, field, _dp(arr)), "emd_system_stage")
+
+    def commit(self):
+        """emd_system_commit: moves every staged field into place."""
+        self._ok(self.lib.emd_system_commit(self.h), "emd_system_commit")
 
     def zero_forces(self):
         self._ok(self.lib.emd_zero_forces(self.h), "emd_zero_forces")

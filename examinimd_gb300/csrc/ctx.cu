@@ -337,6 +337,7 @@ void emd_destroy(emd_ctx* ctx) {
   cudaSetDevice(c.device);
   if (c.stream) cudaStreamSynchronize(c.stream);
   if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
+  if (c.up_stream) cudaStreamSynchronize(c.up_stream);
   free_snap(c);
   for (auto* b : {&c.v, &c.f, &c.q, &c.mass_d, &c.stage_d, &c.stage_dl, &c.lj_params, &c.red, &c.red2, &c.dtfm_d,
                   &c.lj_intensity, &c.lj_pe_part})
@@ -345,6 +346,7 @@ void emd_destroy(emd_ctx* ctx) {
                   &c.bincount, &c.binoffsets, &c.permute, &c.binof, &c.bin_cursor, &c.perm_tmp, &c.num_neighs,
                   &c.neigh_offsets, &c.neighs, &c.resize_flag, &c.abin})
     b->release();
+  for (auto& b : c.stage_up) b.release();
   c.x4.release();
   c.stage_x4.release();
   c.xl.release();
@@ -368,8 +370,11 @@ void emd_destroy(emd_ctx* ctx) {
   if (c.h_scalar) cudaFreeHost(c.h_scalar);
   if (c.h_ll) cudaFreeHost(c.h_ll);
   if (c.h_int) cudaFreeHost(c.h_int);
-  if (c.copy_after) cudaEventDestroy(c.copy_after);
+  for (auto e : {c.copy_after, c.up_free, c.dl_done[0], c.dl_done[1], c.dl_done[2], c.up_done[0], c.up_done[1],
+                 c.up_done[2]})
+    if (e) cudaEventDestroy(e);
   if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
+  if (c.up_stream) cudaStreamDestroy(c.up_stream);
   if (c.stream) cudaStreamDestroy(c.stream);
   delete ctx;
 }
@@ -513,8 +518,45 @@ emd_status emd_system_get(emd_ctx* ctx, int first, int count, double* x, double*
   EMD_API_END
 }
 
+// The read-back and staged-upload streams with their events, made on first
+// use.  Waiting on an event that was never recorded is a no-op, so every wait
+// below is issued unconditionally.
+static void ensure_copy_streams(Ctx& c) {
+  if (c.copy_stream) return;
+  EMD_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+  EMD_CUDA(cudaStreamCreateWithFlags(&c.up_stream, cudaStreamNonBlocking));
+  EMD_CUDA(cudaEventCreateWithFlags(&c.copy_after, cudaEventDisableTiming));
+  EMD_CUDA(cudaEventCreateWithFlags(&c.up_free, cudaEventDisableTiming));
+  for (int k = 0; k < 3; k++) {
+    EMD_CUDA(cudaEventCreateWithFlags(&c.dl_done[k], cudaEventDisableTiming));
+    EMD_CUDA(cudaEventCreateWithFlags(&c.up_done[k], cudaEventDisableTiming));
+  }
+}
+
+// Staged fields of the owned atoms moved into place: x packed into x4 with
+// the type kept, v and f copied as flat arrays (thread t moves elements t,
+// t + n, t + 2n, so every access is coalesced).  A null source skips its field.
+static __global__ void k_commit_staged(const double* __restrict__ sx, const double* __restrict__ sv,
+                                       const double* __restrict__ sf, double4_32a* __restrict__ x4,
+                                       double* __restrict__ v, double* __restrict__ f, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (sx) {
+    const double4_32a o = x4[i];
+    x4[i] = make_double4_32a(sx[3 * i], sx[3 * i + 1], sx[3 * i + 2], o.w);
+  }
+  const size_t n1 = size_t(n);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const size_t e = size_t(i) + k * n1;
+    if (sv) v[e] = sv[e];
+    if (sf) f[e] = sf[e];
+  }
+}
+
 // Read-back of x, v or f of the owned atoms on the copy stream, ordered after
-// everything issued so far on the context's stream: the copy overlaps the
+// everything issued so far on the context's stream (and after a staged
+// upload still reading the same field's host array): the copy overlaps the
 // work issued after it.
 emd_status emd_system_download(emd_ctx* ctx, int field, double* host) {
   EMD_API_BEGIN
@@ -524,12 +566,10 @@ emd_status emd_system_download(emd_ctx* ctx, int field, double* host) {
   if (n == 0) return EMD_OK;
   if (field == 1) materialize_kick(c);
   if (field == 2) materialize_zero(c, true, false);
-  if (!c.copy_stream) {
-    EMD_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
-    EMD_CUDA(cudaEventCreateWithFlags(&c.copy_after, cudaEventDisableTiming));
-  }
+  ensure_copy_streams(c);
   EMD_CUDA(cudaEventRecord(c.copy_after, c.stream));
   EMD_CUDA(cudaStreamWaitEvent(c.copy_stream, c.copy_after, 0));
+  EMD_CUDA(cudaStreamWaitEvent(c.copy_stream, c.up_done[field], 0));
   const size_t bytes = sizeof(double) * 3 * size_t(n);
   if (field == 0) {
     c.stage_dl.reserve(3 * size_t(n), c.stream);
@@ -539,6 +579,55 @@ emd_status emd_system_download(emd_ctx* ctx, int field, double* host) {
   } else {
     EMD_CUDA(cudaMemcpyAsync(host, field == 1 ? c.v.p : c.f.p, bytes, cudaMemcpyDeviceToHost, c.copy_stream));
   }
+  EMD_CUDA(cudaEventRecord(c.dl_done[field], c.copy_stream));
+  EMD_API_END
+}
+
+emd_status emd_system_stage(emd_ctx* ctx, int field, const double* host) {
+  EMD_API_BEGIN
+  require(field >= 0 && field <= 2, EMD_ERR_ARG, "emd_system_stage: field must be 0 (x), 1 (v) or 2 (f)");
+  const int n = c.N_local;
+  require(host != nullptr || n == 0, EMD_ERR_ARG, "emd_system_stage: null host array");
+  require(c.staged_mask == 0 || c.staged_n == n, EMD_ERR_ARG,
+          "emd_system_stage: the owned count changed since the fields staged before");
+  c.staged_mask |= 1 << field;
+  c.staged_n = n;
+  if (n == 0) return EMD_OK;
+  ensure_copy_streams(c);
+  c.stage_up[field].reserve(3 * size_t(n), c.up_stream);
+  EMD_CUDA(cudaStreamWaitEvent(c.up_stream, c.dl_done[field], 0));
+  EMD_CUDA(cudaStreamWaitEvent(c.up_stream, c.up_free, 0));
+  EMD_CUDA(cudaMemcpyAsync(c.stage_up[field].p, host, sizeof(double) * 3 * size_t(n), cudaMemcpyHostToDevice,
+                           c.up_stream));
+  EMD_CUDA(cudaEventRecord(c.up_done[field], c.up_stream));
+  EMD_API_END
+}
+
+emd_status emd_system_commit(emd_ctx* ctx) {
+  EMD_API_BEGIN
+  const int mask = c.staged_mask;
+  c.staged_mask = 0;
+  if (!mask) return EMD_OK;
+  require(c.staged_n == c.N_local, EMD_ERR_ARG, "emd_system_commit: the owned count changed after the fields were staged");
+  const int n = c.N_local;
+  if (n == 0) return EMD_OK;
+  for (int k = 0; k < 3; k++)
+    if (mask >> k & 1) EMD_CUDA(cudaStreamWaitEvent(c.stream, c.up_done[k], 0));
+  // the bookkeeping of emd_system_update for the same fields
+  materialize_kick(c);
+  if (mask & 4) materialize_zero(c, true, false);
+  if (mask & 1) {
+    c.x_version++;
+    c.xl_ok &= ~1;
+  }
+  {
+    TimedLaunch t(c, "system_commit");
+    k_commit_staged<<<blocks_for(n, 256), 256, 0, c.stream>>>(
+        mask & 1 ? c.stage_up[0].p : nullptr, mask & 2 ? c.stage_up[1].p : nullptr,
+        mask & 4 ? c.stage_up[2].p : nullptr, c.x4.p, c.v.p, c.f.p, n);
+    EMD_CHECK_LAUNCH();
+  }
+  EMD_CUDA(cudaEventRecord(c.up_free, c.stream));
   EMD_API_END
 }
 

@@ -128,7 +128,16 @@ struct Ctx {
   // it waits on, and its own x staging
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_after = nullptr;
+  cudaEvent_t dl_done[3] = {nullptr, nullptr, nullptr};  // last download of x, v, f on the copy stream
   DevBuf<double> stage_dl;
+  // staged uploads (emd_system_stage / emd_system_commit): their own stream,
+  // a staging buffer and a completion event per field, and the point on the
+  // context's stream after the last commit read the staging buffers
+  cudaStream_t up_stream = nullptr;
+  cudaEvent_t up_done[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t up_free = nullptr;
+  DevBuf<double> stage_up[3];
+  int staged_mask = 0, staged_n = 0;
   DevBuf<int> stage_i;
   DevBuf<double4_32a> stage_x4;
 

@@ -176,10 +176,14 @@ void ExaMiniMD::thermo(int step, bool print, double elapsed, double rate) {
 void ExaMiniMD::run(int nsteps) { run_host(nsteps, nullptr, nullptr, nullptr); }
 
 // The step loop of ExaMiniMD::run (examinimd.cpp:192-276).  With host arrays
-// (hx non-null) every step first uploads x, v, f of the owned particles and
-// reads them back as soon as each is final: x after the initial integration
-// (after the rebuild's re-sort on rebuild steps), overlapping the force; f
-// after the force, overlapping the final integration; v last.
+// (hx non-null) every step uploads x, v, f of the owned particles from them
+// and reads them back into them as soon as each is final: x after the initial
+// integration (after the rebuild's re-sort on rebuild steps), overlapping the
+// force; f after the force, overlapping the final integration; v last.  The
+// first step's upload is a plain update; every later step's upload of a field
+// is staged as soon as the previous step's read-back of that field has
+// landed in the host array, so uploads and read-backs run in both directions
+// of the host link at once, and the step commits the staged fields first.
 void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
   emd_ctx* ctx = system->ctx;
   const bool host = hx != nullptr;
@@ -187,14 +191,21 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
   PhaseClock clk(emd_stream(system->ctx));
   const double t0 = wall();
   double last_time = 0.0;
-  for (int step = step_done + 1; step <= step_done + nsteps; step++) {
+  const int first_step = step_done + 1, last_step = step_done + nsteps;
+  // read-back of one field, and the next step's upload of it behind it
+  auto read_back = [&](int field, double* h, int step) {
+    check(emd_system_download(ctx, field, h), ctx, "emd_system_download");
+    if (step < last_step) check(emd_system_stage(ctx, field, h), ctx, "emd_system_stage");
+  };
+  for (int step = first_step; step <= last_step; step++) {
     const bool rebuild = step % input->comm_exchange_rate == 0 && step > 0;
-    if (host) check(emd_system_update(ctx, 0, system->N_local, hx, hv, hf), ctx, "emd_system_update");
+    if (host && step == first_step) check(emd_system_update(ctx, 0, system->N_local, hx, hv, hf), ctx, "emd_system_update");
+    if (host && step > first_step) check(emd_system_commit(ctx), ctx, "emd_system_commit");
     clk.anchor();
     integrator->initial_integrate();
     clk.split(B_OTHER);
     if (host && !rebuild) {
-      check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
+      read_back(0, hx, step);
       clk.anchor();
     }
 
@@ -209,7 +220,7 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
       neighbor->create_neigh_list(system, binning, force->half_neigh, false);
       clk.split(B_NEIGH);
       if (host) {
-        check(emd_system_download(ctx, 0, hx), ctx, "emd_system_download");
+        read_back(0, hx, step);
         clk.anchor();
       }
     } else {
@@ -228,14 +239,14 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
     }
 
     if (host) {
-      check(emd_system_download(ctx, 2, hf), ctx, "emd_system_download");
+      read_back(2, hf, step);
       clk.anchor();
     }
     integrator->final_integrate();
     clk.split(B_OTHER);
     if (host) {
-      check(emd_system_download(ctx, 1, hv), ctx, "emd_system_download");
-      check(emd_system_download_wait(ctx), ctx, "emd_system_download_wait");
+      read_back(1, hv, step);
+      clk.anchor();
     }
 
     if (input->thermo_rate > 0 && step % input->thermo_rate == 0) {
@@ -247,6 +258,7 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
     if (input->dumpbinaryflag) dump_binary(step);
     if (input->correctnessflag) check_correctness(step);
   }
+  if (host) check(emd_system_download_wait(ctx), ctx, "emd_system_download_wait");
   check(emd_synchronize(system->ctx), system->ctx, "emd_synchronize");
   const double time = wall() - t0;
   step_done += nsteps;

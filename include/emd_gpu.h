@@ -93,6 +93,22 @@ emd_status emd_system_info(emd_ctx* ctx, int* n_local, int* n_ghost, int* n_max)
  * callers that keep the particle state in host memory (emd_md_run_host). */
 emd_status emd_system_download(emd_ctx* ctx, int field, double* host);
 emd_status emd_system_download_wait(emd_ctx* ctx);
+/* Staged upload of one field of the owned particles, N_local x 3 doubles
+ * (field 0 = x, 1 = v, 2 = f), into a staging buffer on a third stream.  The
+ * copy starts once every emd_system_download of the same field issued so far
+ * has landed (it reads what that download wrote) and the last commit has
+ * consumed the staging buffer; nothing on the context's stream waits for it.
+ * A later download of the same field waits for the copy, so the host array is
+ * not overwritten while it is read.  Arrays of different fields must not
+ * overlap.  emd_system_commit makes the context's stream wait for every
+ * staged field and moves them into place exactly as emd_system_update(0,
+ * N_local, ...) would (x keeps the types); N_local must not change in
+ * between.  The caller must not write a staged host array before a later
+ * synchronisation (emd_synchronize, or a download_wait after a download of
+ * that field).  No reference counterpart: emd_md_run_host uses the pair to
+ * upload the next step's fields while this step's read-backs are running. */
+emd_status emd_system_stage(emd_ctx* ctx, int field, const double* host);
+emd_status emd_system_commit(emd_ctx* ctx);
 /* Kokkos::deep_copy(system->f, 0.0) over all N_max rows (examinimd.cpp:232). */
 emd_status emd_zero_forces(emd_ctx* ctx);
 

@@ -14,8 +14,24 @@ from tests.golden.decks import CASES, write_case
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_run_host_equals_update_run_get(precision, tmp_path):
+def _host_arrays(src, pinned):
+    """x, v, f of ``src`` in new host arrays: pageable numpy arrays, or
+    page-locked ones (the staged uploads and read-backs then overlap for
+    real instead of each copy waiting on the host)."""
+    out = []
+    for k in ("x", "v", "f"):
+        if pinned:
+            import torch
+            a = torch.empty(src[k].shape, dtype=torch.float64, pin_memory=True).numpy()
+            a[...] = src[k]
+        else:
+            a = np.ascontiguousarray(src[k])
+        out.append(a)
+    return out
+
+
+@pytest.mark.parametrize("precision,pinned", [("fp64", False), ("mixed", False), ("fp64", True), ("mixed", True)])
+def test_run_host_equals_update_run_get(precision, pinned, tmp_path):
     from examinimd_gb300 import MD
     case = dict(CASES["lj_fcc6_full_csr"])
     deck, args = write_case(case, str(tmp_path))
@@ -24,14 +40,13 @@ def test_run_host_equals_update_run_get(precision, tmp_path):
     n = a.info()["N_local"]
     ref = a.ctx.get(0, n)
     hx, hv, hf = (np.ascontiguousarray(ref[k]) for k in ("x", "v", "f"))
-    steps = 25  # the rebuild at step 20 re-sorts the atoms in between
+    steps = 45  # the rebuilds at steps 20 and 40 re-sort the atoms in between
     for _ in range(steps):
         a.ctx.update(0, hx, hv, hf)
         a.run(1)
         cur = a.ctx.get(0, n)
         hx, hv, hf = (np.ascontiguousarray(cur[k]) for k in ("x", "v", "f"))
-    st = b.ctx.get(0, n)
-    bx, bv, bf = (np.ascontiguousarray(st[k]) for k in ("x", "v", "f"))
+    bx, bv, bf = _host_arrays(b.ctx.get(0, n), pinned)
     b.run_host(steps, bx, bv, bf)
     for name, p, q in (("x", hx, bx), ("v", hv, bv), ("f", hf, bf)):
         np.testing.assert_array_equal(p, q, err_msg=name)
@@ -50,4 +65,57 @@ def test_run_host_rejects_wrong_arrays(tmp_path):
     n = md.info()["N_local"]
     with pytest.raises(EmdError):
         md.run_host(1, np.zeros((n, 3), np.float32), np.zeros((n, 3)), np.zeros((n, 3)))
+    md.close()
+
+
+def test_stage_commit_equals_update(tmp_path):
+    """emd_system_stage + emd_system_commit leave the same state as
+    emd_system_update with the same arrays; unstaged fields stay as they were."""
+    from examinimd_gb300 import MD
+    deck, args = write_case(dict(CASES["lj_fcc6_full_csr"]), str(tmp_path))
+    a, b = MD(["-il", deck, "--quiet"] + args), MD(["-il", deck, "--quiet"] + args)
+    n = a.info()["N_local"]
+    st = a.ctx.get(0, n)
+    rng = np.random.default_rng(5)
+    x = np.ascontiguousarray(st["x"] + rng.uniform(-0.01, 0.01, (n, 3)))
+    v = np.ascontiguousarray(rng.normal(size=(n, 3)))
+    f = np.ascontiguousarray(rng.normal(size=(n, 3)))
+    a.ctx.update(0, x, v, f)
+    for field, arr in ((0, x), (1, v), (2, f)):
+        b.ctx.stage(field, arr)
+    b.ctx.commit()
+    ga, gb = a.ctx.get(0, n), b.ctx.get(0, n)
+    for k in ("x", "v", "f", "type", "id"):
+        np.testing.assert_array_equal(ga[k], gb[k], err_msg=k)
+    # one field staged: the others are untouched
+    v2 = np.ascontiguousarray(v * 0.5)
+    b.ctx.stage(1, v2)
+    b.ctx.commit()
+    gc = b.ctx.get(0, n)
+    np.testing.assert_array_equal(gc["v"], v2)
+    np.testing.assert_array_equal(gc["x"], gb["x"])
+    np.testing.assert_array_equal(gc["f"], gb["f"])
+    # a commit with nothing staged changes nothing
+    b.ctx.commit()
+    np.testing.assert_array_equal(b.ctx.get(0, n)["v"], v2)
+    # the runs continue identically from the two states
+    a.ctx.update(0, None, v2, None)
+    a.run(3)
+    b.run(3)
+    ga, gb = a.ctx.get(0, n), b.ctx.get(0, n)
+    for k in ("x", "v", "f"):
+        np.testing.assert_array_equal(ga[k], gb[k], err_msg=k)
+    a.close()
+    b.close()
+
+
+def test_stage_rejects_bad_arguments(tmp_path):
+    from examinimd_gb300 import MD, EmdError
+    deck, args = write_case(dict(CASES["lj_fcc6_full_csr"]), str(tmp_path))
+    md = MD(["-il", deck, "--quiet"] + args)
+    n = md.info()["N_local"]
+    with pytest.raises(EmdError):
+        md.ctx.stage(3, np.zeros((n, 3)))
+    with pytest.raises(TypeError):
+        md.ctx.stage(0, np.zeros((n, 3), np.float32))
     md.close()
