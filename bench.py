@@ -432,7 +432,7 @@ def run_gpu_arm(a, ws, rank, local):
            "d2h_bytes_per_step": int(nl * 72), "steps": e2e_steps,
            "path": "emd_md_run_host: per step x,v,f pinned H2D, one ExaMiniMD step, x,v,f D2H (x's read-back "
                    "overlapping the force, f's the final integration; each H2D of the next step queued behind "
-                   "the same field's D2H, so the two directions overlap)"}
+                   "the same field's D2H, so the two directions overlap; the step starts in two row chunks)"}
     T, pe, ke = md.thermo(recompute=True)
 
     extra = {}

@@ -52,9 +52,13 @@ _SIGS = {
     "emd_system_download_wait": ([_P], _I),
     "emd_system_stage": ([_P, _I, _DP], _I),
     "emd_system_commit": ([_P], _I),
+    "emd_system_download_range": ([_P, _I, _DP, _I, _I], _I),
+    "emd_system_stage_range": ([_P, _I, _DP, _I, _I], _I),
+    "emd_system_commit_range": ([_P, _I, _I], _I),
     "emd_zero_forces": ([_P], _I),
     "emd_nve_initial": ([_P], _I),
     "emd_nve_final": ([_P], _I),
+    "emd_nve_initial_range": ([_P, _I, _I], _I),
     "emd_comm_init": ([_P, _D], _I),
     "emd_comm_exchange": ([_P], _I),
     "emd_comm_exchange_halo": ([_P, _IP], _I),
@@ -253,6 +257,20 @@ class Context:
         """emd_system_commit: moves every staged field into place."""
         self._ok(self.lib.emd_system_commit(self.h), "emd_system_commit")
 
+    def stage_range(self, field, arr, first):
+        """emd_system_stage_range: queues the upload of rows [first, first +
+        len(arr)) of x (0), v (1) or f (2) from ``arr`` (kept alive and
+        unwritten until a later synchronisation)."""
+        if not (isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.flags.c_contiguous):
+            raise TypeError("stage_range: a C-contiguous float64 array is required")
+        self._ok(self.lib.emd_system_stage_range(self.h, field, _dp(arr), first, arr.shape[0]),
+                 "emd_system_stage_range")
+
+    def commit_range(self, first, count):
+        """emd_system_commit_range: moves the rows staged inside [first,
+        first + count) into place."""
+        self._ok(self.lib.emd_system_commit_range(self.h, first, count), "emd_system_commit_range")
+
     def zero_forces(self):
         self._ok(self.lib.emd_zero_forces(self.h), "emd_zero_forces")
 
@@ -262,6 +280,9 @@ class Context:
 
     def nve_final(self):
         self._ok(self.lib.emd_nve_final(self.h), "emd_nve_final")
+
+    def nve_initial_range(self, first, count):
+        self._ok(self.lib.emd_nve_initial_range(self.h, first, count), "emd_nve_initial_range")
 
     def comm_init(self, depth):
         self._ok(self.lib.emd_comm_init(self.h, depth), "emd_comm_init")

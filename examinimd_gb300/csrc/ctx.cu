@@ -370,9 +370,10 @@ void emd_destroy(emd_ctx* ctx) {
   if (c.h_scalar) cudaFreeHost(c.h_scalar);
   if (c.h_ll) cudaFreeHost(c.h_ll);
   if (c.h_int) cudaFreeHost(c.h_int);
-  for (auto e : {c.copy_after, c.up_free, c.dl_done[0], c.dl_done[1], c.dl_done[2], c.up_done[0], c.up_done[1],
-                 c.up_done[2]})
+  for (auto e : {c.copy_after, c.up_free, c.dl_done[0], c.dl_done[1], c.dl_done[2]})
     if (e) cudaEventDestroy(e);
+  for (const auto& r : c.staged) cudaEventDestroy(r.done);
+  for (auto e : c.staged_pool) cudaEventDestroy(e);
   if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
   if (c.up_stream) cudaStreamDestroy(c.up_stream);
   if (c.stream) cudaStreamDestroy(c.stream);
@@ -527,15 +528,30 @@ static void ensure_copy_streams(Ctx& c) {
   EMD_CUDA(cudaStreamCreateWithFlags(&c.up_stream, cudaStreamNonBlocking));
   EMD_CUDA(cudaEventCreateWithFlags(&c.copy_after, cudaEventDisableTiming));
   EMD_CUDA(cudaEventCreateWithFlags(&c.up_free, cudaEventDisableTiming));
-  for (int k = 0; k < 3; k++) {
-    EMD_CUDA(cudaEventCreateWithFlags(&c.dl_done[k], cudaEventDisableTiming));
-    EMD_CUDA(cudaEventCreateWithFlags(&c.up_done[k], cudaEventDisableTiming));
-  }
+  for (int k = 0; k < 3; k++) EMD_CUDA(cudaEventCreateWithFlags(&c.dl_done[k], cudaEventDisableTiming));
 }
 
-// Staged fields of the owned atoms moved into place: x packed into x4 with
-// the type kept, v and f copied as flat arrays (thread t moves elements t,
-// t + n, t + 2n, so every access is coalesced).  A null source skips its field.
+static void require_field_range(const Ctx& c, int field, int first, int count, const void* host, const char* who) {
+  require(field >= 0 && field <= 2, EMD_ERR_ARG, who);
+  require(first >= 0 && count >= 0 && first <= c.N_local - count, EMD_ERR_ARG, who);
+  require(host != nullptr || count == 0, EMD_ERR_ARG, who);
+}
+
+static bool overlaps(int a0, int an, int b0, int bn) { return a0 < b0 + bn && b0 < a0 + an; }
+
+// Pending staged ranges made before N_local changed are dropped (their rows
+// no longer name the same particles) and the call fails.
+static void require_staged_count(Ctx& c, const char* msg) {
+  if (c.staged.empty() || c.staged_n == c.N_local) return;
+  for (const auto& r : c.staged) c.staged_pool.push_back(r.done);
+  c.staged.clear();
+  throw Error(EMD_ERR_ARG, msg);
+}
+
+// Staged rows of the owned atoms moved into place: x packed into x4 with the
+// type kept, v and f copied as flat arrays (thread t moves elements t, t + n,
+// t + 2n of the rows, so every access is coalesced).  The pointers are at the
+// range's first row; a null source skips its field.
 static __global__ void k_commit_staged(const double* __restrict__ sx, const double* __restrict__ sv,
                                        const double* __restrict__ sf, double4_32a* __restrict__ x4,
                                        double* __restrict__ v, double* __restrict__ f, int n) {
@@ -554,81 +570,119 @@ static __global__ void k_commit_staged(const double* __restrict__ sx, const doub
   }
 }
 
-// Read-back of x, v or f of the owned atoms on the copy stream, ordered after
-// everything issued so far on the context's stream (and after a staged
-// upload still reading the same field's host array): the copy overlaps the
-// work issued after it.
-emd_status emd_system_download(emd_ctx* ctx, int field, double* host) {
+// Read-back of rows [first, first + count) of x, v or f on the copy stream,
+// ordered after everything issued so far on the context's stream and after
+// the staged uploads of the same field that overlap the rows (they may still
+// be reading the host array): the copy overlaps the work issued after it.
+emd_status emd_system_download_range(emd_ctx* ctx, int field, double* host, int first, int count) {
   EMD_API_BEGIN
-  require(field >= 0 && field <= 2, EMD_ERR_ARG, "emd_system_download: field must be 0 (x), 1 (v) or 2 (f)");
-  const int n = c.N_local;
-  require(host != nullptr || n == 0, EMD_ERR_ARG, "emd_system_download: null host array");
-  if (n == 0) return EMD_OK;
+  require_field_range(c, field, first, count, host,
+                      "emd_system_download_range: field must be 0 (x), 1 (v) or 2 (f), rows within the owned "
+                      "particles, host non-null");
+  if (count == 0) return EMD_OK;
   if (field == 1) materialize_kick(c);
   if (field == 2) materialize_zero(c, true, false);
   ensure_copy_streams(c);
   EMD_CUDA(cudaEventRecord(c.copy_after, c.stream));
   EMD_CUDA(cudaStreamWaitEvent(c.copy_stream, c.copy_after, 0));
-  EMD_CUDA(cudaStreamWaitEvent(c.copy_stream, c.up_done[field], 0));
-  const size_t bytes = sizeof(double) * 3 * size_t(n);
+  for (const auto& r : c.staged)
+    if (r.field == field && overlaps(r.first, r.count, first, count))
+      EMD_CUDA(cudaStreamWaitEvent(c.copy_stream, r.done, 0));
+  const size_t bytes = sizeof(double) * 3 * size_t(count);
   if (field == 0) {
-    c.stage_dl.reserve(3 * size_t(n), c.stream);
-    k_unpack_x4<<<blocks_for(n, 256), 256, 0, c.copy_stream>>>(c.x4.p, c.stage_dl.p, n);
+    c.stage_dl.reserve(3 * size_t(c.N_local), c.stream);
+    double* dst = c.stage_dl.p + 3 * size_t(first);
+    k_unpack_x4<<<blocks_for(count, 256), 256, 0, c.copy_stream>>>(c.x4.p + first, dst, count);
     EMD_CHECK_LAUNCH();
-    EMD_CUDA(cudaMemcpyAsync(host, c.stage_dl.p, bytes, cudaMemcpyDeviceToHost, c.copy_stream));
+    EMD_CUDA(cudaMemcpyAsync(host, dst, bytes, cudaMemcpyDeviceToHost, c.copy_stream));
   } else {
-    EMD_CUDA(cudaMemcpyAsync(host, field == 1 ? c.v.p : c.f.p, bytes, cudaMemcpyDeviceToHost, c.copy_stream));
+    const double* src = (field == 1 ? c.v.p : c.f.p) + 3 * size_t(first);
+    EMD_CUDA(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, c.copy_stream));
   }
   EMD_CUDA(cudaEventRecord(c.dl_done[field], c.copy_stream));
   EMD_API_END
 }
 
-emd_status emd_system_stage(emd_ctx* ctx, int field, const double* host) {
+emd_status emd_system_download(emd_ctx* ctx, int field, double* host) {
+  return emd_system_download_range(ctx, field, host, 0, ctx ? ctx->c.N_local : 0);
+}
+
+emd_status emd_system_stage_range(emd_ctx* ctx, int field, const double* host, int first, int count) {
   EMD_API_BEGIN
-  require(field >= 0 && field <= 2, EMD_ERR_ARG, "emd_system_stage: field must be 0 (x), 1 (v) or 2 (f)");
-  const int n = c.N_local;
-  require(host != nullptr || n == 0, EMD_ERR_ARG, "emd_system_stage: null host array");
-  require(c.staged_mask == 0 || c.staged_n == n, EMD_ERR_ARG,
-          "emd_system_stage: the owned count changed since the fields staged before");
-  c.staged_mask |= 1 << field;
-  c.staged_n = n;
-  if (n == 0) return EMD_OK;
+  require_field_range(c, field, first, count, host,
+                      "emd_system_stage_range: field must be 0 (x), 1 (v) or 2 (f), rows within the owned "
+                      "particles, host non-null");
+  require_staged_count(c, "emd_system_stage_range: the owned count changed since the pending ranges were staged");
+  if (count == 0) return EMD_OK;
   ensure_copy_streams(c);
-  c.stage_up[field].reserve(3 * size_t(n), c.up_stream);
+  c.stage_up[field].reserve(3 * size_t(c.N_local), c.up_stream, true);
   EMD_CUDA(cudaStreamWaitEvent(c.up_stream, c.dl_done[field], 0));
   EMD_CUDA(cudaStreamWaitEvent(c.up_stream, c.up_free, 0));
-  EMD_CUDA(cudaMemcpyAsync(c.stage_up[field].p, host, sizeof(double) * 3 * size_t(n), cudaMemcpyHostToDevice,
-                           c.up_stream));
-  EMD_CUDA(cudaEventRecord(c.up_done[field], c.up_stream));
+  EMD_CUDA(cudaMemcpyAsync(c.stage_up[field].p + 3 * size_t(first), host, sizeof(double) * 3 * size_t(count),
+                           cudaMemcpyHostToDevice, c.up_stream));
+  cudaEvent_t done = nullptr;
+  if (!c.staged_pool.empty()) {
+    done = c.staged_pool.back();
+    c.staged_pool.pop_back();
+  } else {
+    EMD_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+  }
+  EMD_CUDA(cudaEventRecord(done, c.up_stream));
+  c.staged.push_back({field, first, count, done});
+  c.staged_n = c.N_local;
   EMD_API_END
 }
 
-emd_status emd_system_commit(emd_ctx* ctx) {
+emd_status emd_system_stage(emd_ctx* ctx, int field, const double* host) {
+  return emd_system_stage_range(ctx, field, host, 0, ctx ? ctx->c.N_local : 0);
+}
+
+emd_status emd_system_commit_range(emd_ctx* ctx, int first, int count) {
   EMD_API_BEGIN
-  const int mask = c.staged_mask;
-  c.staged_mask = 0;
-  if (!mask) return EMD_OK;
-  require(c.staged_n == c.N_local, EMD_ERR_ARG, "emd_system_commit: the owned count changed after the fields were staged");
-  const int n = c.N_local;
-  if (n == 0) return EMD_OK;
-  for (int k = 0; k < 3; k++)
-    if (mask >> k & 1) EMD_CUDA(cudaStreamWaitEvent(c.stream, c.up_done[k], 0));
+  require(first >= 0 && count >= 0 && first <= c.N_local - count, EMD_ERR_ARG,
+          "emd_system_commit_range: rows within the owned particles");
+  std::vector<Ctx::Staged> mine, rest;
+  for (const auto& r : c.staged) (overlaps(r.first, r.count, first, count) ? mine : rest).push_back(r);
+  if (mine.empty()) return EMD_OK;
+  require_staged_count(c, "emd_system_commit_range: the owned count changed after the rows were staged");
+  for (const auto& r : mine)
+    require(r.first >= first && r.first + r.count <= first + count, EMD_ERR_ARG,
+            "emd_system_commit_range: a staged range straddles the committed rows");
+  for (const auto& r : mine) EMD_CUDA(cudaStreamWaitEvent(c.stream, r.done, 0));
   // the bookkeeping of emd_system_update for the same fields
+  int mask = 0;
+  for (const auto& r : mine) mask |= 1 << r.field;
   materialize_kick(c);
   if (mask & 4) materialize_zero(c, true, false);
   if (mask & 1) {
     c.x_version++;
     c.xl_ok &= ~1;
   }
-  {
+  // one launch per distinct row range, all its staged fields together (a
+  // range staged twice is moved once: the later copy overwrote the rows)
+  std::vector<std::pair<int, int>> done_ranges;
+  for (const auto& r : mine) {
+    const std::pair<int, int> key(r.first, r.count);
+    if (std::find(done_ranges.begin(), done_ranges.end(), key) != done_ranges.end()) continue;
+    done_ranges.push_back(key);
+    int fm = 0;
+    for (const auto& q : mine)
+      if (q.first == r.first && q.count == r.count) fm |= 1 << q.field;
+    const size_t o = 3 * size_t(r.first);
     TimedLaunch t(c, "system_commit");
-    k_commit_staged<<<blocks_for(n, 256), 256, 0, c.stream>>>(
-        mask & 1 ? c.stage_up[0].p : nullptr, mask & 2 ? c.stage_up[1].p : nullptr,
-        mask & 4 ? c.stage_up[2].p : nullptr, c.x4.p, c.v.p, c.f.p, n);
+    k_commit_staged<<<blocks_for(r.count, 256), 256, 0, c.stream>>>(
+        fm & 1 ? c.stage_up[0].p + o : nullptr, fm & 2 ? c.stage_up[1].p + o : nullptr,
+        fm & 4 ? c.stage_up[2].p + o : nullptr, c.x4.p + r.first, c.v.p + o, c.f.p + o, r.count);
     EMD_CHECK_LAUNCH();
   }
   EMD_CUDA(cudaEventRecord(c.up_free, c.stream));
+  for (const auto& r : mine) c.staged_pool.push_back(r.done);
+  c.staged.swap(rest);
   EMD_API_END
+}
+
+emd_status emd_system_commit(emd_ctx* ctx) {
+  return emd_system_commit_range(ctx, 0, ctx ? ctx->c.N_local : 0);
 }
 
 emd_status emd_system_download_wait(emd_ctx* ctx) {

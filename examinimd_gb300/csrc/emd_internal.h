@@ -130,14 +130,21 @@ struct Ctx {
   cudaEvent_t copy_after = nullptr;
   cudaEvent_t dl_done[3] = {nullptr, nullptr, nullptr};  // last download of x, v, f on the copy stream
   DevBuf<double> stage_dl;
-  // staged uploads (emd_system_stage / emd_system_commit): their own stream,
-  // a staging buffer and a completion event per field, and the point on the
-  // context's stream after the last commit read the staging buffers
+  // staged uploads (emd_system_stage_range / emd_system_commit_range): their
+  // own stream, a staging buffer per field (N_local rows), one record with a
+  // completion event per staged row range not yet committed, spare events,
+  // and the point on the context's stream after the last commit read the
+  // staging buffers
+  struct Staged {
+    int field, first, count;
+    cudaEvent_t done;
+  };
   cudaStream_t up_stream = nullptr;
-  cudaEvent_t up_done[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t up_free = nullptr;
   DevBuf<double> stage_up[3];
-  int staged_mask = 0, staged_n = 0;
+  std::vector<Staged> staged;
+  std::vector<cudaEvent_t> staged_pool;
+  int staged_n = 0;  // N_local when the pending ranges were staged
   DevBuf<int> stage_i;
   DevBuf<double4_32a> stage_x4;
 
@@ -289,7 +296,8 @@ struct BinCentres {
 };
 BinCentres bin_centres(const Ctx& c);
 void lj_mixed_after_build(Ctx& c);
-void nve_initial_mixed(Ctx& c, bool kick_first);
+// rows [first, first + count); count < 0: to N_local
+void nve_initial_mixed(Ctx& c, bool kick_first, int first = 0, int count = -1);
 void nve_final_mixed(Ctx& c);
 
 }  // namespace emd

@@ -110,6 +110,29 @@ emd_status emd_nve_initial(emd_ctx* ctx) {
   EMD_API_END
 }
 
+emd_status emd_nve_initial_range(emd_ctx* ctx, int first, int count) {
+  EMD_API_BEGIN
+  require(first >= 0 && count >= 0 && first <= c.N_local - count, EMD_ERR_ARG,
+          "emd_nve_initial_range: rows within the owned particles");
+  c.x_version++;
+  // a pending final kick, then a pending zero of the forces, each applied to
+  // every row as its own pass first
+  materialize_kick(c);
+  materialize_zero(c, true, false);
+  if (count == 0) return EMD_OK;
+  if (c.lj_ready && c.lj_prec == EMD_PREC_MIXED) {
+    nve_initial_mixed(c, false, first, count);
+    return EMD_OK;
+  }
+  TimedLaunch t(c, "nve_initial");
+  const size_t o = 3 * size_t(first);
+  k_nve_initial<false><<<blocks_for(count, 256), 256, 0, c.stream>>>(c.x4.p + first, c.v.p + o, c.f.p + o,
+                                                                     c.type.p + first, c.dtfm_d.p, c.dt, count);
+  EMD_CHECK_LAUNCH();
+  c.xl_ok &= ~1;
+  EMD_API_END
+}
+
 // The final half kick is recorded, not run: the next emd_nve_initial applies
 // it and its own kick in one pass over v and f, and every other call that
 // reads or writes v or f applies it first.

@@ -67,14 +67,15 @@ __global__ void __launch_bounds__(256) k_pos_remainder(const double4_32a* __rest
 }
 
 // IntegratorNVE::initial_integrate (integrator_nve.cpp:64-73) with FMA, plus
-// the FP32 bin-relative copy of the new position
+// the FP32 bin-relative copy of the new position; rows [first, end)
 template <bool KICK>
 __global__ void __launch_bounds__(256) k_nve_initial_mixed(double4_32a* __restrict__ x4, double* __restrict__ v,
                                                            const double* __restrict__ f, const int* __restrict__ type,
                                                            const double* __restrict__ dtfm_t, double dtv,
-                                                           BinCentres ctr, float4* __restrict__ xl, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+                                                           BinCentres ctr, float4* __restrict__ xl, int first,
+                                                           int end) {
+  const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= end) return;
   const int ti = type[i];
   const double fx = f[3 * i], fy = f[3 * i + 1], fz = f[3 * i + 2];
   double vx = v[3 * i], vy = v[3 * i + 1], vz = v[3 * i + 2];
@@ -314,14 +315,15 @@ bool mixed_xl_active(const Ctx& c) {
   return c.lj_ready && c.lj_prec == EMD_PREC_MIXED && c.neigh_ready && c.neigh_packed;
 }
 
-void nve_initial_mixed(Ctx& c, bool kick_first) {
+void nve_initial_mixed(Ctx& c, bool kick_first, int first, int count) {
+  if (count < 0) count = c.N_local - first;
+  if (count == 0) return;
   const bool live = mixed_xl_active(c);
   TimedLaunch t(c, kick_first ? "nve_final_initial" : "nve_initial");
   auto k = kick_first ? k_nve_initial_mixed<true> : k_nve_initial_mixed<false>;
-  k<<<blocks_for(c.N_local, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p,
-                                                       c.dtfm_d.p + (kick_first ? c.ntypes : 0), c.dt,
-                                                       bin_centres(c), live ? c.xl.p : nullptr,
-                                                       c.N_local);
+  k<<<blocks_for(count, 256), 256, 0, c.stream>>>(c.x4.p, c.v.p, c.f.p, c.type.p,
+                                                   c.dtfm_d.p + (kick_first ? c.ntypes : 0), c.dt, bin_centres(c),
+                                                   live ? c.xl.p : nullptr, first, first + count);
   EMD_CHECK_LAUNCH();
   if (!live) c.xl_ok &= ~1;
 }

@@ -184,6 +184,9 @@ class Integrator {
   explicit Integrator(System* s) : system(s) {}
   virtual ~Integrator() {}
   virtual void initial_integrate() = 0;
+  // initial_integrate on rows [first, first + count) of the owned particles
+  // (the chunked start of a host-resident step)
+  virtual void initial_integrate_range(int first, int count) = 0;
   virtual void final_integrate() = 0;
   virtual const char* name() = 0;
 };
@@ -192,6 +195,7 @@ class IntegratorNVE_GB300 : public Integrator {
  public:
   explicit IntegratorNVE_GB300(System* s) : Integrator(s) {}
   void initial_integrate() override;
+  void initial_integrate_range(int first, int count) override;
   void final_integrate() override;
   const char* name() override { return "IntegratorNVE_GB300"; }
 };

@@ -180,10 +180,12 @@ void ExaMiniMD::run(int nsteps) { run_host(nsteps, nullptr, nullptr, nullptr); }
 // and reads them back into them as soon as each is final: x after the initial
 // integration (after the rebuild's re-sort on rebuild steps), overlapping the
 // force; f after the force, overlapping the final integration; v last.  The
-// first step's upload is a plain update; every later step's upload of a field
-// is staged as soon as the previous step's read-back of that field has
-// landed in the host array, so uploads and read-backs run in both directions
-// of the host link at once, and the step commits the staged fields first.
+// first step's upload is a plain update.  Every later step's upload is staged
+// chunk by chunk, each chunk of a field as soon as the previous step's
+// read-back of that chunk has landed in the host array, so uploads and
+// read-backs use both directions of the host link at once.  The step then
+// starts chunk by chunk too: commit the chunk's staged rows, integrate them,
+// read their x back, while the next chunk's upload of v is still running.
 void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
   emd_ctx* ctx = system->ctx;
   const bool host = hx != nullptr;
@@ -192,22 +194,47 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
   const double t0 = wall();
   double last_time = 0.0;
   const int first_step = step_done + 1, last_step = step_done + nsteps;
-  // read-back of one field, and the next step's upload of it behind it
-  auto read_back = [&](int field, double* h, int step) {
-    check(emd_system_download(ctx, field, h), ctx, "emd_system_download");
-    if (step < last_step) check(emd_system_stage(ctx, field, h), ctx, "emd_system_stage");
+  // Two chunks: measured at LJ-4M, 2 / 4 / 8 / 16 chunks gave 2.43 / 2.51 /
+  // 2.69 / 3.03 ms per step (every chunk adds six host-link copies and two
+  // kernels).  3 chunks, whose edges fell on host addresses aligned to 8
+  // bytes only, gave 2.74, so chunk edges fall on multiples of 512 rows
+  // (12 KiB of host array).
+  constexpr int kChunks = 2;
+  constexpr long long kAlign = 512;
+  // rows [first, first + count) of chunk k of the owned particles
+  auto edge = [&](int k) {
+    const long long n = system->N_local;
+    return k >= kChunks ? n : (n * k / kChunks) / kAlign * kAlign;
+  };
+  auto rows = [&](int k, int& first, int& count) {
+    first = int(edge(k));
+    count = int(edge(k + 1)) - first;
+  };
+  // read-back of chunk k of one field, and the next step's upload of it
+  // behind it
+  auto read_back = [&](int field, double* h, int k, int step) {
+    int first, count;
+    rows(k, first, count);
+    double* hk = h + 3 * size_t(first);
+    check(emd_system_download_range(ctx, field, hk, first, count), ctx, "emd_system_download_range");
+    if (step < last_step) check(emd_system_stage_range(ctx, field, hk, first, count), ctx, "emd_system_stage_range");
   };
   for (int step = first_step; step <= last_step; step++) {
     const bool rebuild = step % input->comm_exchange_rate == 0 && step > 0;
     if (host && step == first_step) check(emd_system_update(ctx, 0, system->N_local, hx, hv, hf), ctx, "emd_system_update");
-    if (host && step > first_step) check(emd_system_commit(ctx), ctx, "emd_system_commit");
     clk.anchor();
-    integrator->initial_integrate();
-    clk.split(B_OTHER);
-    if (host && !rebuild) {
-      read_back(0, hx, step);
-      clk.anchor();
+    if (host) {
+      for (int k = 0; k < kChunks; k++) {
+        int first, count;
+        rows(k, first, count);
+        if (step > first_step) check(emd_system_commit_range(ctx, first, count), ctx, "emd_system_commit_range");
+        integrator->initial_integrate_range(first, count);
+        if (!rebuild) read_back(0, hx, k, step);
+      }
+    } else {
+      integrator->initial_integrate();
     }
+    clk.split(B_OTHER);
 
     if (rebuild) {
       comm->exchange();
@@ -220,7 +247,7 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
       neighbor->create_neigh_list(system, binning, force->half_neigh, false);
       clk.split(B_NEIGH);
       if (host) {
-        read_back(0, hx, step);
+        for (int k = 0; k < kChunks; k++) read_back(0, hx, k, step);
         clk.anchor();
       }
     } else {
@@ -239,13 +266,13 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
     }
 
     if (host) {
-      read_back(2, hf, step);
+      for (int k = 0; k < kChunks; k++) read_back(2, hf, k, step);
       clk.anchor();
     }
     integrator->final_integrate();
     clk.split(B_OTHER);
     if (host) {
-      read_back(1, hv, step);
+      for (int k = 0; k < kChunks; k++) read_back(1, hv, k, step);
       clk.anchor();
     }
 

@@ -223,6 +223,9 @@ void ForceSNAP_GB300::request_energy() {
 
 // ---------------------------------------------------------------- NVE
 void IntegratorNVE_GB300::initial_integrate() { check(emd_nve_initial(system->ctx), system->ctx, "emd_nve_initial"); }
+void IntegratorNVE_GB300::initial_integrate_range(int first, int count) {
+  check(emd_nve_initial_range(system->ctx, first, count), system->ctx, "emd_nve_initial_range");
+}
 void IntegratorNVE_GB300::final_integrate() { check(emd_nve_final(system->ctx), system->ctx, "emd_nve_final"); }
 
 }  // namespace emdhost

@@ -109,6 +109,18 @@ emd_status emd_system_download_wait(emd_ctx* ctx);
  * upload the next step's fields while this step's read-backs are running. */
 emd_status emd_system_stage(emd_ctx* ctx, int field, const double* host);
 emd_status emd_system_commit(emd_ctx* ctx);
+/* The same three on rows [first, first+count) of the owned particles; host
+ * holds those rows (count x 3 doubles).  A download waits only for the
+ * staged ranges of its field that overlap its rows, and a commit only for
+ * the staged ranges inside its rows (one straddling them is an error), so a
+ * caller can split the start of a step into chunks: commit a chunk,
+ * integrate it (emd_nve_initial_range), read its x back, while the next
+ * chunk's upload is still running.  A stage waits for the latest download of
+ * its field, so each chunk's stage belongs right after that chunk's
+ * download.  The whole-array calls above are these over [0, N_local). */
+emd_status emd_system_download_range(emd_ctx* ctx, int field, double* host, int first, int count);
+emd_status emd_system_stage_range(emd_ctx* ctx, int field, const double* host, int first, int count);
+emd_status emd_system_commit_range(emd_ctx* ctx, int first, int count);
 /* Kokkos::deep_copy(system->f, 0.0) over all N_max rows (examinimd.cpp:232). */
 emd_status emd_zero_forces(emd_ctx* ctx);
 
@@ -117,6 +129,11 @@ emd_status emd_zero_forces(emd_ctx* ctx);
  * (integrator_nve.cpp:41-44, 64-83, 105-121): dtv = dt, dtf = 0.5*dt/mvv2e. */
 emd_status emd_nve_initial(emd_ctx* ctx);
 emd_status emd_nve_final(emd_ctx* ctx);
+/* emd_nve_initial on rows [first, first+count) of the owned particles.  A
+ * pending final kick and a pending zero of the forces are applied to every
+ * row first, each as its own pass (emd_nve_initial folds a pending kick into
+ * its own pass, which rounds differently in the mixed form). */
+emd_status emd_nve_initial_range(emd_ctx* ctx, int first, int count);
 
 /* ------------------------------------------------------- CommSerial
  * CommSerial (comm_serial.h:95-213, comm_serial.cpp:41-127). */

@@ -119,3 +119,48 @@ def test_stage_rejects_bad_arguments(tmp_path):
     with pytest.raises(TypeError):
         md.ctx.stage(0, np.zeros((n, 3), np.float32))
     md.close()
+
+
+def test_ranged_stage_commit_and_initial_integration(tmp_path):
+    """Rows staged and committed chunk by chunk, then integrated chunk by
+    chunk, leave the bits of update + one whole initial integration."""
+    from examinimd_gb300 import MD
+    deck, args = write_case(dict(CASES["lj_fcc6_full_csr"]), str(tmp_path))
+    for precision in ("fp64", "mixed"):
+        a, b = (MD(["-il", deck, "--quiet", "--precision", precision] + args) for _ in range(2))
+        n = a.info()["N_local"]
+        st = a.ctx.get(0, n)
+        rng = np.random.default_rng(7)
+        x = np.ascontiguousarray(st["x"] + rng.uniform(-0.01, 0.01, (n, 3)))
+        v = np.ascontiguousarray(rng.normal(size=(n, 3)))
+        f = np.ascontiguousarray(rng.normal(size=(n, 3)))
+        a.ctx.update(0, x, v, f)
+        a.ctx.nve_initial()
+        cuts = [0, n // 3, n // 2, n]
+        for lo, hi in zip(cuts[:-1], cuts[1:]):
+            for field, arr in ((0, x), (1, v), (2, f)):
+                b.ctx.stage_range(field, np.ascontiguousarray(arr[lo:hi]), lo)
+        for lo, hi in zip(cuts[:-1], cuts[1:]):
+            b.ctx.commit_range(lo, hi - lo)
+            b.ctx.nve_initial_range(lo, hi - lo)
+        ga, gb = a.ctx.get(0, n), b.ctx.get(0, n)
+        for k in ("x", "v", "f"):
+            np.testing.assert_array_equal(ga[k], gb[k], err_msg=f"{precision} {k}")
+        a.close()
+        b.close()
+
+
+def test_commit_range_rejects_a_straddling_stage(tmp_path):
+    from examinimd_gb300 import MD, EmdError
+    deck, args = write_case(dict(CASES["lj_fcc6_full_csr"]), str(tmp_path))
+    md = MD(["-il", deck, "--quiet"] + args)
+    n = md.info()["N_local"]
+    v = np.ascontiguousarray(md.ctx.get(0, n)["v"])
+    md.ctx.stage_range(1, np.ascontiguousarray(v[: n // 2]), 0)
+    with pytest.raises(EmdError):
+        md.ctx.commit_range(0, n // 4)
+    md.ctx.commit_range(0, n)  # the whole range takes it
+    np.testing.assert_array_equal(md.ctx.get(0, n)["v"], v)
+    with pytest.raises(EmdError):
+        md.ctx.commit_range(0, n + 1)
+    md.close()
