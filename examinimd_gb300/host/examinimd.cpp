@@ -178,9 +178,9 @@ void ExaMiniMD::run(int nsteps) { run_host(nsteps, nullptr, nullptr, nullptr); }
 // The step loop of ExaMiniMD::run (examinimd.cpp:192-276).  With host arrays
 // (hx non-null) every step uploads x, v, f of the owned particles from them
 // and reads them back into them as soon as each is final: x after the initial
-// integration (after the rebuild's re-sort on rebuild steps), overlapping the
-// force; f after the force, overlapping the final integration; v last.  The
-// first step's upload is a plain update.  Every later step's upload is staged
+// integration, overlapping the force (on rebuild steps after the re-sort,
+// overlapping the list build); f after the force, overlapping the final
+// integration; v last.  The first step's upload is a plain update.  Every later step's upload is staged
 // chunk by chunk, each chunk of a field as soon as the previous step's
 // read-back of that chunk has landed in the host array, so uploads and
 // read-backs use both directions of the host link at once.  The step then
@@ -241,15 +241,18 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
       clk.split(B_COMM);
       binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, false, true);
       clk.split(B_OTHER);
+      // the owned x is final once re-sorted: the halo exchange, the ghost
+      // binning and the list build leave it alone, so its read-back runs
+      // beside them
+      if (host) {
+        for (int k = 0; k < kChunks; k++) read_back(0, hx, k, step);
+        clk.anchor();
+      }
       comm->exchange_halo();
       clk.split(B_COMM);
       binning->create_binning(neigh_cutoff, neigh_cutoff, neigh_cutoff, 1, true, true, false);
       neighbor->create_neigh_list(system, binning, force->half_neigh, false);
       clk.split(B_NEIGH);
-      if (host) {
-        for (int k = 0; k < kChunks; k++) read_back(0, hx, k, step);
-        clk.anchor();
-      }
     } else {
       comm->update_halo();
       clk.split(B_COMM);
