@@ -235,7 +235,8 @@ emd_status emd_binning_get(emd_ctx* ctx, int* bincount, int* binoffsets, int* pe
       bounds[2 * d] = c.bmin[d];
       bounds[2 * d + 1] = c.bmax[d];
     }
-  EMD_CUDA(cudaStreamSynchronize(c.stream));
+  // the bounds are host values: no wait unless a device array was copied
+  if (bincount || binoffsets || permute) EMD_CUDA(cudaStreamSynchronize(c.stream));
   EMD_API_END
 }
 
