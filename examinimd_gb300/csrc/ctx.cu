@@ -539,13 +539,14 @@ static void require_field_range(const Ctx& c, int field, int first, int count, c
 
 static bool overlaps(int a0, int an, int b0, int bn) { return a0 < b0 + bn && b0 < a0 + an; }
 
-// Pending staged ranges made before N_local changed are dropped (their rows
-// no longer name the same particles) and the call fails.
-static void require_staged_count(Ctx& c, const char* msg) {
+// Pending staged ranges made before N_local changed are dropped: their rows
+// no longer name the same particles.  A commit that finds such ranges fails
+// (the rows it was to move are gone); a new stage just starts afresh.
+static void drop_stale_staged(Ctx& c, const char* fail_msg) {
   if (c.staged.empty() || c.staged_n == c.N_local) return;
   for (const auto& r : c.staged) c.staged_pool.push_back(r.done);
   c.staged.clear();
-  throw Error(EMD_ERR_ARG, msg);
+  if (fail_msg) throw Error(EMD_ERR_ARG, fail_msg);
 }
 
 // Staged rows of the owned atoms moved into place: x packed into x4 with the
@@ -612,7 +613,7 @@ emd_status emd_system_stage_range(emd_ctx* ctx, int field, const double* host, i
   require_field_range(c, field, first, count, host,
                       "emd_system_stage_range: field must be 0 (x), 1 (v) or 2 (f), rows within the owned "
                       "particles, host non-null");
-  require_staged_count(c, "emd_system_stage_range: the owned count changed since the pending ranges were staged");
+  drop_stale_staged(c, nullptr);
   if (count == 0) return EMD_OK;
   ensure_copy_streams(c);
   c.stage_up[field].reserve(3 * size_t(c.N_local), c.up_stream, true);
@@ -644,7 +645,7 @@ emd_status emd_system_commit_range(emd_ctx* ctx, int first, int count) {
   std::vector<Ctx::Staged> mine, rest;
   for (const auto& r : c.staged) (overlaps(r.first, r.count, first, count) ? mine : rest).push_back(r);
   if (mine.empty()) return EMD_OK;
-  require_staged_count(c, "emd_system_commit_range: the owned count changed after the rows were staged");
+  drop_stale_staged(c, "emd_system_commit_range: the owned count changed after the rows were staged");
   for (const auto& r : mine)
     require(r.first >= first && r.first + r.count <= first + count, EMD_ERR_ARG,
             "emd_system_commit_range: a staged range straddles the committed rows");

@@ -180,9 +180,9 @@ void ExaMiniMD::run(int nsteps) { run_host(nsteps, nullptr, nullptr, nullptr); }
 // and reads them back into them as soon as each is final: x after the initial
 // integration, overlapping the force (on rebuild steps after the re-sort,
 // overlapping the list build); f after the force, overlapping the final
-// integration; v last.  The first step's upload is a plain update.  Every later step's upload is staged
-// chunk by chunk, each chunk of a field as soon as the previous step's
-// read-back of that chunk has landed in the host array, so uploads and
+// integration; v last.  Every upload is staged chunk by chunk: the first
+// step's at once, every later step's chunk of a field as soon as the previous
+// step's read-back of that chunk has landed in the host array, so uploads and
 // read-backs use both directions of the host link at once.  The step then
 // starts chunk by chunk too: commit the chunk's staged rows, integrate them,
 // read their x back, while the next chunk's upload of v is still running.
@@ -221,13 +221,23 @@ void ExaMiniMD::run_host(int nsteps, double* hx, double* hv, double* hf) {
   };
   for (int step = first_step; step <= last_step; step++) {
     const bool rebuild = step % input->comm_exchange_rate == 0 && step > 0;
-    if (host && step == first_step) check(emd_system_update(ctx, 0, system->N_local, hx, hv, hf), ctx, "emd_system_update");
+    if (host && step == first_step) {
+      // the first step's upload, staged chunk by chunk like every later one
+      for (int k = 0; k < kChunks; k++) {
+        int first, count;
+        rows(k, first, count);
+        const size_t o = 3 * size_t(first);
+        for (int field = 0; field < 3; field++)
+          check(emd_system_stage_range(ctx, field, (field == 0 ? hx : field == 1 ? hv : hf) + o, first, count), ctx,
+                "emd_system_stage_range");
+      }
+    }
     clk.anchor();
     if (host) {
       for (int k = 0; k < kChunks; k++) {
         int first, count;
         rows(k, first, count);
-        if (step > first_step) check(emd_system_commit_range(ctx, first, count), ctx, "emd_system_commit_range");
+        check(emd_system_commit_range(ctx, first, count), ctx, "emd_system_commit_range");
         integrator->initial_integrate_range(first, count);
         if (!rebuild) read_back(0, hx, k, step);
       }

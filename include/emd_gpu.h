@@ -102,8 +102,9 @@ emd_status emd_system_download_wait(emd_ctx* ctx);
  * not overwritten while it is read.  Arrays of different fields must not
  * overlap.  emd_system_commit makes the context's stream wait for every
  * staged field and moves them into place exactly as emd_system_update(0,
- * N_local, ...) would (x keeps the types); N_local must not change in
- * between.  The caller must not write a staged host array before a later
+ * N_local, ...) would (x keeps the types).  Ranges staged before N_local
+ * changed are dropped by the next stage, and a commit that finds them
+ * fails.  The caller must not write a staged host array before a later
  * synchronisation (emd_synchronize, or a download_wait after a download of
  * that field).  No reference counterpart: emd_md_run_host uses the pair to
  * upload the next step's fields while this step's read-backs are running. */
