@@ -251,6 +251,9 @@ class Context:
         and unwritten until a later synchronisation); applied by commit()."""
         if not (isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.flags.c_contiguous):
             raise TypeError("stage: a C-contiguous float64 array is required")
+        n = self.info()[0]
+        if arr.shape != (n, 3):
+            raise EmdError(f"stage: the array must hold the {n} owned rows, shape ({n}, 3)")
         self._ok(self.lib.emd_system_stage(self.h, field, _dp(arr)), "emd_system_stage")
 
     def commit(self):
@@ -261,8 +264,9 @@ class Context:
         """emd_system_stage_range: queues the upload of rows [first, first +
         len(arr)) of x (0), v (1) or f (2) from ``arr`` (kept alive and
         unwritten until a later synchronisation)."""
-        if not (isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.flags.c_contiguous):
-            raise TypeError("stage_range: a C-contiguous float64 array is required")
+        if not (isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.flags.c_contiguous
+                and arr.ndim == 2 and arr.shape[1] == 3):
+            raise TypeError("stage_range: a C-contiguous float64 array of shape (rows, 3) is required")
         self._ok(self.lib.emd_system_stage_range(self.h, field, _dp(arr), first, arr.shape[0]),
                  "emd_system_stage_range")
 

@@ -164,3 +164,29 @@ def test_commit_range_rejects_a_straddling_stage(tmp_path):
     with pytest.raises(EmdError):
         md.ctx.commit_range(0, n + 1)
     md.close()
+
+
+def test_staged_ranges_from_before_a_count_change_are_dropped(tmp_path):
+    """Rows staged before N_local changed no longer name the same particles:
+    a commit that finds them fails, and a new stage starts afresh."""
+    from examinimd_gb300 import MD, EmdError
+    deck, args = write_case(dict(CASES["lj_fcc6_full_csr"]), str(tmp_path))
+    md = MD(["-il", deck, "--quiet"] + args)
+    ctx = md.ctx
+    n = md.info()["N_local"]
+    st = ctx.get(0, n)
+    x, v, t, i = (np.ascontiguousarray(st[k]) for k in ("x", "v", "type", "id"))
+    stale = np.ascontiguousarray(np.full((n, 3), 7.0))
+    ctx.stage(1, stale)
+    m = n - 4
+    ctx.set_local(x[:m], t[:m], i[:m], v=v[:m])
+    with pytest.raises(EmdError):
+        ctx.commit()
+    # the stale range is gone: a new stage and commit move only the new rows
+    ctx.commit()
+    with pytest.raises(EmdError):  # the whole-array form wants all N_local rows
+        ctx.stage(1, stale)
+    ctx.stage(1, np.ascontiguousarray(v[:m] * 2.0))
+    ctx.commit()
+    np.testing.assert_array_equal(ctx.get(0, m)["v"], v[:m] * 2.0)
+    md.close()
