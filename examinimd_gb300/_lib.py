@@ -93,6 +93,7 @@ _SIGS = {
     "emd_batch_stream": ([_P], _P),
     "emd_snap_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_snap_init": ([_P, _I, _D, _D, _I, _D, _I, _DP, _DP, _DP, _I, _I, _IP, _I], _I),
+    "emd_snap_info": ([_P, _IP, _IP], _I),
     "emd_snap_set_beta": ([_P, _DP], _I),
     "emd_snap_compute": ([_P], _I),
     "emd_snap_energy": ([_P, _DP], _I),
@@ -368,14 +369,24 @@ class Context:
 
     def lj_adjoint(self, dL_dF, dL_dE: float):
         """(dL/deps, dL/dsigma) for dL/dF (N_local x 3, current order) and dL/dE."""
-        g = _f64(dL_dF, (-1, 3))
+        g = self._owned_rows(dL_dF, "lj_adjoint")
         out = np.zeros(2)
         self._ok(self.lib.emd_lj_adjoint(self.h, _dp(g), float(dL_dE), _dp(out)), "emd_lj_adjoint")
         return out
 
+    def _owned_rows(self, a, what):
+        """``a`` as a C-ordered float64 array of the N_local x 3 rows the library reads."""
+        g = _f64(a, (-1, 3))
+        n = self.info()[0]
+        if g.shape[0] != n:
+            raise EmdError(f"{what}: {n} rows of 3 expected, got {g.shape[0]}")
+        return g
+
     def snap_adjoint(self, dL_dF, dL_dE: float, nelem: int, ncoeffall: int):
         """dL/dbeta (nelem x ncoeffall) for dL/dF (N_local x 3, current order) and dL/dE."""
-        g = _f64(dL_dF, (-1, 3))
+        g = self._owned_rows(dL_dF, "snap_adjoint")
+        if (nelem, ncoeffall) != self.snap_info():
+            raise EmdError(f"snap_adjoint: the SNAP force has coefficients of shape {self.snap_info()}")
         out = np.zeros((nelem, ncoeffall))
         self._ok(self.lib.emd_snap_adjoint(self.h, _dp(g), float(dL_dE), _dp(out)), "emd_snap_adjoint")
         return out
@@ -421,9 +432,17 @@ class Context:
                                         _dp(radelem), _dp(wjelem), _dp(beta), beta.shape[1], len(tmap), _ip(tmap),
                                         precision), "emd_snap_init")
 
+    def snap_info(self):
+        """(nelem, ncoeffall) of the initialised SNAP force (emd_snap_info)."""
+        a, b = _I(), _I()
+        self._ok(self.lib.emd_snap_info(self.h, C.byref(a), C.byref(b)), "emd_snap_info")
+        return a.value, b.value
+
     def snap_set_beta(self, beta):
         """emd_snap_set_beta: new linear coefficients (nelem x ncoeffall), same tables."""
         b = np.ascontiguousarray(beta, dtype=np.float64)
+        if b.shape != self.snap_info():
+            raise EmdError(f"snap_set_beta: coefficients of shape {self.snap_info()} expected")
         self._ok(self.lib.emd_snap_set_beta(self.h, _dp(b)), "emd_snap_set_beta")
 
     def snap_compute(self):

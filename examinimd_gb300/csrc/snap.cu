@@ -536,6 +536,15 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   EMD_API_END
 }
 
+emd_status emd_snap_info(emd_ctx* ctx, int* nelem, int* ncoeffall) {
+  EMD_API_BEGIN
+  const SnapHost* h = static_cast<const SnapHost*>(c.snap);
+  require(h != nullptr, EMD_ERR_STATE, "emd_snap_info: SNAP not initialised");
+  if (nelem) *nelem = h->d.nelem;
+  if (ncoeffall) *ncoeffall = h->d.ncoeffall;
+  EMD_API_END
+}
+
 emd_status emd_snap_set_beta(emd_ctx* ctx, const double* beta) {
   EMD_API_BEGIN
   SnapHost* h = static_cast<SnapHost*>(c.snap);

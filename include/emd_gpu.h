@@ -259,6 +259,10 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
 /* Replaces the linear coefficients (nelem x ncoeffall, as in emd_snap_init)
  * of an initialised SNAP force without rebuilding its tables. */
 emd_status emd_snap_set_beta(emd_ctx* ctx, const double* beta);
+/* The element and coefficient counts of the initialised SNAP force: the
+ * shape of beta in emd_snap_set_beta and of grad_beta in emd_snap_adjoint.
+ * No counterpart in ExaMiniMD. */
+emd_status emd_snap_info(emd_ctx* ctx, int* nelem, int* ncoeffall);
 /* compute(): f += SNAP forces (owner and ghost rows; update_force follows). */
 emd_status emd_snap_compute(emd_ctx* ctx);
 /* SNAP energy sum_i (beta_0 + sum_k beta_k B_k^i) plus the 1.25e5/r^12 term
