@@ -207,14 +207,22 @@ class Context:
         dom = _f64(domain)
         lo = _f64(sub_lo)
         hi = _f64(domain if sub_hi is None else sub_hi)
+        if dom.size != 3 or lo.size != 3 or hi.size != 3:
+            raise EmdError("system_init: domain, sub_lo and sub_hi need three components each")
         self._ok(self.lib.emd_system_init(self.h, len(mass), _dp(mass), boltz, mvv2e, dt, _dp(dom), _dp(lo), _dp(hi)),
                  "emd_system_init")
 
     def set_local(self, x, type_, id_, v=None, f=None, q=None):
         x = _f64(x, (-1, 3))
         n = x.shape[0]
-        self._ok(self.lib.emd_system_set_local(self.h, n, _dp(x), _dp(_f64(v, (-1, 3))), _dp(_f64(f, (-1, 3))),
-                                               _ip(_i32(type_)), _ip(_i32(id_)), _dp(_f64(q))), "emd_system_set_local")
+        v, f, q = _f64(v, (-1, 3)), _f64(f, (-1, 3)), _f64(q)
+        t, i = _i32(type_), _i32(id_)
+        # the library reads n rows of every array it is given
+        for name, a, rows in (("v", v, n), ("f", f, n), ("q", q, n), ("type", t, n), ("id", i, n)):
+            if a is not None and a.shape[0] != rows:
+                raise EmdError(f"set_local: {name} must have {rows} rows like x")
+        self._ok(self.lib.emd_system_set_local(self.h, n, _dp(x), _dp(v), _dp(f), _ip(t), _ip(i), _dp(q)),
+                 "emd_system_set_local")
 
     def info(self):
         a, b, c = _I(), _I(), _I()
@@ -244,6 +252,8 @@ class Context:
         particles' x, v, f (None = unchanged)."""
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x, v, f)]
         n = next((a.shape[0] for a in arrs if a is not None), 0)
+        if any(a is not None and a.shape != (n, 3) for a in arrs):
+            raise EmdError(f"update: x, v, f must all have shape ({n}, 3)")
         self._ok(self.lib.emd_system_update(self.h, first, n, *[_dp(a) for a in arrs]), "emd_system_update")
 
     def stage(self, field, arr):
@@ -356,6 +366,8 @@ class Context:
     def lj_init(self, lj1, lj2, cutsq, half=False, precision=EMD_PREC_FP64):
         lj1, lj2, cutsq = _f64(lj1), _f64(lj2), _f64(cutsq)
         nt = int(round(np.sqrt(lj1.size)))
+        if nt * nt != lj1.size or lj2.size != lj1.size or cutsq.size != lj1.size:
+            raise EmdError("lj_init: lj1, lj2 and cutsq must be ntypes x ntypes tables")
         self._ok(self.lib.emd_lj_init(self.h, nt, _dp(lj1), _dp(lj2), _dp(cutsq), int(half), precision),
                  "emd_lj_init")
 
@@ -428,6 +440,8 @@ class Context:
         radelem, wjelem = _f64(radelem), _f64(wjelem)
         beta = _f64(beta, (len(radelem), -1))
         tmap = _i32(type_map)
+        if wjelem.size != radelem.size:
+            raise EmdError("snap_init: one weight per element radius")
         self._ok(self.lib.emd_snap_init(self.h, twojmax, rfac0, rmin0, switchflag, rcutfac, len(radelem),
                                         _dp(radelem), _dp(wjelem), _dp(beta), beta.shape[1], len(tmap), _ip(tmap),
                                         precision), "emd_snap_init")
