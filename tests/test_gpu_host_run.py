@@ -30,10 +30,13 @@ def _host_arrays(src, pinned):
     return out
 
 
+# 6^3 fcc cells (864 atoms) fit in one chunk of the step start (chunk edges
+# fall on multiples of 512 rows); 9^3 cells (2,916 atoms) split into two
+@pytest.mark.parametrize("cells", [6, 9])
 @pytest.mark.parametrize("precision,pinned", [("fp64", False), ("mixed", False), ("fp64", True), ("mixed", True)])
-def test_run_host_equals_update_run_get(precision, pinned, tmp_path):
+def test_run_host_equals_update_run_get(precision, pinned, cells, tmp_path):
     from examinimd_gb300 import MD
-    case = dict(CASES["lj_fcc6_full_csr"])
+    case = dict(CASES["lj_fcc6_full_csr"], n=cells)
     deck, args = write_case(case, str(tmp_path))
     args = args + ["--precision", precision]
     a, b = MD(["-il", deck, "--quiet"] + args), MD(["-il", deck, "--quiet"] + args)
