@@ -817,7 +817,8 @@ def fit_measure(local: int, evals: int) -> dict:
         out[name] = {"gradient_evals_per_s": evals / t, "configs": len(cfgs), "atoms": atoms,
                      "atom_evals_per_s": atoms * evals / t, "grad_norm": float(g.norm()),
                      "how": "wall time of loss + backward through torch.autograd (FP64 forward of every "
-                            "configuration, then the adjoint), each configuration on its own context"}
+                            "configuration, then the adjoint; SNAP: the adjoint reads the U_tot and Z its "
+                            "forward kept), each configuration on its own context"}
     for c in scfg + lcfg:
         c.close()
     return out

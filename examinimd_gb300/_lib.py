@@ -94,6 +94,7 @@ _SIGS = {
     "emd_snap_adjoint": ([_P, _DP, _D, _DP], _I),
     "emd_snap_init": ([_P, _I, _D, _D, _I, _D, _I, _DP, _DP, _DP, _I, _I, _IP, _I], _I),
     "emd_snap_info": ([_P, _IP, _IP], _I),
+    "emd_snap_keep_for_adjoint": ([_P, _I], _I),
     "emd_snap_set_beta": ([_P, _DP], _I),
     "emd_snap_compute": ([_P], _I),
     "emd_snap_energy": ([_P, _DP], _I),
@@ -445,6 +446,12 @@ class Context:
         self._ok(self.lib.emd_snap_init(self.h, twojmax, rfac0, rmin0, switchflag, rcutfac, len(radelem),
                                         _dp(radelem), _dp(wjelem), _dp(beta), beta.shape[1], len(tmap), _ip(tmap),
                                         precision), "emd_snap_init")
+
+    def snap_keep_for_adjoint(self, on=True):
+        """emd_snap_keep_for_adjoint: FP64 force passes keep U_tot and Z for
+        the adjoint that follows on the same positions (bit-identical
+        gradients, the adjoint's phases B and C skipped)."""
+        self._ok(self.lib.emd_snap_keep_for_adjoint(self.h, int(bool(on))), "emd_snap_keep_for_adjoint")
 
     def snap_info(self):
         """(nelem, ncoeffall) of the initialised SNAP force (emd_snap_info)."""

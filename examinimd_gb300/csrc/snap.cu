@@ -29,6 +29,13 @@ struct SnapHost {
   std::vector<int> k_t1, k_t2, k_t3;
   std::vector<double> k_f2, k_f3;
   std::vector<int> k_j;  // (j1, j2, j) of coefficient k
+  // U_tot and Z jobs of the last FP64 force pass, kept for an adjoint on the
+  // same positions and list (emd_snap_keep_for_adjoint)
+  bool keep_on = false, keep_valid = false;
+  unsigned long long keep_xver = 0;
+  long long keep_builds = -1;
+  int keep_n = -1;
+  DevBuf<double> keep_u, keep_z;
 };
 
 
@@ -188,7 +195,7 @@ void free_snap(Ctx& c) {
   h->zord.release();
   h->inside_max.release();
   for (auto* b : {&h->cg, &h->cY, &h->beta0, &h->radelem, &h->wjelem, &h->eatom, &h->adj, &h->adj_sum,
-                  &h->adj_g, &h->invf, &h->yscale})
+                  &h->adj_g, &h->invf, &h->yscale, &h->keep_u, &h->keep_z})
     b->release();
   for (auto* b : {&h->cg_f, &h->cY_f, &h->yscale_f}) b->release();
   delete h;
@@ -288,6 +295,12 @@ static void snap_launch(Ctx& c, bool energy) {
       h->eatom.reserve(size_t(n), c.stream);
       A.eatom = h->eatom.p;
     }
+    if (h->keep_on) {
+      h->keep_u.reserve(2 * size_t(h->d.nuf) * n, c.stream);
+      h->keep_z.reserve(2 * size_t(h->d.njobs) * n, c.stream);
+      A.keep_u = reinterpret_cast<Cplx<double>*>(h->keep_u.p);
+      A.keep_z = reinterpret_cast<Cplx<double>*>(h->keep_z.p);
+    }
     auto k = k_snap<double, 0>;
     EMD_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     TimedLaunch t(c, fused ? "snap_fp64_energy" : "snap_fp64");
@@ -295,6 +308,12 @@ static void snap_launch(Ctx& c, bool energy) {
     if (fused) {
       c.snap_pe_fused_valid = true;
       c.snap_pe_fused_version = c.x_version;
+    }
+    if (h->keep_on) {
+      h->keep_valid = true;
+      h->keep_xver = c.x_version;
+      h->keep_builds = c.neigh_builds;
+      h->keep_n = n;
     }
   } else {
     TimedLaunch t(c, "snap_mixed");
@@ -333,6 +352,12 @@ static void snap_adjoint(Ctx& c, const double* dL_dF, double dL_dE, double* grad
     A.newton = c.comm_newton;
     A.adj = h->adj.p;
     A.work_bytes = snap_work_bytes(S, 8);
+    // B and C from the last FP64 force pass, when it ran on these positions and this list
+    if (h->keep_on && h->keep_valid && h->keep_xver == c.x_version && h->keep_builds == c.neigh_builds &&
+        h->keep_n == n) {
+      A.keep_u = reinterpret_cast<Cplx<double>*>(h->keep_u.p);
+      A.keep_z = reinterpret_cast<Cplx<double>*>(h->keep_z.p);
+    }
     const size_t smem = snap_smem_bytes(S, A.cap, 8) + snap_adjoint_bytes(S);
     require(smem <= 227 * 1024, EMD_ERR_ARG, "SNAP adjoint: neighbour rows too long for shared memory");
     auto k = k_snap<double, 2>;
@@ -533,6 +558,19 @@ emd_status emd_snap_init(emd_ctx* ctx, int twojmax, double rfac0, double rmin0, 
   S.radelem = h->radelem.p;
   S.wjelem = h->wjelem.p;
   S.map = h->map.p;
+  EMD_API_END
+}
+
+emd_status emd_snap_keep_for_adjoint(emd_ctx* ctx, int on) {
+  EMD_API_BEGIN
+  SnapHost* h = static_cast<SnapHost*>(c.snap);
+  require(h != nullptr, EMD_ERR_STATE, "emd_snap_keep_for_adjoint: SNAP not initialised");
+  h->keep_on = on != 0;
+  h->keep_valid = false;
+  if (!h->keep_on) {
+    h->keep_u.release();
+    h->keep_z.release();
+  }
   EMD_API_END
 }
 

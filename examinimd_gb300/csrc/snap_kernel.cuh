@@ -544,6 +544,11 @@ struct SnapArgs {
   int newton;                // ghost forces fold back to their owners
   double* adj;               // column-major per-atom outputs, (2 nfull + 1) x n_local
   size_t work_bytes;         // size of the shared `work` region
+  // U_tot (nuf) and the Z jobs (njobs) of every owned atom, FP64 form only:
+  // a force pass (MODE 0) writes them when non-null, and an adjoint (MODE 2)
+  // on the same positions and list reads them instead of running B and C
+  Cplx<double>* keep_u = nullptr;
+  Cplx<double>* keep_z = nullptr;
 };
 
 // MODE 0: forces; 1: per-atom energy; 2: adjoint columns (FP64 only).
@@ -740,21 +745,35 @@ __global__ void __launch_bounds__(SNAP_THREADS, sizeof(R) == sizeof(float) ? 4 :
   }
   __syncthreads();
 
-  // ---- B: U_tot (FP64, both forms); layer loops unrolled at the SNAP-W setting
-  if (S.twojmax == 8)
-    b_stage<R, 8>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
-  else
-    b_stage<R>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
-
-  // ---- C: Z jobs and Y = sum_t cY_t Z_t
   // (the adjoint keeps Z for its final contraction, beyond `work`)
   Cplx<R>* zs = reinterpret_cast<Cplx<R>*>(MODE == 2 ? work + A.work_bytes : work);
   const R* cg = sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cg) : reinterpret_cast<const R*>(S.cg_f);
-  if (S.twojmax == 8)
-    z_jobs<R, 9>(S, utot_r, cg, zs);
-  else
-    z_jobs<R, 0>(S, utot_r, cg, zs);
+  if (MODE == 2 && kF64 && A.keep_u != nullptr) {
+    // B and C as the force pass on the same positions and list left them
+    // (the same operations: the values are bit for bit those of a rerun)
+    const Cplx<double>* ku = A.keep_u + size_t(i) * S.nuf;
+    const Cplx<double>* kz = A.keep_z + size_t(i) * S.njobs;
+    for (int e = tid; e < S.nuf; e += SNAP_THREADS) utot[e] = ku[e];
+    for (int e = tid; e < S.njobs; e += SNAP_THREADS) zs[e] = Cplx<R>{R(kz[e].r), R(kz[e].i)};
+  } else {
+    // ---- B: U_tot (FP64, both forms); layer loops unrolled at the SNAP-W setting
+    if (S.twojmax == 8)
+      b_stage<R, 8>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
+    else
+      b_stage<R>(S, nd, A.cap, ninside, reinterpret_cast<Cplx<double>*>(work), utot, utot_r);
+    // ---- C: Z jobs and Y = sum_t cY_t Z_t
+    if (S.twojmax == 8)
+      z_jobs<R, 9>(S, utot_r, cg, zs);
+    else
+      z_jobs<R, 0>(S, utot_r, cg, zs);
+  }
   __syncthreads();
+  if (MODE == 0 && kF64 && A.keep_u != nullptr) {  // kept for a following adjoint
+    Cplx<double>* ku = A.keep_u + size_t(i) * S.nuf;
+    Cplx<double>* kz = A.keep_z + size_t(i) * S.njobs;
+    for (int e = tid; e < S.nuf; e += SNAP_THREADS) ku[e] = utot[e];
+    for (int e = tid; e < S.njobs; e += SNAP_THREADS) kz[e] = Cplx<double>{double(zs[e].r), double(zs[e].i)};
+  }
   const R* cY = (sizeof(R) == 8 ? reinterpret_cast<const R*>(S.cY) : reinterpret_cast<const R*>(S.cY_f)) +
                 (size_t)ei * S.nfull;
   // FP64 forces with A.eatom set: the atom's energy in the same pass, the

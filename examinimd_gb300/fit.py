@@ -130,6 +130,8 @@ class SnapConfig(_Config):
         self.ctx.snap_init(int(p["twojmax"]), float(p.get("rfac0", 0.99363)), float(p.get("rmin0", 0.0)),
                            int(p.get("switchflag", 1)), float(p["rcutfac"]), [self.radius], [self.weight],
                            np.asarray(beta, float)[None, :], [0], precision=EMD_PREC_FP64)
+        # the forward pass keeps U_tot and Z for the adjoint of the backward pass
+        self.ctx.snap_keep_for_adjoint(True)
         self.build()
 
     def _compute(self):

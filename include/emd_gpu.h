@@ -292,6 +292,14 @@ emd_status emd_snap_ncoeff(emd_ctx* ctx, int* ncoeff);
  * (the reaction term only where j's force reaches an owned atom).  Needs the
  * current full neighbour list of the forces; computed in FP64. */
 emd_status emd_snap_adjoint(emd_ctx* ctx, const double* dL_dF, double dL_dE, double* grad_beta);
+/* on != 0: every FP64 force pass (emd_snap_compute) also keeps U_tot and the
+ * Z contraction of every owned atom in device memory (about 43 KB per atom
+ * at twojmax 8), and an emd_snap_adjoint on the same positions and list reads
+ * them instead of recomputing them (its two costliest FP64 phases).  The
+ * gradient is bit-identical either way.  on == 0 frees the memory.  No
+ * counterpart in ExaMiniMD: it serves fitting, a forward pass and then its
+ * adjoint. */
+emd_status emd_snap_keep_for_adjoint(emd_ctx* ctx, int on);
 
 /* ------------------------------------------------------ Properties
  * Temperature / KinE (property_temperature.cpp:43-62, property_kine.cpp:43-61):

@@ -63,6 +63,44 @@ def test_snap_adjoint_vs_assembled_and_fd():
         c.close()
 
 
+def test_snap_adjoint_from_kept_phases_is_bit_identical():
+    """On one force pass and the same dL/dF, the adjoint reading the U_tot and
+    Z that the force pass kept gives the bits of one that recomputes them
+    (two force passes would not do: the pair forces reach j through FP64
+    atomics, so forces, and a loss gradient built from them, can differ in
+    the last bit from pass to pass).  After the positions move, the kept copy
+    is stale and the adjoint recomputes."""
+    fit, cfgs, ncoef, E_ref, F_ref = _snap_setup(3)
+    beta = torch.tensor(fit.synthetic_beta(11, ncoef))
+    rng = np.random.default_rng(3)
+    for c in cfgs:
+        gF = rng.normal(size=(c.n, 3))
+        c.ctx.snap_keep_for_adjoint(True)
+        with torch.no_grad():
+            fit.SnapEnergyForces.apply(beta, [c])  # the force pass keeps U_tot and Z
+        g_kept = c.adjoint(gF, 0.5, ncoef)
+        g_again = c.adjoint(gF, 0.5, ncoef)
+        c.ctx.snap_keep_for_adjoint(False)
+        g_fresh = c.adjoint(gF, 0.5, ncoef)
+        np.testing.assert_array_equal(g_kept, g_fresh)
+        np.testing.assert_array_equal(g_again, g_fresh)
+    c = cfgs[0]
+    n = c.n
+    gF = rng.normal(size=(n, 3))
+    c.ctx.snap_keep_for_adjoint(True)
+    with torch.no_grad():
+        fit.SnapEnergyForces.apply(beta, [c])
+    g_kept = c.adjoint(gF, 0.5, ncoef)
+    c.ctx.update(0, x=c.ctx.get(0, n)["x"] + rng.uniform(-1e-3, 1e-3, (n, 3)))  # moved: the kept copy is stale
+    g_moved = c.adjoint(gF, 0.5, ncoef)
+    c.ctx.snap_keep_for_adjoint(False)
+    g_fresh = c.adjoint(gF, 0.5, ncoef)
+    np.testing.assert_array_equal(g_moved, g_fresh)
+    assert not np.array_equal(g_kept, g_moved)
+    for c in cfgs:
+        c.close()
+
+
 def test_lj_adjoint_vs_fd():
     from examinimd_gb300 import fit
     cfgs = [fit.LJConfig(x, box) for x, box in fit.lj_config_set(3)]
