@@ -939,7 +939,9 @@ def main():
     os.dup2(2, 1)
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    # default: 1000 LJ steps (about 0.8 s of timed work at LJ-4M, 50 rebuild
+    # cycles and several 200 ms clock samples inside the timed region), 20 SNAP
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="lj4m", choices=list(WORKLOADS))
@@ -961,6 +963,8 @@ def main():
     ap.add_argument("--thermo-steps", type=int, default=100)
     ap.add_argument("--fit-evals", type=int, default=5)
     a = ap.parse_args()
+    if a.steps is None:
+        a.steps = 20 if a.workload == "snapw" else 1000
     if a.warmup < 3:
         sys.exit("--warmup must be >= 3")
     if a.cells:
